@@ -1,0 +1,319 @@
+"""Benchmark of the screen-space NL-PF pass on the synthetic 1920x1080 x 4 spp x 5 depth records.
+
+One step = one full NL-PF pass: the 5 depths filtered deepest-first through the C ABI
+(sty_pf_screen_filter_depth), each depth's styled output feeding the parent depth.
+  value : Mpath-vertices/s with the records already resident in HBM (valid records filtered per
+          second; 41.47 M records, ~90 % valid, per step). Inputs (2.2 GB) exceed the 129 MB L2,
+          so no explicit flush is needed between steps.
+  e2e   : the same metric through the public API with HOST buffers: every step copies the
+          records from pinned host memory, runs the pass and reads back the depth-0 result.
+  roofline: the dominant kernel (k_pf_screen) against measured HBM bandwidth, from CUDA events
+          around each launch on the launching stream; `alu_roofline` gives the binding FP32 roof.
+  cpu_baseline: the FP32 CPU restatement (oracle, all host cores) on a bounded band of rows.
+`--impl reference` times the reference's CPU path (the restatement; the reference's own Rust /
+LuisaCompute CPU backend cannot be built on these machines) and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "NL-PF Mpath-vertices/s; NL-NRC BF16 vs FP32 Msamples/s at equal image MSE"
+W_, H_, S_, D_ = 1920, 1080, 4, 5
+WORKLOAD = "NL-PF screen-space filter, synthetic records 1920x1080 x 4 spp x 5 depths, radius 16 px"
+# HBM traffic (dram read + write) of one k_pf_screen launch at this size, from the ncu capture
+# summarised in profiles/k_pf_screen_1080p.md (None until captured)
+NCU_TRAFFIC_PER_LAUNCH = None
+
+
+def _rank_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(sty, orc, planes, valid, budget_s: float = 12.0):
+    """FP32 CPU restatement on all host threads over a band of query rows of depth 1 (with the
+    depth-2 result as input); grows the band until it takes >= budget_s / 4."""
+    n = W_ * H_ * S_
+    rec = sty.pf.host_records(planes, valid, W_, H_, S_, D_)
+    prm = sty.c2_params().c()
+    style = sty.c2_style()
+    nxt = np.zeros((3, n), dtype=np.float32)
+    rows, elapsed = 1, 0.0
+    while True:
+        y0 = 540
+        t0 = time.perf_counter()
+        orc.pf_screen_filter_depth_f32(rec, 1, prm, style, out_next=nxt, y0=y0, y1=y0 + rows)
+        elapsed = time.perf_counter() - t0
+        if elapsed >= budget_s / 4 or rows >= 256:
+            break
+        rows = min(256, max(rows * 2, int(rows * (budget_s / 4) / max(elapsed, 1e-3))))
+    nvalid = int(valid[n + 540 * W_ * S_: n + (540 + rows) * W_ * S_].sum())
+    return {"value": nvalid / elapsed / 1e6, "unit": "Mpath-vertices/s", "cores": orc.num_threads(),
+            "kind": "port",
+            "sample": f"depth-1 query rows {540}..{540 + rows - 1} of 1080 (x 1920 px x 4 spp, radius 16), "
+                      f"{nvalid} valid vertices in {elapsed:.2f} s, FP32 restatement of the filter"}
+
+
+def run_reference(args):
+    rank, world, _ = _rank_env()
+    if rank != 0:
+        return
+    import __graft_entry__ as g
+    sty = g.package()
+    import oracle as orc
+    planes, valid = sty.synth.records(W_, H_, S_, D_, seed=0)
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        last = cpu_baseline(sty, orc, planes, valid, budget_s=args.ref_budget)
+        if i >= args.warmup:
+            vals.append(last["value"])
+    v = statistics.median(vals)
+    last["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mpath-vertices/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "records": W_ * H_ * S_ * D_, "l2": "inputs > L2"},
+            "cpu_baseline": last,
+            "note": "reference CPU backend (Rust + LuisaCompute LLVM) cannot be built here; "
+                    "timed path is the oracle's FP32 restatement of the same filter",
+            "e2e": {"value": v, "unit": "Mpath-vertices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run(args):
+    import torch
+    rank, world, local = _rank_env()
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import __graft_entry__ as g
+    sty = g.package()
+    lib = sty.abi.lib()
+
+    planes, valid = sty.synth.records(W_, H_, S_, D_, seed=rank)
+    rs = sty.RecordSet.from_numpy(planes, valid, W_, H_, S_, D_, device=dev)
+    n = rs.n_per_depth
+    prm = sty.c2_params()
+    style = sty.c2_style()
+    nvalid = int(valid.sum())
+    stream = torch.cuda.current_stream(dev)
+    out = torch.empty((D_, 3, n), dtype=torch.float32, device=dev)
+
+    def barrier():
+        if dist:
+            torch.distributed.barrier()
+
+    def one_pass(evs=None):
+        for d in range(D_ - 1, -1, -1):
+            nxt = out[d + 1] if d + 1 < D_ else None
+            if evs is not None:
+                evs[d][0].record(stream)
+            sty.pf_screen_filter_depth(rs, d, prm, style, out_next=nxt, out=out[d], stream=stream)
+            if evs is not None:
+                evs[d][1].record(stream)
+
+    for _ in range(args.warmup):
+        one_pass()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.sty_launch_count()
+    kev = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(D_)] for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    t_start.record(stream)
+    for k in range(args.steps):
+        one_pass(kev[k])
+    t_end.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = lib.sty_launch_count() - launches0
+    ms_total = t_start.elapsed_time(t_end)
+    launch_ms = [kev[k][d][0].elapsed_time(kev[k][d][1]) for k in range(args.steps) for d in range(D_)]
+    clk = clocks.stop()
+
+    # ---- end-to-end through the public API with host buffers
+    h_planes = torch.from_numpy(planes).pin_memory()
+    h_valid = torch.from_numpy(valid).pin_memory()
+    h_out = torch.empty((3, n), dtype=torch.float32).pin_memory()
+    d_planes, d_valid = rs.planes, rs.valid
+
+    def e2e_step():
+        d_planes.copy_(h_planes, non_blocking=True)
+        d_valid.copy_(h_valid, non_blocking=True)
+        one_pass()
+        h_out.copy_(out[0], non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+
+    # ---- max over ranks
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    ms_total = max_over_ranks(ms_total)
+    e2e_ms = max_over_ranks(e2e_ms)
+    ms_step = ms_total / args.steps
+    value = nvalid * world * args.steps / (ms_total / 1e3) / 1e6
+    e2e_value = nvalid * world * args.steps / (e2e_ms / 1e3) / 1e6
+
+    # ---- roofline of k_pf_screen (algorithmic bytes per launch / mean launch time)
+    bytes_step = (52 * D_ + 12 * (D_ - 1) + 12 * D_) * n
+    bytes_launch = bytes_step / D_
+    mean_launch_s = statistics.mean(launch_ms) / 1e3
+    hbm_peak, peak_kind = _load_peaks()
+    achieved = bytes_launch / mean_launch_s / 1e9
+    pairs_launch = n * (2 * prm.radius + 1) ** 2 * S_
+    sm_clock = (clk or {}).get("sm_mhz") or 1900.0
+    fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12  # TFLOP/s, FFMA = 2 FLOP, at the sampled clock
+    flops_pair = 2 * 13  # 13 FP32 FMA/ADD-class instructions per pair (exponent 9, accumulate 4)
+    alu_achieved = pairs_launch * flops_pair / mean_launch_s / 1e12
+
+    if rank != 0:
+        if dist:
+            torch.distributed.destroy_process_group()
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mpath-vertices/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded records, distributions of the workload)",
+        "config": {"workload": WORKLOAD, "width": W_, "height": H_, "spp": S_, "depths": D_,
+                   "radius": prm.radius, "sigma_pixel": prm.sigma_pixel, "sigma_pos": prm.sigma_pos,
+                   "sigma_nrm": prm.sigma_nrm, "style": "toon 0.1/0.3/0.6 at depth 1",
+                   "records_per_step": W_ * H_ * S_ * D_, "valid_vertices_per_step": nvalid,
+                   "l2": "inputs (2.2 GB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_value, "unit": "Mpath-vertices/s",
+                "h2d_bytes_per_step": int(planes.nbytes + valid.nbytes), "d2h_bytes_per_step": int(3 * n * 4)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": NCU_TRAFFIC_PER_LAUNCH,
+                     "kernel": "k_pf_screen", "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
+        "alu_roofline": {"bound": "fp32", "achieved": alu_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                         "frac": alu_achieved / fp32_peak, "pairs_per_launch": pairs_launch,
+                         "flops_per_pair": flops_pair,
+                         "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 at the sampled SM clock"},
+        "clocks": clk,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        import oracle as orc
+        line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid)
+    print(json.dumps(line), flush=True)
+    if dist:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=8.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run(args)
+
+
+if __name__ == "__main__":
+    main()

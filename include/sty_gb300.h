@@ -1,0 +1,197 @@
+/*
+ * sty_gb300.h -- C ABI of the GB300-native stylized nonlinear rendering hot path.
+ *
+ * Plain C, bindgen-clean: opaque handles, plain pointers and sizes, int32 status codes.
+ * No call aborts the process; every entry point returns a sty_status and leaves a
+ * human-readable message for sty_last_error().
+ *
+ * Memory: every pointer argument documented as "device" must point into CUDA device memory of
+ * the current device (or managed memory); the caller owns it. Streams are plain cudaStream_t
+ * values passed as void* (NULL = the legacy default stream). No entry point performs a
+ * device-wide synchronisation unless documented.
+ *
+ * Record layout of the screen-space path-vertex buffers (sty_pf_records): every field is a
+ * separate array of `depths * height * width * spp` elements indexed as
+ *     i = ((d * height + y) * width + x) * spp + s
+ * i.e. the spp samples of one pixel are adjacent, then pixels in a row, rows, depths.
+ *
+ * Reference interfaces this ABI replaces (paths relative to the reference project):
+ *   - crates/akari_integrator/src/lm_path_filtering.rs:758-1060 (evaluate_filtered_radiance,
+ *     kernel_filter) and :974-998 (kernel_propagate): the NL-PF per-depth filter pass.
+ *   - crates/akari_render/src/svm/surface/mod.rs:492-1346 (the sty_* style nodes applied by
+ *     Surface::apply_stylization).
+ *   - crates/akari_integrator/src/lm_path_filtering.rs:20-59 (hash, get_cell, cell index).
+ *   - crates/akari_render/src/sampler/mod.rs:82-137 (Pcg32).
+ */
+#ifndef STY_GB300_H
+#define STY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define STY_API __attribute__((visibility("default")))
+#else
+#define STY_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------------------------
+ * Status codes
+ * -------------------------------------------------------------------------------------- */
+typedef int32_t sty_status;
+#define STY_OK 0
+#define STY_ERR_ARG 1         /* invalid argument (null pointer, bad size, bad enum)        */
+#define STY_ERR_OOM 2         /* a device allocation failed                                  */
+#define STY_ERR_CUDA 3        /* a CUDA runtime call failed (message in sty_last_error())    */
+#define STY_ERR_ITER_LIMIT 4  /* a bounded device loop hit its iteration cap                 */
+#define STY_ERR_NAN 5         /* a non-finite value was detected where it is not allowed     */
+#define STY_ERR_UNSUPPORTED 6 /* the request is valid but not supported by this build/device */
+
+/* Version of this ABI: major * 10000 + minor * 100 + patch. */
+STY_API int32_t sty_version(void);
+/* Static string naming a status code. */
+STY_API const char *sty_status_string(sty_status status);
+/* Message of the last failing call on the calling host thread ("" if none). */
+STY_API const char *sty_last_error(void);
+/* Number of kernels this library launched since load (all threads, all devices). Used by
+ * benchmarks to count launches inside a timed region. */
+STY_API uint64_t sty_launch_count(void);
+
+/* ----------------------------------------------------------------------------------------
+ * Style programs: the nonlinear "svm/surface" style nodes
+ *
+ * A program is a chain of up to STY_STYLE_MAX_NODES nodes applied innermost first, exactly as
+ * the reference applies `inner.apply_stylization` before its own operation
+ * (crates/akari_render/src/svm/surface/mod.rs:573-610 and siblings). Node i runs at path depth
+ * d only if bit min(d,31) of nodes[i].depth_mask is set.
+ *
+ * Parameter layout per kind (p[] = node.p, n = node.n):
+ *   STY_STYLE_TOON        reference sty_toon (mod.rs:573-610):        p[0] = color_band_width
+ *   STY_STYLE_PALETTE     reference sty_color_palette (mod.rs:697-735): p[0] = indirect_scale,
+ *                         p[1] = gamma, n = palette length (<= 19), p[2+3k .. 4+3k] = colour k
+ *   STY_STYLE_SAT_ADJUST  reference sty_saturation_adjust (mod.rs:821-851): p[0] = power,
+ *                         p[1] = indirect_scale
+ *   STY_STYLE_SAT_REX     reference sty_saturation_adjust_rex (mod.rs:1060-1089): p[0] = blend
+ *   STY_STYLE_EIGHT_BIT   reference sty_8bit (mod.rs:1316-1345): p[0] = indirect_scale
+ *   STY_STYLE_TOON_STEPS  hard threshold toon on Rec.709 luminance, hue preserving:
+ *                         n thresholds (1..8) p[0..n-1] ascending, n+1 output luminance levels
+ *                         p[8..8+n]; out = rgb / lum * level(#{t_k <= lum})
+ *   STY_STYLE_RAMP_SMOOTH smoothed colour ramp on Rec.709 luminance (differentiable):
+ *                         n steps (1..8), p[0] = sharpness s, p[1..8] = thresholds t_k,
+ *                         p[9+3k .. 11+3k] = colour c_k;
+ *                         out = sum_k sigmoid(s * (lum - t_k)) * (c_k - c_{k-1}), c_{-1} = 0
+ * -------------------------------------------------------------------------------------- */
+#define STY_STYLE_NONE 0
+#define STY_STYLE_TOON 1
+#define STY_STYLE_PALETTE 2
+#define STY_STYLE_SAT_ADJUST 3
+#define STY_STYLE_SAT_REX 4
+#define STY_STYLE_EIGHT_BIT 5
+#define STY_STYLE_TOON_STEPS 7
+#define STY_STYLE_RAMP_SMOOTH 8
+
+#define STY_STYLE_MAX_NODES 4
+#define STY_STYLE_MAX_PARAMS 60
+
+typedef struct sty_style_node {
+    int32_t kind;
+    uint32_t depth_mask;
+    int32_t n;
+    int32_t reserved;
+    float p[STY_STYLE_MAX_PARAMS];
+} sty_style_node;
+
+typedef struct sty_style_program {
+    int32_t n_nodes;
+    int32_t reserved[3];
+    sty_style_node nodes[STY_STYLE_MAX_NODES];
+} sty_style_program;
+
+/* Apply a style program to `n` RGB triples (device, interleaved rgb, in-place allowed) at path
+ * depth `depth`. Replaces Surface::apply_stylization for one material
+ * (crates/akari_render/src/svm/surface/mod.rs:262-285). */
+STY_API sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
+                           float *rgb_out, uint64_t n, void *stream);
+
+/* ----------------------------------------------------------------------------------------
+ * Screen-space NL-PF filter
+ *
+ * Per depth d (processed from the deepest to 0, like the reference's backward loop
+ * lm_path_filtering.rs:1673-1774), for every valid record i = (d, y, x, s):
+ *   in_d(j)  = rad(d, j) + thr(d, j) * out_{d+1}(j)          (out_{D} = 0)
+ *   f_d(i)   = sum_j w_ij in_d(j) / sum_j w_ij,   j over valid records (d, y', x', s') with
+ *              |x'-x| <= radius, |y'-y| <= radius, inside the image, any s'
+ *   w_ij     = exp(-((x'-x)^2 + (y'-y)^2) / (2 sigma_pixel^2)
+ *                  - |pos_i - pos_j|^2 / (2 sigma_pos^2) - (1 - nrm_i . nrm_j) / sigma_nrm^2)
+ *   out_d(i) = style(d, f_d(i))                              (0 for invalid records)
+ * The inner sums are FP32 with compensated (Kahan) accumulation. sigma_pixel <= 0 drops the
+ * pixel-distance term. The throughput product thr(d-1) * out_d is the "indirect" term that
+ * lm_path_filtering.rs:864-885 forms as f * L * mis / pdf.
+ * -------------------------------------------------------------------------------------- */
+typedef struct sty_pf_records {
+    const float *pos[3];  /* device, world-space vertex position                     */
+    const float *nrm[3];  /* device, unit shading normal                             */
+    const float *rad[3];  /* device, radiance leaving the vertex without the next bounce */
+    const float *thr[3];  /* device, throughput from this vertex to the next one     */
+    const int32_t *valid; /* device, nonzero if the record holds a vertex            */
+    int32_t width, height, spp, depths;
+} sty_pf_records;
+
+typedef struct sty_pf_screen_params {
+    int32_t radius;    /* half window in pixels, 0..32 */
+    float sigma_pixel; /* pixels; <= 0 disables the pixel-distance term */
+    float sigma_pos;   /* world units, > 0 */
+    float sigma_nrm;   /* > 0 */
+} sty_pf_screen_params;
+
+/* Filter one depth. `out_next` (device, 3 planes of width*height*spp floats: r plane, g plane,
+ * b plane) holds out_{d+1} or is NULL at the deepest depth. `out` receives out_d with the same
+ * layout. `filtered` (optional, same layout) receives f_d before the style node. */
+STY_API sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth,
+                                      const sty_pf_screen_params *params,
+                                      const sty_style_program *style, const float *out_next,
+                                      float *out, float *filtered, void *stream);
+
+/* Filter all depths, deepest first. `out` (device) holds 3 * depths planes laid out as
+ * [depth][channel][height*width*spp]; on return out[d] = out_d for every depth. */
+STY_API sty_status sty_pf_screen_filter(const sty_pf_records *rec, const sty_pf_screen_params *params,
+                                const sty_style_program *style, float *out, void *stream);
+
+/* Average the depth-0 outputs of each pixel over its spp samples and add them into an FP64
+ * progressive film (device, width*height*3 doubles, interleaved rgb):
+ *   film[p] += weight * mean_s out_0(p, s)
+ * Replaces kernel_splat + kernel_update_film (lm_path_filtering.rs:429-506); FP64 is used only
+ * for this accumulation across iterations. */
+STY_API sty_status sty_film_accumulate(const float *out0, int32_t width, int32_t height, int32_t spp,
+                               double weight, double *film, void *stream);
+
+/* ----------------------------------------------------------------------------------------
+ * Integer helpers (bit-exact with the reference)
+ * -------------------------------------------------------------------------------------- */
+typedef struct sty_pcg32 {
+    uint64_t state;
+    uint64_t inc;
+} sty_pcg32;
+
+/* Pcg32::new_seq_offset (sampler/mod.rs:94-100) for seq = first_seq + i, seed = seeds[i]
+ * (device arrays of n), then `draws` calls of gen_u32 per stream written to out (device,
+ * n * draws, stream-major) and the final states to states (device, n). */
+STY_API sty_status sty_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n,
+                             uint32_t draws, uint32_t *out, sty_pcg32 *states, void *stream);
+
+/* Hash-grid cell index of each point (lm_path_filtering.rs:20-59): cell = clamp((p - pmin) /
+ * (pmax - pmin), 0, 1) * res truncated and clamped to res-1; index = (x*73856093 ^ y*19349663
+ * ^ z*83492791) mod table_size in 64-bit. `points` is device xyz-interleaved, n points. */
+STY_API sty_status sty_hash_cells(const float *points, uint64_t n, const float pmin[3],
+                          const float pmax[3], const uint32_t res[3], uint32_t table_size,
+                          uint32_t *cell_xyz, uint32_t *cell_index, void *stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* STY_GB300_H */

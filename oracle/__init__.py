@@ -1,0 +1,94 @@
+"""CPU oracle of the stylized NL-PF hot path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes binding of oracle/_build/liboracle.so (built by oracle/build.py from sty_oracle.cpp).
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this package;
+the product library never calls it. See sty_oracle.h for the parity status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liboracle.so"
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from . import build as _b
+            _b.build()
+        L = C.CDLL(str(LIB_PATH))
+        vp = C.c_void_p
+        L.orc_num_threads.restype = C.c_int32
+        L.orc_set_num_threads.argtypes = [C.c_int32]
+        L.orc_style_apply_f64.argtypes = [vp, C.c_uint32, vp, vp, C.c_uint64]
+        L.orc_pf_screen_filter_depth_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp]
+        L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
+        L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
+        L.orc_hash_cells.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, vp, vp]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def style_apply(program, depth: int, rgb: np.ndarray) -> np.ndarray:
+    rgb = np.ascontiguousarray(rgb, dtype=np.float64).reshape(-1, 3)
+    out = np.empty_like(rgb)
+    lib().orc_style_apply_f64(C.addressof(program) if program is not None else None, depth, _p(rgb), _p(out),
+                              rgb.shape[0])
+    return out
+
+
+def pf_screen_filter_depth(rec, depth, params, style, out_next=None, want_filtered=False):
+    """FP64 filter of one depth on host records (abi.PfRecords over numpy arrays).
+    Returns (out [3, n], filtered [3, n] or None) as float64."""
+    n = rec.width * rec.height * rec.spp
+    out = np.zeros((3, n), dtype=np.float64)
+    filt = np.zeros((3, n), dtype=np.float64) if want_filtered else None
+    nxt = None if out_next is None else np.ascontiguousarray(out_next, dtype=np.float64)
+    lib().orc_pf_screen_filter_depth_f64(C.addressof(rec), depth, C.addressof(params),
+                                         C.addressof(style) if style is not None else None,
+                                         _p(nxt), _p(out), _p(filt))
+    return out, filt
+
+
+def pf_screen_filter_depth_f32(rec, depth, params, style, out_next=None, y0=0, y1=None):
+    n = rec.width * rec.height * rec.spp
+    out = np.zeros((3, n), dtype=np.float32)
+    nxt = None if out_next is None else np.ascontiguousarray(out_next, dtype=np.float32)
+    lib().orc_pf_screen_filter_depth_f32(C.addressof(rec), depth, C.addressof(params),
+                                         C.addressof(style) if style is not None else None,
+                                         _p(nxt), _p(out), None, y0, rec.height if y1 is None else y1)
+    return out
+
+
+def pcg32_streams(seeds: np.ndarray, first_seq: int, draws: int):
+    seeds = np.ascontiguousarray(seeds, dtype=np.uint64)
+    out = np.zeros((seeds.size, draws), dtype=np.uint32)
+    states = np.zeros((seeds.size, 2), dtype=np.uint64)
+    lib().orc_pcg32_streams(_p(seeds), first_seq, seeds.size, draws, _p(out), _p(states))
+    return out, states
+
+
+def hash_cells(points: np.ndarray, pmin, pmax, res, table_size: int):
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    pmin = np.asarray(pmin, dtype=np.float32)
+    pmax = np.asarray(pmax, dtype=np.float32)
+    res = np.asarray(res, dtype=np.uint32)
+    cells = np.zeros((pts.shape[0], 3), dtype=np.uint32)
+    idx = np.zeros(pts.shape[0], dtype=np.uint32)
+    lib().orc_hash_cells(_p(pts), pts.shape[0], _p(pmin), _p(pmax), _p(res), table_size, _p(cells), _p(idx))
+    return cells, idx
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()

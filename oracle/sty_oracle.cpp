@@ -1,0 +1,460 @@
+// sty_oracle.cpp -- CPU restatement of the reference arithmetic (test infrastructure only;
+// see sty_oracle.h). Reference paths are relative to the reference project root.
+#include "sty_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+template <class T>
+struct V3 {
+    T x, y, z;
+};
+template <class T>
+inline V3<T> v3(T x, T y, T z) {
+    return {x, y, z};
+}
+
+// ---- colour helpers: crates/akari_render/src/color.rs:328-361, 536-600 ----------------------
+template <class T>
+inline T lum709(V3<T> c) {  // Color::lum, color.rs:356-361
+    return c.x * T(0.2126) + c.y * T(0.7152) + c.z * T(0.0722);
+}
+template <class T>
+inline T linear_to_srgb1(T v) {  // color.rs:545-549
+    return v <= T(0.0031308) ? v * T(12.92) : std::pow(v, T(1) / T(2.4)) * T(1.055) - T(0.055);
+}
+template <class T>
+inline T srgb_to_linear1(T v) {  // color.rs:540-544
+    return v <= T(0.04045) ? v / T(12.92) : std::pow((v + T(0.055)) / T(1.055), T(2.4));
+}
+template <class T>
+inline V3<T> linear_to_srgb(V3<T> c) {
+    return {linear_to_srgb1(c.x), linear_to_srgb1(c.y), linear_to_srgb1(c.z)};
+}
+template <class T>
+inline V3<T> srgb_to_linear(V3<T> c) {
+    return {srgb_to_linear1(c.x), srgb_to_linear1(c.y), srgb_to_linear1(c.z)};
+}
+template <class T>
+inline T clampv(T v, T lo, T hi) {
+    return std::min(std::max(v, lo), hi);
+}
+template <class T>
+inline T rem_euclid(T a, T b) {
+    T r = std::fmod(a, b);
+    return r < T(0) ? r + std::fabs(b) : r;
+}
+template <class T>
+V3<T> rgb_to_hsv(V3<T> c) {  // color.rs:551-575
+    T mx = std::max(c.x, std::max(c.y, c.z));
+    T mn = std::min(c.x, std::min(c.y, c.z));
+    T diff = mx - mn;
+    T h;
+    if (mx == mn)
+        h = 0;
+    else if (mx == c.x)
+        h = rem_euclid((c.y - c.z) / diff, T(6));
+    else if (mx == c.y)
+        h = (c.z - c.x) / diff + T(2);
+    else
+        h = (c.x - c.y) / diff + T(4);
+    h = h / T(6);
+    T s = mx == T(0) ? T(0) : diff / mx;
+    return {h, s, mx};
+}
+template <class T>
+V3<T> hsv_to_rgb(V3<T> hsv) {  // color.rs:577-590
+    auto f = [&](int n) {
+        T k = rem_euclid(T(n) + hsv.x * T(6), T(6));
+        T m = std::max(std::min(std::min(k, T(4) - k), T(1)), T(0));
+        return hsv.z - hsv.z * hsv.y * m;
+    };
+    return {f(5), f(3), f(1)};
+}
+template <class T>
+inline T round_half_away(T v) {
+    return std::round(v);
+}
+
+// ---- style nodes: crates/akari_render/src/svm/surface/mod.rs ---------------------------------
+template <class T>
+V3<T> style_node(const sty_style_node &nd, uint32_t depth, V3<T> li) {
+    switch (nd.kind) {
+        case STY_STYLE_TOON: {  // ToonSurface::apply_stylization, mod.rs:573-610
+            T w = T(nd.p[0]);
+            V3<T> c = {clampv(li.x, T(0), T(1e5)), clampv(li.y, T(0), T(1e5)),
+                       clampv(li.z, T(0), T(1e5))};
+            T lum = lum709(c);
+            if (lum <= T(0)) return c;
+            V3<T> hue = {c.x / lum, c.y / lum, c.z / lum};
+            T nl;
+            if (lum > T(1)) {
+                nl = std::floor(lum / w) * w;
+            } else {
+                T a = linear_to_srgb1(lum);
+                nl = srgb_to_linear1(std::floor(a / w) * w);
+            }
+            return {hue.x * nl, hue.y * nl, hue.z * nl};
+        }
+        case STY_STYLE_PALETTE: {  // ColorPaletteSurface::apply_stylization, mod.rs:697-735
+            T indirect_scale = T(nd.p[0]), gamma = T(nd.p[1]);
+            V3<T> c = li;
+            T lum = (c.x + c.y + c.z) / T(3);
+            if (depth != 0) c = {c.x / indirect_scale, c.y / indirect_scale, c.z / indirect_scale};
+            c = {clampv(c.x, T(0), T(1)), clampv(c.y, T(0), T(1)), clampv(c.z, T(0), T(1))};
+            c = {std::pow(c.x, gamma), std::pow(c.y, gamma), std::pow(c.z, gamma)};
+            T min_dist = T(1e16);
+            V3<T> best = {0, 0, 0};
+            for (int k = 0; k < nd.n; k++) {
+                V3<T> q = {T(nd.p[2 + 3 * k]), T(nd.p[3 + 3 * k]), T(nd.p[4 + 3 * k])};
+                T dx = q.x - c.x, dy = q.y - c.y, dz = q.z - c.z;
+                T dist = dx * dx + dy * dy + dz * dz;
+                if (dist < min_dist) {
+                    min_dist = dist;
+                    best = q;
+                }
+            }
+            T ig = T(1) / gamma;
+            c = {std::pow(best.x, ig), std::pow(best.y, ig), std::pow(best.z, ig)};
+            if (depth != 0) {
+                T nl = (c.x + c.y + c.z) / T(3);
+                if (nl != T(0)) {
+                    T s = lum / nl;
+                    c = {c.x * s, c.y * s, c.z * s};
+                }
+            }
+            return c;
+        }
+        case STY_STYLE_SAT_ADJUST: {  // SaturationAdjustSurface, mod.rs:821-851
+            T power = T(nd.p[0]), indirect_scale = T(nd.p[1]);
+            T lum = std::max(li.x, std::max(li.y, li.z));
+            if (lum == T(0)) return li;
+            V3<T> c = li;
+            if (depth != 0) c = {c.x / indirect_scale, c.y / indirect_scale, c.z / indirect_scale};
+            c = {clampv(c.x, T(0), T(1)), clampv(c.y, T(0), T(1)), clampv(c.z, T(0), T(1))};
+            c = linear_to_srgb(c);
+            V3<T> hsv = rgb_to_hsv(c);
+            hsv.y = std::pow(hsv.y, power);
+            c = srgb_to_linear(hsv_to_rgb(hsv));
+            if (depth != 0) c = {c.x * indirect_scale, c.y * indirect_scale, c.z * indirect_scale};
+            return c;
+        }
+        case STY_STYLE_SAT_REX: {  // SaturationAdjustRexSurface, mod.rs:1060-1089
+            T blend = T(nd.p[0]);
+            T lum = (li.x + li.y + li.z) / T(3);
+            T cmin = std::min(li.x, std::min(li.y, li.z));
+            if (lum <= T(0) || cmin < T(0)) return li;
+            T cmax = std::max(li.x, std::max(li.y, li.z));
+            V3<T> imax = {(li.x - cmin) / cmax, (li.y - cmin) / cmax, (li.z - cmin) / cmax};
+            T u = (imax.x + imax.y + imax.z) / T(3);
+            if (u != T(0)) {
+                T k = (T(1) - blend);
+                return {blend * lum + k * imax.x * lum / u, blend * lum + k * imax.y * lum / u,
+                        blend * lum + k * imax.z * lum / u};
+            }
+            T v = blend * lum + (T(1) - blend) * lum;
+            return {v, v, v};
+        }
+        case STY_STYLE_EIGHT_BIT: {  // EightBitSurface, mod.rs:1316-1345
+            T indirect_scale = T(nd.p[0]);
+            auto map8 = [&](V3<T> c) {
+                V3<T> s = linear_to_srgb(c);
+                V3<T> q = {round_half_away(s.x * T(8)) / T(8), round_half_away(s.y * T(8)) / T(8),
+                           round_half_away(s.z * T(4)) / T(4)};
+                return srgb_to_linear(q);
+            };
+            T lum = std::max(li.x, std::max(li.y, li.z));
+            if (lum == T(0)) return li;
+            if (depth > 0) {
+                V3<T> m = map8({li.x / indirect_scale, li.y / indirect_scale, li.z / indirect_scale});
+                return {m.x * indirect_scale, m.y * indirect_scale, m.z * indirect_scale};
+            }
+            T nl = std::min(lum, T(1));
+            return map8({li.x / lum * nl, li.y / lum * nl, li.z / lum * nl});
+        }
+        case STY_STYLE_TOON_STEPS: {  // threshold toon (no reference counterpart)
+            V3<T> c = {clampv(li.x, T(0), T(1e5)), clampv(li.y, T(0), T(1e5)),
+                       clampv(li.z, T(0), T(1e5))};
+            T lum = lum709(c);
+            if (lum <= T(0)) return c;
+            int k = 0;
+            for (int t = 0; t < nd.n; t++) k += (T(nd.p[t]) <= lum) ? 1 : 0;
+            T level = T(nd.p[8 + k]);
+            return {c.x / lum * level, c.y / lum * level, c.z / lum * level};
+        }
+        case STY_STYLE_RAMP_SMOOTH: {  // smoothed colour ramp (no reference counterpart)
+            V3<T> c = {clampv(li.x, T(0), T(1e5)), clampv(li.y, T(0), T(1e5)),
+                       clampv(li.z, T(0), T(1e5))};
+            T lum = lum709(c);
+            T s = T(nd.p[0]);
+            V3<T> o = {0, 0, 0};
+            V3<T> prev = {0, 0, 0};
+            for (int k = 0; k < nd.n; k++) {
+                V3<T> ck = {T(nd.p[9 + 3 * k]), T(nd.p[10 + 3 * k]), T(nd.p[11 + 3 * k])};
+                T sg = T(1) / (T(1) + std::exp(-s * (lum - T(nd.p[1 + k]))));
+                o.x += sg * (ck.x - prev.x);
+                o.y += sg * (ck.y - prev.y);
+                o.z += sg * (ck.z - prev.z);
+                prev = ck;
+            }
+            return o;
+        }
+        default:
+            return li;
+    }
+}
+
+template <class T>
+V3<T> style_apply(const sty_style_program *prog, uint32_t depth, V3<T> li) {
+    if (!prog) return li;
+    uint32_t bit = depth > 31 ? 31 : depth;
+    for (int i = 0; i < prog->n_nodes && i < STY_STYLE_MAX_NODES; i++) {
+        const sty_style_node &nd = prog->nodes[i];
+        if (!((nd.depth_mask >> bit) & 1u)) continue;
+        li = style_node<T>(nd, depth, li);
+    }
+    return li;
+}
+
+inline size_t rec_index(const sty_pf_records *r, int d, int y, int x, int s) {
+    return (((size_t)d * r->height + y) * r->width + x) * r->spp + s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t orc_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+void orc_set_num_threads(int32_t n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+void orc_style_apply_f64(const sty_style_program *prog, uint32_t depth, const double *in,
+                         double *out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        V3<double> c = style_apply<double>(prog, depth, v3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        out[3 * i] = c.x;
+        out[3 * i + 1] = c.y;
+        out[3 * i + 2] = c.z;
+    }
+}
+
+// Screen-space NL-PF restated in FP64. The neighbour set, weights and recursion are the ones
+// documented in include/sty_gb300.h; the per-depth backward order and the propagation of the
+// styled result into the parent's "indirect" term follow lm_path_filtering.rs:1673-1764 and
+// :974-998, the style call follows :947-971.
+void orc_pf_screen_filter_depth_f64(const sty_pf_records *r, uint32_t depth,
+                                    const sty_pf_screen_params *prm,
+                                    const sty_style_program *style, const double *out_next,
+                                    double *out, double *filtered) {
+    const int W = r->width, H = r->height, S = r->spp, R = prm->radius;
+    const size_t N = (size_t)W * H * S;
+    const int d = (int)depth;
+    const double inv2s2 = prm->sigma_pixel > 0 ? 1.0 / (2.0 * (double)prm->sigma_pixel * prm->sigma_pixel) : 0.0;
+    const double inv2p2 = 1.0 / (2.0 * (double)prm->sigma_pos * prm->sigma_pos);
+    const double invn2 = 1.0 / ((double)prm->sigma_nrm * prm->sigma_nrm);
+    // in_d(j) = rad + thr * out_{d+1}
+    std::vector<double> in(3 * N);
+    for (size_t j = 0; j < N; j++) {
+        size_t gj = (size_t)d * N + j;
+        for (int c = 0; c < 3; c++) {
+            double v = r->rad[c][gj];
+            if (out_next) v += (double)r->thr[c][gj] * out_next[c * N + j];
+            in[3 * j + c] = v;
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < H; y++) {
+        for (int x = 0; x < W; x++) {
+            for (int s = 0; s < S; s++) {
+                size_t qi = ((size_t)y * W + x) * S + s;
+                size_t gq = (size_t)d * N + qi;
+                if (!r->valid[gq]) {
+                    for (int c = 0; c < 3; c++) {
+                        out[c * N + qi] = 0.0;
+                        if (filtered) filtered[c * N + qi] = 0.0;
+                    }
+                    continue;
+                }
+                double px = r->pos[0][gq], py = r->pos[1][gq], pz = r->pos[2][gq];
+                double nx = r->nrm[0][gq], ny = r->nrm[1][gq], nz = r->nrm[2][gq];
+                double sw = 0, sr = 0, sg = 0, sb = 0;
+                for (int yy = std::max(0, y - R); yy <= std::min(H - 1, y + R); yy++) {
+                    for (int xx = std::max(0, x - R); xx <= std::min(W - 1, x + R); xx++) {
+                        double dd2 = (double)(xx - x) * (xx - x) + (double)(yy - y) * (yy - y);
+                        for (int t = 0; t < S; t++) {
+                            size_t j = ((size_t)yy * W + xx) * S + t;
+                            size_t gj = (size_t)d * N + j;
+                            if (!r->valid[gj]) continue;
+                            double dx = px - r->pos[0][gj], dy = py - r->pos[1][gj], dz = pz - r->pos[2][gj];
+                            double nd = nx * r->nrm[0][gj] + ny * r->nrm[1][gj] + nz * r->nrm[2][gj];
+                            double arg = -dd2 * inv2s2 - (dx * dx + dy * dy + dz * dz) * inv2p2 - (1.0 - nd) * invn2;
+                            double w = std::exp(arg);
+                            sw += w;
+                            sr += w * in[3 * j];
+                            sg += w * in[3 * j + 1];
+                            sb += w * in[3 * j + 2];
+                        }
+                    }
+                }
+                V3<double> f = {sr / sw, sg / sw, sb / sw};
+                V3<double> o = style_apply<double>(style, depth, f);
+                out[qi] = o.x;
+                out[N + qi] = o.y;
+                out[2 * N + qi] = o.z;
+                if (filtered) {
+                    filtered[qi] = f.x;
+                    filtered[N + qi] = f.y;
+                    filtered[2 * N + qi] = f.z;
+                }
+            }
+        }
+    }
+}
+
+// FP32 restatement (CPU baseline). Per candidate pixel row the partial sums are plain FP32 and
+// are folded into Kahan-compensated totals (CompensatedSum, crates/akari_render/src/util/mod.rs:
+// 337-356).
+void orc_pf_screen_filter_depth_f32(const sty_pf_records *r, uint32_t depth,
+                                    const sty_pf_screen_params *prm,
+                                    const sty_style_program *style, const float *out_next,
+                                    float *out, float *filtered, int32_t y0, int32_t y1) {
+    const int W = r->width, H = r->height, S = r->spp, R = prm->radius;
+    const size_t N = (size_t)W * H * S;
+    const int d = (int)depth;
+    const float inv2s2 = prm->sigma_pixel > 0 ? 1.0f / (2.0f * prm->sigma_pixel * prm->sigma_pixel) : 0.0f;
+    const float inv2p2 = 1.0f / (2.0f * prm->sigma_pos * prm->sigma_pos);
+    const float invn2 = 1.0f / (prm->sigma_nrm * prm->sigma_nrm);
+    y0 = std::max(0, y0);
+    y1 = std::min(H, y1);
+    if (y1 <= y0) return;
+    // candidate rows needed: [y0-R, y1+R)
+    const int cy0 = std::max(0, y0 - R), cy1 = std::min(H, y1 + R);
+    const size_t c0 = (size_t)cy0 * W * S, cn = (size_t)(cy1 - cy0) * W * S;
+    std::vector<float> in(3 * cn);
+    for (size_t k = 0; k < cn; k++) {
+        size_t j = c0 + k, gj = (size_t)d * N + j;
+        for (int c = 0; c < 3; c++) {
+            float v = r->rad[c][gj];
+            if (out_next) v += r->thr[c][gj] * out_next[c * N + j];
+            in[3 * k + c] = v;
+        }
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int y = y0; y < y1; y++) {
+        for (int x = 0; x < W; x++) {
+            for (int s = 0; s < S; s++) {
+                size_t qi = ((size_t)y * W + x) * S + s;
+                size_t gq = (size_t)d * N + qi;
+                if (!r->valid[gq]) {
+                    for (int c = 0; c < 3; c++) {
+                        out[c * N + qi] = 0.0f;
+                        if (filtered) filtered[c * N + qi] = 0.0f;
+                    }
+                    continue;
+                }
+                float px = r->pos[0][gq], py = r->pos[1][gq], pz = r->pos[2][gq];
+                float nx = r->nrm[0][gq], ny = r->nrm[1][gq], nz = r->nrm[2][gq];
+                float tot[4] = {0, 0, 0, 0}, cmp[4] = {0, 0, 0, 0};
+                for (int yy = std::max(0, y - R); yy <= std::min(H - 1, y + R); yy++) {
+                    float part[4] = {0, 0, 0, 0};
+                    for (int xx = std::max(0, x - R); xx <= std::min(W - 1, x + R); xx++) {
+                        float dd2 = (float)((xx - x) * (xx - x) + (yy - y) * (yy - y));
+                        for (int t = 0; t < S; t++) {
+                            size_t j = ((size_t)yy * W + xx) * S + t;
+                            size_t gj = (size_t)d * N + j;
+                            if (!r->valid[gj]) continue;
+                            float dx = px - r->pos[0][gj], dy = py - r->pos[1][gj], dz = pz - r->pos[2][gj];
+                            float nd = nx * r->nrm[0][gj] + ny * r->nrm[1][gj] + nz * r->nrm[2][gj];
+                            float arg = -dd2 * inv2s2 - (dx * dx + dy * dy + dz * dz) * inv2p2 - (1.0f - nd) * invn2;
+                            float w = std::exp(arg);
+                            size_t k = j - c0;
+                            part[0] += w;
+                            part[1] += w * in[3 * k];
+                            part[2] += w * in[3 * k + 1];
+                            part[3] += w * in[3 * k + 2];
+                        }
+                    }
+                    for (int c = 0; c < 4; c++) {  // Kahan update
+                        float yv = part[c] - cmp[c];
+                        float t = tot[c] + yv;
+                        cmp[c] = (t - tot[c]) - yv;
+                        tot[c] = t;
+                    }
+                }
+                V3<float> f = {tot[1] / tot[0], tot[2] / tot[0], tot[3] / tot[0]};
+                V3<float> o = style_apply<float>(style, depth, f);
+                out[qi] = o.x;
+                out[N + qi] = o.y;
+                out[2 * N + qi] = o.z;
+                if (filtered) {
+                    filtered[qi] = f.x;
+                    filtered[N + qi] = f.y;
+                    filtered[2 * N + qi] = f.z;
+                }
+            }
+        }
+    }
+}
+
+// Pcg32 restated from crates/akari_render/src/sampler/mod.rs:82-123.
+static inline uint32_t pcg_next(sty_pcg32 &g) {
+    uint64_t old = g.state;
+    g.state = old * 0x5851f42d4c957f2dULL + g.inc;
+    uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+}
+
+void orc_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n, uint32_t draws,
+                       uint32_t *out, sty_pcg32 *states) {
+    for (uint64_t i = 0; i < n; i++) {
+        sty_pcg32 g;
+        g.state = 0;
+        g.inc = ((first_seq + i) << 1) | 1u;  // set_seq_offset, mod.rs:94-100
+        pcg_next(g);
+        g.state += seeds[i];
+        pcg_next(g);
+        for (uint32_t k = 0; k < draws; k++) out[i * draws + k] = pcg_next(g);
+        if (states) states[i] = g;
+    }
+}
+
+// HashGridVar::get_cell / cell_pos_to_index, lm_path_filtering.rs:20-59 (float arithmetic).
+void orc_hash_cells(const float *pts, uint64_t n, const float pmin[3], const float pmax[3],
+                    const uint32_t res[3], uint32_t table_size, uint32_t *cell_xyz,
+                    uint32_t *cell_index) {
+    for (uint64_t i = 0; i < n; i++) {
+        uint32_t c[3];
+        for (int a = 0; a < 3; a++) {
+            float p = (pts[3 * i + a] - pmin[a]) / (pmax[a] - pmin[a]);
+            p = std::min(std::max(p, 0.0f), 1.0f);
+            p = p * (float)res[a];
+            uint32_t u = (uint32_t)p;
+            c[a] = std::min(u, res[a] - 1u);
+            if (cell_xyz) cell_xyz[3 * i + a] = c[a];
+        }
+        uint64_t h = ((uint64_t)c[0] * 73856093ULL) ^ ((uint64_t)c[1] * 19349663ULL) ^
+                     ((uint64_t)c[2] * 83492791ULL);
+        if (cell_index) cell_index[i] = (uint32_t)(h % (uint64_t)table_size);
+    }
+}
+
+}  // extern "C"

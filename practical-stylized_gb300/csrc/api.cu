@@ -1,0 +1,214 @@
+// api.cu -- status/error plumbing and the small element-wise entry points of the C ABI:
+// style application, Pcg32 streams, hash-grid cells and the FP64 film accumulation.
+#include <cstdarg>
+#include <cstring>
+
+#include "common.cuh"
+#include "style.cuh"
+
+namespace sty {
+
+static thread_local char g_last_error[512] = {0};
+static std::atomic<uint64_t> g_launches{0};
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_last_error, sizeof(g_last_error), fmt, ap);
+    va_end(ap);
+}
+void clear_error() { g_last_error[0] = 0; }
+void count_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+sty_status check_cuda(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return STY_OK;
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    if (e == cudaErrorMemoryAllocation) return STY_ERR_OOM;
+    return STY_ERR_CUDA;
+}
+sty_status check_launch(const char *what) {
+    count_launch();
+    return check_cuda(cudaGetLastError(), what);
+}
+
+bool style_program_valid(const sty_style_program *p) {
+    if (!p) return true;
+    if (p->n_nodes < 0 || p->n_nodes > STY_STYLE_MAX_NODES) return false;
+    for (int i = 0; i < p->n_nodes; i++) {
+        const sty_style_node &n = p->nodes[i];
+        switch (n.kind) {
+            case STY_STYLE_NONE:
+            case STY_STYLE_TOON:
+            case STY_STYLE_SAT_ADJUST:
+            case STY_STYLE_SAT_REX:
+            case STY_STYLE_EIGHT_BIT:
+                break;
+            case STY_STYLE_PALETTE:
+                if (n.n < 0 || n.n > 19) return false;
+                break;
+            case STY_STYLE_TOON_STEPS:
+            case STY_STYLE_RAMP_SMOOTH:
+                if (n.n < 1 || n.n > 8) return false;
+                break;
+            default:
+                return false;
+        }
+    }
+    return true;
+}
+
+// ---- kernels ------------------------------------------------------------------------------
+__global__ void k_style_apply(sty_style_program prog, uint32_t depth, const float *in, float *out,
+                              uint64_t n) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 c = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
+    c = style_apply(prog, depth, c);
+    out[3 * i] = c.x;
+    out[3 * i + 1] = c.y;
+    out[3 * i + 2] = c.z;
+}
+
+__device__ __forceinline__ uint32_t pcg_next(sty_pcg32 &g) {
+    uint64_t old = g.state;
+    g.state = old * 0x5851f42d4c957f2dULL + g.inc;
+    uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+}
+
+// Pcg32::new_seq_offset + gen_u32 (crates/akari_render/src/sampler/mod.rs:94-123).
+__global__ void k_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n, uint32_t draws,
+                                uint32_t *out, sty_pcg32 *states) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sty_pcg32 g;
+    g.state = 0;
+    g.inc = ((first_seq + i) << 1) | 1ull;
+    pcg_next(g);
+    g.state += seeds[i];
+    pcg_next(g);
+    if (out)
+        for (uint32_t k = 0; k < draws; k++) out[i * draws + k] = pcg_next(g);
+    else
+        for (uint32_t k = 0; k < draws; k++) pcg_next(g);
+    if (states) states[i] = g;
+}
+
+struct GridDesc {
+    float pmin[3], pmax[3];
+    uint32_t res[3];
+    uint32_t table_size;
+};
+
+// HashGridVar::get_cell + cell_pos_to_index (lm_path_filtering.rs:20-59).
+__global__ void k_hash_cells(const float *pts, uint64_t n, GridDesc g, uint32_t *cell_xyz,
+                             uint32_t *cell_index) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t c[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float p = __fdiv_rn(pts[3 * i + a] - g.pmin[a], g.pmax[a] - g.pmin[a]);
+        p = fminf(fmaxf(p, 0.0f), 1.0f);
+        p = __fmul_rn(p, (float)g.res[a]);
+        uint32_t u = (uint32_t)p;
+        c[a] = min(u, g.res[a] - 1u);
+        if (cell_xyz) cell_xyz[3 * i + a] = c[a];
+    }
+    uint64_t h = ((uint64_t)c[0] * 73856093ull) ^ ((uint64_t)c[1] * 19349663ull) ^ ((uint64_t)c[2] * 83492791ull);
+    if (cell_index) cell_index[i] = (uint32_t)(h % (uint64_t)g.table_size);
+}
+
+// Pixel mean of the depth-0 outputs over spp, accumulated in FP64 (kernel_splat +
+// kernel_update_film, lm_path_filtering.rs:429-506).
+__global__ void k_film_accumulate(const float *out0, int32_t npix, int32_t spp, double weight, double *film) {
+    int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const size_t N = (size_t)npix * spp;
+    for (int c = 0; c < 3; c++) {
+        double s = 0.0;
+        for (int k = 0; k < spp; k++) s += (double)out0[c * N + (size_t)p * spp + k];
+        film[3 * (size_t)p + c] += weight * (s / spp);
+    }
+}
+
+}  // namespace sty
+
+using namespace sty;
+
+extern "C" {
+
+int32_t sty_version(void) { return 100; }
+
+const char *sty_status_string(sty_status s) {
+    switch (s) {
+        case STY_OK: return "STY_OK";
+        case STY_ERR_ARG: return "STY_ERR_ARG";
+        case STY_ERR_OOM: return "STY_ERR_OOM";
+        case STY_ERR_CUDA: return "STY_ERR_CUDA";
+        case STY_ERR_ITER_LIMIT: return "STY_ERR_ITER_LIMIT";
+        case STY_ERR_NAN: return "STY_ERR_NAN";
+        case STY_ERR_UNSUPPORTED: return "STY_ERR_UNSUPPORTED";
+        default: return "STY_ERR_UNKNOWN";
+    }
+}
+
+const char *sty_last_error(void) { return g_last_error; }
+
+uint64_t sty_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
+                           float *rgb_out, uint64_t n, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(program && rgb_in && rgb_out, "sty_style_apply: null argument");
+    STY_ARG_CHECK(style_program_valid(program), "sty_style_apply: invalid style program");
+    if (n == 0) return STY_OK;
+    const int bs = 256;
+    k_style_apply<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(*program, depth, rgb_in, rgb_out, n);
+    return check_launch("sty_style_apply");
+}
+
+sty_status sty_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n, uint32_t draws,
+                             uint32_t *out, sty_pcg32 *states, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(seeds, "sty_pcg32_streams: null seeds");
+    STY_ARG_CHECK(out || states, "sty_pcg32_streams: nothing to write");
+    if (n == 0) return STY_OK;
+    const int bs = 256;
+    k_pcg32_streams<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(seeds, first_seq, n, draws, out, states);
+    return check_launch("sty_pcg32_streams");
+}
+
+sty_status sty_hash_cells(const float *points, uint64_t n, const float pmin[3], const float pmax[3],
+                          const uint32_t res[3], uint32_t table_size, uint32_t *cell_xyz,
+                          uint32_t *cell_index, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(points && pmin && pmax && res, "sty_hash_cells: null argument");
+    STY_ARG_CHECK(table_size > 0 && res[0] > 0 && res[1] > 0 && res[2] > 0, "sty_hash_cells: empty grid");
+    STY_ARG_CHECK(cell_xyz || cell_index, "sty_hash_cells: nothing to write");
+    if (n == 0) return STY_OK;
+    GridDesc g;
+    for (int a = 0; a < 3; a++) {
+        g.pmin[a] = pmin[a];
+        g.pmax[a] = pmax[a];
+        g.res[a] = res[a];
+    }
+    g.table_size = table_size;
+    const int bs = 256;
+    k_hash_cells<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(points, n, g, cell_xyz, cell_index);
+    return check_launch("sty_hash_cells");
+}
+
+sty_status sty_film_accumulate(const float *out0, int32_t width, int32_t height, int32_t spp, double weight,
+                               double *film, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(out0 && film, "sty_film_accumulate: null argument");
+    STY_ARG_CHECK(width > 0 && height > 0 && spp > 0, "sty_film_accumulate: bad size %dx%dx%d", width, height, spp);
+    const int npix = width * height;
+    const int bs = 256;
+    k_film_accumulate<<<(npix + bs - 1) / bs, bs, 0, as_stream(stream)>>>(out0, npix, spp, weight, film);
+    return check_launch("sty_film_accumulate");
+}
+
+}  // extern "C"
