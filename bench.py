@@ -103,11 +103,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_baseline(sty, orc, planes, valid, budget_s: float = 12.0):
+def cpu_baseline(sty, orc, planes, valid, depths: int = D_, budget_s: float = 12.0):
     """FP32 CPU restatement on all host threads over a band of query rows of depth 1 (with the
     depth-2 result as input); grows the band until it takes >= budget_s / 4."""
     n = W_ * H_ * S_
-    rec = sty.pf.host_records(planes, valid, W_, H_, S_, D_)
+    assert depths >= 2 and planes.shape[1] == n * depths
+    rec = sty.pf.host_records(planes, valid, W_, H_, S_, depths)
     prm = sty.c2_params().c()
     style = sty.c2_style()
     nxt = np.zeros((3, n), dtype=np.float32)
@@ -167,6 +168,7 @@ def run(args):
     sty = g.package()
     lib = sty.abi.lib()
 
+    D_ = args.depths
     planes, valid = sty.synth.records(W_, H_, S_, D_, seed=rank)
     rs = sty.RecordSet.from_numpy(planes, valid, W_, H_, S_, D_, device=dev)
     n = rs.n_per_depth
@@ -214,6 +216,8 @@ def run(args):
     clk = clocks.stop()
 
     # ---- end-to-end through the public API with host buffers
+    if args.no_e2e:
+        e2e_step = None
     h_planes = torch.from_numpy(planes).pin_memory()
     h_valid = torch.from_numpy(valid).pin_memory()
     h_out = torch.empty((3, n), dtype=torch.float32).pin_memory()
@@ -225,20 +229,22 @@ def run(args):
         one_pass()
         h_out.copy_(out[0], non_blocking=True)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_ms = float("nan")
+    if not args.no_e2e:
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_ms = e0.elapsed_time(e1)
 
     # ---- max over ranks
     def max_over_ranks(x):
@@ -294,7 +300,7 @@ def run(args):
     }
     if world == 1 and not args.no_cpu_baseline:
         import oracle as orc
-        line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid)
+        line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid, D_)
     print(json.dumps(line), flush=True)
     if dist:
         torch.distributed.destroy_process_group()
@@ -308,6 +314,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-budget", type=float, default=8.0)
+    ap.add_argument("--depths", type=int, default=D_, help="path depths (profiling cases use fewer)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -61,6 +61,12 @@ STY_API const char *sty_last_error(void);
  * benchmarks to count launches inside a timed region. */
 STY_API uint64_t sty_launch_count(void);
 
+/* Device status word of the current device: kernels that hit a bounded wait (instead of
+ * hanging) OR a STY_DEV_* bit into it and return. Reading synchronises the device;
+ * clear != 0 resets the word to 0 after reading. */
+#define STY_DEV_WAIT_TIMEOUT 1u
+STY_API sty_status sty_device_status(uint32_t *status_out, int32_t clear);
+
 /* ----------------------------------------------------------------------------------------
  * Style programs: the nonlinear "svm/surface" style nodes
  *

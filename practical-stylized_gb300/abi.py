@@ -33,6 +33,16 @@ STY_STYLE_MAX_NODES = 4
 STY_STYLE_MAX_PARAMS = 60
 
 
+STY_DEV_WAIT_TIMEOUT = 1
+
+
+def device_status(clear: bool = True) -> int:
+    """Read (and by default clear) the device status word of the current device."""
+    v = C.c_uint32(0)
+    check(lib().sty_device_status(C.byref(v), 1 if clear else 0))
+    return v.value
+
+
 class StyError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"{status_name(status)}: {msg}")
@@ -80,6 +90,7 @@ SIGNATURES = {
     "sty_status_string": (C.c_char_p, [C.c_int32]),
     "sty_last_error": (C.c_char_p, []),
     "sty_launch_count": (C.c_uint64, []),
+    "sty_device_status": (C.c_int32, [C.POINTER(C.c_uint32), C.c_int32]),
     "sty_style_apply": (C.c_int32, [C.POINTER(StyleProgram), C.c_uint32, _VP, _VP, C.c_uint64, _VP]),
     "sty_pf_screen_filter_depth": (C.c_int32, [C.POINTER(PfRecords), C.c_uint32, C.POINTER(PfScreenParams),
                                                C.POINTER(StyleProgram), _VP, _VP, _VP, _VP]),

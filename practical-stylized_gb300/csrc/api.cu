@@ -57,6 +57,21 @@ bool style_program_valid(const sty_style_program *p) {
     return true;
 }
 
+// Device status word: one per device (a __device__ variable exists once per device context).
+static __device__ uint32_t g_device_status = 0;
+
+uint32_t *device_status_ptr() {
+    static uint32_t *cache[64] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!cache[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
+        cache[dev] = static_cast<uint32_t *>(p);
+    }
+    return cache[dev];
+}
+
 // ---- kernels ------------------------------------------------------------------------------
 __global__ void k_style_apply(sty_style_program prog, uint32_t depth, const float *in, float *out,
                               uint64_t n) {
@@ -157,6 +172,17 @@ const char *sty_status_string(sty_status s) {
 const char *sty_last_error(void) { return g_last_error; }
 
 uint64_t sty_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+sty_status sty_device_status(uint32_t *status_out, int32_t clear) {
+    clear_error();
+    STY_ARG_CHECK(status_out, "sty_device_status: null status_out");
+    STY_TRY(check_cuda(cudaMemcpyFromSymbol(status_out, g_device_status, sizeof(uint32_t)), "read device status"));
+    if (clear) {
+        const uint32_t zero = 0;
+        STY_TRY(check_cuda(cudaMemcpyToSymbol(g_device_status, &zero, sizeof(uint32_t)), "clear device status"));
+    }
+    return STY_OK;
+}
 
 sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
                            float *rgb_out, uint64_t n, void *stream) {

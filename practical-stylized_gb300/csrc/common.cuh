@@ -19,6 +19,9 @@ void clear_error();
 // Counts kernel launches issued by this library.
 void count_launch(uint64_t n = 1);
 
+// Device status word of the current device (bits STY_DEV_*); kernels OR failure bits into it.
+uint32_t *device_status_ptr();
+
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // Checks the launch that was just issued; returns STY_ERR_CUDA with the CUDA message on failure.

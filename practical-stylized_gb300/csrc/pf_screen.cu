@@ -13,6 +13,7 @@
 // FP32 across one candidate row (at most (2R+1) * S terms) and are then folded into
 // Kahan-compensated totals.
 #include "common.cuh"
+#include "pf_screen.cuh"
 #include "style.cuh"
 
 namespace sty {
@@ -26,21 +27,6 @@ constexpr int NF = 9;  // staged fields: p'xyz, nxyz, in rgb
 constexpr float kL2E = 1.4426950408889634f;
 constexpr float kFar = 1e18f;  // staged position of an excluded candidate
 
-struct ScreenArgs {
-    const float *pos[3];
-    const float *nrm[3];
-    const float *rad[3];
-    const float *thr[3];
-    const int32_t *valid;
-    const float *out_next;
-    float *out;
-    float *filtered;
-    int32_t W, H, R;
-    uint32_t depth;
-    float pscale;   // sqrt(log2 e / (2 sigma_pos^2))
-    float nscale;   // log2 e / sigma_nrm^2
-    float pix2;     // log2 e / (2 sigma_pixel^2), 0 if disabled
-};
 
 template <int S>
 struct Vec;
@@ -77,7 +63,7 @@ struct Vec<8> {
 };
 
 template <int S>
-__global__ void __launch_bounds__(NT, 2) k_pf_screen(const ScreenArgs a, const sty_style_program style) {
+__global__ void __launch_bounds__(NT, S >= 8 ? 1 : 2) k_pf_screen(const ScreenArgs a, const sty_style_program style) {
     extern __shared__ __align__(16) float sm[];
     const int R = a.R;
     const int CW = TW + 2 * R;            // staged columns
@@ -229,12 +215,8 @@ template <int S>
 sty_status launch_screen(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st) {
     const int CW = TW + 2 * a.R;
     const size_t smem = (size_t)NF * CH * CW * S * sizeof(float);
-    static bool attr_set = false;  // per template instance; idempotent if raced
-    if (!attr_set) {
-        STY_TRY(check_cuda(cudaFuncSetAttribute(k_pf_screen<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024),
-                           "cudaFuncSetAttribute(k_pf_screen)"));
-        attr_set = true;
-    }
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_pf_screen<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "cudaFuncSetAttribute(k_pf_screen)"));
     dim3 grid((a.W + TW - 1) / TW, (a.H + TH - 1) / TH);
     k_pf_screen<S><<<grid, NT, smem, st>>>(a, style);
     return check_launch("k_pf_screen");
@@ -293,11 +275,14 @@ sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth,
     a.pscale = sqrtf(kL2E / (2.0f * params->sigma_pos * params->sigma_pos));
     a.nscale = kL2E / (params->sigma_nrm * params->sigma_nrm);
     a.pix2 = params->sigma_pixel > 0.0f ? kL2E / (2.0f * params->sigma_pixel * params->sigma_pixel) : 0.0f;
+    a.status = device_status_ptr();
+    STY_ARG_CHECK(a.status, "device status word unavailable (no CUDA device?)");
     cudaStream_t st = as_stream(stream);
     switch (rec->spp) {
         case 1: return launch_screen<1>(a, prog, st);
         case 2: return launch_screen<2>(a, prog, st);
-        case 4: return launch_screen<4>(a, prog, st);
+        case 4:  // the warp-specialised kernel's shared-memory ring fits up to radius 24
+            return a.R <= 24 ? launch_screen_s4(a, prog, st) : launch_screen<4>(a, prog, st);
         default: return launch_screen<8>(a, prog, st);
     }
 }

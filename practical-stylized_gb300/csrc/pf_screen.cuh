@@ -1,0 +1,28 @@
+// pf_screen.cuh -- arguments shared by the screen-space NL-PF kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace sty {
+
+struct ScreenArgs {
+    const float *pos[3];
+    const float *nrm[3];
+    const float *rad[3];
+    const float *thr[3];
+    const int32_t *valid;
+    const float *out_next;
+    float *out;
+    float *filtered;
+    int32_t W, H, R;
+    uint32_t depth;
+    float pscale;  // sqrt(log2 e / (2 sigma_pos^2))
+    float nscale;  // log2 e / sigma_nrm^2
+    float pix2;    // log2 e / (2 sigma_pixel^2), 0 if disabled
+    uint32_t *status;  // device status word (STY_DEV_* bits)
+};
+
+// Warp-specialised spp=4 kernel (pf_screen4.cu).
+sty_status launch_screen_s4(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st);
+
+}  // namespace sty

@@ -38,7 +38,7 @@ def _depth_parity(sty, orc, rs, hrec, valid, d, prm, style, out_next_dev=None):
 
 
 @pytest.mark.parametrize("S", [1, 2, 4, 8])
-@pytest.mark.parametrize("R", [0, 3, 16])
+@pytest.mark.parametrize("R", [0, 3, 16, 24, 30])
 def test_filter_depth_matches_oracle(sty, orc, cuda, S, R):
     W, H, D = 70, 37, 1  # not multiples of the 32x8 tile
     planes, valid, rs, hrec = _setup(sty, W, H, S, D, seed=S * 100 + R)
@@ -74,6 +74,35 @@ def test_full_chain_c2_style(sty, orc, cuda):
         keep = m & ~near
         assert near.sum() <= max(3, n // 1000)
         assert rel_err(got_o[:, keep], ref_o[:, keep], 1e-6).max() < TOL
+
+
+@pytest.mark.parametrize("case", ["wide_spread", "step"])
+def test_direct_form_fallback_tiles(sty, orc, cuda, case):
+    """Tiles whose positions are spread too widely for the expanded exponent take the direct
+    form; both forms (and tiles of each kind side by side) must match the oracle."""
+    W, H, S, D = 96, 48, 4, 1
+    if case == "wide_spread":
+        planes, valid = sty.synth.records(W, H, S, D, seed=21, offset_scale=40.0)
+    else:
+        planes, valid = sty.synth.records(W, H, S, D, seed=22)
+        xs = (np.arange(W * H * S) // S) % W
+        planes[0, xs >= W // 2] += 50.0  # depth step in the middle of the image
+        planes[2, (xs % 7) == 3] -= 9.0  # scattered far records
+    rs = sty.RecordSet.from_numpy(planes, valid, W, H, S, D)
+    hrec = sty.pf.host_records(planes, valid, W, H, S, D)
+    prm = sty.ScreenParams(radius=16, sigma_pixel=8.0, sigma_pos=0.5, sigma_nrm=0.2)
+    _, got_o, ref_o, _, m, ef = _depth_parity(sty, orc, rs, hrec, valid, 0, prm, None)
+    assert ef < TOL, f"filtered rel err {ef:.3e}"
+    assert sty.abi.device_status() == 0
+
+
+def test_device_status_clean_after_runs(sty, cuda):
+    import torch
+    W, H, S, D = 64, 32, 4, 2
+    _, _, rs, _ = _setup(sty, W, H, S, D, seed=12)
+    sty.pf_screen_filter(rs, sty.c2_params(), sty.c2_style())
+    torch.cuda.synchronize()
+    assert sty.abi.device_status() == 0
 
 
 def test_deterministic(sty, cuda):
