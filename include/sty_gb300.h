@@ -51,6 +51,12 @@ typedef int32_t sty_status;
 #define STY_ERR_NAN 5         /* a non-finite value was detected where it is not allowed     */
 #define STY_ERR_UNSUPPORTED 6 /* the request is valid but not supported by this build/device */
 
+/* Pcg32 generator state (crates/akari_render/src/sampler/mod.rs:82-88). */
+typedef struct sty_pcg32 {
+    uint64_t state;
+    uint64_t inc;
+} sty_pcg32;
+
 /* Version of this ABI: major * 10000 + minor * 100 + patch. */
 STY_API int32_t sty_version(void);
 /* Static string naming a status code. */
@@ -176,13 +182,91 @@ STY_API sty_status sty_film_accumulate(const float *out0, int32_t width, int32_t
                                double weight, double *film, void *stream);
 
 /* ----------------------------------------------------------------------------------------
+ * Reference-mode NL-PF (world-space hash grid + SMIS), one path depth per call
+ *
+ * Restates lm_path_filtering.rs with a fixed evaluation order:
+ *   grid     HashGrid (:20-255): cell = clamp((p-pmin)/(pmax-pmin),0,1)*res, res = floor(extent/r),
+ *            bucket = hash(cell) mod table_size; the 27-cell walk (:61-123, dz outer, dx inner).
+ *            The reference's buckets are CAS-built linked lists (order = thread timing); here each
+ *            bucket lists its points in ascending path index.
+ *   cluster  kernel_init_cluster / kernel_cluster (:533-623, loop :1675-1710) with deterministic
+ *            claims: per round every unclustered vertex's bucket elects its lowest-index vertex as
+ *            a centre; every other unclustered vertex proposes to the first centre (walk order) within
+ *            r that had room at the start of the round; each centre accepts proposals in walk order
+ *            while it has room (cluster_size < reuse). Rounds repeat until every vertex is clustered.
+ *   filter   evaluate_filtered_radiance (:758-972): neighbours = active vertices within r of the query
+ *            point (own position, or the cluster centre's), same cluster, same flags; reservoir of
+ *            `reuse` slots fed by the path's Pcg32 (gen_u32 % (cnt+1)); direct term with balance MIS;
+ *            indirect term with SMIS (sum of the kept neighbours' BSDF pdfs) or 1/(pdf*k); then the
+ *            material's style program (skipped at depth 0 if no_first_hit_stylization, and when the
+ *            vertex's flags have bit 0 "stylization disabled" set).
+ * All per-vertex arrays below are device arrays of `n` elements indexed by path slot.
+ * -------------------------------------------------------------------------------------- */
+#define STY_MAT_DIFFUSE 0 /* Lambert: f = albedo/pi |cos|, pdf = |cos|/pi (diffuse.rs:17-48)       */
+#define STY_MAT_GGX 1     /* microfacet reflection, Trowbridge-Reitz alpha, unit Fresnel,                                        visible-normal pdf (mod.rs:1877-1910, microfacet.rs:44-206)           */
+
+typedef struct sty_pf_material {
+    int32_t kind;        /* STY_MAT_* */
+    float albedo[3];
+    float alpha;         /* GGX roughness alpha (>= 1e-4) */
+    int32_t style[4];    /* style program per style index 0..3 (flags bits 1..3), -1 = none */
+} sty_pf_material;
+
+typedef struct sty_pf_vertices {
+    const int32_t *active;      /* nonzero: the path has a vertex at this depth              */
+    const float *p[3];          /* hit position                                              */
+    const float *wo[3];         /* outgoing direction (towards the previous vertex)         */
+    const float *ns[3];         /* shading normal                                            */
+    const float *ng[3];         /* geometric normal                                          */
+    const float *le[3];         /* emitted radiance at the vertex                            */
+    const float *mis;           /* MIS weight of the emission (1 if not an emitter)          */
+    const float *dir_wi[3];     /* NEE record: direction, stylised irradiance, light pdf     */
+    const float *dir_l[3];
+    const float *dir_pdf;       /*   (0 = no record)                                         */
+    const float *ind_wi[3];     /* direction to the next vertex (-wo of it); 0 = no record   */
+    const float *ind_mis;       /* that vertex's emission MIS weight (record.mis)            */
+    const uint32_t *flags;      /* new_flags: bit0 disabled, bits1..3 use_style_2..4          */
+    const uint32_t *material;   /* index into the material table                             */
+    uint64_t n;
+} sty_pf_vertices;
+
+typedef struct sty_pf_ref_params {
+    uint32_t depth;
+    float radius;               /* world-space filter radius                                 */
+    uint32_t reuse;             /* reservoir size (reuse[d])                                 */
+    int32_t smis;
+    int32_t cluster;
+    int32_t disable_flag_check;
+    int32_t no_first_hit_stylization;
+    uint32_t table_size;        /* hash table size (the reference uses 2^26)                 */
+    float pmin[3], pmax[3];     /* grid bounds (scene AABB or config scene_bounds)           */
+    uint32_t max_cluster_rounds;/* cap on clustering rounds (STY_ERR_ITER_LIMIT beyond)      */
+} sty_pf_ref_params;
+
+typedef struct sty_pf_ref_ctx sty_pf_ref_ctx;
+
+/* Create / destroy a reference-mode context owning the scratch for up to `max_vertices` path
+ * slots (grid keys, sorted point lists, bucket ranges for `table_size` buckets, cluster state). */
+STY_API sty_status sty_pf_ref_create(uint64_t max_vertices, uint32_t table_size, sty_pf_ref_ctx **out);
+STY_API sty_status sty_pf_ref_destroy(sty_pf_ref_ctx *ctx);
+
+/* One depth of the reference-mode filter. `in_next` (device, 3 planes of n floats) is the
+ * styled result of the next depth for the same path slots (the record kernel_propagate copies,
+ * :974-998; its pdf field is never read by the filter), NULL at the deepest depth. `rng` (device,
+ * n Pcg32 states) is advanced by the reservoir draws.
+ * `materials` (<= 256) and `programs` (<= 64) are HOST arrays, copied on the stream per call.
+ * Outputs: `out` (device, 3 planes of n) = styled filtered radiance (0 for inactive slots);
+ * optional `neighbours` (device, n) = neighbour count before the reservoir cap, `cluster_id`
+ * (device, n; written only when params->cluster) = cluster centre slot (UINT32_MAX inactive). */
+STY_API sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, const float *in_next, const sty_pf_ref_params *params,
+                                     const sty_pf_material *materials, uint32_t n_materials,
+                                     const sty_style_program *programs, uint32_t n_programs,
+                                     sty_pcg32 *rng, float *out, uint32_t *neighbours,
+                                     uint32_t *cluster_id, void *stream);
+
+/* ----------------------------------------------------------------------------------------
  * Integer helpers (bit-exact with the reference)
  * -------------------------------------------------------------------------------------- */
-typedef struct sty_pcg32 {
-    uint64_t state;
-    uint64_t inc;
-} sty_pcg32;
-
 /* Pcg32::new_seq_offset (sampler/mod.rs:94-100) for seq = first_seq + i, seed = seeds[i]
  * (device arrays of n), then `draws` calls of gen_u32 per stream written to out (device,
  * n * draws, stream-major) and the final states to states (device, n). */

@@ -32,6 +32,8 @@ def lib() -> C.CDLL:
         L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
         L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
         L.orc_hash_cells.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, vp, vp]
+        L.orc_pf_ref_filter.restype = C.c_int32
+        L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -88,6 +90,28 @@ def hash_cells(points: np.ndarray, pmin, pmax, res, table_size: int):
     idx = np.zeros(pts.shape[0], dtype=np.uint32)
     lib().orc_hash_cells(_p(pts), pts.shape[0], _p(pmin), _p(pmax), _p(res), table_size, _p(cells), _p(idx))
     return cells, idx
+
+
+def pf_ref_filter(arrays: dict, params_c, mats, progs, n_progs: int, rng_states: np.ndarray, in_next=None):
+    """Reference-mode filter of one depth on host arrays (dict from synth.ref_vertices).
+    Returns (status, out [3, n] float64, neighbours [n], cluster_id [n], rng_states_after)."""
+    import importlib
+    pfr = importlib.import_module(__package_name__() + ".pf_ref")
+    n = int(arrays["active"].shape[0])
+    v = pfr.vertices_struct(arrays, ptr=lambda a: a.ctypes.data)
+    out = np.zeros((3, n), dtype=np.float64)
+    nb = np.zeros(n, dtype=np.uint32)
+    cid = np.zeros(n, dtype=np.uint32)
+    st = np.ascontiguousarray(rng_states.copy())
+    nxt = None if in_next is None else np.ascontiguousarray(in_next, dtype=np.float32)
+    status = lib().orc_pf_ref_filter(C.addressof(v), _p(nxt), C.addressof(params_c), C.addressof(mats), len(mats),
+                                     C.addressof(progs) if progs is not None else None, n_progs, _p(st), _p(out),
+                                     _p(nb), _p(cid))
+    return status, out, nb, cid, st
+
+
+def __package_name__() -> str:
+    return "practical_stylized_gb300"
 
 
 def num_threads() -> int:

@@ -22,7 +22,8 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
         t = LIB.stat().st_mtime
         if all(p.stat().st_mtime <= t for p in [*SRCS, *HDRS]):
             return LIB
-    base = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", str(LIB), *map(str, SRCS)]
+    # no FMA contraction: the geometric tests restate the reference's separate f32 mul/add
+    base = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(LIB), *map(str, SRCS)]
     for extra in (["-fopenmp"], []):
         cmd = base[:1] + extra + base[1:]
         if verbose:

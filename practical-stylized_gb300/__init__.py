@@ -22,5 +22,6 @@ from .pf import (  # noqa: F401
     c2_params, c2_style,
 )
 from . import synth  # noqa: F401
+from . import pf_ref  # noqa: F401
 
 PKG_DIR = pathlib.Path(__file__).resolve().parent

@@ -70,3 +70,56 @@ def records(width: int, height: int, spp: int, depths: int, seed: int = 0, *,
             planes[9 + k, sl] = thr[:, k]
         valid[sl] = val
     return planes, valid
+
+
+REF_FIELDS = ("p", "wo", "ns", "ng", "le", "dir_wi", "dir_l", "ind_wi")  # float3 fields
+REF_SCALARS = ("mis", "dir_pdf", "ind_mis")
+
+
+def _hemisphere(n_dir: np.ndarray, rng: np.random.Generator) -> np.ndarray:
+    """Cosine-ish random unit directions in the hemisphere around unit vectors n_dir."""
+    v = rng.normal(size=n_dir.shape)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    v = np.where((v * n_dir).sum(1, keepdims=True) < 0, -v, v)
+    v = v + 0.3 * n_dir
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def ref_vertices(n: int, seed: int = 0, *, p_active: float = 0.9, n_materials: int = 3, p_flags: float = 0.1,
+                 p_direct: float = 0.7, p_indirect: float = 0.8, p_emit: float = 0.05):
+    """Synthetic path vertices of one depth for the reference-mode filter: points on 4 planes of a
+    unit room ([-1,1]^3), shading normal = geometric normal tilted slightly, outgoing and NEE /
+    continuation directions in the upper hemisphere, 'n_materials' material ids, a few emitters
+    and a few vertices with non-zero stylization flags. Returns a dict of numpy arrays
+    (float3 fields as [3, n] float32)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    plane = rng.integers(0, 4, n)
+    axes = np.array([1, 1, 0, 2])
+    sides = np.array([-1.0, 1.0, -1.0, 1.0])
+    p = rng.uniform(-1.0, 1.0, size=(n, 3))
+    p[np.arange(n), axes[plane]] = sides[plane]
+    ng = np.zeros((n, 3))
+    ng[np.arange(n), axes[plane]] = -sides[plane]  # pointing into the room
+    ns = ng + 0.05 * rng.normal(size=(n, 3))
+    ns /= np.linalg.norm(ns, axis=1, keepdims=True)
+    wo = _hemisphere(ng, rng)
+    dir_wi = _hemisphere(ng, rng)
+    ind_wi = _hemisphere(ng, rng)
+    has_dir = rng.random(n) < p_direct
+    has_ind = rng.random(n) < p_indirect
+    out = {
+        "active": (rng.random(n) < p_active).astype(np.int32),
+        "p": p.T.astype(np.float32), "wo": wo.T.astype(np.float32),
+        "ns": ns.T.astype(np.float32), "ng": ng.T.astype(np.float32),
+        "le": (np.where(rng.random((n, 1)) < p_emit, 5.0, 0.0) * rng.random((n, 3))).T.astype(np.float32),
+        "mis": np.where(rng.random(n) < 0.3, rng.uniform(0.2, 1.0, n), 1.0).astype(np.float32),
+        "dir_wi": (dir_wi * has_dir[:, None]).T.astype(np.float32),
+        "dir_l": rng.lognormal(-1.0, 1.0, size=(3, n)).astype(np.float32),
+        "dir_pdf": np.where(has_dir, rng.uniform(0.1, 3.0, n), 0.0).astype(np.float32),
+        "ind_wi": (ind_wi * has_ind[:, None]).T.astype(np.float32),
+        "ind_mis": np.where(rng.random(n) < 0.2, rng.uniform(0.1, 1.0, n), 1.0).astype(np.float32),
+        "flags": np.where(rng.random(n) < p_flags, rng.integers(0, 16, n), 0).astype(np.uint32),
+        "material": rng.integers(0, n_materials, n).astype(np.uint32),
+        "in_next": rng.lognormal(-1.5, 1.0, size=(3, n)).astype(np.float32),
+    }
+    return {k: np.ascontiguousarray(v) for k, v in out.items()}
