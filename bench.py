@@ -32,9 +32,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "NL-PF Mpath-vertices/s; NL-NRC BF16 vs FP32 Msamples/s at equal image MSE"
 W_, H_, S_, D_ = 1920, 1080, 4, 5
 WORKLOAD = "NL-PF screen-space filter, synthetic records 1920x1080 x 4 spp x 5 depths, radius 16 px"
-# HBM traffic (dram read + write) of one k_pf_screen launch at this size, from the ncu capture
-# summarised in profiles/k_pf_screen_1080p.md (None until captured)
-NCU_TRAFFIC_PER_LAUNCH = None
+# HBM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one k_pf_screen4 launch at this
+# size (1080p x 4 spp, child input present), from the ncu capture summarised in
+# profiles/k_pf_screen_1080p_x4spp.md
+NCU_TRAFFIC_PER_LAUNCH = 535.2e6 + 90.8e6
 
 
 def _rank_env():
@@ -290,7 +291,7 @@ def run(args):
                 "h2d_bytes_per_step": int(planes.nbytes + valid.nbytes), "d2h_bytes_per_step": int(3 * n * 4)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": NCU_TRAFFIC_PER_LAUNCH,
-                     "kernel": "k_pf_screen", "peak_source": peak_kind,
+                     "kernel": "k_pf_screen4", "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
         "alu_roofline": {"bound": "fp32", "achieved": alu_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": alu_achieved / fp32_peak, "pairs_per_launch": pairs_launch,
