@@ -265,6 +265,68 @@ STY_API sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices 
                                      uint32_t *cluster_id, void *stream);
 
 /* ----------------------------------------------------------------------------------------
+ * Neural radiance cache (NL-NRC): one-to-one with the reference's tiny-cuda-nn wrapper
+ * (crates/akari_cpp_ext/cpp_ext/akari_nrc.h:1-17, akari_tcnn.cu:84-292).
+ *
+ * Network: frequency encoding of `input_dims` raw inputs (dim d gets freqs[d] pairs
+ * sin(2^k pi x), cos(2^k pi x), k < freqs[d]; sum 2*freqs = 64), then `hidden_layers` ReLU layers
+ * of width 64 and a linear output layer of `output_dims` (<= 16); no biases. Weights are FP32
+ * masters; precision STY_NRC_BF16 runs the MLP on the tcgen05 tensor cores (BF16 operands, FP32
+ * accumulation in TMEM), STY_NRC_FP32 runs it in FP32 on the CUDA cores.
+ * Loss: relative L2, (pred - target)^2 / (pred^2 + 0.01) with pred treated as constant in the
+ * denominator, averaged over the batch and channels. Optimiser: Adam (beta1, beta2, eps) with
+ * learning rate lr * decay_base^(step / decay_interval) (tcnn ExponentialDecay, nrc_pt.rs:1199-1216);
+ * inference uses EMA weights with the debiased update of akari_tcnn.cu:42-83.
+ * Matrices are sample-major: input[i * input_dims + d], output[i * output_dims + c] (tcnn's
+ * column-major [dims x count]). All pointers are device pointers unless stated.
+ * -------------------------------------------------------------------------------------- */
+#define STY_NRC_FP32 0
+#define STY_NRC_BF16 1
+#define STY_NRC_MAX_INPUTS 16
+
+typedef struct sty_nrc_config {
+    uint32_t input_dims;     /* raw input dims (<= 16) */
+    uint32_t output_dims;    /* <= 16 */
+    uint32_t batch_size;     /* training samples per step, multiple of 128 */
+    uint32_t hidden_layers;  /* >= 1 (width fixed at 64) */
+    uint32_t precision;      /* STY_NRC_FP32 or STY_NRC_BF16 */
+    uint32_t freqs[STY_NRC_MAX_INPUTS];
+    float learning_rate, beta1, beta2, epsilon;
+    float ema_decay;
+    float decay_base;
+    uint32_t decay_interval;
+    uint64_t seed;
+} sty_nrc_config;
+
+typedef struct sty_nrc sty_nrc;
+
+STY_API sty_status sty_nrc_create(const sty_nrc_config *config, sty_nrc **out);       /* akr_create_nrc */
+STY_API sty_status sty_nrc_destroy(sty_nrc *nrc);                                      /* akr_destroy_nrc */
+STY_API sty_status sty_nrc_param_count(sty_nrc *nrc, uint64_t *count);                 /* akr_nrc_param_count */
+/* FP32 master weights to / from a HOST array of param_count floats (akr_nrc_save/load_params);
+ * loading also resets the EMA copy to the loaded weights. Synchronous. */
+STY_API sty_status sty_nrc_save_params(sty_nrc *nrc, float *host_params);
+STY_API sty_status sty_nrc_load_params(sty_nrc *nrc, const float *host_params);
+STY_API sty_status sty_nrc_set_learning_rate(sty_nrc *nrc, float lr);                  /* akr_nrc_set_learning_rate */
+STY_API sty_status sty_nrc_get_learning_rate(sty_nrc *nrc, float *lr);                 /* akr_nrc_get_learning_rate */
+STY_API sty_status sty_nrc_reset_optimizer(sty_nrc *nrc);                              /* akr_nrc_reset_optimizer */
+/* Inference with the EMA weights (akr_nrc_inference) / the training weights
+ * (akr_nrc_train_inference). Asynchronous on `stream`. */
+STY_API sty_status sty_nrc_inference(sty_nrc *nrc, uint64_t count, const float *input, float *output, void *stream);
+STY_API sty_status sty_nrc_train_inference(sty_nrc *nrc, uint64_t count, const float *input, float *output,
+                                           void *stream);
+/* n_iters training steps, each on batch_size samples drawn uniformly (Pcg32) from the `count`
+ * rows of input/target (akr_nrc_train / collect_batch, akari_tcnn.cu:15-38,136-168). If loss_out is
+ * non-NULL it receives the mean loss over the steps (synchronises the stream). */
+STY_API sty_status sty_nrc_train(sty_nrc *nrc, uint64_t count, uint64_t n_iters, const float *input,
+                                 const float *target, float *loss_out, void *stream);
+/* Gradient of the batch loss w.r.t. the FP32 master weights for an explicit batch (rows
+ * input[0..batch), no sampling, no optimiser step): `grad` (device, param_count floats). Used to
+ * check the backward pass. */
+STY_API sty_status sty_nrc_gradient(sty_nrc *nrc, uint32_t batch, const float *input, const float *target,
+                                    float *grad, float *loss_out, void *stream);
+
+/* ----------------------------------------------------------------------------------------
  * Integer helpers (bit-exact with the reference)
  * -------------------------------------------------------------------------------------- */
 /* Pcg32::new_seq_offset (sampler/mod.rs:94-100) for seq = first_seq + i, seed = seeds[i]

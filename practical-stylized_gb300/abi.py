@@ -101,6 +101,18 @@ SIGNATURES = {
     "sty_pf_ref_destroy": (C.c_int32, [C.c_void_p]),
     "sty_pf_ref_filter": (C.c_int32, [C.c_void_p, _VP, _VP, _VP, _VP, C.c_uint32, _VP, C.c_uint32, _VP, _VP,
                                       _VP, _VP, _VP]),
+    "sty_nrc_create": (C.c_int32, [_VP, C.POINTER(C.c_void_p)]),
+    "sty_nrc_destroy": (C.c_int32, [C.c_void_p]),
+    "sty_nrc_param_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),
+    "sty_nrc_save_params": (C.c_int32, [C.c_void_p, _VP]),
+    "sty_nrc_load_params": (C.c_int32, [C.c_void_p, _VP]),
+    "sty_nrc_set_learning_rate": (C.c_int32, [C.c_void_p, C.c_float]),
+    "sty_nrc_get_learning_rate": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
+    "sty_nrc_reset_optimizer": (C.c_int32, [C.c_void_p]),
+    "sty_nrc_inference": (C.c_int32, [C.c_void_p, C.c_uint64, _VP, _VP, _VP]),
+    "sty_nrc_train_inference": (C.c_int32, [C.c_void_p, C.c_uint64, _VP, _VP, _VP]),
+    "sty_nrc_train": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint64, _VP, _VP, C.POINTER(C.c_float), _VP]),
+    "sty_nrc_gradient": (C.c_int32, [C.c_void_p, C.c_uint32, _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
     "sty_pcg32_streams": (C.c_int32, [_VP, C.c_uint64, C.c_uint64, C.c_uint32, _VP, _VP, _VP]),
     "sty_hash_cells": (C.c_int32, [_VP, C.c_uint64, C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
                                    C.POINTER(C.c_uint32 * 3), C.c_uint32, _VP, _VP, _VP]),

@@ -1,0 +1,509 @@
+// nrc.cu -- neural radiance cache: host object, FP32 CUDA-core path, loss, Adam / EMA, sampling.
+//
+// The object mirrors `struct NRC` of crates/akari_cpp_ext/cpp_ext/akari_tcnn.cu:84-248: it owns the
+// weights, the optimiser state and its scratch; the caller owns the input / output / target
+// matrices. Unlike the reference, no call synchronises the device unless documented.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "nrc.cuh"
+
+namespace sty {
+namespace {
+
+constexpr int W = kNrcWidth;
+
+// ---- FP32 forward: one thread per sample, all weights in shared memory ----------------------
+// acts (optional): [layers+1][count][64] post-activation rows (row 0 = encoded input).
+__global__ void __launch_bounds__(128) k_fwd_f32(NrcNet n, const float *__restrict__ wg, uint64_t count,
+                                                 const float *__restrict__ input, float *__restrict__ output,
+                                                 float *__restrict__ acts) {
+    extern __shared__ float ws[];
+    const size_t np = nrc_param_count(n);
+    for (size_t k = threadIdx.x; k < np; k += blockDim.x) ws[k] = wg[k];
+    __syncthreads();
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    float enc[W];
+    nrc_encode(n, input + i * n.in_dims, enc);
+    float h[W];
+#pragma unroll
+    for (int k = 0; k < W; k++) h[k] = enc[k];
+    if (acts)
+#pragma unroll
+        for (int k = 0; k < W; k += 4)
+            *reinterpret_cast<float4 *>(acts + i * W + k) = make_float4(h[k], h[k + 1], h[k + 2], h[k + 3]);
+#pragma unroll 1
+    for (int l = 0; l < n.layers; l++) {
+        const float *wl = ws + nrc_w_offset(l);
+        float z[W];
+#pragma unroll
+        for (int j = 0; j < W; j++) {
+            float a = 0.0f;
+#pragma unroll
+            for (int k = 0; k < W; k += 4) {
+                const float4 w4 = *reinterpret_cast<const float4 *>(wl + j * W + k);
+                a = fmaf(w4.x, h[k], a);
+                a = fmaf(w4.y, h[k + 1], a);
+                a = fmaf(w4.z, h[k + 2], a);
+                a = fmaf(w4.w, h[k + 3], a);
+            }
+            z[j] = a;
+        }
+#pragma unroll
+        for (int j = 0; j < W; j++) h[j] = fmaxf(z[j], 0.0f);
+        if (acts) {
+            float *dst = acts + ((size_t)(l + 1) * count + i) * W;
+#pragma unroll
+            for (int k = 0; k < W; k += 4)
+                *reinterpret_cast<float4 *>(dst + k) = make_float4(h[k], h[k + 1], h[k + 2], h[k + 3]);
+        }
+    }
+    const float *wo = ws + nrc_w_offset(n.layers);
+    for (int c = 0; c < n.out_dims; c++) {
+        float a = 0.0f;
+#pragma unroll
+        for (int k = 0; k < W; k++) a = fmaf(wo[c * W + k], h[k], a);
+        output[i * n.out_dims + c] = a;
+    }
+}
+
+// ---- loss gradient + FP32 backward: one thread per sample -----------------------------------
+// dpre: [layers+1][B][64]: row l < layers = dL/d(pre-activation of hidden layer l),
+// row `layers` = dL/d(output) (first out_dims entries).
+__global__ void __launch_bounds__(128) k_bwd_f32(NrcNet n, const float *__restrict__ wg, uint32_t B,
+                                                 const float *__restrict__ pred, const float *__restrict__ target,
+                                                 const float *__restrict__ acts, float *__restrict__ dpre,
+                                                 float *__restrict__ loss_acc) {
+    extern __shared__ float ws[];
+    __shared__ float red[4];
+    const size_t np = nrc_param_count(n);
+    for (size_t k = threadIdx.x; k < np; k += blockDim.x) ws[k] = wg[k];
+    __syncthreads();
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float lsum = 0.0f;
+    if (i < B) {
+        const float norm = 1.0f / ((float)B * (float)n.out_dims);
+        float g[kNrcOutPad];
+        for (int c = 0; c < n.out_dims; c++) {
+            const float p = pred[(size_t)i * n.out_dims + c], t = target[(size_t)i * n.out_dims + c];
+            const float den = p * p + 0.01f;  // relative L2, prediction treated as constant below
+            lsum += (p - t) * (p - t) / den;
+            g[c] = 2.0f * (p - t) / den * norm;
+            dpre[((size_t)n.layers * B + i) * W + c] = g[c];
+        }
+        // dH = W_out^T g
+        float dh[W];
+        const float *wo = ws + nrc_w_offset(n.layers);
+#pragma unroll
+        for (int k = 0; k < W; k++) dh[k] = 0.0f;
+        for (int c = 0; c < n.out_dims; c++)
+#pragma unroll
+            for (int k = 0; k < W; k++) dh[k] = fmaf(wo[c * W + k], g[c], dh[k]);
+#pragma unroll 1
+        for (int l = n.layers - 1; l >= 0; l--) {
+            const float *hl = acts + ((size_t)(l + 1) * B + i) * W;  // post-activation of layer l
+            float dp[W];
+#pragma unroll
+            for (int k = 0; k < W; k += 4) {
+                const float4 h4 = *reinterpret_cast<const float4 *>(hl + k);
+                dp[k] = h4.x > 0.0f ? dh[k] : 0.0f;
+                dp[k + 1] = h4.y > 0.0f ? dh[k + 1] : 0.0f;
+                dp[k + 2] = h4.z > 0.0f ? dh[k + 2] : 0.0f;
+                dp[k + 3] = h4.w > 0.0f ? dh[k + 3] : 0.0f;
+            }
+            float *dst = dpre + ((size_t)l * B + i) * W;
+#pragma unroll
+            for (int k = 0; k < W; k += 4) *reinterpret_cast<float4 *>(dst + k) = make_float4(dp[k], dp[k + 1], dp[k + 2], dp[k + 3]);
+            if (l == 0) break;
+            const float *wl = ws + nrc_w_offset(l);
+#pragma unroll
+            for (int k = 0; k < W; k++) dh[k] = 0.0f;
+#pragma unroll
+            for (int j = 0; j < W; j++) {
+                const float dj = dp[j];
+#pragma unroll
+                for (int k = 0; k < W; k += 4) {
+                    const float4 w4 = *reinterpret_cast<const float4 *>(wl + j * W + k);
+                    dh[k] = fmaf(w4.x, dj, dh[k]);
+                    dh[k + 1] = fmaf(w4.y, dj, dh[k + 1]);
+                    dh[k + 2] = fmaf(w4.z, dj, dh[k + 2]);
+                    dh[k + 3] = fmaf(w4.w, dj, dh[k + 3]);
+                }
+            }
+        }
+    }
+    // block-reduce the loss
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = lsum;
+    __syncthreads();
+    if (threadIdx.x == 0 && loss_acc) {
+        float t = 0.0f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        atomicAdd(loss_acc, t / ((float)B * (float)n.out_dims));
+    }
+}
+
+// ---- weight gradient: grad_l[j][k] = sum_i dpre_l[i][j] * acts_l[i][k] ----------------------
+// grid: (chunks, layers+1); 256 threads; rows R = 64 (hidden) or out_dims (output layer).
+constexpr int kWgChunk = 1024;
+__global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const float *__restrict__ acts,
+                                                   const float *__restrict__ dpre, float *__restrict__ grad) {
+    __shared__ float sd[64][W + 1];
+    __shared__ float sh[64][W + 1];
+    const int l = blockIdx.y;
+    const int rows = l < n.layers ? W : n.out_dims;
+    const uint32_t i0 = blockIdx.x * kWgChunk, i1 = min(B, i0 + kWgChunk);
+    const int j = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 16;
+    float acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; c++) acc[c] = 0.0f;
+    const float *dl = dpre + (size_t)l * B * W;
+    const float *al = acts + (size_t)l * B * W;  // input of weight matrix l = post-activation row l
+    for (uint32_t s0 = i0; s0 < i1; s0 += 64) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 64 * W; e += 256) {
+            const int r = e / W, c = e % W;
+            const uint32_t s = s0 + r;
+            sd[r][c] = s < i1 ? dl[(size_t)s * W + c] : 0.0f;
+            sh[r][c] = s < i1 ? al[(size_t)s * W + c] : 0.0f;
+        }
+        __syncthreads();
+        if (j < rows) {
+            for (int r = 0; r < 64; r++) {
+                const float a = sd[r][j];
+#pragma unroll
+                for (int c = 0; c < 16; c++) acc[c] = fmaf(a, sh[r][k0 + c], acc[c]);
+            }
+        }
+    }
+    if (j < rows) {
+        float *g = grad + nrc_w_offset(l) + (size_t)j * W + k0;
+#pragma unroll
+        for (int c = 0; c < 16; c++) atomicAdd(g + c, acc[c]);
+    }
+}
+
+// ---- batch sampling (collect_batch, akari_tcnn.cu:15-38) -------------------------------------
+__device__ __forceinline__ uint32_t pcg_step(uint64_t &state, uint64_t inc) {
+    const uint64_t old = state;
+    state = old * 0x5851f42d4c957f2dULL + inc;
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    const uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+}
+__global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t count, int in_dims, int out_dims,
+                          const float *in, const float *tg, float *bin, float *btg) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    uint64_t st = 0, inc = ((step * (uint64_t)B + b) << 1) | 1ull;
+    pcg_step(st, inc);
+    st += seed;
+    pcg_step(st, inc);
+    const uint64_t r = ((uint64_t)pcg_step(st, inc) << 32) | pcg_step(st, inc);
+    const uint64_t idx = r % count;
+    for (int d = 0; d < in_dims; d++) bin[(size_t)b * in_dims + d] = in[idx * in_dims + d];
+    for (int c = 0; c < out_dims; c++) btg[(size_t)b * out_dims + c] = tg[idx * out_dims + c];
+}
+
+// ---- Adam + EMA (akari_tcnn.cu:42-83 for the EMA) --------------------------------------------
+__global__ void k_adam(size_t np, float *w, float *m, float *v, const float *g, float *ema, float lr, float b1,
+                       float b2, float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new) {
+    const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const float gr = g[p];
+    const float mm = b1 * m[p] + (1.0f - b1) * gr;
+    const float vv = b2 * v[p] + (1.0f - b2) * gr * gr;
+    m[p] = mm;
+    v[p] = vv;
+    const float wn = w[p] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+    w[p] = wn;
+    ema[p] = (ema[p] * ema_decay * ema_old + wn * (1.0f - ema_decay)) * ema_new;
+}
+
+__global__ void k_init_weights(size_t np, NrcNet n, uint64_t seed, float *w) {
+    const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    uint64_t st = 0, inc = ((uint64_t)p << 1) | 1ull;
+    pcg_step(st, inc);
+    st += seed;
+    pcg_step(st, inc);
+    const float u = (float)pcg_step(st, inc) * (1.0f / 4294967296.0f);
+    const size_t hid = (size_t)n.layers * W * W;
+    const float fan_out = p < hid ? (float)W : (float)n.out_dims;
+    const float s = sqrtf(6.0f / ((float)W + fan_out));  // uniform Xavier
+    w[p] = (2.0f * u - 1.0f) * s;
+}
+
+}  // namespace
+}  // namespace sty
+
+using namespace sty;
+
+struct sty_nrc {
+    sty_nrc_config cfg;
+    NrcNet net;
+    size_t np = 0;
+    float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr, *ema = nullptr;
+    uint16_t *img = nullptr, *img_ema = nullptr;  // BF16 tensor-core images of w / ema
+    float *bin = nullptr, *btg = nullptr, *bpred = nullptr, *acts = nullptr, *dpre = nullptr, *loss = nullptr;
+    uint32_t bcap = 0;
+    uint64_t step = 0;  // optimiser steps taken (Adam t, EMA iteration)
+    float lr = 0.0f;
+    bool img_dirty = true;
+};
+
+namespace {
+
+sty_status ensure_batch(sty_nrc *nr, uint32_t B) {
+    if (B <= nr->bcap) return STY_OK;
+    void *ptrs[] = {nr->bin, nr->btg, nr->bpred, nr->acts, nr->dpre};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    nr->bin = nr->btg = nr->bpred = nr->acts = nr->dpre = nullptr;
+    const NrcNet &n = nr->net;
+    STY_TRY(check_cuda(cudaMalloc(&nr->bin, (size_t)B * n.in_dims * 4), "alloc batch input"));
+    STY_TRY(check_cuda(cudaMalloc(&nr->btg, (size_t)B * n.out_dims * 4), "alloc batch target"));
+    STY_TRY(check_cuda(cudaMalloc(&nr->bpred, (size_t)B * n.out_dims * 4), "alloc batch pred"));
+    STY_TRY(check_cuda(cudaMalloc(&nr->acts, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc activations"));
+    STY_TRY(check_cuda(cudaMalloc(&nr->dpre, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc gradients"));
+    nr->bcap = B;
+    return STY_OK;
+}
+
+size_t fwd_smem(const sty_nrc *nr) { return nr->np * sizeof(float); }
+
+sty_status fwd_f32(sty_nrc *nr, const float *wts, uint64_t count, const float *in, float *out, float *acts,
+                   cudaStream_t st) {
+    const size_t smem = fwd_smem(nr);
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "attr k_fwd_f32"));
+    k_fwd_f32<<<(unsigned)((count + 127) / 128), 128, smem, st>>>(nr->net, wts, count, in, out, acts);
+    return check_launch("k_fwd_f32");
+}
+
+// Loss gradient, backward and weight gradient for the batch already forwarded into nr->bpred /
+// nr->acts (FP32 CUDA-core path, also used for the BF16 path's weight update).
+sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t st) {
+    const NrcNet &n = nr->net;
+    const size_t smem = fwd_smem(nr);
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "attr k_bwd_f32"));
+    k_bwd_f32<<<(B + 127) / 128, 128, smem, st>>>(n, nr->w, B, nr->bpred, target, nr->acts, nr->dpre, nr->loss);
+    STY_TRY(check_launch("k_bwd_f32"));
+    STY_TRY(check_cuda(cudaMemsetAsync(nr->g, 0, nr->np * 4, st), "zero grad"));
+    dim3 grid((B + kWgChunk - 1) / kWgChunk, n.layers + 1);
+    k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->g);
+    return check_launch("k_wgrad_f32");
+}
+
+sty_status forward_batch(sty_nrc *nr, uint32_t B, const float *in, cudaStream_t st) {
+    // training forward (stores the activations the backward pass reads)
+    return fwd_f32(nr, nr->w, B, in, nr->bpred, nr->acts, st);
+}
+
+sty_status refresh_images(sty_nrc *nr, cudaStream_t st) {
+    if (nr->cfg.precision != STY_NRC_BF16 || !nr->img_dirty) return STY_OK;
+    STY_TRY(nrc_tc_pack(nr->net, nr->w, nr->img, st));
+    STY_TRY(nrc_tc_pack(nr->net, nr->ema, nr->img_ema, st));
+    nr->img_dirty = false;
+    return STY_OK;
+}
+
+sty_status infer(sty_nrc *nr, bool ema, uint64_t count, const float *in, float *out, cudaStream_t st) {
+    if (count == 0) return STY_OK;
+    if (nr->cfg.precision == STY_NRC_BF16) {
+        STY_TRY(refresh_images(nr, st));
+        return nrc_tc_forward(nr->net, ema ? nr->img_ema : nr->img, count, in, out, st);
+    }
+    return fwd_f32(nr, ema ? nr->ema : nr->w, count, in, out, nullptr, st);
+}
+
+void free_nrc(sty_nrc *nr) {
+    void *ptrs[] = {nr->w, nr->m, nr->v, nr->g, nr->ema, nr->img, nr->img_ema, nr->bin,
+                    nr->btg, nr->bpred, nr->acts, nr->dpre, nr->loss};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete nr;
+}
+
+}  // namespace
+
+extern "C" {
+
+sty_status sty_nrc_create(const sty_nrc_config *cfg, sty_nrc **out) {
+    clear_error();
+    STY_ARG_CHECK(cfg && out, "sty_nrc_create: null argument");
+    STY_ARG_CHECK(cfg->input_dims >= 1 && cfg->input_dims <= STY_NRC_MAX_INPUTS, "input_dims must be in [1, 16]");
+    STY_ARG_CHECK(cfg->output_dims >= 1 && cfg->output_dims <= (uint32_t)kNrcOutPad, "output_dims must be in [1, 16]");
+    STY_ARG_CHECK(cfg->hidden_layers >= 1 && cfg->hidden_layers <= (uint32_t)kNrcMaxLayers,
+                  "hidden_layers must be in [1, 8]");
+    STY_ARG_CHECK(cfg->batch_size >= 128 && cfg->batch_size % 128 == 0, "batch_size must be a multiple of 128");
+    STY_ARG_CHECK(cfg->precision == STY_NRC_FP32 || cfg->precision == STY_NRC_BF16, "unknown precision");
+    uint32_t enc = 0;
+    for (uint32_t d = 0; d < cfg->input_dims; d++) enc += 2 * cfg->freqs[d];
+    STY_ARG_CHECK(enc <= (uint32_t)kNrcWidth, "encoded width %u exceeds 64", enc);
+    STY_ARG_CHECK(cfg->decay_interval > 0 && cfg->learning_rate > 0.0f, "decay_interval and learning_rate must be > 0");
+    sty_nrc *nr = new sty_nrc();
+    nr->cfg = *cfg;
+    nr->net.in_dims = (int)cfg->input_dims;
+    nr->net.out_dims = (int)cfg->output_dims;
+    nr->net.layers = (int)cfg->hidden_layers;
+    for (int d = 0; d < STY_NRC_MAX_INPUTS; d++) nr->net.freqs[d] = cfg->freqs[d];
+    nr->np = nrc_param_count(nr->net);
+    nr->lr = cfg->learning_rate;
+    sty_status s = STY_OK;
+    auto alloc = [&](void **p, size_t bytes, const char *what) {
+        if (s == STY_OK) s = check_cuda(cudaMalloc(p, bytes), what);
+    };
+    alloc((void **)&nr->w, nr->np * 4, "alloc weights");
+    alloc((void **)&nr->m, nr->np * 4, "alloc adam m");
+    alloc((void **)&nr->v, nr->np * 4, "alloc adam v");
+    alloc((void **)&nr->g, nr->np * 4, "alloc grad");
+    alloc((void **)&nr->ema, nr->np * 4, "alloc ema");
+    alloc((void **)&nr->loss, 4, "alloc loss");
+    if (cfg->precision == STY_NRC_BF16) {
+        alloc((void **)&nr->img, nrc_tc_image_elems(nr->net) * 2, "alloc bf16 image");
+        alloc((void **)&nr->img_ema, nrc_tc_image_elems(nr->net) * 2, "alloc bf16 ema image");
+    }
+    if (s == STY_OK) s = ensure_batch(nr, cfg->batch_size);
+    if (s == STY_OK) {
+        k_init_weights<<<(unsigned)((nr->np + 255) / 256), 256>>>(nr->np, nr->net, cfg->seed, nr->w);
+        s = check_launch("k_init_weights");
+    }
+    if (s == STY_OK) s = check_cuda(cudaMemcpy(nr->ema, nr->w, nr->np * 4, cudaMemcpyDeviceToDevice), "init ema");
+    if (s == STY_OK) s = check_cuda(cudaMemset(nr->m, 0, nr->np * 4), "zero m");
+    if (s == STY_OK) s = check_cuda(cudaMemset(nr->v, 0, nr->np * 4), "zero v");
+    if (s == STY_OK) s = check_cuda(cudaDeviceSynchronize(), "sty_nrc_create");
+    if (s != STY_OK) {
+        free_nrc(nr);
+        return s;
+    }
+    *out = nr;
+    return STY_OK;
+}
+
+sty_status sty_nrc_destroy(sty_nrc *nr) {
+    clear_error();
+    if (!nr) return STY_OK;
+    cudaDeviceSynchronize();
+    free_nrc(nr);
+    return STY_OK;
+}
+
+sty_status sty_nrc_param_count(sty_nrc *nr, uint64_t *count) {
+    clear_error();
+    STY_ARG_CHECK(nr && count, "sty_nrc_param_count: null argument");
+    *count = nr->np;
+    return STY_OK;
+}
+
+sty_status sty_nrc_save_params(sty_nrc *nr, float *host) {
+    clear_error();
+    STY_ARG_CHECK(nr && host, "sty_nrc_save_params: null argument");
+    STY_TRY(check_cuda(cudaDeviceSynchronize(), "sync before save"));
+    return check_cuda(cudaMemcpy(host, nr->w, nr->np * 4, cudaMemcpyDeviceToHost), "save params");
+}
+
+sty_status sty_nrc_load_params(sty_nrc *nr, const float *host) {
+    clear_error();
+    STY_ARG_CHECK(nr && host, "sty_nrc_load_params: null argument");
+    STY_TRY(check_cuda(cudaDeviceSynchronize(), "sync before load"));
+    STY_TRY(check_cuda(cudaMemcpy(nr->w, host, nr->np * 4, cudaMemcpyHostToDevice), "load params"));
+    STY_TRY(check_cuda(cudaMemcpy(nr->ema, host, nr->np * 4, cudaMemcpyHostToDevice), "load ema"));
+    nr->img_dirty = true;
+    return STY_OK;
+}
+
+sty_status sty_nrc_set_learning_rate(sty_nrc *nr, float lr) {
+    clear_error();
+    STY_ARG_CHECK(nr && lr > 0.0f, "sty_nrc_set_learning_rate: bad argument");
+    nr->lr = lr;
+    return STY_OK;
+}
+
+sty_status sty_nrc_get_learning_rate(sty_nrc *nr, float *lr) {
+    clear_error();
+    STY_ARG_CHECK(nr && lr, "sty_nrc_get_learning_rate: null argument");
+    *lr = nr->lr;
+    return STY_OK;
+}
+
+sty_status sty_nrc_reset_optimizer(sty_nrc *nr) {
+    clear_error();
+    STY_ARG_CHECK(nr, "sty_nrc_reset_optimizer: null nrc");
+    STY_TRY(check_cuda(cudaMemset(nr->m, 0, nr->np * 4), "zero m"));
+    STY_TRY(check_cuda(cudaMemset(nr->v, 0, nr->np * 4), "zero v"));
+    nr->step = 0;
+    return STY_OK;
+}
+
+sty_status sty_nrc_inference(sty_nrc *nr, uint64_t count, const float *in, float *out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(nr && (count == 0 || (in && out)), "sty_nrc_inference: null argument");
+    return infer(nr, true, count, in, out, as_stream(stream));
+}
+
+sty_status sty_nrc_train_inference(sty_nrc *nr, uint64_t count, const float *in, float *out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(nr && (count == 0 || (in && out)), "sty_nrc_train_inference: null argument");
+    return infer(nr, false, count, in, out, as_stream(stream));
+}
+
+sty_status sty_nrc_gradient(sty_nrc *nr, uint32_t B, const float *in, const float *target, float *grad,
+                            float *loss_out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(nr && in && target && grad && B > 0, "sty_nrc_gradient: bad argument");
+    cudaStream_t st = as_stream(stream);
+    STY_TRY(ensure_batch(nr, B));
+    STY_TRY(check_cuda(cudaMemsetAsync(nr->loss, 0, 4, st), "zero loss"));
+    STY_TRY(forward_batch(nr, B, in, st));
+    STY_TRY(backward(nr, B, target, st));
+    STY_TRY(check_cuda(cudaMemcpyAsync(grad, nr->g, nr->np * 4, cudaMemcpyDeviceToDevice, st), "copy grad"));
+    if (loss_out) {
+        STY_TRY(check_cuda(cudaMemcpyAsync(loss_out, nr->loss, 4, cudaMemcpyDeviceToHost, st), "read loss"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync loss"));
+    }
+    return STY_OK;
+}
+
+sty_status sty_nrc_train(sty_nrc *nr, uint64_t count, uint64_t n_iters, const float *in, const float *target,
+                         float *loss_out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(nr && in && target && count > 0, "sty_nrc_train: bad argument");
+    cudaStream_t st = as_stream(stream);
+    const sty_nrc_config &c = nr->cfg;
+    const uint32_t B = c.batch_size;
+    STY_TRY(check_cuda(cudaMemsetAsync(nr->loss, 0, 4, st), "zero loss"));
+    for (uint64_t it = 0; it < n_iters; it++) {
+        k_collect<<<(B + 255) / 256, 256, 0, st>>>(B, c.seed, nr->step, count, nr->net.in_dims, nr->net.out_dims, in,
+                                                   target, nr->bin, nr->btg);
+        STY_TRY(check_launch("k_collect"));
+        STY_TRY(forward_batch(nr, B, nr->bin, st));
+        STY_TRY(backward(nr, B, nr->btg, st));
+        nr->step++;
+        const double t = (double)nr->step;
+        const float lr_t = nr->lr * (float)std::pow((double)c.decay_base, std::floor((t - 1.0) / c.decay_interval));
+        const float bc1 = (float)(1.0 - std::pow((double)c.beta1, t));
+        const float bc2 = (float)(1.0 - std::pow((double)c.beta2, t));
+        const float ema_old = (float)(1.0 - std::pow((double)c.ema_decay, t - 1.0));
+        const float ema_new = (float)(1.0 / (1.0 - std::pow((double)c.ema_decay, t)));
+        k_adam<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, nr->w, nr->m, nr->v, nr->g, nr->ema, lr_t,
+                                                                 c.beta1, c.beta2, c.epsilon, bc1, bc2, c.ema_decay,
+                                                                 ema_old, ema_new);
+        STY_TRY(check_launch("k_adam"));
+        nr->img_dirty = true;
+    }
+    if (loss_out) {
+        float l = 0.0f;
+        STY_TRY(check_cuda(cudaMemcpyAsync(&l, nr->loss, 4, cudaMemcpyDeviceToHost, st), "read loss"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync loss"));
+        *loss_out = n_iters ? l / (float)n_iters : 0.0f;
+    }
+    return STY_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,52 @@
+// nrc.cuh -- neural radiance cache: shared definitions of the FP32 and BF16 (tcgen05) paths.
+#pragma once
+
+#include "common.cuh"
+
+namespace sty {
+
+constexpr int kNrcWidth = 64;      // hidden width and encoded input width
+constexpr int kNrcMaxLayers = 8;   // hidden layers supported
+constexpr int kNrcOutPad = 16;     // output rows padded to one MMA N tile
+
+struct NrcNet {
+    int in_dims, out_dims, layers;     // layers = hidden layers; weight matrices = layers + 1
+    uint32_t freqs[STY_NRC_MAX_INPUTS];
+};
+
+// offsets (floats) of the weight matrices in the flat FP32 parameter vector:
+// layer l < layers: [64 out][64 in]; output layer: [out_dims][64]
+__host__ __device__ inline size_t nrc_w_offset(int l) { return (size_t)l * kNrcWidth * kNrcWidth; }
+__host__ __device__ inline size_t nrc_param_count(const NrcNet &n) {
+    return (size_t)n.layers * kNrcWidth * kNrcWidth + (size_t)n.out_dims * kNrcWidth;
+}
+
+// Frequency encoding of one sample: dim d contributes sin(2^k pi x), cos(2^k pi x), k < freqs[d],
+// in order (d, k, sin, cos); the tail up to 64 is zero. One sincosf per dim, higher octaves by the
+// double-angle identities sin 2a = 2 sin a cos a, cos 2a = 1 - 2 sin^2 a.
+__device__ __forceinline__ void nrc_encode(const NrcNet &n, const float *x, float enc[kNrcWidth]) {
+    int o = 0;
+#pragma unroll 1
+    for (int d = 0; d < n.in_dims; d++) {
+        float s, c;
+        sincospif(x[d], &s, &c);
+        for (uint32_t k = 0; k < n.freqs[d]; k++) {
+            enc[o] = s;
+            enc[o + 1] = c;
+            o += 2;
+            const float s2 = 2.0f * s * c;
+            c = fmaf(-2.0f * s, s, 1.0f);
+            s = s2;
+        }
+    }
+    for (; o < kNrcWidth; o++) enc[o] = 0.0f;
+}
+
+// BF16 tensor-core path (nrc_tc.cu)
+struct NrcTcWeights;  // device buffers in the UMMA shared-memory image layout
+sty_status nrc_tc_pack(const NrcNet &n, const float *w_fp32, uint16_t *w_img, cudaStream_t st);
+size_t nrc_tc_image_elems(const NrcNet &n);
+sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *w_img, uint64_t count, const float *input, float *output,
+                          cudaStream_t st);
+
+}  // namespace sty

@@ -1,0 +1,285 @@
+// nrc_tc.cu -- BF16 tcgen05 forward of the NRC MLP (inference), FP32 accumulation in TMEM.
+//
+// One CTA = one warpgroup (128 threads), persistent over tiles of 128 samples (one sample per TMEM
+// lane / thread). Shared memory holds every layer's weights as BF16 UMMA operand images plus one
+// 128 x 64 BF16 activation tile; TMEM holds the 128 x 64 FP32 accumulator. Per layer:
+//   thread 0 issues 4 x tcgen05.mma (M=128, N=64 (16 for the output layer), K=16) and commits to an
+//   mbarrier; all threads wait (bounded), tcgen05.ld their row, apply ReLU, convert to BF16 and write
+//   the row back as the next layer's A operand (generic-proxy writes fenced for the async proxy).
+// Operand images are K-major with no swizzle: an R x 64 matrix is stored as R/8 x 8 "core matrices"
+// of 8 rows x 16 bytes, core matrix (rb, kb) at byte ((rb * 8) + kb) * 128, so the leading
+// (K-direction) byte offset is 128 and the stride (8-row) byte offset is 1024.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "nrc.cuh"
+
+namespace sty {
+namespace {
+
+constexpr int W = kNrcWidth;
+constexpr int TM = 128;                      // samples per tile (MMA M)
+constexpr int kTileBytes = TM * W * 2;       // 16 KB activation tile
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// byte offset of element (row, k) in a K-major no-swizzle image with 64 columns
+__host__ __device__ __forceinline__ uint32_t img_off(uint32_t row, uint32_t k) {
+    return (((row >> 3) * 8u + (k >> 3)) * 128u) + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+    const uint64_t lbo = 128, sbo = 1024;
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+}
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
+    // D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1), K-major A and B, N>>3, M>>4
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t *status) {
+    const uint32_t a = smem_u32(bar);
+    unsigned long long t0 = 0;
+    for (uint32_t it = 0;; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (it == 0) t0 = gtimer();
+        else if ((it & 63) == 0 && gtimer() - t0 > kWaitNs) {
+            atomicOr(status, (uint32_t)STY_DEV_WAIT_TIMEOUT);
+            return false;
+        }
+    }
+}
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 32 lanes x 32 columns of FP32 from TMEM (this warp's lane quarter)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    const __nv_bfloat16_raw ra = __float2bfloat16_rn(a), rb = __float2bfloat16_rn(b);
+    return (uint32_t)ra.x | ((uint32_t)rb.x << 16);
+}
+// write one 64-wide row of BF16 (from FP32 v) into a K-major image
+__device__ __forceinline__ void store_row(uint8_t *img, uint32_t row, const float *v) {
+#pragma unroll
+    for (int kb = 0; kb < 8; kb++) {
+        uint4 q;
+        q.x = pack_bf16(v[kb * 8 + 0], v[kb * 8 + 1]);
+        q.y = pack_bf16(v[kb * 8 + 2], v[kb * 8 + 3]);
+        q.z = pack_bf16(v[kb * 8 + 4], v[kb * 8 + 5]);
+        q.w = pack_bf16(v[kb * 8 + 6], v[kb * 8 + 7]);
+        *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) = q;
+    }
+}
+
+struct TcArgs {
+    NrcNet n;
+    const uint16_t *wimg;  // global weight image
+    uint64_t count;
+    const float *input;
+    float *output;
+    uint32_t *status;
+};
+
+__global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int L = a.n.layers;
+    const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
+    uint8_t *wimg = smem;                 // weights
+    uint8_t *act = smem + ((wbytes + 1023u) & ~1023u);  // activation tile (1 KB aligned)
+
+    // weights -> shared memory (16-byte copies)
+    for (uint32_t o = tid * 16u; o < wbytes; o += 128u * 16u)
+        *reinterpret_cast<uint4 *>(wimg + o) = *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
+    const uint32_t wbase = smem_u32(wimg), abase = smem_u32(act);
+    uint32_t phase = 0;
+    bool failed = false;  // CTA-uniform (decided through __syncthreads_and)
+
+    const uint64_t ntiles = (a.count + TM - 1) / TM;
+    for (uint64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const uint64_t row = tile * TM + tid;
+        // encode this thread's sample into row tid of the activation tile
+        {
+            float enc[W];
+            if (row < a.count) {
+                nrc_encode(a.n, a.input + row * a.n.in_dims, enc);
+            } else {
+#pragma unroll
+                for (int k = 0; k < W; k++) enc[k] = 0.0f;
+            }
+            store_row(act, tid, enc);
+        }
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+        for (int l = 0; l <= L; l++) {
+            const bool out_layer = l == L;
+            if (tid == 0) {
+                fence_after();
+                const uint32_t wl = wbase + (uint32_t)l * W * W * 2u;
+                const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++)
+                    mma_bf16(tmem, make_desc(abase + kk * 256u), make_desc(wl + kk * 256u), idesc, kk > 0 ? 1u : 0u);
+                mma_commit(&mbar);
+            }
+            const bool got = mbar_wait(&mbar, phase, a.status);
+            if (!__syncthreads_and(got)) {
+                failed = true;
+                break;
+            }
+            phase ^= 1u;
+            fence_after();
+            if (!out_layer) {
+                float v[32];
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    tmem_ld32(lane_base + half * 32u, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int k = 0; k < 32; k++) v[k] = fmaxf(v[k], 0.0f);
+                    // columns half*32 .. half*32+31 -> k-blocks half*4 .. half*4+3
+#pragma unroll
+                    for (int kb = 0; kb < 4; kb++) {
+                        uint4 q;
+                        q.x = pack_bf16(v[kb * 8 + 0], v[kb * 8 + 1]);
+                        q.y = pack_bf16(v[kb * 8 + 2], v[kb * 8 + 3]);
+                        q.z = pack_bf16(v[kb * 8 + 4], v[kb * 8 + 5]);
+                        q.w = pack_bf16(v[kb * 8 + 6], v[kb * 8 + 7]);
+                        *reinterpret_cast<uint4 *>(act + img_off(tid, half * 32 + kb * 8)) = q;
+                    }
+                }
+                fence_async_smem();
+            } else {
+                float v[32];
+                tmem_ld32(lane_base, v);  // columns 0..31 (the first out_dims are the output)
+                tmem_wait_ld();
+                if (row < a.count)
+                    for (int c = 0; c < a.n.out_dims; c++) a.output[row * a.n.out_dims + c] = v[c];
+            }
+            fence_before();
+            __syncthreads();
+        }
+    }
+    if (failed) {
+        // the last commit never arrived within the limit: give the MMA one more bounded wait before
+        // the accumulator columns are released
+        mbar_wait(&mbar, phase, a.status);
+    }
+    __syncthreads();
+    fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+}
+
+// FP32 [out][in] -> BF16 K-major images; output layer padded to 16 rows of zeros
+__global__ void k_pack(NrcNet n, const float *w, uint16_t *img) {
+    const int L = n.layers;
+    const uint32_t total = (uint32_t)(L * W * W + kNrcOutPad * W);
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total) return;
+    uint32_t l, r, k;
+    if (e < (uint32_t)(L * W * W)) {
+        l = e / (W * W);
+        r = (e % (W * W)) / W;
+        k = e % W;
+    } else {
+        l = L;
+        r = (e - L * W * W) / W;
+        k = (e - L * W * W) % W;
+    }
+    float val = 0.0f;
+    if (l < (uint32_t)L) val = w[nrc_w_offset(l) + r * W + k];
+    else if (r < (uint32_t)n.out_dims) val = w[nrc_w_offset(L) + r * W + k];
+    const __nv_bfloat16_raw b = __float2bfloat16_rn(val);
+    const uint32_t base = l * W * W;  // elements; the output image (16 rows) starts after layer L-1
+    img[base + img_off(r, k) / 2] = b.x;
+}
+
+}  // namespace
+
+size_t nrc_tc_image_elems(const NrcNet &n) { return (size_t)n.layers * W * W + (size_t)kNrcOutPad * W; }
+
+sty_status nrc_tc_pack(const NrcNet &n, const float *w, uint16_t *img, cudaStream_t st) {
+    const uint32_t total = (uint32_t)nrc_tc_image_elems(n);
+    k_pack<<<(total + 255) / 256, 256, 0, st>>>(n, w, img);
+    return check_launch("k_pack");
+}
+
+sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, const float *input, float *output,
+                          cudaStream_t st) {
+    TcArgs a;
+    a.n = n;
+    a.wimg = img;
+    a.count = count;
+    a.input = input;
+    a.output = output;
+    a.status = device_status_ptr();
+    if (!a.status) {
+        set_error("device status word unavailable");
+        return STY_ERR_CUDA;
+    }
+    const size_t wbytes = nrc_tc_image_elems(n) * 2;
+    const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + kTileBytes + 1024;
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "attr k_nrc_fwd_tc"));
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t ntiles = (count + TM - 1) / TM;
+    const uint64_t grid = ntiles < (uint64_t)sms * 3 ? ntiles : (uint64_t)sms * 3;
+    k_nrc_fwd_tc<<<(unsigned)grid, 128, smem, st>>>(a);
+    return check_launch("k_nrc_fwd_tc");
+}
+
+}  // namespace sty
