@@ -2,9 +2,9 @@
 the tcgen05 BF16 path against it (GPU).
 
 Tolerances: FP32 path vs FP64 oracle 1e-4 relative (5 chained 64-wide FP32 matmuls); BF16 path vs
-the oracle's BF16 emulation (weights and layer inputs rounded to bfloat16) 2e-3 relative, the
-remaining difference being FP32 accumulation order in TMEM and BF16 rounding-boundary flips of
-intermediate activations; BF16 vs exact FP64 only statistically (relative RMS < 3 %)."""
+the oracle's BF16 emulation (weights and layer inputs rounded to bfloat16): 99 % of outputs within
+1e-4 of the output scale and all within 1e-2 (FP32 accumulation order in TMEM, and BF16
+rounding-boundary flips of intermediate activations); BF16 vs exact FP64 only statistically (relative RMS < 3 %)."""
 import numpy as np
 import pytest
 
@@ -110,7 +110,11 @@ def test_bf16_tensor_core_inference(sty, cuda, layers):
     scale = np.abs(emu).max()
     err = np.abs(out - emu)
     assert np.isfinite(out).all()
-    assert err.max() <= 2e-3 * scale, f"max err {err.max():.3e} vs scale {scale:.3e}"
+    # almost every output equals the emulation up to FP32 accumulation order; a few differ through a
+    # BF16 rounding-boundary flip of an intermediate activation
+    # (a flip in an early layer moves all outputs of that sample; a layout error would move all)
+    assert np.mean(err <= 1e-4 * scale) >= 0.99, f"{np.mean(err > 1e-4 * scale):.4%} outputs off"
+    assert err.max() <= 1e-2 * scale, f"max err {err.max():.3e} vs scale {scale:.3e}"
     rms = np.sqrt(((out - ref) ** 2).mean()) / np.sqrt((ref ** 2).mean())
     assert rms < 3e-2
     assert sty.abi.device_status() == 0
