@@ -129,6 +129,70 @@ def cpu_baseline(sty, orc, planes, valid, depths: int = D_, budget_s: float = 12
                       f"{nvalid} valid vertices in {elapsed:.2f} s, FP32 restatement of the filter"}
 
 
+def nrc_target(x):
+    """Smooth synthetic radiance field of the 11 NRC inputs (RGB)."""
+    import torch
+    r = 0.5 + 0.4 * torch.sin(3.0 * x[:, 0] + 2.0 * x[:, 3]) * torch.cos(2.0 * x[:, 1])
+    g = 0.3 + 0.25 * torch.cos(4.0 * x[:, 2] - x[:, 5]) + 0.2 * x[:, 8]
+    b = 0.2 + 0.3 * x[:, 9] * x[:, 10] + 0.1 * torch.sin(5.0 * x[:, 4])
+    return torch.stack([r, g, b], 1).contiguous()
+
+
+def nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
+    """NL-NRC frames on the BASELINE network (frequency encoding to 64, 5 x 64 ReLU, RGB): per frame
+    one training step on 2^16 samples and inference of 2^21 queries, for the BF16 tcgen05 path and
+    the FP32 CUDA-core path. Same seeds, data and schedule for both; quality = relative-L2 loss of
+    the EMA network on held-out samples after the timed frames."""
+    import torch
+    nq, nt = 1 << 21, 1 << 16
+    gen = torch.Generator(device=dev).manual_seed(0)
+    pool_x = torch.rand((1 << 18, 11), generator=gen, device=dev)
+    pool_t = nrc_target(pool_x)
+    qx = torch.rand((nq, 11), generator=gen, device=dev)
+    vx = torch.rand((1 << 16, 11), generator=gen, device=dev)
+    vt = nrc_target(vx)
+    out = torch.empty((nq, 3), device=dev)
+    res = {}
+    stream = torch.cuda.current_stream(dev)
+    for name, prec in (("fp32", sty.nrc.STY_NRC_FP32), ("bf16", sty.nrc.STY_NRC_BF16)):
+        net = sty.nrc.NRC(sty.nrc.config(sty.nrc.C4_FREQS, 3, nt, 5, prec, learning_rate=1e-2, seed=1))
+        for _ in range(warmup):
+            net.train(pool_x, pool_t, 1, stream=stream, want_loss=False)
+            net.inference(qx, out, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            net.train(pool_x, pool_t, 1, stream=stream, want_loss=False)
+            net.inference(qx, out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        # inference alone (the tensor-core kernel for bf16), for the roofline
+        i0, i1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        i0.record(stream)
+        for _ in range(frames):
+            net.inference(qx, out, stream=stream)
+        i1.record(stream)
+        torch.cuda.synchronize()
+        inf_ms = i0.elapsed_time(i1) / frames
+        pv = net.inference(vx)
+        vloss = float(((pv - vt) ** 2 / (pv.detach() ** 2 + 0.01)).mean())
+        flops_q = 2.0 * (5 * 64 * 64 + (16 if prec else 3) * 64)  # MMA work incl. the padded output rows
+        res[name] = {"ms_per_frame": ms, "msamples_per_s": (nq + nt) / ms / 1e3,
+                     "inference_ms": inf_ms, "inference_tflops": nq * flops_q / (inf_ms / 1e3) / 1e12,
+                     "val_rel_l2": vloss, "frames": frames}
+        net.close()
+    res["speedup_bf16_over_fp32"] = res["bf16"]["msamples_per_s"] / res["fp32"]["msamples_per_s"]
+    res["val_loss_ratio_bf16_over_fp32"] = res["bf16"]["val_rel_l2"] / res["fp32"]["val_rel_l2"]
+    ach = res["bf16"]["inference_tflops"]
+    res["roofline"] = {"bound": "tensor", "kernel": "k_nrc_fwd_tc", "achieved": ach, "peak": bf16_peak,
+                       "unit": "TFLOP/s", "frac": ach / bf16_peak, "peak_source": "measured (bf16 burst)"}
+    res["config"] = {"queries_per_frame": nq, "train_samples_per_frame": nt, "network": "freq-enc 11->64, 5x64 ReLU, 3",
+                     "data": "synthetic smooth radiance field", "lr": 1e-2, "loss": "relative L2"}
+    return res
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -168,6 +232,9 @@ def run(args):
     import __graft_entry__ as g
     sty = g.package()
     lib = sty.abi.lib()
+    if args.nrc_only:  # profiling case: the NL-NRC frames alone
+        print(json.dumps({"nrc": nrc_bench(sty, args.nrc_frames, 2, dev, 1943.8)}), flush=True)
+        return
 
     D_ = args.depths
     planes, valid = sty.synth.records(W_, H_, S_, D_, seed=rank)
@@ -299,6 +366,12 @@ def run(args):
                          "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 at the sampled SM clock"},
         "clocks": clk,
     }
+    if world == 1 and not args.no_nrc:
+        bf16_peak = 1943.8
+        p = ROOT / "MEASURED_PEAKS.json"
+        if p.exists():
+            bf16_peak = float(json.loads(p.read_text())["bf16_tflops"])
+        line["nrc"] = nrc_bench(sty, args.nrc_frames, 2, dev, bf16_peak)
     if world == 1 and not args.no_cpu_baseline:
         import oracle as orc
         line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid, D_)
@@ -317,6 +390,9 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=8.0)
     ap.add_argument("--depths", type=int, default=D_, help="path depths (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling cases)")
+    ap.add_argument("--no-nrc", action="store_true", help="skip the NL-NRC frames")
+    ap.add_argument("--nrc-frames", type=int, default=20)
+    ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
