@@ -265,6 +265,23 @@ STY_API sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices 
                                      uint32_t *cluster_id, void *stream);
 
 /* ----------------------------------------------------------------------------------------
+ * Adjoint of the screen-space NL-PF filter + smoothed ramp style node (one depth)
+ *
+ * Forward (as sty_pf_screen_filter_depth with a single STY_STYLE_RAMP_SMOOTH node applied at this
+ * depth): f_i = sum_j w_ij in_j / sum_j w_ij, out_i = ramp(f_i); image = per-pixel mean over spp of
+ * out (invalid records count as 0); loss = sum over pixels and channels of (image - target)^2.
+ * Parameters (36 floats, this order): [0] sharpness s, [1..8] thresholds t_k, [9..32] colours
+ * c_k (rgb), [33] sigma_pixel, [34] sigma_pos, [35] sigma_nrm. `n_steps` (1..8) ramp steps are used;
+ * gradients of unused thresholds / colours are 0. The backward recomputes the neighbourhood
+ * weights (two sweeps per query) instead of storing them.
+ * `target` (device, width*height*3 floats, interleaved rgb); `grad` (device, 36 floats);
+ * `loss_out` (host, optional; synchronises). `in_next` as in sty_pf_screen_filter_depth.
+ * -------------------------------------------------------------------------------------- */
+STY_API sty_status sty_pf_adjoint(const sty_pf_records *rec, uint32_t depth, int32_t radius, const float params[36],
+                                  uint32_t n_steps, const float *in_next, const float *target, float *grad,
+                                  float *loss_out, void *stream);
+
+/* ----------------------------------------------------------------------------------------
  * Neural radiance cache (NL-NRC): one-to-one with the reference's tiny-cuda-nn wrapper
  * (crates/akari_cpp_ext/cpp_ext/akari_nrc.h:1-17, akari_tcnn.cu:84-292).
  *

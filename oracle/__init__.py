@@ -32,6 +32,12 @@ def lib() -> C.CDLL:
         L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
         L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
         L.orc_hash_cells.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, vp, vp]
+        L.orc_pf_adjoint_loss_f64.restype = C.c_double
+        L.orc_pf_adjoint_loss_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
+        L.orc_pf_adjoint_f64.restype = C.c_double
+        L.orc_pf_adjoint_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp, vp]
+        L.orc_pf_adjoint_image_f64.restype = C.c_double
+        L.orc_pf_adjoint_image_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
@@ -112,6 +118,32 @@ def pf_ref_filter(arrays: dict, params_c, mats, progs, n_progs: int, rng_states:
 
 def __package_name__() -> str:
     return "practical_stylized_gb300"
+
+
+def pf_adjoint_loss(rec, depth, radius, params, n_steps, target, in_next=None) -> float:
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    nxt = None if in_next is None else np.ascontiguousarray(in_next, dtype=np.float64)
+    return lib().orc_pf_adjoint_loss_f64(C.addressof(rec), depth, radius, _p(prm), n_steps, _p(nxt), _p(tg))
+
+
+def pf_adjoint_image(rec, depth, radius, params, n_steps, in_next=None) -> np.ndarray:
+    """FP64 image (pixel-mean over spp of the ramp-styled filter output), interleaved rgb."""
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    nxt = None if in_next is None else np.ascontiguousarray(in_next, dtype=np.float64)
+    img = np.zeros(3 * rec.width * rec.height, dtype=np.float64)
+    lib().orc_pf_adjoint_image_f64(C.addressof(rec), depth, radius, _p(prm), n_steps, _p(nxt), _p(img))
+    return img
+
+
+def pf_adjoint(rec, depth, radius, params, n_steps, target, in_next=None):
+    """(loss, grad[36]) in FP64 (analytic adjoint)."""
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    nxt = None if in_next is None else np.ascontiguousarray(in_next, dtype=np.float64)
+    g = np.zeros(36, dtype=np.float64)
+    loss = lib().orc_pf_adjoint_f64(C.addressof(rec), depth, radius, _p(prm), n_steps, _p(nxt), _p(tg), _p(g))
+    return loss, g
 
 
 def num_threads() -> int:

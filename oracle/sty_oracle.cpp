@@ -458,3 +458,188 @@ void orc_hash_cells(const float *pts, uint64_t n, const float pmin[3], const flo
 }
 
 }  // extern "C"
+
+// ---- adjoint of the screen filter + smoothed ramp (FP64) -------------------------------------
+// Loss and gradient of the 36 parameters exactly as documented for sty_pf_adjoint in
+// include/sty_gb300.h, evaluated in double: the forward restates the screen filter above with a
+// single ramp node, the backward the chain rule written out in the CUDA file's header comment.
+namespace {
+struct AdjFwd {
+    std::vector<double> f, D;  // f: 3 per query record; D: weight sum
+    std::vector<double> img;   // 3 per pixel
+};
+double adj_forward(const sty_pf_records *r, uint32_t depth, int R, const double *prm, int nsteps,
+                   const double *in_next, const double *target, AdjFwd *keep) {
+    const int W = r->width, H = r->height, S = r->spp;
+    const size_t N = (size_t)W * H * S;
+    const int d = (int)depth;
+    const double sx = prm[33], sp = prm[34], sn = prm[35];
+    std::vector<double> in(3 * N);
+    for (size_t j = 0; j < N; j++)
+        for (int c = 0; c < 3; c++) {
+            size_t g = (size_t)d * N + j;
+            double v = r->rad[c][g];
+            if (in_next) v += (double)r->thr[c][g] * in_next[c * N + j];
+            in[3 * j + c] = v;
+        }
+    std::vector<double> f(3 * N, 0.0), D(N, 0.0), out(3 * N, 0.0);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < H; y++)
+        for (int x = 0; x < W; x++)
+            for (int s = 0; s < S; s++) {
+                size_t qi = ((size_t)y * W + x) * S + s, gq = (size_t)d * N + qi;
+                if (!r->valid[gq]) continue;
+                double sw = 0, a[3] = {0, 0, 0};
+                for (int yy = std::max(0, y - R); yy <= std::min(H - 1, y + R); yy++)
+                    for (int xx = std::max(0, x - R); xx <= std::min(W - 1, x + R); xx++)
+                        for (int t = 0; t < S; t++) {
+                            size_t j = ((size_t)yy * W + xx) * S + t, gj = (size_t)d * N + j;
+                            if (!r->valid[gj]) continue;
+                            double rho = (double)(xx - x) * (xx - x) + (double)(yy - y) * (yy - y);
+                            double d2 = 0, nn = 0;
+                            for (int k = 0; k < 3; k++) {
+                                double e = (double)r->pos[k][gq] - r->pos[k][gj];
+                                d2 += e * e;
+                                nn += (double)r->nrm[k][gq] * r->nrm[k][gj];
+                            }
+                            double w = std::exp(-rho / (2 * sx * sx) - d2 / (2 * sp * sp) - (1 - nn) / (sn * sn));
+                            sw += w;
+                            for (int c = 0; c < 3; c++) a[c] += w * in[3 * j + c];
+                        }
+                D[qi] = sw;
+                double cl[3];
+                for (int c = 0; c < 3; c++) {
+                    f[3 * qi + c] = a[c] / sw;
+                    cl[c] = std::min(std::max(f[3 * qi + c], 0.0), 1e5);
+                }
+                double lum = cl[0] * 0.2126 + cl[1] * 0.7152 + cl[2] * 0.0722;
+                double prev[3] = {0, 0, 0};
+                for (int k = 0; k < nsteps; k++) {
+                    double sg = 1.0 / (1.0 + std::exp(-prm[0] * (lum - prm[1 + k])));
+                    for (int c = 0; c < 3; c++) {
+                        out[3 * qi + c] += sg * (prm[9 + 3 * k + c] - prev[c]);
+                        prev[c] = prm[9 + 3 * k + c];
+                    }
+                }
+            }
+    std::vector<double> img(3 * (size_t)W * H, 0.0);
+    double loss = 0;
+    for (size_t p = 0; p < (size_t)W * H; p++)
+        for (int c = 0; c < 3; c++) {
+            double m = 0;
+            for (int s = 0; s < S; s++) m += out[3 * (p * S + s) + c];
+            m /= S;
+            img[3 * p + c] = m;
+            double e = m - target[3 * p + c];
+            loss += e * e;
+        }
+    if (keep) {
+        keep->f = std::move(f);
+        keep->D = std::move(D);
+        keep->img = std::move(img);
+    }
+    return loss;
+}
+}  // namespace
+
+extern "C" {
+
+double orc_pf_adjoint_loss_f64(const sty_pf_records *r, uint32_t depth, int32_t radius, const double *prm,
+                               uint32_t n_steps, const double *in_next, const double *target) {
+    return adj_forward(r, depth, radius, prm, (int)n_steps, in_next, target, nullptr);
+}
+
+double orc_pf_adjoint_f64(const sty_pf_records *r, uint32_t depth, int32_t R, const double *prm, uint32_t n_steps,
+                          const double *in_next, const double *target, double *grad) {
+    AdjFwd fw;
+    const double loss = adj_forward(r, depth, R, prm, (int)n_steps, in_next, target, &fw);
+    const int W = r->width, H = r->height, S = r->spp, d = (int)depth;
+    const size_t N = (size_t)W * H * S;
+    const double sx = prm[33], sp = prm[34], sn = prm[35], s = prm[0];
+    std::vector<double> in(3 * N);
+    for (size_t j = 0; j < N; j++)
+        for (int c = 0; c < 3; c++) {
+            size_t g = (size_t)d * N + j;
+            double v = r->rad[c][g];
+            if (in_next) v += (double)r->thr[c][g] * in_next[c * N + j];
+            in[3 * j + c] = v;
+        }
+    std::vector<double> acc((size_t)H * 36, 0.0);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < H; y++) {
+        double *gs = &acc[(size_t)y * 36];
+        for (int x = 0; x < W; x++)
+            for (int q = 0; q < S; q++) {
+                size_t qi = ((size_t)y * W + x) * S + q, gq = (size_t)d * N + qi;
+                if (!r->valid[gq]) continue;
+                const size_t p = (size_t)y * W + x;
+                double g[3];
+                for (int c = 0; c < 3; c++) g[c] = 2.0 * (fw.img[3 * p + c] - target[3 * p + c]) / S;
+                const double *f = &fw.f[3 * qi];
+                double cl[3];
+                for (int c = 0; c < 3; c++) cl[c] = std::min(std::max(f[c], 0.0), 1e5);
+                double lum = cl[0] * 0.2126 + cl[1] * 0.7152 + cl[2] * 0.0722;
+                double dlum = 0, prev[3] = {0, 0, 0};
+                std::vector<double> sgv(n_steps + 1, 0.0);
+                for (uint32_t k = 0; k < n_steps; k++) {
+                    double sg = 1.0 / (1.0 + std::exp(-s * (lum - prm[1 + k])));
+                    sgv[k] = sg;
+                    double dsg = sg * (1 - sg);
+                    double gdc = 0;
+                    for (int c = 0; c < 3; c++) {
+                        gdc += g[c] * (prm[9 + 3 * k + c] - prev[c]);
+                        prev[c] = prm[9 + 3 * k + c];
+                    }
+                    dlum += s * dsg * gdc;
+                    gs[0] += dsg * (lum - prm[1 + k]) * gdc;
+                    gs[1 + k] += -s * dsg * gdc;
+                }
+                for (uint32_t k = 0; k < n_steps; k++)
+                    for (int c = 0; c < 3; c++) gs[9 + 3 * k + c] += g[c] * (sgv[k] - sgv[k + 1]);
+                const double Yw[3] = {0.2126, 0.7152, 0.0722};
+                double h[3];
+                for (int c = 0; c < 3; c++) h[c] = (f[c] > 0 && f[c] < 1e5) ? dlum * Yw[c] : 0.0;
+                const double hf = h[0] * f[0] + h[1] * f[1] + h[2] * f[2];
+                double e0 = 0, e1 = 0, e2 = 0;
+                for (int yy = std::max(0, y - R); yy <= std::min(H - 1, y + R); yy++)
+                    for (int xx = std::max(0, x - R); xx <= std::min(W - 1, x + R); xx++)
+                        for (int t = 0; t < S; t++) {
+                            size_t j = ((size_t)yy * W + xx) * S + t, gj = (size_t)d * N + j;
+                            if (!r->valid[gj]) continue;
+                            double rho = (double)(xx - x) * (xx - x) + (double)(yy - y) * (yy - y);
+                            double d2 = 0, nn = 0;
+                            for (int k = 0; k < 3; k++) {
+                                double ee = (double)r->pos[k][gq] - r->pos[k][gj];
+                                d2 += ee * ee;
+                                nn += (double)r->nrm[k][gq] * r->nrm[k][gj];
+                            }
+                            double w = std::exp(-rho / (2 * sx * sx) - d2 / (2 * sp * sp) - (1 - nn) / (sn * sn));
+                            double tt = w * (h[0] * in[3 * j] + h[1] * in[3 * j + 1] + h[2] * in[3 * j + 2] - hf);
+                            e0 += tt * rho;
+                            e1 += tt * d2;
+                            e2 += tt * (1 - nn);
+                        }
+                const double iD = 1.0 / fw.D[qi];
+                gs[33] += e0 * iD / (sx * sx * sx);
+                gs[34] += e1 * iD / (sp * sp * sp);
+                gs[35] += 2.0 * e2 * iD / (sn * sn * sn);
+            }
+    }
+    for (int k = 0; k < 36; k++) {
+        double t = 0;
+        for (int y = 0; y < H; y++) t += acc[(size_t)y * 36 + k];
+        grad[k] = t;
+    }
+    return loss;
+}
+
+}  // extern "C"
+
+extern "C" double orc_pf_adjoint_image_f64(const sty_pf_records *r, uint32_t depth, int32_t radius, const double *prm,
+                                           uint32_t n_steps, const double *in_next, double *img) {
+    AdjFwd fw;
+    std::vector<double> zero(3 * (size_t)r->width * r->height, 0.0);
+    double l = adj_forward(r, depth, radius, prm, (int)n_steps, in_next, zero.data(), &fw);
+    std::copy(fw.img.begin(), fw.img.end(), img);
+    return l;
+}
