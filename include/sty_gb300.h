@@ -281,6 +281,20 @@ STY_API sty_status sty_pf_adjoint(const sty_pf_records *rec, uint32_t depth, int
                                   uint32_t n_steps, const float *in_next, const float *target, float *grad,
                                   float *loss_out, void *stream);
 
+/* Allocation-free variant of sty_pf_adjoint (no counterpart in the reference). For callers that
+ * cannot allocate device memory -- a host integrator whose device memory is owned and budgeted by
+ * another runtime, or a render loop that must not fail on an allocation mid-frame -- the scratch
+ * lives in one fixed device array of 4.31 MiB that every device holds from the library's first use
+ * on it until the process exits. Same arguments and results as sty_pf_adjoint; limits: at most
+ * 2^18 records per depth (width * height * spp), 2^16 pixels and 4096 32x8 tiles, larger inputs
+ * are rejected with STY_ERR_ARG. It calls no cudaMalloc / cudaFree. Its first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture. All calls share the one array: calls whose work overlaps on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller. */
+STY_API sty_status sty_pf_adjoint_noalloc(const sty_pf_records *rec, uint32_t depth, int32_t radius,
+                                          const float params[36], uint32_t n_steps, const float *in_next,
+                                          const float *target, float *grad, float *loss_out, void *stream);
+
 /* ----------------------------------------------------------------------------------------
  * Neural radiance cache (NL-NRC): one-to-one with the reference's tiny-cuda-nn wrapper
  * (crates/akari_cpp_ext/cpp_ext/akari_nrc.h:1-17, akari_tcnn.cu:84-292).

@@ -103,6 +103,9 @@ SIGNATURES = {
                                       _VP, _VP, _VP]),
     "sty_pf_adjoint": (C.c_int32, [C.POINTER(PfRecords), C.c_uint32, C.c_int32, C.POINTER(C.c_float * 36),
                                    C.c_uint32, _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
+    "sty_pf_adjoint_noalloc": (C.c_int32, [C.POINTER(PfRecords), C.c_uint32, C.c_int32,
+                                           C.POINTER(C.c_float * 36), C.c_uint32, _VP, _VP, _VP,
+                                           C.POINTER(C.c_float), _VP]),
     "sty_nrc_create": (C.c_int32, [_VP, C.POINTER(C.c_void_p)]),
     "sty_nrc_destroy": (C.c_int32, [C.c_void_p]),
     "sty_nrc_param_count": (C.c_int32, [C.c_void_p, C.POINTER(C.c_uint64)]),

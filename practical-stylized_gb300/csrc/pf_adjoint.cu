@@ -378,3 +378,135 @@ extern "C" sty_status sty_pf_adjoint(const sty_pf_records *rec, uint32_t depth, 
         if (p) cudaFreeAsync(p, st);
     return s;
 }
+
+// ---- allocation-free variant ---------------------------------------------------------------
+// For callers that cannot allocate device memory: a host integrator whose device memory is owned
+// and budgeted by another runtime (the reference sizes its NL-PF scratch from the `vram` config key
+// and allocates every buffer through its own device layer), or a render loop that must not fail on
+// an allocation half-way through a frame. Their scratch lives in one fixed device array, reserved
+// when the library is loaded on a device and held until the process exits.
+namespace sty {
+namespace {
+constexpr size_t kNaMaxRecords = size_t(1) << 18;           // width * height * spp of the depth
+constexpr size_t kNaMaxPixels = size_t(1) << 16;            // width * height
+constexpr size_t kNaMaxBlocks = 4096;                       // 32 x 8 pixel tiles
+constexpr size_t kNaMaxLossBlocks = kNaMaxPixels / 256;
+constexpr size_t kNaOut = 0;                                // 3 * kNaMaxRecords floats
+constexpr size_t kNaDimg = kNaOut + 3 * kNaMaxRecords;      // 3 * kNaMaxPixels
+constexpr size_t kNaParts = kNaDimg + 3 * kNaMaxPixels;     // kNaMaxBlocks * 36
+constexpr size_t kNaLParts = kNaParts + kNaMaxBlocks * NG;  // kNaMaxLossBlocks
+constexpr size_t kNaLoss = kNaLParts + kNaMaxLossBlocks;    // 1 (padded)
+constexpr size_t kNaFloats = kNaLoss + 64;                  // 1,130,816 floats = 4.31 MiB
+
+// The scratch itself. Host code must not pass this name to a kernel: on the host it is only a
+// stand-in for the symbol; the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) float g_adjoint_scratch[kNaFloats];
+
+// Device address of g_adjoint_scratch on the current device, looked up once per device.
+sty_status noalloc_scratch(float **out) {
+    static std::atomic<float *> cache[64];
+    int dev = -1;
+    STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return STY_ERR_UNSUPPORTED;
+    }
+    float *p = cache[dev].load();
+    if (!p) {
+        void *addr = nullptr;
+        STY_TRY(check_cuda(cudaGetSymbolAddress(&addr, g_adjoint_scratch), "cudaGetSymbolAddress(adjoint scratch)"));
+        p = static_cast<float *>(addr);
+        cache[dev].store(p);
+    }
+    *out = p;
+    return STY_OK;
+}
+}  // namespace
+}  // namespace sty
+
+extern "C" sty_status sty_pf_adjoint_noalloc(const sty_pf_records *rec, uint32_t depth, int32_t radius,
+                                             const float prm[36], uint32_t n_steps, const float *in_next,
+                                             const float *target, float *grad, float *loss_out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(rec && prm && target && grad, "sty_pf_adjoint_noalloc: null argument");
+    STY_ARG_CHECK(n_steps >= 1 && n_steps <= 8, "n_steps must be in [1, 8]");
+    STY_ARG_CHECK(radius >= 0 && radius <= 32, "radius must be in [0, 32]");
+    STY_ARG_CHECK(prm[33] > 0.0f && prm[34] > 0.0f && prm[35] > 0.0f, "bandwidths must be > 0");
+    STY_ARG_CHECK(depth < (uint32_t)rec->depths, "depth out of range");
+    STY_ARG_CHECK(rec->spp == 1 || rec->spp == 2 || rec->spp == 4 || rec->spp == 8, "spp must be 1, 2, 4 or 8");
+    STY_ARG_CHECK(rec->width > 0 && rec->height > 0, "empty image");
+    const int Wd = rec->width, Hd = rec->height, S = rec->spp;
+    const size_t N = (size_t)Wd * Hd * S, npix = (size_t)Wd * Hd;
+    const int gx = (Wd + 31) / 32, gy = (Hd + 7) / 8;
+    const size_t nb = (size_t)gx * gy, lb = (npix + 255) / 256;
+    STY_ARG_CHECK(N <= kNaMaxRecords,
+                  "sty_pf_adjoint_noalloc: %zu records per depth exceed the fixed scratch limit of %zu "
+                  "(width * height * spp); use sty_pf_adjoint", N, kNaMaxRecords);
+    STY_ARG_CHECK(npix <= kNaMaxPixels,
+                  "sty_pf_adjoint_noalloc: %zu pixels exceed the fixed scratch limit of %zu; use sty_pf_adjoint",
+                  npix, kNaMaxPixels);
+    STY_ARG_CHECK(nb <= kNaMaxBlocks, "sty_pf_adjoint_noalloc: %zu tiles exceed the fixed scratch limit of %zu",
+                  nb, kNaMaxBlocks);
+    float *scratch = nullptr;
+    STY_TRY(noalloc_scratch(&scratch));
+    float *out = scratch + kNaOut, *dimg = scratch + kNaDimg, *parts = scratch + kNaParts;
+    float *lparts = scratch + kNaLParts, *lsum = scratch + kNaLoss;
+    cudaStream_t st = as_stream(stream);
+    sty_style_program prog;
+    memset(&prog, 0, sizeof(prog));
+    prog.n_nodes = 1;
+    sty_style_node &nd = prog.nodes[0];
+    nd.kind = STY_STYLE_RAMP_SMOOTH;
+    nd.depth_mask = 1u << (depth > 31 ? 31 : depth);
+    nd.n = (int32_t)n_steps;
+    nd.p[0] = prm[0];
+    for (uint32_t k = 0; k < n_steps; k++) {
+        nd.p[1 + k] = prm[1 + k];
+        for (int c = 0; c < 3; c++) nd.p[9 + 3 * k + c] = prm[9 + 3 * k + c];
+    }
+    sty_pf_screen_params sp = {radius, prm[33], prm[34], prm[35]};
+    // Every scratch region below is fully overwritten before it is read (no accumulation into
+    // scratch), so nothing has to be cleared between calls.
+    STY_TRY(sty_pf_screen_filter_depth(rec, depth, &sp, &prog, in_next, out, nullptr, stream));
+    k_img_loss<<<(unsigned)lb, 256, 0, st>>>(out, Wd, Hd, S, target, dimg, lparts);
+    STY_TRY(check_launch("k_img_loss"));
+    AdjArgs a;
+    for (int k = 0; k < 3; k++) {
+        a.pos[k] = rec->pos[k];
+        a.nrm[k] = rec->nrm[k];
+        a.rad[k] = rec->rad[k];
+        a.thr[k] = rec->thr[k];
+    }
+    a.valid = rec->valid;
+    a.in_next = in_next;
+    a.dimg = dimg;
+    a.W = Wd;
+    a.H = Hd;
+    a.R = radius;
+    a.depth = depth;
+    a.sx = prm[33];
+    a.sp = prm[34];
+    a.sn = prm[35];
+    a.s = prm[0];
+    for (int k = 0; k < 8; k++) {
+        a.t[k] = prm[1 + k];
+        for (int c = 0; c < 3; c++) a.c[k][c] = prm[9 + 3 * k + c];
+    }
+    a.nsteps = (int)n_steps;
+    a.partials = parts;
+    switch (S) {
+        case 1: STY_TRY(launch_adj<1>(a, st)); break;
+        case 2: STY_TRY(launch_adj<2>(a, st)); break;
+        case 4: STY_TRY(launch_adj<4>(a, st)); break;
+        default: STY_TRY(launch_adj<8>(a, st)); break;
+    }
+    k_reduce_partials<<<1, 64, 0, st>>>(parts, (int)nb, NG, grad);
+    STY_TRY(check_launch("k_reduce_partials"));
+    k_reduce_partials<<<1, 32, 0, st>>>(lparts, (int)lb, 1, lsum);
+    STY_TRY(check_launch("k_reduce_partials(loss)"));
+    if (loss_out) {
+        STY_TRY(check_cuda(cudaMemcpyAsync(loss_out, lsum, 4, cudaMemcpyDeviceToHost, st), "read loss"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync loss"));
+    }
+    return STY_OK;
+}
