@@ -38,6 +38,7 @@ def lib() -> C.CDLL:
         L.orc_pf_adjoint_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp, vp]
         L.orc_pf_adjoint_image_f64.restype = C.c_double
         L.orc_pf_adjoint_image_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
+        L.orc_closest_hit.argtypes = [vp, C.c_uint32, vp, C.c_uint64, vp, vp, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
@@ -144,6 +145,18 @@ def pf_adjoint(rec, depth, radius, params, n_steps, target, in_next=None):
     g = np.zeros(36, dtype=np.float64)
     loss = lib().orc_pf_adjoint_f64(C.addressof(rec), depth, radius, _p(prm), n_steps, _p(nxt), _p(tg), _p(g))
     return loss, g
+
+
+def closest_hit(tri_pos: np.ndarray, rays: np.ndarray):
+    """Brute-force closest hit: (prim [n] uint32, t [n], bary [n,2])."""
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float32).reshape(-1)
+    r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+    n = r.shape[0]
+    prim = np.zeros(n, dtype=np.uint32)
+    t = np.zeros(n, dtype=np.float32)
+    b = np.zeros((n, 2), dtype=np.float32)
+    lib().orc_closest_hit(_p(pos), pos.size // 9, _p(r), n, _p(prim), _p(t), _p(b))
+    return prim, t, b
 
 
 def num_threads() -> int:

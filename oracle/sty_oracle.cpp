@@ -643,3 +643,59 @@ extern "C" double orc_pf_adjoint_image_f64(const sty_pf_records *r, uint32_t dep
     std::copy(fw.img.begin(), fw.img.end(), img);
     return l;
 }
+
+// ---- closest hit by brute force (watertight ray/triangle test of Woop, Benthin and Wald 2013, the
+// published algorithm, in f32 with the double fallback on exact zeros); ties -> lowest id ----------
+extern "C" void orc_closest_hit(const float *pos, uint32_t n_tris, const float *rays, uint64_t n, uint32_t *prim,
+                                float *tout, float *bary) {
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const float *r = rays + 8 * i;
+        const float o[3] = {r[0], r[1], r[2]}, d[3] = {r[3], r[4], r[5]};
+        const float ax = std::fabs(d[0]), ay = std::fabs(d[1]), az = std::fabs(d[2]);
+        int kz = 0;
+        if (ay > ax) kz = 1;
+        if (az > (kz == 0 ? ax : ay)) kz = 2;
+        int kx = kz + 1 == 3 ? 0 : kz + 1, ky = kx + 1 == 3 ? 0 : kx + 1;
+        if (d[kz] < 0.0f) std::swap(kx, ky);
+        const float Sx = d[kx] / d[kz], Sy = d[ky] / d[kz], Sz = 1.0f / d[kz];
+        float best = r[7], bb1 = 0, bb2 = 0;
+        uint32_t bp = 0xffffffffu;
+        for (uint32_t t = 0; t < n_tris; t++) {
+            const float *p = pos + 9 * (size_t)t;
+            float A[3], B[3], C[3];
+            for (int a = 0; a < 3; a++) {
+                A[a] = p[a] - o[a];
+                B[a] = p[3 + a] - o[a];
+                C[a] = p[6 + a] - o[a];
+            }
+            const float Ax = A[kx] - Sx * A[kz], Ay = A[ky] - Sy * A[kz];
+            const float Bx = B[kx] - Sx * B[kz], By = B[ky] - Sy * B[kz];
+            const float Cx = C[kx] - Sx * C[kz], Cy = C[ky] - Sy * C[kz];
+            float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+            if (U == 0.0f || V == 0.0f || W == 0.0f) {
+                U = (float)((double)Cx * By - (double)Cy * Bx);
+                V = (float)((double)Ax * Cy - (double)Ay * Cx);
+                W = (float)((double)Bx * Ay - (double)By * Ax);
+            }
+            if ((U < 0 || V < 0 || W < 0) && (U > 0 || V > 0 || W > 0)) continue;
+            const float det = (U + V) + W;
+            if (det == 0.0f) continue;
+            const float Az = Sz * A[kz], Bz = Sz * B[kz], Cz = Sz * C[kz];
+            const float T = ((U * Az) + (V * Bz)) + (W * Cz);
+            const float tt = T / det;
+            if (!(tt > r[6])) continue;
+            if (tt > best || (tt == best && t >= bp)) continue;
+            best = tt;
+            bb1 = V / det;
+            bb2 = W / det;
+            bp = t;
+        }
+        prim[i] = bp;
+        if (tout) tout[i] = best;
+        if (bary) {
+            bary[2 * i] = bb1;
+            bary[2 * i + 1] = bb2;
+        }
+    }
+}

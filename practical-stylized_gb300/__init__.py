@@ -24,5 +24,6 @@ from .pf import (  # noqa: F401
 from . import synth  # noqa: F401
 from . import pf_ref  # noqa: F401
 from . import nrc  # noqa: F401
+from . import scene  # noqa: F401
 
 PKG_DIR = pathlib.Path(__file__).resolve().parent

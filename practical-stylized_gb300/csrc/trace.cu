@@ -1,0 +1,622 @@
+// trace.cu -- wavefront tracer and the end-to-end NL-PF render.
+//
+// k_trace restates one bounce of kernel_mk_trace (crates/akari_integrator/src/lm_path_filtering.rs:
+// 1063-1218) for every path slot: camera ray at depth 0 (camera/mod.rs:73-126, box pixel filter
+// film.rs:31-33), closest hit, emitter radiance with balance MIS against the light pdf
+// (handle_surface_light :388-426, mis_weight :305-316), stylization-flag update, NEE with the
+// light's style node applied at the next depth (sample_light :1261-1316, light/area.rs:51-132),
+// BSDF sampling (diffuse.rs:40-53, microfacet.rs:117-152) and the continuation ray
+// (offset_ray_origin, face_forward). Sampler draws follow the reference order: 2 for the camera,
+// then per bounce 3 for the light and 1 + 2 for the BSDF. Each depth's vertices are written as SoA
+// planes (sty_pf_vertices) that stay on the device; the record the reference's kernel_propagate
+// copies into the parent (wi = -wo, mis) is written into the parent depth's slot when the child
+// vertex is found.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "scene.cuh"
+#include "style.cuh"
+
+namespace sty {
+const sty_camera &scene_camera(const sty_scene *s);
+void scene_bounds(const sty_scene *s, float mn[3], float mx[3]);
+const std::vector<sty_scene_material> &scene_materials(const sty_scene *s);
+}  // namespace sty
+
+namespace sty {
+namespace {
+
+constexpr uint32_t NONE = 0xffffffffu;
+constexpr float kPi = 3.14159265358979323846f;
+
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3m(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 operator-(F3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 a, F3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ F3 normalize(F3 a) { return a * (1.0f / sqrtf(dot(a, a))); }
+
+__device__ __forceinline__ uint32_t pcg_next(sty_pcg32 &s) {
+    const uint64_t old = s.state;
+    s.state = old * 0x5851f42d4c957f2dULL + s.inc;
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    const uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+}
+// IndependentSampler::next_1d (sampler/mod.rs:208-212): u32 * (1 / u32::MAX as f32)
+__device__ __forceinline__ float next_1d(sty_pcg32 &s) { return (float)pcg_next(s) * 2.3283064e-10f; }
+
+// Wachter & Binder, "A Fast and Robust Method for Avoiding Self-Intersection" (Ray Tracing Gems,
+// ch. 6): offset along the normal in integer ulps, absolute offset near the origin.
+__device__ __forceinline__ F3 offset_ray_origin(F3 p, F3 n) {
+    const float origin = 1.0f / 32.0f, float_scale = 1.0f / 65536.0f, int_scale = 256.0f;
+    const float pv[3] = {p.x, p.y, p.z}, nv[3] = {n.x, n.y, n.z};
+    float o[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const int of = (int)(int_scale * nv[a]);
+        const float pi = __int_as_float(__float_as_int(pv[a]) + (pv[a] < 0.0f ? -of : of));
+        o[a] = fabsf(pv[a]) < origin ? pv[a] + float_scale * nv[a] : pi;
+    }
+    return {o[0], o[1], o[2]};
+}
+__device__ __forceinline__ F3 face_forward(F3 n, F3 v) { return dot(n, v) < 0.0f ? -n : n; }
+
+// Frame::from_n (geometry.rs:163-171)
+struct Frame {
+    F3 t, s, n;
+};
+__device__ __forceinline__ Frame frame_from_n(F3 n) {
+    F3 t;
+    if (fabsf(n.x) > fabsf(n.y))
+        t = f3m(-n.z, 0.0f, n.x) * (1.0f / sqrtf(n.x * n.x + n.z * n.z));
+    else
+        t = f3m(0.0f, n.z, -n.y) * (1.0f / sqrtf(n.y * n.y + n.z * n.z));
+    return {t, cross(n, t), n};
+}
+__device__ __forceinline__ F3 to_local(const Frame &f, F3 v) { return {dot(f.t, v), dot(f.s, v), dot(f.n, v)}; }
+__device__ __forceinline__ F3 to_world(const Frame &f, F3 v) { return f.t * v.x + f.s * v.y + f.n * v.z; }
+
+__device__ __forceinline__ float2 uniform_sample_disk(float u0, float u1) {  // sampling.rs:5-9
+    const float r = sqrtf(u0), phi = u1 * 2.0f * kPi;
+    return make_float2(r * cosf(phi), r * sinf(phi));
+}
+__device__ __forceinline__ float2 uniform_sample_triangle(float u0, float u1) {  // sampling.rs:32-44
+    if (u0 < u1) {
+        const float b0 = u0 / 2.0f;
+        return make_float2(b0, u1 - b0);
+    }
+    const float b1 = u1 / 2.0f;
+    return make_float2(u0 - b1, b1);
+}
+
+__device__ __forceinline__ uint32_t style_index(uint32_t f) {
+    uint32_t i = 0;
+    if (f & 2u) i = 1;
+    if (f & 4u) i = 2;
+    if (f & 8u) i = 3;
+    return i;
+}
+
+// ---- BSDF (same forms as pf_ref.cu's evaluation; sampling restated here) --------------------
+__device__ __forceinline__ bool wo_wi_valid(F3 ns, F3 ng, F3 wo, F3 wi) {
+    auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
+    const float fl = sgn(dot(ng, ns));
+    return sgn(fl * dot(wo, ns)) * sgn(dot(wo, ng)) > 0.0f && sgn(fl * dot(wi, ns)) * sgn(dot(wi, ng)) > 0.0f;
+}
+__device__ __forceinline__ float tr_d(float ch, float a) {
+    const float c2 = ch * ch, s2 = fmaxf(0.0f, 1.0f - c2);
+    const float tan2 = s2 / c2, e = tan2 / (a * a);
+    const float inv_d = kPi * a * a * c2 * c2 * (1.0f + e) * (1.0f + e);
+    if (!isfinite(tan2) || !isfinite(inv_d) || inv_d == 0.0f) return 0.0f;
+    return 1.0f / inv_d;
+}
+__device__ __forceinline__ float tr_lambda(float cw, float a) {
+    const float c2 = cw * cw, s2 = fmaxf(0.0f, 1.0f - c2);
+    const float at = fabsf(sqrtf(s2) / cw);
+    const float l = (-1.0f + sqrtf(1.0f + a * a * at * at)) * 0.5f;
+    return isfinite(at) ? l : 0.0f;
+}
+__device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi) {
+    if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
+    const float co = dot(wo, ns), ci = dot(wi, ns);
+    if (m.kind == STY_MAT_DIFFUSE) return co * ci >= 0.0f ? fabsf(ci) / kPi : 0.0f;
+    const float a = fmaxf(m.alpha, 1e-4f);
+    F3 wh = wo + wi;
+    if (dot(wh, wo) * dot(wi, wh) < 0.0f || (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) || ci == 0.0f ||
+        co == 0.0f || !(co * ci >= 0.0f))
+        return 0.0f;
+    wh = normalize(wh);
+    const float d = tr_d(dot(wh, ns), a), g1 = 1.0f / (1.0f + tr_lambda(co, a));
+    const float owh = fabsf(dot(wo, wh));
+    return d * g1 * owh / fabsf(co) / (4.0f * owh);
+}
+// Surface::sample: wi (world) and its pdf (0 = invalid)
+__device__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, float u_sel, float u0, float u1,
+                          float *pdf) {
+    (void)u_sel;
+    const Frame fr = frame_from_n(ns);
+    const F3 wol = to_local(fr, wo);
+    F3 wil;
+    bool valid = true;
+    if (m.kind == STY_MAT_DIFFUSE) {  // cos_sample_hemisphere, flipped into wo's hemisphere
+        const float2 d = uniform_sample_disk(u0, u1);
+        const float z = sqrtf(fmaxf(1.0f - d.x * d.x - d.y * d.y, 0.0f));
+        wil = f3m(d.x, d.y, z);
+        if (!(wol.z * wil.z >= 0.0f)) wil = -wil;
+    } else {  // visible-normal sampling (microfacet.rs:117-152) + reflect
+        const float a = fmaxf(m.alpha, 1e-4f);
+        F3 wh = normalize(f3m(a * wol.x, a * wol.y, wol.z));
+        if (wh.z < 0.0f) wh = -wh;
+        const F3 t1 = wh.z < 0.99999f ? normalize(cross(f3m(0.0f, 0.0f, 1.0f), wh)) : f3m(1.0f, 0.0f, 0.0f);
+        const F3 t2 = normalize(cross(wh, t1));
+        float2 p = uniform_sample_disk(u0, u1);
+        const float h = sqrtf(1.0f - p.x * p.x);
+        p.y = h + (p.y - h) * ((1.0f + wh.z) * 0.5f);
+        const float pz = sqrtf(fmaxf(1.0f - (p.x * p.x + p.y * p.y), 0.0f));
+        const F3 nh = t1 * p.x + t2 * p.y + wh * pz;
+        wh = normalize(f3m(a * nh.x, a * nh.y, fmaxf(nh.z, 1e-6f)));
+        wil = wh * (2.0f * dot(wol, wh)) - wol;
+        valid = wol.z * wil.z >= 0.0f;
+    }
+    const F3 wi = to_world(fr, wil);
+    valid = valid && wo_wi_valid(ns, ng, wo, wi);
+    *pdf = valid ? bsdf_pdf(m, ns, ng, wo, wi) : 0.0f;
+    return wi;
+}
+
+// ---- per-path state (SoA) and per-depth vertex planes ---------------------------------------
+struct PathState {
+    float *o[3], *d[3];
+    float *prev_p[3];
+    float *prev_pdf;
+    uint32_t *flags, *exclude, *terminated;
+};
+struct VertOut {  // mutable view of one depth's sty_pf_vertices planes
+    int32_t *active;
+    float *p[3], *wo[3], *ns[3], *ng[3], *le[3], *mis, *dir_wi[3], *dir_l[3], *dir_pdf, *ind_wi[3], *ind_mis;
+    uint32_t *flags, *material;
+};
+struct CamArgs {
+    float eye[3], fwd[3], right[3], up[3];
+    float tan_half, aspect, radius;
+    uint32_t W, H;
+};
+
+__global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t depth, uint32_t max_depth,
+                        PathState ps, VertOut v, VertOut parent, sty_pcg32 *rng, const sty_style_program *progs,
+                        uint32_t n_progs, unsigned long long *vcount) {
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid >= n_paths) return;
+    sty_pcg32 st = rng[tid];
+    F3 ro, rd;
+    uint32_t flags, exclude;
+    float prev_pdf;
+    F3 prev_p;
+    if (depth == 0) {
+        const uint32_t npx = cam.W * cam.H, px = tid % npx;
+        const float fx = (float)(px % cam.W) + 0.5f, fy = (float)(px / cam.W) + 0.5f;
+        const float u0 = next_1d(st), u1 = next_1d(st);
+        const float ox = (u0 - 0.5f) * cam.radius, oy = (u1 - 0.5f) * cam.radius;
+        const float sx = (2.0f * (fx + ox) / (float)cam.W - 1.0f) * cam.tan_half * cam.aspect;
+        const float sy = (1.0f - 2.0f * (fy + oy) / (float)cam.H) * cam.tan_half;
+        const F3 fwd = f3m(cam.fwd[0], cam.fwd[1], cam.fwd[2]), rt = f3m(cam.right[0], cam.right[1], cam.right[2]),
+                 up = f3m(cam.up[0], cam.up[1], cam.up[2]);
+        ro = f3m(cam.eye[0], cam.eye[1], cam.eye[2]);
+        rd = normalize(fwd + rt * sx + up * sy);
+        flags = 0;
+        exclude = NONE;
+        prev_pdf = 0.0f;
+        prev_p = ro;
+        ps.terminated[tid] = 0;
+    } else {
+        if (ps.terminated[tid]) return;
+        ro = f3m(ps.o[0][tid], ps.o[1][tid], ps.o[2][tid]);
+        rd = f3m(ps.d[0][tid], ps.d[1][tid], ps.d[2][tid]);
+        flags = ps.flags[tid];
+        exclude = ps.exclude[tid];
+        prev_pdf = ps.prev_pdf[tid];
+        prev_p = f3m(ps.prev_p[0][tid], ps.prev_p[1][tid], ps.prev_p[2][tid]);
+    }
+    const float o3[3] = {ro.x, ro.y, ro.z}, d3[3] = {rd.x, rd.y, rd.z};
+    const Hit h = trace_closest(sc, o3, d3, 0.0f, 1e20f, exclude);
+    if (h.prim == NONE) {
+        ps.terminated[tid] = 1;
+        rng[tid] = st;
+        return;
+    }
+    atomicAdd(vcount, 1ull);
+    const uint32_t prim = h.prim;
+    const float *tp = sc.tri_pos + 9 * (size_t)prim;
+    const float b0 = 1.0f - h.b1 - h.b2;
+    const F3 p = f3m(b0 * tp[0] + h.b1 * tp[3] + h.b2 * tp[6], b0 * tp[1] + h.b1 * tp[4] + h.b2 * tp[7],
+                     b0 * tp[2] + h.b1 * tp[5] + h.b2 * tp[8]);
+    const F3 ng = f3m(sc.tri_normal[3 * prim], sc.tri_normal[3 * prim + 1], sc.tri_normal[3 * prim + 2]);
+    const F3 ns = ng;
+    const F3 wo = -rd;
+    const uint32_t mi = sc.tri_material[prim];
+    const sty_scene_material m = sc.materials[mi];
+    // emitter (handle_surface_light)
+    F3 le = f3m(0.0f, 0.0f, 0.0f);
+    float mis = 1.0f;
+    const bool emitter = m.emission[0] > 0.0f || m.emission[1] > 0.0f || m.emission[2] > 0.0f;
+    if (emitter) {
+        if (dot(ng, rd) < 0.0f) le = f3m(m.emission[0], m.emission[1], m.emission[2]);
+        if (depth > 0) {
+            // light pdf of this point from prev_p (pdf_direct, light/area.rs:108-130)
+            float sel = 0.0f;
+            for (uint32_t k = 0; k < sc.n_lights; k++)
+                if (sc.light_tris[k] == prim) sel = sc.light_cdf[k + 1] - sc.light_cdf[k];
+            const F3 w = p - prev_p;
+            const float dist2 = dot(w, w);
+            const F3 wn = w * (1.0f / sqrtf(dist2));
+            const float lpdf = sel / sc.tri_area[prim] * dist2 / fmaxf(fabsf(dot(ng, wn)), 1e-6f);
+            mis = prev_pdf / (prev_pdf + lpdf);
+        }
+    }
+    // stylization flags (update_stylization_flags via sty_set_idx)
+    uint32_t new_flags = flags;
+    if (m.set_style >= 0) {
+        new_flags &= 1u;
+        if (m.set_style == 1) new_flags |= 2u;
+        if (m.set_style == 2) new_flags |= 4u;
+        if (m.set_style == 3) new_flags |= 8u;
+    }
+    v.active[tid] = 1;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float pa = a == 0 ? p.x : a == 1 ? p.y : p.z;
+        v.p[a][tid] = pa;
+    }
+    v.wo[0][tid] = wo.x; v.wo[1][tid] = wo.y; v.wo[2][tid] = wo.z;
+    v.ns[0][tid] = ns.x; v.ns[1][tid] = ns.y; v.ns[2][tid] = ns.z;
+    v.ng[0][tid] = ng.x; v.ng[1][tid] = ng.y; v.ng[2][tid] = ng.z;
+    v.le[0][tid] = le.x; v.le[1][tid] = le.y; v.le[2][tid] = le.z;
+    v.mis[tid] = mis;
+    v.flags[tid] = new_flags;
+    v.material[tid] = mi;
+    v.dir_pdf[tid] = 0.0f;
+    v.dir_wi[0][tid] = v.dir_wi[1][tid] = v.dir_wi[2][tid] = 0.0f;
+    v.dir_l[0][tid] = v.dir_l[1][tid] = v.dir_l[2][tid] = 0.0f;
+    v.ind_wi[0][tid] = v.ind_wi[1][tid] = v.ind_wi[2][tid] = 0.0f;
+    v.ind_mis[tid] = 0.0f;
+    if (depth > 0) {  // the parent's indirect record: wi = -wo, mis (kernel_filter :1043-1047)
+        parent.ind_wi[0][tid] = rd.x;
+        parent.ind_wi[1][tid] = rd.y;
+        parent.ind_wi[2][tid] = rd.z;
+        parent.ind_mis[tid] = mis;
+    }
+    if (depth >= max_depth) {
+        ps.terminated[tid] = 1;
+        rng[tid] = st;
+        return;
+    }
+    // NEE (sample_light)
+    {
+        const float ux = next_1d(st), uy = next_1d(st), uz = next_1d(st);
+        if (sc.n_lights > 0) {
+            uint32_t lo = 0, hi = sc.n_lights - 1;
+            while (lo < hi) {  // first k with cdf[k+1] > ux
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sc.light_cdf[mid + 1] > ux) hi = mid;
+                else lo = mid + 1;
+            }
+            const uint32_t lt = sc.light_tris[lo];
+            const float sel = sc.light_cdf[lo + 1] - sc.light_cdf[lo];
+            const float2 bb = uniform_sample_triangle(uy, uz);
+            const float *lp = sc.tri_pos + 9 * (size_t)lt;
+            const float c0 = 1.0f - bb.x - bb.y;
+            const F3 q = f3m(c0 * lp[0] + bb.x * lp[3] + bb.y * lp[6], c0 * lp[1] + bb.x * lp[4] + bb.y * lp[7],
+                             c0 * lp[2] + bb.x * lp[5] + bb.y * lp[8]);
+            const F3 ln = f3m(sc.tri_normal[3 * lt], sc.tri_normal[3 * lt + 1], sc.tri_normal[3 * lt + 2]);
+            F3 wi = q - p;
+            const float dist2 = dot(wi, wi);
+            if (dist2 > 0.0f) {
+                const float dist = sqrtf(dist2);
+                wi = wi * (1.0f / dist);
+                const sty_scene_material lm = sc.materials[sc.tri_material[lt]];
+                f3 li = {0.0f, 0.0f, 0.0f};
+                if (dot(wi, ln) < 0.0f) li = {lm.emission[0], lm.emission[1], lm.emission[2]};
+                const float lpdf = sel / sc.tri_area[lt] * dist2 / fabsf(dot(ln, wi));
+                if (isfinite(lpdf) && lpdf > 0.0f) {
+                    // the light's style node at the next depth (sample_light :1286-1305)
+                    if (!(new_flags & 1u)) {
+                        const int32_t pi = lm.style[style_index(new_flags)];
+                        if (pi >= 0 && (uint32_t)pi < n_progs) li = style_apply(progs[pi], depth + 1, li);
+                    }
+                    const F3 so = offset_ray_origin(p, face_forward(ng, wi));
+                    const float s3[3] = {so.x, so.y, so.z}, w3[3] = {wi.x, wi.y, wi.z};
+                    if (!trace_any(sc, s3, w3, 0.0f, dist * (1.0f - 1e-3f), prim, lt)) {
+                        v.dir_wi[0][tid] = wi.x;
+                        v.dir_wi[1][tid] = wi.y;
+                        v.dir_wi[2][tid] = wi.z;
+                        v.dir_l[0][tid] = li.x;
+                        v.dir_l[1][tid] = li.y;
+                        v.dir_l[2][tid] = li.z;
+                        v.dir_pdf[tid] = lpdf;
+                    }
+                }
+            }
+        }
+    }
+    // BSDF sample and continuation
+    const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
+    float pdf = 0.0f;
+    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf);
+    if (pdf > 0.0f) {
+        const F3 no = offset_ray_origin(p, face_forward(ng, wi));
+        ps.o[0][tid] = no.x; ps.o[1][tid] = no.y; ps.o[2][tid] = no.z;
+        ps.d[0][tid] = wi.x; ps.d[1][tid] = wi.y; ps.d[2][tid] = wi.z;
+        ps.prev_p[0][tid] = p.x; ps.prev_p[1][tid] = p.y; ps.prev_p[2][tid] = p.z;
+        ps.prev_pdf[tid] = pdf;
+        ps.flags[tid] = new_flags;
+        ps.exclude[tid] = prim;
+    } else {
+        ps.terminated[tid] = 1;
+    }
+    rng[tid] = st;
+}
+
+// splat + first-hit stylization + film (kernel_splat / kernel_update_film, :429-506)
+__global__ void k_splat(uint32_t npx, uint32_t branch, const float *out0, VertOut v0, const sty_scene_material *mats,
+                        const sty_style_program *progs, uint32_t n_progs, int no_first_hit, double weight,
+                        double *film) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npx) return;
+    const size_t n = (size_t)npx * branch;
+    f3 sum = {0.0f, 0.0f, 0.0f};
+    for (uint32_t b = 0; b < branch; b++) {
+        const size_t i = (size_t)b * npx + px;
+        if (!v0.active[i]) continue;
+        sum.x += out0[i];
+        sum.y += out0[n + i];
+        sum.z += out0[2 * n + i];
+    }
+    const float sc = 1.0f / (float)branch;
+    const f3 mean = {sum.x * sc, sum.y * sc, sum.z * sc};
+    double acc[3] = {0, 0, 0};
+    uint32_t cnt = 0;
+    for (uint32_t b = 0; b < branch; b++) {
+        const size_t i = (size_t)b * npx + px;
+        if (!v0.active[i]) continue;
+        f3 c = mean;
+        if (!no_first_hit) {
+            // the path's flags before its first hit are all clear: style index 0
+            const int32_t pi = mats[v0.material[i]].style[0];
+            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c);
+        }
+        acc[0] += c.x;
+        acc[1] += c.y;
+        acc[2] += c.z;
+        cnt++;
+    }
+    if (cnt)
+        for (int c = 0; c < 3; c++) film[3 * (size_t)px + c] += weight * acc[c] / cnt;
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+// Pcg32::new_seq_offset(i, seed_i) with seed_i = splitmix64(seed + i) (the reference draws seed_i
+// from rand's StdRng, sampler/mod.rs:157-173)
+__global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sty_pcg32 g;
+    g.state = 0;
+    g.inc = ((uint64_t)i << 1) | 1ull;
+    pcg_next(g);
+    g.state += splitmix64(seed + i);
+    pcg_next(g);
+    rng[i] = g;
+}
+
+}  // namespace
+}  // namespace sty
+
+using namespace sty;
+
+extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *cfg,
+                                    const sty_style_program *programs, uint32_t n_programs, double *film,
+                                    uint64_t *vertex_count, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && cfg && film, "sty_pf_render: null argument");
+    STY_ARG_CHECK(cfg->branch >= 1 && cfg->repeats >= 1 && cfg->max_depth <= 30, "bad branch / repeats / max_depth");
+    STY_ARG_CHECK(cfg->n_radius_scale >= 1 && cfg->n_radius_scale <= 16 && cfg->n_reuse >= 1 && cfg->n_reuse <= 16,
+                  "radius_scale and reuse need 1..16 entries");
+    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
+    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
+    cudaStream_t st = as_stream(stream);
+    const sty_camera &cam = scene_camera(scene);
+    const uint32_t npx = cam.width * cam.height;
+    const uint64_t np64 = (uint64_t)npx * cfg->branch;
+    STY_ARG_CHECK(np64 < (1ull << 31), "too many paths");
+    const uint32_t n = (uint32_t)np64, D = cfg->max_depth + 1;
+    // camera basis (look-at)
+    CamArgs ca;
+    {
+        float f[3], r[3], u[3];
+        for (int a = 0; a < 3; a++) f[a] = cam.target[a] - cam.eye[a];
+        float l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+        for (int a = 0; a < 3; a++) f[a] /= l;
+        r[0] = f[1] * cam.up[2] - f[2] * cam.up[1];
+        r[1] = f[2] * cam.up[0] - f[0] * cam.up[2];
+        r[2] = f[0] * cam.up[1] - f[1] * cam.up[0];
+        l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+        for (int a = 0; a < 3; a++) r[a] /= l;
+        u[0] = r[1] * f[2] - r[2] * f[1];
+        u[1] = r[2] * f[0] - r[0] * f[2];
+        u[2] = r[0] * f[1] - r[1] * f[0];
+        for (int a = 0; a < 3; a++) {
+            ca.eye[a] = cam.eye[a];
+            ca.fwd[a] = f[a];
+            ca.right[a] = r[a];
+            ca.up[a] = u[a];
+        }
+        ca.tan_half = std::tan(cam.fov_y * 0.5f * 3.14159265358979f / 180.0f);
+        ca.aspect = (float)cam.width / (float)cam.height;
+        ca.radius = cam.filter_radius;
+        ca.W = cam.width;
+        ca.H = cam.height;
+    }
+    // device scratch of this render
+    const size_t vfloats = 30;  // planes per depth: active, 27 float planes, flags, material
+    std::vector<void *> owned;
+    sty_status s = STY_OK;
+    auto alloc = [&](size_t bytes, const char *what) -> void * {
+        void *p = nullptr;
+        if (s == STY_OK) s = check_cuda(cudaMalloc(&p, bytes), what);
+        if (p) owned.push_back(p);
+        return p;
+    };
+    float *verts = (float *)alloc((size_t)D * vfloats * n * 4, "alloc vertices");
+    float *outs = (float *)alloc((size_t)D * 3 * n * 4, "alloc outputs");
+    float *psb = (float *)alloc((size_t)13 * n * 4, "alloc path state");
+    sty_pcg32 *rng = (sty_pcg32 *)alloc((size_t)n * sizeof(sty_pcg32), "alloc rng");
+    sty_style_program *dprog = (sty_style_program *)alloc(64 * sizeof(sty_style_program), "alloc programs");
+    unsigned long long *vc = (unsigned long long *)alloc(8, "alloc counter");
+    sty_pf_ref_ctx *ctx = nullptr;
+    if (s == STY_OK) s = sty_pf_ref_create(n, 1u << 26, &ctx);
+    auto cleanup = [&]() {
+        if (ctx) sty_pf_ref_destroy(ctx);
+        for (void *p : owned) cudaFree(p);
+    };
+    if (s != STY_OK) {
+        cleanup();
+        return s;
+    }
+    if (n_programs)
+        s = check_cuda(cudaMemcpyAsync(dprog, programs, n_programs * sizeof(sty_style_program), cudaMemcpyHostToDevice, st),
+                       "upload programs");
+    if (s == STY_OK) s = check_cuda(cudaMemsetAsync(vc, 0, 8, st), "zero counter");
+    // views
+    std::vector<VertOut> vo(D);
+    std::vector<sty_pf_vertices> vin(D);
+    for (uint32_t d = 0; d < D; d++) {
+        float *b = verts + (size_t)d * vfloats * n;
+        int k = 0;
+        auto pl = [&]() { return b + (size_t)(k++) * n; };
+        VertOut &w = vo[d];
+        w.active = (int32_t *)pl();
+        for (int a = 0; a < 3; a++) w.p[a] = pl();
+        for (int a = 0; a < 3; a++) w.wo[a] = pl();
+        for (int a = 0; a < 3; a++) w.ns[a] = pl();
+        for (int a = 0; a < 3; a++) w.ng[a] = pl();
+        for (int a = 0; a < 3; a++) w.le[a] = pl();
+        w.mis = pl();
+        for (int a = 0; a < 3; a++) w.dir_wi[a] = pl();
+        for (int a = 0; a < 3; a++) w.dir_l[a] = pl();
+        w.dir_pdf = pl();
+        for (int a = 0; a < 3; a++) w.ind_wi[a] = pl();
+        w.ind_mis = pl();
+        w.flags = (uint32_t *)pl();
+        w.material = (uint32_t *)pl();
+        sty_pf_vertices &r = vin[d];
+        r.active = w.active;
+        for (int a = 0; a < 3; a++) {
+            r.p[a] = w.p[a];
+            r.wo[a] = w.wo[a];
+            r.ns[a] = w.ns[a];
+            r.ng[a] = w.ng[a];
+            r.le[a] = w.le[a];
+            r.dir_wi[a] = w.dir_wi[a];
+            r.dir_l[a] = w.dir_l[a];
+            r.ind_wi[a] = w.ind_wi[a];
+        }
+        r.mis = w.mis;
+        r.dir_pdf = w.dir_pdf;
+        r.ind_mis = w.ind_mis;
+        r.flags = w.flags;
+        r.material = w.material;
+        r.n = n;
+    }
+    PathState ps;
+    {
+        int k = 0;
+        auto pl = [&]() { return psb + (size_t)(k++) * n; };
+        for (int a = 0; a < 3; a++) ps.o[a] = pl();
+        for (int a = 0; a < 3; a++) ps.d[a] = pl();
+        for (int a = 0; a < 3; a++) ps.prev_p[a] = pl();
+        ps.prev_pdf = pl();
+        ps.flags = (uint32_t *)pl();
+        ps.exclude = (uint32_t *)pl();
+        ps.terminated = (uint32_t *)pl();
+    }
+    const auto &mh = scene_materials(scene);
+    std::vector<sty_pf_material> pm(mh.size());
+    for (size_t i = 0; i < mh.size(); i++) {
+        pm[i].kind = mh[i].kind;
+        for (int c = 0; c < 3; c++) pm[i].albedo[c] = mh[i].albedo[c];
+        pm[i].alpha = mh[i].alpha;
+        for (int c = 0; c < 4; c++) pm[i].style[c] = mh[i].style[c];
+    }
+    float bmin[3], bmax[3];
+    scene_bounds(scene, bmin, bmax);
+    if (cfg->has_scene_bounds)
+        for (int a = 0; a < 3; a++) {
+            bmin[a] = cfg->scene_bounds[a];
+            bmax[a] = cfg->scene_bounds[3 + a];
+        }
+    const float avg = ((bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) + (bmax[2] - bmin[2])) / 3.0f;
+    const SceneView sv = scene_view(scene);
+    const unsigned nb = (n + 255) / 256;
+    if (s == STY_OK) {
+        k_rng_init<<<nb, 256, 0, st>>>(n, cfg->seed, rng);
+        s = check_launch("k_rng_init");
+    }
+    for (uint32_t rep = 0; rep < cfg->repeats && s == STY_OK; rep++) {
+        s = check_cuda(cudaMemsetAsync(verts, 0, (size_t)D * vfloats * n * 4, st), "reset vertices");
+        for (uint32_t d = 0; d < D && s == STY_OK; d++) {
+            k_trace<<<nb, 256, 0, st>>>(sv, ca, n, d, cfg->max_depth, ps, vo[d], vo[d > 0 ? d - 1 : 0], rng, dprog,
+                                        n_programs, vc);
+            s = check_launch("k_trace");
+        }
+        for (int d = (int)D - 1; d >= 0 && s == STY_OK; d--) {
+            sty_pf_ref_params prm;
+            memset(&prm, 0, sizeof(prm));
+            prm.depth = (uint32_t)d;
+            const float rs = cfg->radius_scale[std::min<uint32_t>((uint32_t)d, cfg->n_radius_scale - 1)];
+            prm.radius = avg * 0.01f * rs;
+            prm.reuse = cfg->reuse[std::min<uint32_t>((uint32_t)d, cfg->n_reuse - 1)];
+            prm.smis = cfg->smis;
+            prm.cluster = cfg->cluster;
+            prm.disable_flag_check = cfg->disable_flag_check;
+            prm.no_first_hit_stylization = cfg->no_first_hit_stylization;
+            prm.table_size = 1u << 26;
+            for (int a = 0; a < 3; a++) {
+                prm.pmin[a] = bmin[a];
+                prm.pmax[a] = bmax[a];
+            }
+            prm.max_cluster_rounds = 64;
+            const float *next = (uint32_t)d + 1 < D ? outs + (size_t)(d + 1) * 3 * n : nullptr;
+            s = sty_pf_ref_filter(ctx, &vin[d], next, &prm, pm.data(), (uint32_t)pm.size(), programs, n_programs, rng,
+                                  outs + (size_t)d * 3 * n, nullptr, nullptr, stream);
+        }
+        if (s == STY_OK) {
+            k_splat<<<(npx + 255) / 256, 256, 0, st>>>(npx, cfg->branch, outs, vo[0], sv.materials, dprog, n_programs,
+                                                       cfg->no_first_hit_stylization, 1.0 / cfg->repeats, film);
+            s = check_launch("k_splat");
+        }
+    }
+    if (s == STY_OK && vertex_count) {
+        unsigned long long h = 0;
+        s = check_cuda(cudaMemcpyAsync(&h, vc, 8, cudaMemcpyDeviceToHost, st), "read vertex count");
+        if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
+        *vertex_count = h;
+    }
+    if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
+    cleanup();
+    return s;
+}

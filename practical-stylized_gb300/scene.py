@@ -1,0 +1,182 @@
+"""Scenes, the wavefront tracer and the end-to-end NL-PF render (sty_scene_*, sty_pf_render).
+
+Procedural scenes stand in for the reference's scene files (its teaser geometry is not
+available): the Cornell box of the plain NL-PF workload and an emissive "furnace" box whose
+radiance is known in closed form.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .abi import check, lib
+
+MAT_DIFFUSE = 0
+MAT_GGX = 1
+
+
+class SceneMaterial(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("albedo", C.c_float * 3), ("alpha", C.c_float), ("emission", C.c_float * 3),
+                ("style", C.c_int32 * 4), ("set_style", C.c_int32)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("fov_y", C.c_float),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("filter_radius", C.c_float)]
+
+
+class RenderConfig(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("branch", C.c_uint32), ("repeats", C.c_uint32),
+                ("radius_scale", C.c_float * 16), ("n_radius_scale", C.c_uint32), ("reuse", C.c_uint32 * 16),
+                ("n_reuse", C.c_uint32), ("smis", C.c_int32), ("cluster", C.c_int32),
+                ("disable_flag_check", C.c_int32), ("no_first_hit_stylization", C.c_int32),
+                ("has_scene_bounds", C.c_int32), ("scene_bounds", C.c_float * 6), ("seed", C.c_uint64)]
+
+
+def material(kind=MAT_DIFFUSE, albedo=(0.75, 0.75, 0.75), alpha=0.3, emission=(0, 0, 0), style=(-1, -1, -1, -1),
+             set_style=-1) -> SceneMaterial:
+    m = SceneMaterial()
+    m.kind = kind
+    m.albedo[:] = list(albedo)
+    m.alpha = alpha
+    m.emission[:] = list(emission)
+    m.style[:] = list(style)
+    m.set_style = set_style
+    return m
+
+
+def camera(eye, target, up=(0, 1, 0), fov_y=40.0, width=256, height=256, filter_radius=1.0) -> Camera:
+    c = Camera()
+    c.eye[:] = list(eye)
+    c.target[:] = list(target)
+    c.up[:] = list(up)
+    c.fov_y, c.width, c.height, c.filter_radius = fov_y, width, height, filter_radius
+    return c
+
+
+def render_config(max_depth=5, branch=16, repeats=1, radius_scale=(5.0,), reuse=(64,), smis=True, cluster=False,
+                  disable_flag_check=False, no_first_hit_stylization=False, scene_bounds=None, seed=0) -> RenderConfig:
+    c = RenderConfig()
+    c.max_depth, c.branch, c.repeats = max_depth, branch, repeats
+    for i, v in enumerate(radius_scale):
+        c.radius_scale[i] = v
+    c.n_radius_scale = len(radius_scale)
+    for i, v in enumerate(reuse):
+        c.reuse[i] = v
+    c.n_reuse = len(reuse)
+    c.smis, c.cluster = int(smis), int(cluster)
+    c.disable_flag_check, c.no_first_hit_stylization = int(disable_flag_check), int(no_first_hit_stylization)
+    if scene_bounds is not None:
+        c.has_scene_bounds = 1
+        c.scene_bounds[:] = list(scene_bounds[0]) + list(scene_bounds[1])
+    c.seed = seed
+    return c
+
+
+def _quad(a, b, c, d):
+    """Two triangles (a, b, c), (a, c, d); counter-clockwise seen from the normal side."""
+    return [a + b + c, a + c + d]
+
+
+def _box(lo, hi):
+    x0, y0, z0 = lo
+    x1, y1, z1 = hi
+    p = lambda x, y, z: [x, y, z]  # noqa: E731
+    tris = []
+    tris += _quad(p(x0, y0, z1), p(x1, y0, z1), p(x1, y1, z1), p(x0, y1, z1))  # +z
+    tris += _quad(p(x1, y0, z0), p(x0, y0, z0), p(x0, y1, z0), p(x1, y1, z0))  # -z
+    tris += _quad(p(x1, y0, z1), p(x1, y0, z0), p(x1, y1, z0), p(x1, y1, z1))  # +x
+    tris += _quad(p(x0, y0, z0), p(x0, y0, z1), p(x0, y1, z1), p(x0, y1, z0))  # -x
+    tris += _quad(p(x0, y1, z1), p(x1, y1, z1), p(x1, y1, z0), p(x0, y1, z0))  # +y
+    tris += _quad(p(x0, y0, z0), p(x1, y0, z0), p(x1, y0, z1), p(x0, y0, z1))  # -y
+    return tris
+
+
+def cornell_box(width=256, height=256, style=(-1, -1, -1, -1), light_style=(-1, -1, -1, -1)):
+    """Unit Cornell box (y up, open towards +z): 5 diffuse walls (albedo 0.75 grey, left
+    0.63/0.065/0.05, right 0.14/0.45/0.09), two axis-aligned boxes of 12 triangles, one 0.25 x 0.25
+    area light of radiance 17 under the ceiling. Returns (positions [n, 9], material ids, materials,
+    camera)."""
+    P = lambda x, y, z: [x, y, z]  # noqa: E731
+    tris, mids = [], []
+
+    def add(ts, m):
+        tris.extend(ts)
+        mids.extend([m] * len(ts))
+
+    add(_quad(P(0, 0, 1), P(1, 0, 1), P(1, 0, 0), P(0, 0, 0)), 0)  # floor (normal +y)
+    add(_quad(P(0, 1, 0), P(1, 1, 0), P(1, 1, 1), P(0, 1, 1)), 0)  # ceiling (normal -y)
+    add(_quad(P(0, 0, 0), P(1, 0, 0), P(1, 1, 0), P(0, 1, 0)), 0)  # back wall (normal +z)
+    add(_quad(P(0, 0, 1), P(0, 0, 0), P(0, 1, 0), P(0, 1, 1)), 1)  # left wall (normal +x)
+    add(_quad(P(1, 0, 0), P(1, 0, 1), P(1, 1, 1), P(1, 1, 0)), 2)  # right wall (normal -x)
+    add(_box((0.55, 0.0, 0.15), (0.85, 0.3, 0.45)), 0)             # short box
+    add(_box((0.15, 0.0, 0.35), (0.45, 0.6, 0.65)), 0)             # tall box
+    ly = 1.0 - 1e-3
+    add(_quad(P(0.375, ly, 0.375), P(0.625, ly, 0.375), P(0.625, ly, 0.625), P(0.375, ly, 0.625)), 3)  # light, -y
+    mats = [material(MAT_DIFFUSE, (0.75, 0.75, 0.75), style=style),
+            material(MAT_DIFFUSE, (0.63, 0.065, 0.05), style=style),
+            material(MAT_DIFFUSE, (0.14, 0.45, 0.09), style=style),
+            material(MAT_DIFFUSE, (0.0, 0.0, 0.0), emission=(17.0, 17.0, 17.0), style=light_style)]
+    cam = camera((0.5, 0.5, 2.2), (0.5, 0.5, 0.0), fov_y=36.0, width=width, height=height)
+    return np.array(tris, dtype=np.float32), np.array(mids, dtype=np.uint32), mats, cam
+
+
+def furnace(albedo=0.5, le=1.0, width=32, height=32):
+    """Closed unit cube whose 12 inward-facing triangles all emit `le` and reflect `albedo`
+    (diffuse): the radiance of every path prefix of depth D is le * sum_{k<=D} albedo^k."""
+    tris = _box((0, 0, 0), (1, 1, 1))
+    # flip winding so the normals point into the cube
+    tris = [t[0:3] + t[6:9] + t[3:6] for t in tris]
+    mats = [material(MAT_DIFFUSE, (albedo,) * 3, emission=(le,) * 3)]
+    cam = camera((0.5, 0.5, 0.5), (0.5, 0.5, 0.0), fov_y=60.0, width=width, height=height)
+    return np.array(tris, dtype=np.float32), np.zeros(len(tris), dtype=np.uint32), mats, cam
+
+
+class Scene:
+    def __init__(self, positions: np.ndarray, mat_ids: np.ndarray, materials, cam: Camera):
+        self.positions = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
+        self.mat_ids = np.ascontiguousarray(mat_ids, dtype=np.uint32)
+        self.materials = (SceneMaterial * len(materials))(*materials)
+        self.camera = cam
+        self.h = C.c_void_p()
+        check(lib().sty_scene_create(self.positions.ctypes.data, self.mat_ids.ctypes.data, self.positions.shape[0],
+                                     self.materials, len(materials), C.byref(cam), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            lib().sty_scene_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def closest_hit(self, rays):
+        """rays: device float32 [n, 8] (o, d, tmin, tmax) -> (prim, t, bary) device tensors."""
+        import torch
+        n = rays.shape[0]
+        prim = torch.empty(n, dtype=torch.int32, device=rays.device)
+        t = torch.empty(n, dtype=torch.float32, device=rays.device)
+        b = torch.empty((n, 2), dtype=torch.float32, device=rays.device)
+        check(lib().sty_scene_closest_hit(self.h, rays.data_ptr(), n, prim.data_ptr(), t.data_ptr(), b.data_ptr(),
+                                          None))
+        return prim, t, b
+
+    def render(self, cfg: RenderConfig, programs=(), film=None, stream=None):
+        """Full NL-PF render; returns (film [H, W, 3] float64 device tensor, vertex count)."""
+        import torch
+        from .pf import _stream_ptr
+        W, H = self.camera.width, self.camera.height
+        if film is None:
+            film = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+        progs = list(programs)
+        arr = (abi.StyleProgram * max(1, len(progs)))(*progs) if progs else None
+        vc = C.c_uint64()
+        check(lib().sty_pf_render(self.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(vc),
+                                  _stream_ptr(stream)))
+        return film, vc.value
