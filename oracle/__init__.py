@@ -39,6 +39,7 @@ def lib() -> C.CDLL:
         L.orc_pf_adjoint_image_f64.restype = C.c_double
         L.orc_pf_adjoint_image_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
         L.orc_closest_hit.argtypes = [vp, C.c_uint32, vp, C.c_uint64, vp, vp, vp]
+        L.orc_path_trace.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
@@ -157,6 +158,20 @@ def closest_hit(tri_pos: np.ndarray, rays: np.ndarray):
     b = np.zeros((n, 2), dtype=np.float32)
     lib().orc_closest_hit(_p(pos), pos.size // 9, _p(r), n, _p(prim), _p(t), _p(b))
     return prim, t, b
+
+
+def path_trace(tri_pos, mat_ids, albedo, emission, cam, spp: int, max_depth: int, seed: int = 0):
+    """Independent FP64 CPU path tracer (NEE + balance MIS, diffuse, black emitters) -> image
+    [H, W, 3]. cam = (eye3, target3, up3, fov_y, W, H, filter_radius)."""
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float32).reshape(-1)
+    m = np.ascontiguousarray(mat_ids, dtype=np.uint32)
+    alb = np.ascontiguousarray(albedo, dtype=np.float32).reshape(-1)
+    em = np.ascontiguousarray(emission, dtype=np.float32).reshape(-1)
+    c = np.ascontiguousarray(cam, dtype=np.float32)
+    W, H = int(c[10]), int(c[11])
+    img = np.zeros((H, W, 3), dtype=np.float64)
+    lib().orc_path_trace(_p(pos), _p(m), m.size, _p(alb), _p(em), _p(c), spp, max_depth, seed, _p(img))
+    return img
 
 
 def num_threads() -> int:

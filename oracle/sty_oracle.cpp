@@ -3,6 +3,7 @@
 #include "sty_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -698,4 +699,233 @@ extern "C" void orc_closest_hit(const float *pos, uint32_t n_tris, const float *
             bary[2 * i + 1] = bb2;
         }
     }
+}
+
+// ---- independent CPU path tracer (FP64 radiance, brute-force f32 watertight hits) ---------------
+// The textbook estimator with next-event estimation and balance-heuristic MIS, restated from the
+// reference's per-vertex terms (handle_surface_light lm_path_filtering.rs:388-426, sample_light
+// :1261-1316, the BSDF sample :1180-1211) for diffuse surfaces. With black emitters it is the
+// expectation the NL-PF estimator converges to when every vertex only reuses itself.
+namespace {
+struct PtScene {
+    const float *pos;
+    const uint32_t *mat;
+    uint32_t n;
+    const float *albedo;    // 3 per material
+    const float *emission;  // 3 per material
+    std::vector<uint32_t> lights;
+    std::vector<double> cdf;
+    std::vector<double> area;
+    std::vector<std::array<double, 3>> nrm;
+};
+inline uint32_t pcg_u32(sty_pcg32 &g) { return pcg_next(g); }
+inline double u01(sty_pcg32 &g) { return (double)((float)pcg_u32(g) * 2.3283064e-10f); }
+inline uint32_t hit_bf(const PtScene &s, const double o[3], const double d[3], double tmax, uint32_t ex0,
+                       uint32_t ex1, double *tout, double *b1o, double *b2o) {
+    // double-precision Moller-Trumbore (the oracle only needs unbiased shading, not bit parity)
+    uint32_t best = 0xffffffffu;
+    double bt = tmax;
+    for (uint32_t t = 0; t < s.n; t++) {
+        if (t == ex0 || t == ex1) continue;
+        const float *p = s.pos + 9 * (size_t)t;
+        double e1[3], e2[3], pv[3], tv[3], qv[3];
+        for (int a = 0; a < 3; a++) {
+            e1[a] = (double)p[3 + a] - p[a];
+            e2[a] = (double)p[6 + a] - p[a];
+        }
+        pv[0] = d[1] * e2[2] - d[2] * e2[1];
+        pv[1] = d[2] * e2[0] - d[0] * e2[2];
+        pv[2] = d[0] * e2[1] - d[1] * e2[0];
+        const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+        if (std::fabs(det) < 1e-14) continue;
+        const double inv = 1.0 / det;
+        for (int a = 0; a < 3; a++) tv[a] = o[a] - p[a];
+        const double u = (tv[0] * pv[0] + tv[1] * pv[1] + tv[2] * pv[2]) * inv;
+        if (u < 0 || u > 1) continue;
+        qv[0] = tv[1] * e1[2] - tv[2] * e1[1];
+        qv[1] = tv[2] * e1[0] - tv[0] * e1[2];
+        qv[2] = tv[0] * e1[1] - tv[1] * e1[0];
+        const double v = (d[0] * qv[0] + d[1] * qv[1] + d[2] * qv[2]) * inv;
+        if (v < 0 || u + v > 1) continue;
+        const double tt = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv;
+        if (tt > 1e-7 && tt < bt) {
+            bt = tt;
+            best = t;
+            *b1o = u;
+            *b2o = v;
+        }
+    }
+    *tout = bt;
+    return best;
+}
+}  // namespace
+
+extern "C" void orc_path_trace(const float *pos, const uint32_t *mat, uint32_t n_tris, const float *albedo,
+                               const float *emission, const float *cam /* eye3 target3 up3 fov W H radius */,
+                               uint32_t spp, uint32_t max_depth, uint64_t seed, double *img) {
+    PtScene s;
+    s.pos = pos;
+    s.mat = mat;
+    s.n = n_tris;
+    s.albedo = albedo;
+    s.emission = emission;
+    s.area.resize(n_tris);
+    s.nrm.resize(n_tris);
+    double tot = 0;
+    std::vector<double> w;
+    for (uint32_t t = 0; t < n_tris; t++) {
+        const float *p = pos + 9 * (size_t)t;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; a++) {
+            e1[a] = (double)p[3 + a] - p[a];
+            e2[a] = (double)p[6 + a] - p[a];
+        }
+        double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        s.area[t] = 0.5 * l;
+        s.nrm[t] = {c[0] / l, c[1] / l, c[2] / l};
+        const float *em = emission + 3 * (size_t)mat[t];
+        double lum = 0.2126 * em[0] + 0.7152 * em[1] + 0.0722 * em[2];
+        if (lum > 0) {
+            s.lights.push_back(t);
+            w.push_back(lum * s.area[t]);
+            tot += lum * s.area[t];
+        }
+    }
+    s.cdf.assign(w.size() + 1, 0.0);
+    for (size_t k = 0; k < w.size(); k++) s.cdf[k + 1] = s.cdf[k] + w[k] / tot;
+    const uint32_t W = (uint32_t)cam[10], H = (uint32_t)cam[11];
+    double f[3], r[3], u[3];
+    for (int a = 0; a < 3; a++) f[a] = cam[3 + a] - cam[a];
+    double l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    for (int a = 0; a < 3; a++) f[a] /= l;
+    r[0] = f[1] * cam[8] - f[2] * cam[7];
+    r[1] = f[2] * cam[6] - f[0] * cam[8];
+    r[2] = f[0] * cam[7] - f[1] * cam[6];
+    l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (int a = 0; a < 3; a++) r[a] /= l;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    const double th = std::tan(cam[9] * 0.5 * M_PI / 180.0), asp = (double)W / H, rad = cam[12];
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int py = 0; py < (int)H; py++)
+        for (uint32_t px = 0; px < W; px++) {
+            double acc[3] = {0, 0, 0};
+            for (uint32_t sp = 0; sp < spp; sp++) {
+                sty_pcg32 g;
+                const uint64_t idx = ((uint64_t)py * W + px) * spp + sp;
+                g.state = 0;
+                g.inc = (idx << 1) | 1u;
+                pcg_next(g);
+                g.state += seed * 0x9E3779B97F4A7C15ULL + idx * 0xD1B54A32D192ED03ULL;
+                pcg_next(g);
+                const double fx = px + 0.5 + (u01(g) - 0.5) * rad, fy = py + 0.5 + (u01(g) - 0.5) * rad;
+                const double sx = (2 * fx / W - 1) * th * asp, sy = (1 - 2 * fy / H) * th;
+                double o[3] = {cam[0], cam[1], cam[2]}, d[3];
+                for (int a = 0; a < 3; a++) d[a] = f[a] + r[a] * sx + u[a] * sy;
+                l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+                for (int a = 0; a < 3; a++) d[a] /= l;
+                double thr[3] = {1, 1, 1}, prev_pdf = 0, prev_p[3] = {o[0], o[1], o[2]};
+                uint32_t ex = 0xffffffffu;
+                for (uint32_t depth = 0; depth <= max_depth; depth++) {
+                    double t, b1, b2;
+                    const uint32_t hit = hit_bf(s, o, d, 1e30, ex, ex, &t, &b1, &b2);
+                    if (hit == 0xffffffffu) break;
+                    double p[3];
+                    for (int a = 0; a < 3; a++) p[a] = o[a] + t * d[a];
+                    const auto &n = s.nrm[hit];
+                    const float *em = emission + 3 * (size_t)mat[hit];
+                    const float *alb = albedo + 3 * (size_t)mat[hit];
+                    const double ndd = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+                    if (em[0] > 0 || em[1] > 0 || em[2] > 0) {
+                        double mis = 1.0;
+                        if (depth > 0) {
+                            double sel = 0;
+                            for (size_t k = 0; k < s.lights.size(); k++)
+                                if (s.lights[k] == hit) sel = s.cdf[k + 1] - s.cdf[k];
+                            double wv[3] = {p[0] - prev_p[0], p[1] - prev_p[1], p[2] - prev_p[2]};
+                            double d2 = wv[0] * wv[0] + wv[1] * wv[1] + wv[2] * wv[2];
+                            double lp = sel / s.area[hit] * d2 / std::max(std::fabs(ndd), 1e-6);
+                            mis = prev_pdf / (prev_pdf + lp);
+                        }
+                        if (ndd < 0)
+                            for (int c = 0; c < 3; c++) acc[c] += thr[c] * em[c] * mis;
+                    }
+                    if (depth == max_depth) break;
+                    // shading frame: flat, normal facing the incoming direction side as in the GPU path
+                    double ns[3] = {n[0], n[1], n[2]};
+                    const double wo[3] = {-d[0], -d[1], -d[2]};
+                    const double co = ns[0] * wo[0] + ns[1] * wo[1] + ns[2] * wo[2];
+                    // NEE
+                    {
+                        const double ux = u01(g), uy = u01(g), uz = u01(g);
+                        size_t k = 0;
+                        while (k + 1 < s.lights.size() && !(s.cdf[k + 1] > ux)) k++;
+                        if (!s.lights.empty()) {
+                            const uint32_t lt = s.lights[k];
+                            const double sel = s.cdf[k + 1] - s.cdf[k];
+                            double bx, by;
+                            if (uy < uz) {
+                                bx = uy / 2;
+                                by = uz - bx;
+                            } else {
+                                by = uz / 2;
+                                bx = uy - by;
+                            }
+                            const float *lp = pos + 9 * (size_t)lt;
+                            double q[3];
+                            for (int a = 0; a < 3; a++) q[a] = (1 - bx - by) * lp[a] + bx * lp[3 + a] + by * lp[6 + a];
+                            double wi[3] = {q[0] - p[0], q[1] - p[1], q[2] - p[2]};
+                            const double d2 = wi[0] * wi[0] + wi[1] * wi[1] + wi[2] * wi[2];
+                            const double dist = std::sqrt(d2);
+                            for (int a = 0; a < 3; a++) wi[a] /= dist;
+                            const auto &ln = s.nrm[lt];
+                            const double lnw = ln[0] * wi[0] + ln[1] * wi[1] + ln[2] * wi[2];
+                            const double ci = ns[0] * wi[0] + ns[1] * wi[1] + ns[2] * wi[2];
+                            const double lpdf = sel / s.area[lt] * d2 / std::fabs(lnw);
+                            if (lnw < 0 && co * ci > 0 && std::isfinite(lpdf)) {
+                                double tt, c1, c2;
+                                const uint32_t blk = hit_bf(s, p, wi, dist * (1 - 1e-3), hit, lt, &tt, &c1, &c2);
+                                if (blk == 0xffffffffu) {
+                                    const double bp = std::fabs(ci) / M_PI;
+                                    const double wmis = lpdf / (lpdf + bp);
+                                    const float *lem = emission + 3 * (size_t)mat[lt];
+                                    for (int c = 0; c < 3; c++)
+                                        acc[c] += thr[c] * alb[c] / M_PI * std::fabs(ci) * lem[c] * wmis / lpdf;
+                                }
+                            }
+                        }
+                    }
+                    // BSDF sample (cosine hemisphere around the normal on wo's side)
+                    const double usel = u01(g), u0 = u01(g), u1 = u01(g);
+                    (void)usel;
+                    const double rr = std::sqrt(u0), ph = 2 * M_PI * u1;
+                    double lx = rr * std::cos(ph), ly = rr * std::sin(ph), lz = std::sqrt(std::max(0.0, 1 - lx * lx - ly * ly));
+                    double tx[3];
+                    if (std::fabs(ns[0]) > std::fabs(ns[1])) {
+                        double il = 1.0 / std::sqrt(ns[0] * ns[0] + ns[2] * ns[2]);
+                        tx[0] = -ns[2] * il; tx[1] = 0; tx[2] = ns[0] * il;
+                    } else {
+                        double il = 1.0 / std::sqrt(ns[1] * ns[1] + ns[2] * ns[2]);
+                        tx[0] = 0; tx[1] = ns[2] * il; tx[2] = -ns[1] * il;
+                    }
+                    double sx3[3] = {ns[1] * tx[2] - ns[2] * tx[1], ns[2] * tx[0] - ns[0] * tx[2], ns[0] * tx[1] - ns[1] * tx[0]};
+                    if (co < 0) lz = -lz;
+                    double wi[3];
+                    for (int a = 0; a < 3; a++) wi[a] = tx[a] * lx + sx3[a] * ly + ns[a] * lz;
+                    const double pdf = std::fabs(lz) / M_PI;
+                    if (!(pdf > 0)) break;
+                    for (int c = 0; c < 3; c++) thr[c] *= alb[c];  // f cos / pdf = albedo
+                    prev_pdf = pdf;
+                    for (int a = 0; a < 3; a++) {
+                        prev_p[a] = p[a];
+                        o[a] = p[a];
+                        d[a] = wi[a];
+                    }
+                    ex = hit;
+                }
+            }
+            for (int c = 0; c < 3; c++) img[3 * ((size_t)py * W + px) + c] = acc[c] / spp;
+        }
 }

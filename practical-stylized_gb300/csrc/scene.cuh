@@ -156,7 +156,11 @@ __device__ inline Hit trace_closest(const SceneView &s, const float o[3], const 
     while (sp > 0) {
         const BvhNode n = s.nodes[stack[--sp]];
         float tn;
-        if (!box_hit(n, o, inv, tmin, h.t, &tn)) continue;
+        // cull against a slightly inflated best distance: a flat leaf box's entry can round one ulp
+        // past a triangle hit at exactly the best distance (a tie on a shared edge), and the lower id
+        // must still be found
+        const float tcull = h.t * (1.0f + 1e-6f);
+        if (!box_hit(n, o, inv, tmin, tcull, &tn)) continue;
         if (n.count) {
             for (uint32_t k = 0; k < n.count; k++) {
                 const TriGeom tg = s.tris[n.a + k];
@@ -170,7 +174,7 @@ __device__ inline Hit trace_closest(const SceneView &s, const float o[3], const 
             // push far child first so the near one is popped first
             const BvhNode &l = s.nodes[n.a], &r = s.nodes[n.a + 1];
             float tl, tr;
-            const bool hl = box_hit(l, o, inv, tmin, h.t, &tl), hr = box_hit(r, o, inv, tmin, h.t, &tr);
+            const bool hl = box_hit(l, o, inv, tmin, tcull, &tl), hr = box_hit(r, o, inv, tmin, tcull, &tr);
             if (hl && hr) {
                 if (tl <= tr) {
                     stack[sp++] = n.a + 1;
