@@ -193,6 +193,33 @@ def nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
     return res
 
 
+def c1_bench(sty, repeats: int = 3):
+    """End-to-end NL-PF render of the Cornell box workload: 256x256 px, 16 paths per pixel, vertex
+    depths 0..5, reference-mode filter (radius 0.05 = 1 % of the box x 5, reuse 64, SMIS, clusters
+    off), reference toon (band width 0.2) on every surface. Mpath-vertices/s = traced and filtered
+    vertices / wall time of sty_pf_render (trace + grid + filter + splat)."""
+    import torch
+    a = sty.abi
+    pos, mids, mats, cam = sty.scene.cornell_box(256, 256, style=(0, -1, -1, -1))
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    progs = [a.style_program([a.toon(0.2)])]
+    cfg = sty.scene.render_config(max_depth=5, branch=16, radius_scale=(5.0,), reuse=(64,), seed=0)
+    sc.render(cfg, progs)  # warm-up (module load, allocator)
+    torch.cuda.synchronize()
+    times, nv = [], 0
+    for r in range(repeats):
+        cfg.seed = r + 1
+        t0 = time.perf_counter()
+        film, nv = sc.render(cfg, progs)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    sc.close()
+    return {"workload": "Cornell box 256x256, 16 paths/px, depth 5, reference-mode NL-PF (r=0.05, reuse 64, SMIS)",
+            "mpath_vertices_per_s": nv / t / 1e6, "vertices": nv, "seconds_per_render": t,
+            "image_mean": float(film.mean())}
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -366,6 +393,8 @@ def run(args):
                          "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 at the sampled SM clock"},
         "clocks": clk,
     }
+    if world == 1 and not args.no_c1:
+        line["c1_render"] = c1_bench(sty)
     if world == 1 and not args.no_nrc:
         bf16_peak = 1943.8
         p = ROOT / "MEASURED_PEAKS.json"
@@ -392,6 +421,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling cases)")
     ap.add_argument("--no-nrc", action="store_true", help="skip the NL-NRC frames")
     ap.add_argument("--nrc-frames", type=int, default=20)
+    ap.add_argument("--no-c1", action="store_true", help="skip the end-to-end Cornell box render")
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -420,6 +420,33 @@ STY_API sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *c
                                  const sty_style_program *programs, uint32_t n_programs, double *film,
                                  uint64_t *vertex_count, void *stream);
 
+/* NL-NRC samples generated by the tracer (nrc_pt.rs:231-434 tracing, write_nrc_inputs :583-663,
+ * training targets :723-776).
+ * layout STY_NRC_ROWS_REF: rows of 20 + max_depth floats as the reference writes them: position
+ *   normalised to the scene bounds (3), shading normal * 0.5 + 0.5 (3), outgoing direction * 0.5 +
+ *   0.5 (3), roughness (1 for diffuse, alpha for GGX), albedo (3), [stylization disabled, enabled]
+ *   (2), one-hot style index (4), one-hot depth (max_depth + 1).
+ * layout STY_NRC_ROWS_SPHERICAL: rows of 11 floats for the frequency-encoded cache: normalised
+ *   position (3), shading normal and outgoing direction as (theta / pi, (phi + pi) / 2pi)
+ *   (xyz_to_spherical_normalized, geometry.rs:342-346; 2 + 2), roughness (1), albedo (3).
+ * mode STY_NRC_SAMPLES_TRAIN: `spp` paths per pixel are traced to `max_depth`; every vertex gives
+ *   one row whose target is that vertex's radiance estimate from the traced suffix (emission + NEE
+ *   with MIS + BSDF-sampled continuation, the estimator of sty_pf_render with only the vertex itself
+ *   reused; no style nodes). The reference instead bootstraps the suffix from the cache's own
+ *   prediction at the next vertex; a traced suffix is its unbiased limit.
+ * mode STY_NRC_SAMPLES_QUERY: the first hit of `spp` camera rays per pixel, row order
+ *   sample-major (index = s * width * height + pixel), depth one-hot 0; rows of camera rays that
+ *   miss are zeros and their target (the emission seen at the hit) is 0.
+ * inputs / targets are device arrays of `capacity` rows; *count_out (host) receives the rows
+ * written (training rows beyond the capacity are dropped). */
+#define STY_NRC_SAMPLES_TRAIN 0
+#define STY_NRC_SAMPLES_QUERY 1
+#define STY_NRC_ROWS_REF 0
+#define STY_NRC_ROWS_SPHERICAL 1
+STY_API sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t layout, uint32_t spp,
+                                   uint32_t max_depth, uint64_t seed, float *inputs, float *targets,
+                                   uint64_t capacity, uint64_t *count_out, void *stream);
+
 /* ----------------------------------------------------------------------------------------
  * Integer helpers (bit-exact with the reference)
  * -------------------------------------------------------------------------------------- */

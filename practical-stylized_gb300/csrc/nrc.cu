@@ -148,10 +148,13 @@ __global__ void __launch_bounds__(128) k_bwd_f32(NrcNet n, const float *__restri
 }
 
 // ---- weight gradient: grad_l[j][k] = sum_i dpre_l[i][j] * acts_l[i][k] ----------------------
-// grid: (chunks, layers+1); 256 threads; rows R = 64 (hidden) or out_dims (output layer).
+// grid: (chunks, layers+1); 256 threads; rows R = 64 (hidden) or out_dims (output layer). Each
+// chunk of kWgChunk samples stores its partial sums at part + chunk * np; k_sum_chunks adds the
+// chunks in order, so the gradient does not depend on scheduling.
 constexpr int kWgChunk = 1024;
 __global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const float *__restrict__ acts,
-                                                   const float *__restrict__ dpre, float *__restrict__ grad) {
+                                                   const float *__restrict__ dpre, size_t np,
+                                                   float *__restrict__ part) {
     __shared__ float sd[64][W + 1];
     __shared__ float sh[64][W + 1];
     const int l = blockIdx.y;
@@ -181,10 +184,17 @@ __global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const f
         }
     }
     if (j < rows) {
-        float *g = grad + nrc_w_offset(l) + (size_t)j * W + k0;
+        float *g = part + blockIdx.x * np + nrc_w_offset(l) + (size_t)j * W + k0;
 #pragma unroll
-        for (int c = 0; c < 16; c++) atomicAdd(g + c, acc[c]);
+        for (int c = 0; c < 16; c++) g[c] = acc[c];
     }
+}
+__global__ void k_sum_chunks(size_t np, uint32_t chunks, const float *__restrict__ part, float *__restrict__ grad) {
+    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    float s = 0.0f;
+    for (uint32_t c = 0; c < chunks; c++) s += part[c * np + p];
+    grad[p] = s;
 }
 
 // ---- batch sampling (collect_batch, akari_tcnn.cu:15-38) -------------------------------------
@@ -250,6 +260,7 @@ struct sty_nrc {
     float *w = nullptr, *m = nullptr, *v = nullptr, *g = nullptr, *ema = nullptr;
     uint16_t *img = nullptr, *img_ema = nullptr;  // BF16 tensor-core images of w / ema
     float *bin = nullptr, *btg = nullptr, *bpred = nullptr, *acts = nullptr, *dpre = nullptr, *loss = nullptr;
+    float *gpart = nullptr;  // per-chunk weight-gradient partials
     uint32_t bcap = 0;
     uint64_t step = 0;  // optimiser steps taken (Adam t, EMA iteration)
     float lr = 0.0f;
@@ -260,16 +271,18 @@ namespace {
 
 sty_status ensure_batch(sty_nrc *nr, uint32_t B) {
     if (B <= nr->bcap) return STY_OK;
-    void *ptrs[] = {nr->bin, nr->btg, nr->bpred, nr->acts, nr->dpre};
+    void *ptrs[] = {nr->bin, nr->btg, nr->bpred, nr->acts, nr->dpre, nr->gpart};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    nr->bin = nr->btg = nr->bpred = nr->acts = nr->dpre = nullptr;
+    nr->bin = nr->btg = nr->bpred = nr->acts = nr->dpre = nr->gpart = nullptr;
     const NrcNet &n = nr->net;
     STY_TRY(check_cuda(cudaMalloc(&nr->bin, (size_t)B * n.in_dims * 4), "alloc batch input"));
     STY_TRY(check_cuda(cudaMalloc(&nr->btg, (size_t)B * n.out_dims * 4), "alloc batch target"));
     STY_TRY(check_cuda(cudaMalloc(&nr->bpred, (size_t)B * n.out_dims * 4), "alloc batch pred"));
     STY_TRY(check_cuda(cudaMalloc(&nr->acts, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc activations"));
     STY_TRY(check_cuda(cudaMalloc(&nr->dpre, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc gradients"));
+    const size_t chunks = (B + kWgChunk - 1) / kWgChunk;
+    STY_TRY(check_cuda(cudaMalloc(&nr->gpart, chunks * nr->np * 4), "alloc gradient partials"));
     nr->bcap = B;
     return STY_OK;
 }
@@ -294,10 +307,12 @@ sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t s
                        "attr k_bwd_f32"));
     k_bwd_f32<<<(B + 127) / 128, 128, smem, st>>>(n, nr->w, B, nr->bpred, target, nr->acts, nr->dpre, nr->loss);
     STY_TRY(check_launch("k_bwd_f32"));
-    STY_TRY(check_cuda(cudaMemsetAsync(nr->g, 0, nr->np * 4, st), "zero grad"));
-    dim3 grid((B + kWgChunk - 1) / kWgChunk, n.layers + 1);
-    k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->g);
-    return check_launch("k_wgrad_f32");
+    const uint32_t chunks = (B + kWgChunk - 1) / kWgChunk;
+    dim3 grid(chunks, n.layers + 1);
+    k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->np, nr->gpart);
+    STY_TRY(check_launch("k_wgrad_f32"));
+    k_sum_chunks<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, chunks, nr->gpart, nr->g);
+    return check_launch("k_sum_chunks");
 }
 
 sty_status forward_batch(sty_nrc *nr, uint32_t B, const float *in, cudaStream_t st) {
@@ -324,7 +339,7 @@ sty_status infer(sty_nrc *nr, bool ema, uint64_t count, const float *in, float *
 
 void free_nrc(sty_nrc *nr) {
     void *ptrs[] = {nr->w, nr->m, nr->v, nr->g, nr->ema, nr->img, nr->img_ema, nr->bin,
-                    nr->btg, nr->bpred, nr->acts, nr->dpre, nr->loss};
+                    nr->btg, nr->bpred, nr->acts, nr->dpre, nr->loss, nr->gpart};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete nr;

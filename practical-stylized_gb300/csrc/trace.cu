@@ -11,6 +11,8 @@
 // planes (sty_pf_vertices) that stay on the device; the record the reference's kernel_propagate
 // copies into the parent (wi = -wo, mis) is written into the parent depth's slot when the child
 // vertex is found.
+#include <cub/cub.cuh>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -423,10 +425,303 @@ __global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
     rng[i] = g;
 }
 
+// f * |cos| (rgb) and pdf of a scene material (Surface::evaluate; diffuse.rs:17-48,
+// svm/surface/mod.rs:1877-1910 with unit Fresnel)
+__device__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f) {
+    *f = f3m(0.0f, 0.0f, 0.0f);
+    if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
+    const float co = dot(wo, ns), ci = dot(wi, ns);
+    if (m.kind == STY_MAT_DIFFUSE) {
+        if (!(co * ci >= 0.0f)) return 0.0f;
+        const float k = fabsf(ci) / kPi;
+        *f = f3m(m.albedo[0] * k, m.albedo[1] * k, m.albedo[2] * k);
+        return k;
+    }
+    const float a = fmaxf(m.alpha, 1e-4f);
+    F3 wh = wo + wi;
+    if (dot(wh, wo) * dot(wi, wh) < 0.0f || (wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) || ci == 0.0f ||
+        co == 0.0f || !(co * ci >= 0.0f))
+        return 0.0f;
+    wh = normalize(wh);
+    const float d = tr_d(dot(wh, ns), a);
+    const float g = 1.0f / (1.0f + tr_lambda(co, a) + tr_lambda(ci, a)), g1 = 1.0f / (1.0f + tr_lambda(co, a));
+    const float k = fabsf(0.25f * d * g / (ci * co)) * fabsf(ci);
+    *f = f3m(m.albedo[0] * k, m.albedo[1] * k, m.albedo[2] * k);
+    const float owh = fabsf(dot(wo, wh));
+    return d * g1 * owh / fabsf(co) / (4.0f * owh);
+}
+
+// Per-vertex radiance estimate reusing only the vertex itself: le + own NEE (balance MIS) +
+// f * L_next * mis_next / pdf (evaluate_filtered_radiance :758-972 with a one-element neighbour set)
+__global__ void k_self_radiance(SceneView sc, uint32_t n, VertOut v, const float *next, float *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!v.active[i]) {
+        out[i] = out[n + i] = out[2 * (size_t)n + i] = 0.0f;
+        return;
+    }
+    const sty_scene_material m = sc.materials[v.material[i]];
+    const F3 ns = f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), ng = f3m(v.ng[0][i], v.ng[1][i], v.ng[2][i]);
+    const F3 wo = f3m(v.wo[0][i], v.wo[1][i], v.wo[2][i]);
+    F3 rad = f3m(v.le[0][i], v.le[1][i], v.le[2][i]);
+    const float dpdf = v.dir_pdf[i];
+    if (dpdf > 0.0f) {
+        F3 f;
+        const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f);
+        const float w = dpdf / (dpdf + bp) / dpdf;
+        rad = rad + f3m(f.x * v.dir_l[0][i], f.y * v.dir_l[1][i], f.z * v.dir_l[2][i]) * w;
+    }
+    const F3 wi = f3m(v.ind_wi[0][i], v.ind_wi[1][i], v.ind_wi[2][i]);
+    if (next && dot(wi, wi) != 0.0f) {
+        F3 f;
+        const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+        if (bp > 0.0f) {
+            const float s = v.ind_mis[i] / bp;
+            rad = rad + f3m(f.x * next[i], f.y * next[n + i], f.z * next[2 * (size_t)n + i]) * s;
+        }
+    }
+    out[i] = rad.x;
+    out[n + i] = rad.y;
+    out[2 * (size_t)n + i] = rad.z;
+}
+
+// NRC input rows. Layout STY_NRC_ROWS_REF follows write_nrc_inputs (nrc_pt.rs:583-663): position
+// normalised to the scene box, ns * 0.5 + 0.5, wo * 0.5 + 0.5, roughness (diffuse 1, GGX alpha),
+// albedo, [disabled, enabled], one-hot style index (4), one-hot depth (max_depth + 1):
+// 20 + max_depth floats. Layout STY_NRC_ROWS_SPHERICAL is the 11-input row of the frequency-encoded
+// cache: normalised position, normal and wo as (theta / pi, (phi + pi) / 2pi)
+// (xyz_to_spherical_normalized, geometry.rs:342-346), roughness, albedo.
+struct FeatArgs {
+    float bmin[3], bext[3];
+    uint32_t max_depth, dims, layout;
+};
+__device__ __forceinline__ void sph(F3 w, float *t, float *p) {
+    *t = acosf(fminf(fmaxf(w.z, -1.0f), 1.0f)) * (1.0f / kPi);
+    *p = (atan2f(w.y, w.x) + kPi) * (0.5f / kPi);
+}
+__device__ void write_features(const SceneView &sc, const FeatArgs &fa, F3 p, F3 wo, F3 ns, uint32_t mi,
+                               uint32_t flags, uint32_t depth, float *row) {
+    const sty_scene_material m = sc.materials[mi];
+    row[0] = (p.x - fa.bmin[0]) / fa.bext[0];
+    row[1] = (p.y - fa.bmin[1]) / fa.bext[1];
+    row[2] = (p.z - fa.bmin[2]) / fa.bext[2];
+    const float rough = m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
+    if (fa.layout == STY_NRC_ROWS_SPHERICAL) {
+        sph(ns, &row[3], &row[4]);
+        sph(wo, &row[5], &row[6]);
+        row[7] = rough;
+        row[8] = m.albedo[0];
+        row[9] = m.albedo[1];
+        row[10] = m.albedo[2];
+        return;
+    }
+    row[3] = ns.x * 0.5f + 0.5f;
+    row[4] = ns.y * 0.5f + 0.5f;
+    row[5] = ns.z * 0.5f + 0.5f;
+    row[6] = wo.x * 0.5f + 0.5f;
+    row[7] = wo.y * 0.5f + 0.5f;
+    row[8] = wo.z * 0.5f + 0.5f;
+    row[9] = rough;
+    row[10] = m.albedo[0];
+    row[11] = m.albedo[1];
+    row[12] = m.albedo[2];
+    const bool off = (flags & 1u) != 0;
+    row[13] = off ? 1.0f : 0.0f;
+    row[14] = off ? 0.0f : 1.0f;
+    const uint32_t si = style_index(flags);
+    for (uint32_t k = 0; k < 4; k++) row[15 + k] = k == si ? 1.0f : 0.0f;
+    for (uint32_t k = 0; k <= fa.max_depth; k++) row[19 + k] = k == depth ? 1.0f : 0.0f;
+}
+// Rows of one depth, in path order after the rows of the earlier depths: row = *base + idx[i],
+// idx the exclusive prefix sum of the active flags.
+__global__ void k_nrc_train_rows(SceneView sc, FeatArgs fa, uint32_t n, uint32_t depth, VertOut v, const float *rad,
+                                 const uint32_t *idx, const unsigned long long *base, float *inputs, float *targets,
+                                 uint64_t capacity) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !v.active[i]) return;
+    const unsigned long long k = *base + idx[i];
+    if (k >= capacity) return;
+    write_features(sc, fa, f3m(v.p[0][i], v.p[1][i], v.p[2][i]), f3m(v.wo[0][i], v.wo[1][i], v.wo[2][i]),
+                   f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), v.material[i], v.flags[i], depth, inputs + k * fa.dims);
+    targets[k * 3] = rad[i];
+    targets[k * 3 + 1] = rad[n + i];
+    targets[k * 3 + 2] = rad[2 * (size_t)n + i];
+}
+__global__ void k_advance_rows(uint32_t n, const uint32_t *idx, const int32_t *active, unsigned long long *base) {
+    *base += (unsigned long long)idx[n - 1] + (active[n - 1] ? 1u : 0u);
+}
+__global__ void k_nrc_query_rows(SceneView sc, FeatArgs fa, uint32_t n, VertOut v, float *inputs, float *targets) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float *row = inputs + (size_t)i * fa.dims;
+    float le[3] = {0.0f, 0.0f, 0.0f};
+    if (v.active[i]) {
+        write_features(sc, fa, f3m(v.p[0][i], v.p[1][i], v.p[2][i]), f3m(v.wo[0][i], v.wo[1][i], v.wo[2][i]),
+                       f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), v.material[i], v.flags[i], 0, row);
+        le[0] = v.le[0][i];
+        le[1] = v.le[1][i];
+        le[2] = v.le[2][i];
+    } else {
+        for (uint32_t c = 0; c < fa.dims; c++) row[c] = 0.0f;
+    }
+    for (int c = 0; c < 3; c++) targets[(size_t)i * 3 + c] = le[c];
+}
+
 }  // namespace
 }  // namespace sty
 
 using namespace sty;
+
+namespace {
+
+CamArgs make_camera(const sty_camera &cam) {
+    CamArgs ca;
+    float f[3], r[3], u[3];
+    for (int a = 0; a < 3; a++) f[a] = cam.target[a] - cam.eye[a];
+    float l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    for (int a = 0; a < 3; a++) f[a] /= l;
+    r[0] = f[1] * cam.up[2] - f[2] * cam.up[1];
+    r[1] = f[2] * cam.up[0] - f[0] * cam.up[2];
+    r[2] = f[0] * cam.up[1] - f[1] * cam.up[0];
+    l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+    for (int a = 0; a < 3; a++) r[a] /= l;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    for (int a = 0; a < 3; a++) {
+        ca.eye[a] = cam.eye[a];
+        ca.fwd[a] = f[a];
+        ca.right[a] = r[a];
+        ca.up[a] = u[a];
+    }
+    ca.tan_half = std::tan(cam.fov_y * 0.5f * 3.14159265358979f / 180.0f);
+    ca.aspect = (float)cam.width / (float)cam.height;
+    ca.radius = cam.filter_radius;
+    ca.W = cam.width;
+    ca.H = cam.height;
+    return ca;
+}
+
+// Device buffers of one wavefront trace: per-depth vertex planes, path state, per-path Pcg32,
+// per-depth radiance planes; freed with the job.
+struct TraceJob {
+    static constexpr size_t kPlanes = 30;  // per depth: active, 27 float planes, flags, material
+    uint32_t npx = 0, n = 0, D = 0, max_depth = 0, n_programs = 0;
+    CamArgs ca;
+    SceneView sv;
+    std::vector<void *> owned;
+    float *verts = nullptr, *outs = nullptr, *psb = nullptr;
+    sty_pcg32 *rng = nullptr;
+    sty_style_program *dprog = nullptr;
+    unsigned long long *vc = nullptr;
+    std::vector<VertOut> vo;
+    std::vector<sty_pf_vertices> vin;
+    PathState ps;
+    float bmin[3], bmax[3];
+    sty_status s = STY_OK;
+
+    ~TraceJob() {
+        for (void *p : owned) cudaFree(p);
+    }
+    void *alloc(size_t bytes, const char *what) {
+        void *p = nullptr;
+        if (s == STY_OK) s = check_cuda(cudaMalloc(&p, bytes), what);
+        if (p) owned.push_back(p);
+        return p;
+    }
+    sty_status init(sty_scene *scene, uint32_t branch, uint32_t maxd, const sty_style_program *programs,
+                    uint32_t nprog, uint64_t seed, cudaStream_t st) {
+        const sty_camera &cam = scene_camera(scene);
+        npx = cam.width * cam.height;
+        const uint64_t np64 = (uint64_t)npx * branch;
+        if (np64 >= (1ull << 31)) {
+            set_error("too many paths (%llu)", (unsigned long long)np64);
+            return STY_ERR_ARG;
+        }
+        n = (uint32_t)np64;
+        max_depth = maxd;
+        D = maxd + 1;
+        n_programs = nprog;
+        ca = make_camera(cam);
+        sv = scene_view(scene);
+        scene_bounds(scene, bmin, bmax);
+        verts = (float *)alloc((size_t)D * kPlanes * n * 4, "alloc vertices");
+        outs = (float *)alloc((size_t)D * 3 * n * 4, "alloc outputs");
+        psb = (float *)alloc((size_t)13 * n * 4, "alloc path state");
+        rng = (sty_pcg32 *)alloc((size_t)n * sizeof(sty_pcg32), "alloc rng");
+        dprog = (sty_style_program *)alloc(64 * sizeof(sty_style_program), "alloc programs");
+        vc = (unsigned long long *)alloc(8, "alloc counter");
+        if (s != STY_OK) return s;
+        if (nprog)
+            STY_TRY(check_cuda(cudaMemcpyAsync(dprog, programs, nprog * sizeof(sty_style_program),
+                                               cudaMemcpyHostToDevice, st), "upload programs"));
+        STY_TRY(check_cuda(cudaMemsetAsync(vc, 0, 8, st), "zero counter"));
+        vo.resize(D);
+        vin.resize(D);
+        for (uint32_t d = 0; d < D; d++) {
+            float *b = verts + (size_t)d * kPlanes * n;
+            int k = 0;
+            auto pl = [&]() { return b + (size_t)(k++) * n; };
+            VertOut &w = vo[d];
+            w.active = (int32_t *)pl();
+            for (int a = 0; a < 3; a++) w.p[a] = pl();
+            for (int a = 0; a < 3; a++) w.wo[a] = pl();
+            for (int a = 0; a < 3; a++) w.ns[a] = pl();
+            for (int a = 0; a < 3; a++) w.ng[a] = pl();
+            for (int a = 0; a < 3; a++) w.le[a] = pl();
+            w.mis = pl();
+            for (int a = 0; a < 3; a++) w.dir_wi[a] = pl();
+            for (int a = 0; a < 3; a++) w.dir_l[a] = pl();
+            w.dir_pdf = pl();
+            for (int a = 0; a < 3; a++) w.ind_wi[a] = pl();
+            w.ind_mis = pl();
+            w.flags = (uint32_t *)pl();
+            w.material = (uint32_t *)pl();
+            sty_pf_vertices &r = vin[d];
+            r.active = w.active;
+            for (int a = 0; a < 3; a++) {
+                r.p[a] = w.p[a];
+                r.wo[a] = w.wo[a];
+                r.ns[a] = w.ns[a];
+                r.ng[a] = w.ng[a];
+                r.le[a] = w.le[a];
+                r.dir_wi[a] = w.dir_wi[a];
+                r.dir_l[a] = w.dir_l[a];
+                r.ind_wi[a] = w.ind_wi[a];
+            }
+            r.mis = w.mis;
+            r.dir_pdf = w.dir_pdf;
+            r.ind_mis = w.ind_mis;
+            r.flags = w.flags;
+            r.material = w.material;
+            r.n = n;
+        }
+        int k = 0;
+        auto pl = [&]() { return psb + (size_t)(k++) * n; };
+        for (int a = 0; a < 3; a++) ps.o[a] = pl();
+        for (int a = 0; a < 3; a++) ps.d[a] = pl();
+        for (int a = 0; a < 3; a++) ps.prev_p[a] = pl();
+        ps.prev_pdf = pl();
+        ps.flags = (uint32_t *)pl();
+        ps.exclude = (uint32_t *)pl();
+        ps.terminated = (uint32_t *)pl();
+        k_rng_init<<<(n + 255) / 256, 256, 0, st>>>(n, seed, rng);
+        return check_launch("k_rng_init");
+    }
+    // all depths of one wavefront (kernel_trace dispatch loop, lm_path_filtering.rs:1646-1654)
+    sty_status trace(cudaStream_t st) {
+        STY_TRY(check_cuda(cudaMemsetAsync(verts, 0, (size_t)D * kPlanes * n * 4, st), "reset vertices"));
+        for (uint32_t d = 0; d < D; d++) {
+            k_trace<<<(n + 255) / 256, 256, 0, st>>>(sv, ca, n, d, max_depth, ps, vo[d], vo[d > 0 ? d - 1 : 0], rng,
+                                                     dprog, n_programs, vc);
+            STY_TRY(check_launch("k_trace"));
+        }
+        return STY_OK;
+    }
+    float *out(uint32_t d) { return outs + (size_t)d * 3 * n; }
+};
+
+}  // namespace
 
 extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *cfg,
                                     const sty_style_program *programs, uint32_t n_programs, double *film,
@@ -439,121 +734,11 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
     STY_ARG_CHECK(programs || n_programs == 0, "null programs");
     STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
     cudaStream_t st = as_stream(stream);
-    const sty_camera &cam = scene_camera(scene);
-    const uint32_t npx = cam.width * cam.height;
-    const uint64_t np64 = (uint64_t)npx * cfg->branch;
-    STY_ARG_CHECK(np64 < (1ull << 31), "too many paths");
-    const uint32_t n = (uint32_t)np64, D = cfg->max_depth + 1;
-    // camera basis (look-at)
-    CamArgs ca;
-    {
-        float f[3], r[3], u[3];
-        for (int a = 0; a < 3; a++) f[a] = cam.target[a] - cam.eye[a];
-        float l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
-        for (int a = 0; a < 3; a++) f[a] /= l;
-        r[0] = f[1] * cam.up[2] - f[2] * cam.up[1];
-        r[1] = f[2] * cam.up[0] - f[0] * cam.up[2];
-        r[2] = f[0] * cam.up[1] - f[1] * cam.up[0];
-        l = std::sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-        for (int a = 0; a < 3; a++) r[a] /= l;
-        u[0] = r[1] * f[2] - r[2] * f[1];
-        u[1] = r[2] * f[0] - r[0] * f[2];
-        u[2] = r[0] * f[1] - r[1] * f[0];
-        for (int a = 0; a < 3; a++) {
-            ca.eye[a] = cam.eye[a];
-            ca.fwd[a] = f[a];
-            ca.right[a] = r[a];
-            ca.up[a] = u[a];
-        }
-        ca.tan_half = std::tan(cam.fov_y * 0.5f * 3.14159265358979f / 180.0f);
-        ca.aspect = (float)cam.width / (float)cam.height;
-        ca.radius = cam.filter_radius;
-        ca.W = cam.width;
-        ca.H = cam.height;
-    }
-    // device scratch of this render
-    const size_t vfloats = 30;  // planes per depth: active, 27 float planes, flags, material
-    std::vector<void *> owned;
-    sty_status s = STY_OK;
-    auto alloc = [&](size_t bytes, const char *what) -> void * {
-        void *p = nullptr;
-        if (s == STY_OK) s = check_cuda(cudaMalloc(&p, bytes), what);
-        if (p) owned.push_back(p);
-        return p;
-    };
-    float *verts = (float *)alloc((size_t)D * vfloats * n * 4, "alloc vertices");
-    float *outs = (float *)alloc((size_t)D * 3 * n * 4, "alloc outputs");
-    float *psb = (float *)alloc((size_t)13 * n * 4, "alloc path state");
-    sty_pcg32 *rng = (sty_pcg32 *)alloc((size_t)n * sizeof(sty_pcg32), "alloc rng");
-    sty_style_program *dprog = (sty_style_program *)alloc(64 * sizeof(sty_style_program), "alloc programs");
-    unsigned long long *vc = (unsigned long long *)alloc(8, "alloc counter");
+    TraceJob job;
+    STY_TRY(job.init(scene, cfg->branch, cfg->max_depth, programs, n_programs, cfg->seed, st));
+    const uint32_t n = job.n, D = job.D, npx = job.npx;
     sty_pf_ref_ctx *ctx = nullptr;
-    if (s == STY_OK) s = sty_pf_ref_create(n, 1u << 26, &ctx);
-    auto cleanup = [&]() {
-        if (ctx) sty_pf_ref_destroy(ctx);
-        for (void *p : owned) cudaFree(p);
-    };
-    if (s != STY_OK) {
-        cleanup();
-        return s;
-    }
-    if (n_programs)
-        s = check_cuda(cudaMemcpyAsync(dprog, programs, n_programs * sizeof(sty_style_program), cudaMemcpyHostToDevice, st),
-                       "upload programs");
-    if (s == STY_OK) s = check_cuda(cudaMemsetAsync(vc, 0, 8, st), "zero counter");
-    // views
-    std::vector<VertOut> vo(D);
-    std::vector<sty_pf_vertices> vin(D);
-    for (uint32_t d = 0; d < D; d++) {
-        float *b = verts + (size_t)d * vfloats * n;
-        int k = 0;
-        auto pl = [&]() { return b + (size_t)(k++) * n; };
-        VertOut &w = vo[d];
-        w.active = (int32_t *)pl();
-        for (int a = 0; a < 3; a++) w.p[a] = pl();
-        for (int a = 0; a < 3; a++) w.wo[a] = pl();
-        for (int a = 0; a < 3; a++) w.ns[a] = pl();
-        for (int a = 0; a < 3; a++) w.ng[a] = pl();
-        for (int a = 0; a < 3; a++) w.le[a] = pl();
-        w.mis = pl();
-        for (int a = 0; a < 3; a++) w.dir_wi[a] = pl();
-        for (int a = 0; a < 3; a++) w.dir_l[a] = pl();
-        w.dir_pdf = pl();
-        for (int a = 0; a < 3; a++) w.ind_wi[a] = pl();
-        w.ind_mis = pl();
-        w.flags = (uint32_t *)pl();
-        w.material = (uint32_t *)pl();
-        sty_pf_vertices &r = vin[d];
-        r.active = w.active;
-        for (int a = 0; a < 3; a++) {
-            r.p[a] = w.p[a];
-            r.wo[a] = w.wo[a];
-            r.ns[a] = w.ns[a];
-            r.ng[a] = w.ng[a];
-            r.le[a] = w.le[a];
-            r.dir_wi[a] = w.dir_wi[a];
-            r.dir_l[a] = w.dir_l[a];
-            r.ind_wi[a] = w.ind_wi[a];
-        }
-        r.mis = w.mis;
-        r.dir_pdf = w.dir_pdf;
-        r.ind_mis = w.ind_mis;
-        r.flags = w.flags;
-        r.material = w.material;
-        r.n = n;
-    }
-    PathState ps;
-    {
-        int k = 0;
-        auto pl = [&]() { return psb + (size_t)(k++) * n; };
-        for (int a = 0; a < 3; a++) ps.o[a] = pl();
-        for (int a = 0; a < 3; a++) ps.d[a] = pl();
-        for (int a = 0; a < 3; a++) ps.prev_p[a] = pl();
-        ps.prev_pdf = pl();
-        ps.flags = (uint32_t *)pl();
-        ps.exclude = (uint32_t *)pl();
-        ps.terminated = (uint32_t *)pl();
-    }
+    STY_TRY(sty_pf_ref_create(n, 1u << 26, &ctx));
     const auto &mh = scene_materials(scene);
     std::vector<sty_pf_material> pm(mh.size());
     for (size_t i = 0; i < mh.size(); i++) {
@@ -563,32 +748,20 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
         for (int c = 0; c < 4; c++) pm[i].style[c] = mh[i].style[c];
     }
     float bmin[3], bmax[3];
-    scene_bounds(scene, bmin, bmax);
-    if (cfg->has_scene_bounds)
-        for (int a = 0; a < 3; a++) {
-            bmin[a] = cfg->scene_bounds[a];
-            bmax[a] = cfg->scene_bounds[3 + a];
-        }
-    const float avg = ((bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) + (bmax[2] - bmin[2])) / 3.0f;
-    const SceneView sv = scene_view(scene);
-    const unsigned nb = (n + 255) / 256;
-    if (s == STY_OK) {
-        k_rng_init<<<nb, 256, 0, st>>>(n, cfg->seed, rng);
-        s = check_launch("k_rng_init");
+    for (int a = 0; a < 3; a++) {
+        bmin[a] = cfg->has_scene_bounds ? cfg->scene_bounds[a] : job.bmin[a];
+        bmax[a] = cfg->has_scene_bounds ? cfg->scene_bounds[3 + a] : job.bmax[a];
     }
+    const float avg = ((bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) + (bmax[2] - bmin[2])) / 3.0f;
+    sty_status s = STY_OK;
     for (uint32_t rep = 0; rep < cfg->repeats && s == STY_OK; rep++) {
-        s = check_cuda(cudaMemsetAsync(verts, 0, (size_t)D * vfloats * n * 4, st), "reset vertices");
-        for (uint32_t d = 0; d < D && s == STY_OK; d++) {
-            k_trace<<<nb, 256, 0, st>>>(sv, ca, n, d, cfg->max_depth, ps, vo[d], vo[d > 0 ? d - 1 : 0], rng, dprog,
-                                        n_programs, vc);
-            s = check_launch("k_trace");
-        }
+        s = job.trace(st);
         for (int d = (int)D - 1; d >= 0 && s == STY_OK; d--) {
             sty_pf_ref_params prm;
             memset(&prm, 0, sizeof(prm));
             prm.depth = (uint32_t)d;
             const float rs = cfg->radius_scale[std::min<uint32_t>((uint32_t)d, cfg->n_radius_scale - 1)];
-            prm.radius = avg * 0.01f * rs;
+            prm.radius = avg * 0.01f * rs;  // lm_path_filtering.rs:1579-1586
             prm.reuse = cfg->reuse[std::min<uint32_t>((uint32_t)d, cfg->n_reuse - 1)];
             prm.smis = cfg->smis;
             prm.cluster = cfg->cluster;
@@ -600,23 +773,86 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
                 prm.pmax[a] = bmax[a];
             }
             prm.max_cluster_rounds = 64;
-            const float *next = (uint32_t)d + 1 < D ? outs + (size_t)(d + 1) * 3 * n : nullptr;
-            s = sty_pf_ref_filter(ctx, &vin[d], next, &prm, pm.data(), (uint32_t)pm.size(), programs, n_programs, rng,
-                                  outs + (size_t)d * 3 * n, nullptr, nullptr, stream);
+            const float *next = (uint32_t)d + 1 < D ? job.out((uint32_t)d + 1) : nullptr;
+            s = sty_pf_ref_filter(ctx, &job.vin[d], next, &prm, pm.data(), (uint32_t)pm.size(), programs, n_programs,
+                                  job.rng, job.out((uint32_t)d), nullptr, nullptr, stream);
         }
         if (s == STY_OK) {
-            k_splat<<<(npx + 255) / 256, 256, 0, st>>>(npx, cfg->branch, outs, vo[0], sv.materials, dprog, n_programs,
-                                                       cfg->no_first_hit_stylization, 1.0 / cfg->repeats, film);
+            k_splat<<<(npx + 255) / 256, 256, 0, st>>>(npx, cfg->branch, job.out(0), job.vo[0], job.sv.materials,
+                                                       job.dprog, n_programs, cfg->no_first_hit_stylization,
+                                                       1.0 / cfg->repeats, film);
             s = check_launch("k_splat");
         }
     }
     if (s == STY_OK && vertex_count) {
         unsigned long long h = 0;
-        s = check_cuda(cudaMemcpyAsync(&h, vc, 8, cudaMemcpyDeviceToHost, st), "read vertex count");
+        s = check_cuda(cudaMemcpyAsync(&h, job.vc, 8, cudaMemcpyDeviceToHost, st), "read vertex count");
         if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
         *vertex_count = h;
     }
     if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
-    cleanup();
+    sty_pf_ref_destroy(ctx);
     return s;
+}
+
+extern "C" sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t layout, uint32_t spp, uint32_t max_depth,
+                                      uint64_t seed,
+                                      float *inputs, float *targets, uint64_t capacity, uint64_t *count_out,
+                                      void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && inputs && targets && count_out, "sty_nrc_samples: null argument");
+    STY_ARG_CHECK(mode == STY_NRC_SAMPLES_TRAIN || mode == STY_NRC_SAMPLES_QUERY, "unknown mode");
+    STY_ARG_CHECK(layout == STY_NRC_ROWS_REF || layout == STY_NRC_ROWS_SPHERICAL, "unknown row layout");
+    STY_ARG_CHECK(spp >= 1 && max_depth <= 30, "bad spp / max_depth");
+    cudaStream_t st = as_stream(stream);
+    TraceJob job;
+    STY_TRY(job.init(scene, spp, mode == STY_NRC_SAMPLES_QUERY ? 0u : max_depth, nullptr, 0, seed, st));
+    STY_ARG_CHECK(mode == STY_NRC_SAMPLES_TRAIN || capacity >= job.n,
+                  "query mode writes %u rows; capacity %llu is too small", job.n, (unsigned long long)capacity);
+    FeatArgs fa;
+    for (int a = 0; a < 3; a++) {
+        fa.bmin[a] = job.bmin[a];
+        fa.bext[a] = std::max(job.bmax[a] - job.bmin[a], 1e-6f);
+    }
+    fa.max_depth = max_depth;
+    fa.layout = layout;
+    fa.dims = layout == STY_NRC_ROWS_SPHERICAL ? 11 : 20 + max_depth;
+    STY_TRY(job.trace(st));
+    const unsigned nb = (job.n + 255) / 256;
+    if (mode == STY_NRC_SAMPLES_QUERY) {
+        k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, job.n, job.vo[0], inputs, targets);
+        STY_TRY(check_launch("k_nrc_query_rows"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync samples"));
+        *count_out = job.n;
+        return STY_OK;
+    }
+    for (int d = (int)job.D - 1; d >= 0; d--) {
+        k_self_radiance<<<nb, 256, 0, st>>>(job.sv, job.n, job.vo[d], (uint32_t)d + 1 < job.D ? job.out(d + 1) : nullptr,
+                                            job.out(d));
+        STY_TRY(check_launch("k_self_radiance"));
+    }
+    unsigned long long *cnt = (unsigned long long *)job.alloc(8, "alloc row counter");
+    uint32_t *idx = (uint32_t *)job.alloc((size_t)job.n * 4, "alloc row index");
+    size_t tmp_bytes = 0;
+    STY_TRY(job.s);
+    STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, (const uint32_t *)job.vo[0].active, idx,
+                                                      (int)job.n, st),
+                       "scan size"));
+    void *tmp = job.alloc(tmp_bytes, "alloc scan scratch");
+    STY_TRY(job.s);
+    STY_TRY(check_cuda(cudaMemsetAsync(cnt, 0, 8, st), "zero rows"));
+    for (uint32_t d = 0; d < job.D; d++) {
+        const uint32_t *act = (const uint32_t *)job.vo[d].active;  // 0 / 1 flags
+        STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, act, idx, (int)job.n, st), "scan rows"));
+        k_nrc_train_rows<<<nb, 256, 0, st>>>(job.sv, fa, job.n, d, job.vo[d], job.out(d), idx, cnt, inputs, targets,
+                                             capacity);
+        STY_TRY(check_launch("k_nrc_train_rows"));
+        k_advance_rows<<<1, 1, 0, st>>>(job.n, idx, job.vo[d].active, cnt);
+        STY_TRY(check_launch("k_advance_rows"));
+    }
+    unsigned long long h = 0;
+    STY_TRY(check_cuda(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, st), "read rows"));
+    STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync samples"));
+    *count_out = h < capacity ? h : capacity;
+    return STY_OK;
 }

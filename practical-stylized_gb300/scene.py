@@ -16,6 +16,10 @@ from .abi import check, lib
 
 MAT_DIFFUSE = 0
 MAT_GGX = 1
+NRC_SAMPLES_TRAIN = 0
+NRC_SAMPLES_QUERY = 1
+NRC_ROWS_REF = 0
+NRC_ROWS_SPHERICAL = 1
 
 
 class SceneMaterial(C.Structure):
@@ -180,3 +184,21 @@ class Scene:
         check(lib().sty_pf_render(self.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(vc),
                                   _stream_ptr(stream)))
         return film, vc.value
+
+    def nrc_samples(self, mode: int, spp: int, max_depth: int, layout: int = NRC_ROWS_SPHERICAL, seed: int = 0,
+                    capacity: int | None = None, stream=None):
+        """NRC rows from the tracer (sty_nrc_samples): returns (inputs [rows, dims], targets
+        [rows, 3]) float32 device tensors, dims = 11 (spherical layout) or 20 + max_depth (the
+        reference's layout). Query mode gives spp * width * height rows."""
+        import torch
+        from .pf import _stream_ptr
+        W, H = self.camera.width, self.camera.height
+        if capacity is None:
+            capacity = W * H * spp * (max_depth + 1 if mode == NRC_SAMPLES_TRAIN else 1)
+        dims = 11 if layout == NRC_ROWS_SPHERICAL else 20 + max_depth
+        x = torch.empty((capacity, dims), dtype=torch.float32, device="cuda")
+        y = torch.empty((capacity, 3), dtype=torch.float32, device="cuda")
+        cnt = C.c_uint64()
+        check(lib().sty_nrc_samples(self.h, mode, layout, spp, max_depth, seed, x.data_ptr(), y.data_ptr(), capacity,
+                                    C.byref(cnt), _stream_ptr(stream)))
+        return x[:cnt.value], y[:cnt.value]
