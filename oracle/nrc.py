@@ -9,7 +9,9 @@ is absent: its published definitions of these components are what is restated.
 
 `bf16=True` emulates the tensor-core path exactly up to FP32 accumulation order: weights and each
 layer's input activations are rounded to bfloat16 (round to nearest even), products accumulate in
-FP64 here (FP32 in TMEM on the GPU).
+FP64 here (FP32 in TMEM on the GPU). In the gradient the loss gradient and each layer's
+pre-activation gradient are rounded to bfloat16 before they enter a product, and the ReLU mask is
+taken from the rounded activation.
 """
 from __future__ import annotations
 
@@ -61,18 +63,22 @@ def forward(params, x, freqs, layers, out_dims, bf16=False):
     return hin @ mats[layers].T, acts
 
 
-def loss_and_grad(params, x, target, freqs, layers, out_dims):
+def loss_and_grad(params, x, target, freqs, layers, out_dims, bf16=False):
     mats = unflatten(params, layers, out_dims)
-    pred, acts = forward(params, x, freqs, layers, out_dims)
+    pred, acts = forward(params, x, freqs, layers, out_dims, bf16=bf16)
+    rnd = bf16_round if bf16 else (lambda a: a)
+    if bf16:
+        mats = [bf16_round(m) for m in mats]
+        acts = [bf16_round(a) for a in acts]
     B, C = pred.shape
     den = pred * pred + 0.01
     loss = float(((pred - target) ** 2 / den).mean())
-    g = 2.0 * (pred - target) / den / (B * C)
+    g = rnd(2.0 * (pred - target) / den / (B * C))
     grads = [None] * (layers + 1)
     grads[layers] = g.T @ acts[layers]
     dh = g @ mats[layers]
     for l in range(layers - 1, -1, -1):
-        dp = dh * (acts[l + 1] > 0)
+        dp = rnd(dh * (acts[l + 1] > 0))
         grads[l] = dp.T @ acts[l]
         dh = dp @ mats[l]
     flat = np.concatenate([gm.reshape(-1) for gm in grads])

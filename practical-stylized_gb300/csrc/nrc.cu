@@ -3,6 +3,7 @@
 // The object mirrors `struct NRC` of crates/akari_cpp_ext/cpp_ext/akari_tcnn.cu:84-248: it owns the
 // weights, the optimiser state and its scratch; the caller owns the input / output / target
 // matrices. Unlike the reference, no call synchronises the device unless documented.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -281,7 +282,8 @@ sty_status ensure_batch(sty_nrc *nr, uint32_t B) {
     STY_TRY(check_cuda(cudaMalloc(&nr->bpred, (size_t)B * n.out_dims * 4), "alloc batch pred"));
     STY_TRY(check_cuda(cudaMalloc(&nr->acts, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc activations"));
     STY_TRY(check_cuda(cudaMalloc(&nr->dpre, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc gradients"));
-    const size_t chunks = (B + kWgChunk - 1) / kWgChunk;
+    size_t chunks = (B + kWgChunk - 1) / kWgChunk;
+    if (nr->cfg.precision == STY_NRC_BF16) chunks = std::max<size_t>(chunks, nrc_tc_train_ctas(B));
     STY_TRY(check_cuda(cudaMalloc(&nr->gpart, chunks * nr->np * 4), "alloc gradient partials"));
     nr->bcap = B;
     return STY_OK;
@@ -318,6 +320,25 @@ sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t s
 sty_status forward_batch(sty_nrc *nr, uint32_t B, const float *in, cudaStream_t st) {
     // training forward (stores the activations the backward pass reads)
     return fwd_f32(nr, nr->w, B, in, nr->bpred, nr->acts, st);
+}
+
+bool tc_training(const sty_nrc *nr) {
+    return nr->cfg.precision == STY_NRC_BF16 && nr->net.layers <= kNrcTcTrainMaxLayers;
+}
+
+// Weight gradient of one batch into nr->g (loss added to nr->loss): the fused BF16 tensor-core
+// step for BF16 caches, else the FP32 forward / backward / weight-gradient kernels.
+sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float *target, cudaStream_t st) {
+    if (!tc_training(nr)) {
+        STY_TRY(forward_batch(nr, B, in, st));
+        return backward(nr, B, target, st);
+    }
+    STY_TRY(nrc_tc_pack(nr->net, nr->w, nr->img, st));
+    nr->img_dirty = true;  // nr->img now holds w, which the optimiser step is about to change
+    const uint32_t ctas = nrc_tc_train_ctas(B);
+    STY_TRY(nrc_tc_train(nr->net, nr->img, B, in, target, nr->gpart, nr->np, nr->loss, ctas, st));
+    k_sum_chunks<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, ctas, nr->gpart, nr->g);
+    return check_launch("k_sum_chunks");
 }
 
 sty_status refresh_images(sty_nrc *nr, cudaStream_t st) {
@@ -475,8 +496,7 @@ sty_status sty_nrc_gradient(sty_nrc *nr, uint32_t B, const float *in, const floa
     cudaStream_t st = as_stream(stream);
     STY_TRY(ensure_batch(nr, B));
     STY_TRY(check_cuda(cudaMemsetAsync(nr->loss, 0, 4, st), "zero loss"));
-    STY_TRY(forward_batch(nr, B, in, st));
-    STY_TRY(backward(nr, B, target, st));
+    STY_TRY(batch_gradient(nr, B, in, target, st));
     STY_TRY(check_cuda(cudaMemcpyAsync(grad, nr->g, nr->np * 4, cudaMemcpyDeviceToDevice, st), "copy grad"));
     if (loss_out) {
         STY_TRY(check_cuda(cudaMemcpyAsync(loss_out, nr->loss, 4, cudaMemcpyDeviceToHost, st), "read loss"));
@@ -497,8 +517,7 @@ sty_status sty_nrc_train(sty_nrc *nr, uint64_t count, uint64_t n_iters, const fl
         k_collect<<<(B + 255) / 256, 256, 0, st>>>(B, c.seed, nr->step, count, nr->net.in_dims, nr->net.out_dims, in,
                                                    target, nr->bin, nr->btg);
         STY_TRY(check_launch("k_collect"));
-        STY_TRY(forward_batch(nr, B, nr->bin, st));
-        STY_TRY(backward(nr, B, nr->btg, st));
+        STY_TRY(batch_gradient(nr, B, nr->bin, nr->btg, st));
         nr->step++;
         const double t = (double)nr->step;
         const float lr_t = nr->lr * (float)std::pow((double)c.decay_base, std::floor((t - 1.0) / c.decay_interval));

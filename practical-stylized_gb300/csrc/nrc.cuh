@@ -48,5 +48,11 @@ sty_status nrc_tc_pack(const NrcNet &n, const float *w_fp32, uint16_t *w_img, cu
 size_t nrc_tc_image_elems(const NrcNet &n);
 sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *w_img, uint64_t count, const float *input, float *output,
                           cudaStream_t st);
+// Fused BF16 training step (forward, relative-L2 gradient, backward, weight gradient) over a batch
+// of B samples on `ctas` CTAs (nrc_tc_train_ctas); per-CTA gradient sums go to part[ctas][np].
+constexpr int kNrcTcTrainMaxLayers = 6;
+uint32_t nrc_tc_train_ctas(uint32_t B);
+sty_status nrc_tc_train(const NrcNet &n, const uint16_t *w_img, uint32_t B, const float *input, const float *target,
+                        float *part, size_t np, float *loss, uint32_t ctas, cudaStream_t st);
 
 }  // namespace sty

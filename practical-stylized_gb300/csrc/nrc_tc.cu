@@ -32,13 +32,19 @@ __device__ __forceinline__ unsigned long long gtimer() {
 __host__ __device__ __forceinline__ uint32_t img_off(uint32_t row, uint32_t k) {
     return (((row >> 3) * 8u + (k >> 3)) * 128u) + (row & 7u) * 16u + (k & 7u) * 2u;
 }
-__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
-    const uint64_t lbo = 128, sbo = 1024;
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((lbo >> 4) << 16) | ((sbo >> 4) << 32) | (1ull << 46);
+// Shared-memory matrix descriptor of an image. Read K-major (K = the 64 columns): the K-adjacent
+// core matrices are 128 bytes apart (LBO) and 8-row groups 1024 bytes (SBO). The same image read
+// MN-major (K = the rows, MN = the columns) has LBO = 1024 (next 8 rows along K) and SBO = 128
+// (next 8 columns along MN); a K step of 16 rows then advances the start by 2048 bytes.
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo = 128, uint32_t sbo = 1024) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
 }
-__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
-    // D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1), K-major A and B, N>>3, M>>4
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+__device__ __forceinline__ uint64_t make_desc_mn(uint32_t saddr) { return make_desc(saddr, 1024, 128); }
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n, uint32_t a_mn = 0, uint32_t b_mn = 0) {
+    // D f32 (bit 4), A bf16 (bits 7-9 = 1), B bf16 (bits 10-12 = 1), A / B major-ness (bits 15 / 16,
+    // 1 = MN-major), N>>3 (bits 17-22), M>>4 (bits 24-28)
+    return (1u << 4) | (1u << 7) | (1u << 10) | (a_mn << 15) | (b_mn << 16) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
     asm volatile(
@@ -222,6 +228,276 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
 }
 
+// ---- fused BF16 training step --------------------------------------------------------------
+// One CTA (one warpgroup) per SM, persistent over tiles of 128 samples of the batch. Per tile:
+//   forward   act_{l+1} = relu(act_l W_l^T) (M=128, N=64, K=64), every act_l kept in shared memory
+//             as a K-major image; pred = act_L W_out^T (N=16); g = dLoss/dpred (relative L2)
+//   backward  dH_{L-1} = g W_out (K=16), dP_l = dH_l * [act_{l+1} > 0], dH_{l-1} = dP_l W_l
+//             (B = the forward weight image read MN-major)
+//   gradient  dW_l += dP_l^T act_l (M=64, N=64, K=128; both images read MN-major) and
+//             dW_out^T += act_L^T g (M=64, N=16), accumulated in TMEM across the CTA's tiles.
+// TMEM columns: 0-63 forward / backward accumulator (M=128: lane = sample); 64 + 64 l the M=64
+// accumulator of dW_l (row j in lane (j / 16) * 32 + j % 16); 64 + 64 L the dW_out^T accumulator.
+// At the end each CTA stores its sums to part + blockIdx.x * np (the flat parameter order) and the
+// caller adds the CTAs' partials in order, so the gradient is deterministic for a device.
+struct TrainArgs {
+    NrcNet n;
+    const uint16_t *wimg;
+    uint32_t B;
+    const float *input, *target;
+    float *part;  // [gridDim.x][np]
+    size_t np;
+    float *loss;
+    uint32_t *status;
+};
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+
+__global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ float red[4];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int L = a.n.layers, O = a.n.out_dims;
+    const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
+    uint8_t *wimg = smem;
+    uint8_t *acts = smem + ((wbytes + 1023u) & ~1023u);  // L + 1 activation images
+    uint8_t *dtile = acts + (size_t)(L + 1) * kTileBytes;  // g, then dP_l
+    for (uint32_t o = tid * 16u; o < wbytes; o += 128u * 16u)
+        *reinterpret_cast<uint4 *>(wimg + o) =
+            *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
+    const uint32_t wbase = smem_u32(wimg), abase = smem_u32(acts), dbase = smem_u32(dtile);
+    const uint32_t wout = wbase + (uint32_t)L * W * W * 2u;
+    const uint32_t c_out = 64u + 64u * (uint32_t)L;
+    const float norm = 1.0f / ((float)a.B * (float)O);
+    uint32_t phase = 0;
+    bool failed = false;
+    float lsum = 0.0f;
+    bool first = true;  // first tile of this CTA: the dW accumulators start from zero
+
+    // wait for the MMAs committed so far; CTA-uniform result
+    auto sync_mma = [&]() -> bool {
+        const bool got = mbar_wait(&mbar, phase, a.status);
+        phase ^= 1u;
+        if (!__syncthreads_and(got)) return false;
+        fence_after();
+        return true;
+    };
+    auto publish = [&]() {  // generic-proxy smem writes -> visible to the next MMAs
+        fence_async_smem();
+        fence_before();
+        __syncthreads();
+    };
+
+    const uint32_t ntiles = (a.B + TM - 1) / TM;
+    for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const uint32_t row = tile * TM + tid;
+        const bool valid = row < a.B;
+        {
+            float enc[W];
+            if (valid) {
+                nrc_encode(a.n, a.input + (size_t)row * a.n.in_dims, enc);
+            } else {
+#pragma unroll
+                for (int k = 0; k < W; k++) enc[k] = 0.0f;
+            }
+            store_row(acts, tid, enc);
+        }
+        publish();
+        // ---- forward
+        for (int l = 0; l <= L && !failed; l++) {
+            const bool out_layer = l == L;
+            if (tid == 0) {
+                fence_after();
+                const uint32_t al = abase + (uint32_t)l * kTileBytes, wl = wbase + (uint32_t)l * W * W * 2u;
+                const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++)
+                    mma_bf16(tmem, make_desc(al + kk * 256u), make_desc(wl + kk * 256u), idesc, kk > 0 ? 1u : 0u);
+                mma_commit(&mbar);
+            }
+            if (!sync_mma()) {
+                failed = true;
+                break;
+            }
+            if (!out_layer) {
+                uint8_t *nxt = acts + (size_t)(l + 1) * kTileBytes;
+                float v[32];
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    tmem_ld32(lane_base + half * 32u, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int kb = 0; kb < 4; kb++) {
+                        uint4 q;
+                        q.x = pack_bf16(fmaxf(v[kb * 8 + 0], 0.0f), fmaxf(v[kb * 8 + 1], 0.0f));
+                        q.y = pack_bf16(fmaxf(v[kb * 8 + 2], 0.0f), fmaxf(v[kb * 8 + 3], 0.0f));
+                        q.z = pack_bf16(fmaxf(v[kb * 8 + 4], 0.0f), fmaxf(v[kb * 8 + 5], 0.0f));
+                        q.w = pack_bf16(fmaxf(v[kb * 8 + 6], 0.0f), fmaxf(v[kb * 8 + 7], 0.0f));
+                        *reinterpret_cast<uint4 *>(nxt + img_off(tid, half * 32 + kb * 8)) = q;
+                    }
+                }
+            } else {
+                // loss gradient of the relative L2 loss (prediction treated as a constant in the
+                // denominator) into columns 0..15 of dtile; rows past the batch give zero
+                float v[16], gr[16];
+                tmem_ld16(lane_base, v);
+                tmem_wait_ld();
+#pragma unroll
+                for (int c = 0; c < 16; c++) {
+                    gr[c] = 0.0f;
+                    if (valid && c < O) {
+                        const float p = v[c], t = a.target[(size_t)row * O + c];
+                        const float den = p * p + 0.01f;
+                        lsum += (p - t) * (p - t) / den;
+                        gr[c] = 2.0f * (p - t) / den * norm;
+                    }
+                }
+#pragma unroll
+                for (int kb = 0; kb < 2; kb++) {
+                    uint4 q;
+                    q.x = pack_bf16(gr[kb * 8 + 0], gr[kb * 8 + 1]);
+                    q.y = pack_bf16(gr[kb * 8 + 2], gr[kb * 8 + 3]);
+                    q.z = pack_bf16(gr[kb * 8 + 4], gr[kb * 8 + 5]);
+                    q.w = pack_bf16(gr[kb * 8 + 6], gr[kb * 8 + 7]);
+                    *reinterpret_cast<uint4 *>(dtile + img_off(tid, kb * 8)) = q;
+                }
+            }
+            publish();
+        }
+        if (failed) break;
+        // ---- output layer: dW_out^T += act_L^T g ; dH_{L-1} = g W_out
+        if (tid == 0) {
+            fence_after();
+            const uint32_t aL = abase + (uint32_t)L * kTileBytes;
+#pragma unroll 1
+            for (int kk = 0; kk < TM / 16; kk++)
+                mma_bf16(tmem + c_out, make_desc_mn(aL + kk * 2048u), make_desc_mn(dbase + kk * 2048u),
+                         idesc_bf16(64, kNrcOutPad, 1, 1), (first && kk == 0) ? 0u : 1u);
+            mma_bf16(tmem, make_desc(dbase), make_desc_mn(wout), idesc_bf16(TM, W, 0, 1), 0u);
+            mma_commit(&mbar);
+        }
+        if (!sync_mma()) {
+            failed = true;
+            break;
+        }
+        // ---- hidden layers, last to first
+        for (int l = L - 1; l >= 0; l--) {
+            {
+                // dP_l = dH_l * [act_{l+1} > 0] -> dtile
+                const uint8_t *hl = acts + (size_t)(l + 1) * kTileBytes;
+                float v[32];
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    tmem_ld32(lane_base + half * 32u, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int kb = 0; kb < 4; kb++) {
+                        const uint32_t off = img_off(tid, half * 32 + kb * 8);
+                        const uint4 h = *reinterpret_cast<const uint4 *>(hl + off);
+                        const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                        uint32_t o[4];
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const float d0 = bf16_lo(hw[e]) > 0.0f ? v[kb * 8 + 2 * e] : 0.0f;
+                            const float d1 = bf16_hi(hw[e]) > 0.0f ? v[kb * 8 + 2 * e + 1] : 0.0f;
+                            o[e] = pack_bf16(d0, d1);
+                        }
+                        *reinterpret_cast<uint4 *>(dtile + off) = make_uint4(o[0], o[1], o[2], o[3]);
+                    }
+                }
+            }
+            publish();
+            if (tid == 0) {
+                fence_after();
+                const uint32_t al = abase + (uint32_t)l * kTileBytes;
+#pragma unroll 1
+                for (int kk = 0; kk < TM / 16; kk++)
+                    mma_bf16(tmem + 64u + 64u * (uint32_t)l, make_desc_mn(dbase + kk * 2048u),
+                             make_desc_mn(al + kk * 2048u), idesc_bf16(64, W, 1, 1), (first && kk == 0) ? 0u : 1u);
+                if (l > 0) {
+                    const uint32_t wl = wbase + (uint32_t)l * W * W * 2u;
+#pragma unroll
+                    for (int kk = 0; kk < 4; kk++)
+                        mma_bf16(tmem, make_desc(dbase + kk * 256u), make_desc_mn(wl + kk * 2048u),
+                                 idesc_bf16(TM, W, 0, 1), kk > 0 ? 1u : 0u);
+                }
+                mma_commit(&mbar);
+            }
+            if (!sync_mma()) {
+                failed = true;
+                break;
+            }
+        }
+        first = false;
+    }
+    if (failed) {
+        mbar_wait(&mbar, phase, a.status);
+    } else if (!first) {
+        // this CTA's weight-gradient sums -> part[blockIdx.x]; M=64 rows live in lanes 0-15 of each
+        // warp's quarter: row j = 16 * warp + lane
+        float *dst = a.part + (size_t)blockIdx.x * a.np;
+        const int j = 16 * warp + lane;
+        for (int l = 0; l < L; l++) {
+            float v[32];
+#pragma unroll
+            for (int half = 0; half < 2; half++) {
+                tmem_ld32(lane_base + 64u + 64u * (uint32_t)l + half * 32u, v);
+                tmem_wait_ld();
+                if (lane < 16) {
+                    float *d = dst + nrc_w_offset(l) + (size_t)j * W + half * 32;
+#pragma unroll
+                    for (int k = 0; k < 32; k += 4)
+                        *reinterpret_cast<float4 *>(d + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+                }
+            }
+        }
+        float v[16];
+        tmem_ld16(lane_base + c_out, v);  // row = input column k, column = output c
+        tmem_wait_ld();
+        if (lane < 16)
+            for (int c = 0; c < O; c++) dst[nrc_w_offset(L) + (size_t)c * W + j] = v[c];
+    } else {
+        // no tile: zero partials keep the ordered sum exact
+        for (size_t p = tid; p < a.np; p += 128) a.part[(size_t)blockIdx.x * a.np + p] = 0.0f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0) red[warp] = lsum;
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (tid == 0 && a.loss) atomicAdd(a.loss, (red[0] + red[1] + red[2] + red[3]) * (1.0f / ((float)a.B * (float)O)));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
 // FP32 [out][in] -> BF16 K-major images; output layer padded to 16 rows of zeros
 __global__ void k_pack(NrcNet n, const float *w, uint16_t *img) {
     const int L = n.layers;
@@ -280,6 +556,48 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
     const uint64_t grid = ntiles < (uint64_t)sms * 3 ? ntiles : (uint64_t)sms * 3;
     k_nrc_fwd_tc<<<(unsigned)grid, 128, smem, st>>>(a);
     return check_launch("k_nrc_fwd_tc");
+}
+
+size_t nrc_tc_train_smem(const NrcNet &n) {
+    const size_t wbytes = nrc_tc_image_elems(n) * 2;
+    const size_t need = ((wbytes + 1023) & ~(size_t)1023) + (size_t)(n.layers + 2) * kTileBytes + 1024;
+    // at least 120 KB so that one CTA (and its 512 TMEM columns) owns the SM
+    return need < 122880 ? 122880 : need;
+}
+
+uint32_t nrc_tc_train_ctas(uint32_t B) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint32_t ntiles = (B + TM - 1) / TM;
+    return ntiles < (uint32_t)sms ? ntiles : (uint32_t)sms;
+}
+
+sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const float *input, const float *target,
+                        float *part, size_t np, float *loss, uint32_t ctas, cudaStream_t st) {
+    if (n.layers > kNrcTcTrainMaxLayers) {
+        set_error("tensor-core training supports at most %d hidden layers", kNrcTcTrainMaxLayers);
+        return STY_ERR_ARG;
+    }
+    TrainArgs a;
+    a.n = n;
+    a.wimg = img;
+    a.B = B;
+    a.input = input;
+    a.target = target;
+    a.part = part;
+    a.np = np;
+    a.loss = loss;
+    a.status = device_status_ptr();
+    if (!a.status) {
+        set_error("device status word unavailable");
+        return STY_ERR_CUDA;
+    }
+    const size_t smem = nrc_tc_train_smem(n);
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                       "attr k_nrc_train_tc"));
+    k_nrc_train_tc<<<ctas, 128, smem, st>>>(a);
+    return check_launch("k_nrc_train_tc");
 }
 
 }  // namespace sty

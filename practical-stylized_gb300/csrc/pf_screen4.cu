@@ -53,7 +53,6 @@ constexpr int CH = 4;   // candidate rows per buffer
 constexpr int NB = STY_PF4_NB;  // ring depth
 constexpr int PU = 4;   // records staged per producer thread per batch (loads in flight)
 constexpr int NF = 10;  // staged fields: p'(3) n(3) m, v(3)   [direct form: m = 1/0, v = in]
-constexpr float kL2E = 1.4426950408889634f;
 constexpr float kLimQ = 16.0f;
 constexpr float kLimC = 120.0f;
 constexpr float kFar = 1e18f;

@@ -4,7 +4,8 @@ the tcgen05 BF16 path against it (GPU).
 Tolerances: FP32 path vs FP64 oracle 1e-4 relative (5 chained 64-wide FP32 matmuls); BF16 path vs
 the oracle's BF16 emulation (weights and layer inputs rounded to bfloat16): 99 % of outputs within
 1e-4 of the output scale and all within 1e-2 (FP32 accumulation order in TMEM, and BF16
-rounding-boundary flips of intermediate activations); BF16 vs exact FP64 only statistically (relative RMS < 3 %)."""
+rounding-boundary flips of intermediate activations); BF16 vs exact FP64 only statistically (relative RMS < 3 %).
+BF16 weight gradient vs the emulation 3e-3 in norm, vs the FP64 gradient 5e-2 in norm and cosine > 0.998."""
 import numpy as np
 import pytest
 
@@ -117,6 +118,34 @@ def test_bf16_tensor_core_inference(sty, cuda, layers):
     assert err.max() <= 1e-2 * scale, f"max err {err.max():.3e} vs scale {scale:.3e}"
     rms = np.sqrt(((out - ref) ** 2).mean()) / np.sqrt((ref ** 2).mean())
     assert rms < 3e-2
+    assert sty.abi.device_status() == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("layers,batch", [(5, 128 * 300 + 77), (1, 200), (6, 1024)])
+def test_bf16_tensor_core_gradient(sty, cuda, layers, batch):
+    """Fused tcgen05 training step (forward, loss gradient, backward, weight gradient) against the
+    oracle's BF16 emulation of the same arithmetic, and against the exact FP64 gradient; ragged
+    batches leave the last tile partly empty, and more tiles than SMs exercise the per-CTA sums."""
+    net = _make(sty, sty.nrc.STY_NRC_BF16, batch=1024, layers=layers, seed=5)
+    p = net.save_params().astype(np.float64)
+    rng = np.random.default_rng(6)
+    x = rng.random((batch, 11))
+    t = target_fn(x)
+    g, loss = net.gradient(_dev(x), _dev(t))
+    g = g.cpu().numpy().astype(np.float64)
+    assert np.isfinite(g).all()
+    el, eg = onrc.loss_and_grad(p, x, t, FREQS, layers, 3, bf16=True)
+    rl, rg = onrc.loss_and_grad(p, x, t, FREQS, layers, 3)
+    # emulation: equal up to FP32 accumulation order and rare BF16 rounding-boundary flips
+    assert np.linalg.norm(g - eg) <= 3e-3 * np.linalg.norm(eg), np.linalg.norm(g - eg) / np.linalg.norm(eg)
+    assert abs(loss - el) <= 1e-3 * abs(el)
+    # exact FP64 gradient: BF16 operands cost about 2^-8 relative per rounding
+    assert np.linalg.norm(g - rg) <= 5e-2 * np.linalg.norm(rg)
+    assert float(g @ rg) / (np.linalg.norm(g) * np.linalg.norm(rg)) > 0.998
+    # deterministic: per-CTA partial sums are added in a fixed order
+    g2, _ = net.gradient(_dev(x), _dev(t))
+    assert (g2.cpu().numpy() == g.astype(np.float32)).all()
     assert sty.abi.device_status() == 0
 
 
