@@ -92,27 +92,95 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 #pragma unroll
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-    const __nv_bfloat16_raw ra = __float2bfloat16_rn(a), rb = __float2bfloat16_rn(b);
-    return (uint32_t)ra.x | ((uint32_t)rb.x << 16);
+// Frequency-encoding plan: encoded column pair p (columns 2p, 2p+1) is (sin, cos) of
+// pi * 2^k * x[pdim[p]], with pfirst[p] marking k = 0 (a fresh sincospif; later octaves by the
+// double-angle identities, in the order of nrc_encode); pdim = 0xff pads the row with zeros.
+struct EncPlan {
+    uint8_t pdim[kNrcWidth / 2];
+    uint8_t pfirst[kNrcWidth / 2];
+};
+EncPlan make_plan(const NrcNet &n) {
+    EncPlan e;
+    int p = 0;
+    for (int d = 0; d < n.in_dims; d++)
+        for (uint32_t k = 0; k < n.freqs[d] && p < kNrcWidth / 2; k++, p++) {
+            e.pdim[p] = (uint8_t)d;
+            e.pfirst[p] = k == 0;
+        }
+    for (; p < kNrcWidth / 2; p++) {
+        e.pdim[p] = 0xff;
+        e.pfirst[p] = 0;
+    }
+    return e;
 }
-// write one 64-wide row of BF16 (from FP32 v) into a K-major image
-__device__ __forceinline__ void store_row(uint8_t *img, uint32_t row, const float *v) {
+
+__device__ __forceinline__ uint32_t pack2_bf16(float lo, float hi) {  // RN, lo in bits 0-15
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+__device__ __forceinline__ uint32_t pack2_relu_bf16(float lo, float hi) {  // max(RN(v), 0)
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+// encode one sample (x = its input row, or nullptr for a padding row) into row `row` of a K-major
+// image, one 16-byte store per 8 columns
+__device__ __forceinline__ void encode_row(const EncPlan &e, const float *x, uint8_t *img, uint32_t row) {
+    float s = 0.0f, c = 0.0f;
 #pragma unroll
     for (int kb = 0; kb < 8; kb++) {
-        uint4 q;
-        q.x = pack_bf16(v[kb * 8 + 0], v[kb * 8 + 1]);
-        q.y = pack_bf16(v[kb * 8 + 2], v[kb * 8 + 3]);
-        q.z = pack_bf16(v[kb * 8 + 4], v[kb * 8 + 5]);
-        q.w = pack_bf16(v[kb * 8 + 6], v[kb * 8 + 7]);
-        *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) = q;
+        uint32_t q[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int p = kb * 4 + j;
+            const uint32_t d = e.pdim[p];
+            float vs = 0.0f, vc = 0.0f;
+            if (d != 0xffu && x) {
+                if (e.pfirst[p]) {
+                    sincospif(x[d], &s, &c);
+                } else {
+                    const float s2 = 2.0f * s * c;
+                    c = fmaf(-2.0f * s, s, 1.0f);
+                    s = s2;
+                }
+                vs = s;
+                vc = c;
+            }
+            q[j] = pack2_bf16(vs, vc);
+        }
+        *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) = make_uint4(q[0], q[1], q[2], q[3]);
     }
+}
+
+// per-warpgroup named barriers (id 1 + warpgroup; id 0 is __syncthreads)
+__device__ __forceinline__ void wg_sync(uint32_t id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
+__device__ __forceinline__ bool wg_sync_and(uint32_t id, bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred pi, po;\n\tsetp.ne.u32 pi, %1, 0;\n\tbar.red.and.pred po, %2, 128, pi;\n\t"
+        "selp.u32 %0, 1, 0, po;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)p), "r"(id)
+        : "memory");
+    return r != 0;
 }
 
 struct TcArgs {
     NrcNet n;
+    EncPlan plan;
     const uint16_t *wimg;  // global weight image
     uint64_t count;
     const float *input;
@@ -120,25 +188,35 @@ struct TcArgs {
     uint32_t *status;
 };
 
-__global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
+// Inference: kFwdWG warpgroups per CTA share one copy of the weight images; each warpgroup owns
+// one 128-sample tile at a time (its own activation image, 64 TMEM columns, mbarrier and named
+// barrier), so 2 CTAs x kFwdWG tiles are in flight per SM and one tile's epilogue overlaps
+// another's MMAs. Per layer: thread 0 of the warpgroup issues 4 x tcgen05.mma (M=128, N=64 (16
+// for the output layer), K=16) and commits to the warpgroup's mbarrier; the warpgroup waits
+// (bounded), tcgen05.ld's its rows and writes ReLU'd BF16 rows back as the next A operand.
+constexpr int kFwdWG = 4;
+__global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[kFwdWG];
     __shared__ uint32_t tmem_slot;
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, wg = tid >> 7, t = tid & 127;
+    const uint32_t bar_id = 1u + (uint32_t)wg;
     const int L = a.n.layers;
     const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
-    uint8_t *wimg = smem;                 // weights
-    uint8_t *act = smem + ((wbytes + 1023u) & ~1023u);  // activation tile (1 KB aligned)
+    uint8_t *wimg = smem;
+    uint8_t *act = smem + ((wbytes + 1023u) & ~1023u) + (size_t)wg * kTileBytes;
 
-    // weights -> shared memory (16-byte copies)
-    for (uint32_t o = tid * 16u; o < wbytes; o += 128u * 16u)
-        *reinterpret_cast<uint4 *>(wimg + o) = *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
+    for (uint32_t o = tid * 16u; o < wbytes; o += 128u * kFwdWG * 16u)
+        *reinterpret_cast<uint4 *>(wimg + o) =
+            *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)) : "memory");
+        for (int g = 0; g < kFwdWG; g++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar[g])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_u32(&tmem_slot))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(64u * kFwdWG)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -146,42 +224,34 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = tmem_slot;
-    const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
+    const uint32_t tmem = tmem_slot + 64u * (uint32_t)wg;
+    const uint32_t lane_base = tmem + (((uint32_t)(warp & 3) * 32u) << 16);
     const uint32_t wbase = smem_u32(wimg), abase = smem_u32(act);
+    uint64_t *bar = &mbar[wg];
     uint32_t phase = 0;
-    bool failed = false;  // CTA-uniform (decided through __syncthreads_and)
+    bool failed = false;  // uniform over the warpgroup (decided through bar.red.and)
 
     const uint64_t ntiles = (a.count + TM - 1) / TM;
-    for (uint64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-        const uint64_t row = tile * TM + tid;
-        // encode this thread's sample into row tid of the activation tile
-        {
-            float enc[W];
-            if (row < a.count) {
-                nrc_encode(a.n, a.input + row * a.n.in_dims, enc);
-            } else {
-#pragma unroll
-                for (int k = 0; k < W; k++) enc[k] = 0.0f;
-            }
-            store_row(act, tid, enc);
-        }
+    for (uint64_t tile = (uint64_t)blockIdx.x * kFwdWG + wg; tile < ntiles && !failed;
+         tile += (uint64_t)gridDim.x * kFwdWG) {
+        const uint64_t row = tile * TM + t;
+        encode_row(a.plan, row < a.count ? a.input + row * a.n.in_dims : nullptr, act, t);
         fence_async_smem();
         fence_before();
-        __syncthreads();
+        wg_sync(bar_id);
         for (int l = 0; l <= L; l++) {
             const bool out_layer = l == L;
-            if (tid == 0) {
+            if (t == 0) {
                 fence_after();
                 const uint32_t wl = wbase + (uint32_t)l * W * W * 2u;
                 const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++)
                     mma_bf16(tmem, make_desc(abase + kk * 256u), make_desc(wl + kk * 256u), idesc, kk > 0 ? 1u : 0u);
-                mma_commit(&mbar);
+                mma_commit(bar);
             }
-            const bool got = mbar_wait(&mbar, phase, a.status);
-            if (!__syncthreads_and(got)) {
+            const bool got = mbar_wait(bar, phase, a.status);
+            if (!wg_sync_and(bar_id, got)) {
                 failed = true;
                 break;
             }
@@ -194,38 +264,37 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
                     tmem_ld32(lane_base + half * 32u, v);
                     tmem_wait_ld();
 #pragma unroll
-                    for (int k = 0; k < 32; k++) v[k] = fmaxf(v[k], 0.0f);
-                    // columns half*32 .. half*32+31 -> k-blocks half*4 .. half*4+3
-#pragma unroll
                     for (int kb = 0; kb < 4; kb++) {
-                        uint4 q;
-                        q.x = pack_bf16(v[kb * 8 + 0], v[kb * 8 + 1]);
-                        q.y = pack_bf16(v[kb * 8 + 2], v[kb * 8 + 3]);
-                        q.z = pack_bf16(v[kb * 8 + 4], v[kb * 8 + 5]);
-                        q.w = pack_bf16(v[kb * 8 + 6], v[kb * 8 + 7]);
-                        *reinterpret_cast<uint4 *>(act + img_off(tid, half * 32 + kb * 8)) = q;
+                        const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
+                                                   pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
+                                                   pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
+                                                   pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
+                        *reinterpret_cast<uint4 *>(act + img_off(t, half * 32 + kb * 8)) = q;
                     }
                 }
                 fence_async_smem();
             } else {
-                float v[32];
-                tmem_ld32(lane_base, v);  // columns 0..31 (the first out_dims are the output)
+                float v[16];
+                tmem_ld16(lane_base, v);
                 tmem_wait_ld();
                 if (row < a.count)
                     for (int c = 0; c < a.n.out_dims; c++) a.output[row * a.n.out_dims + c] = v[c];
             }
             fence_before();
-            __syncthreads();
+            wg_sync(bar_id);
         }
     }
     if (failed) {
         // the last commit never arrived within the limit: give the MMA one more bounded wait before
         // the accumulator columns are released
-        mbar_wait(&mbar, phase, a.status);
+        mbar_wait(bar, phase, a.status);
     }
+    fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"(64u * kFwdWG)
+                     : "memory");
 }
 
 // ---- fused BF16 training step --------------------------------------------------------------
@@ -242,6 +311,7 @@ __global__ void __launch_bounds__(128) k_nrc_fwd_tc(const TcArgs a) {
 // caller adds the CTAs' partials in order, so the gradient is deterministic for a device.
 struct TrainArgs {
     NrcNet n;
+    EncPlan plan;
     const uint16_t *wimg;
     uint32_t B;
     const float *input, *target;
@@ -251,16 +321,6 @@ struct TrainArgs {
     uint32_t *status;
 };
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-#pragma unroll
-    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
 __device__ __forceinline__ float bf16_lo(uint32_t w) { return __uint_as_float(w << 16); }
 __device__ __forceinline__ float bf16_hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
 
@@ -320,16 +380,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
     for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const uint32_t row = tile * TM + tid;
         const bool valid = row < a.B;
-        {
-            float enc[W];
-            if (valid) {
-                nrc_encode(a.n, a.input + (size_t)row * a.n.in_dims, enc);
-            } else {
-#pragma unroll
-                for (int k = 0; k < W; k++) enc[k] = 0.0f;
-            }
-            store_row(acts, tid, enc);
-        }
+        encode_row(a.plan, valid ? a.input + (size_t)row * a.n.in_dims : nullptr, acts, tid);
         publish();
         // ---- forward
         for (int l = 0; l <= L && !failed; l++) {
@@ -356,11 +407,10 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
                     tmem_wait_ld();
 #pragma unroll
                     for (int kb = 0; kb < 4; kb++) {
-                        uint4 q;
-                        q.x = pack_bf16(fmaxf(v[kb * 8 + 0], 0.0f), fmaxf(v[kb * 8 + 1], 0.0f));
-                        q.y = pack_bf16(fmaxf(v[kb * 8 + 2], 0.0f), fmaxf(v[kb * 8 + 3], 0.0f));
-                        q.z = pack_bf16(fmaxf(v[kb * 8 + 4], 0.0f), fmaxf(v[kb * 8 + 5], 0.0f));
-                        q.w = pack_bf16(fmaxf(v[kb * 8 + 6], 0.0f), fmaxf(v[kb * 8 + 7], 0.0f));
+                        const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
+                                                   pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
+                                                   pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
+                                                   pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
                         *reinterpret_cast<uint4 *>(nxt + img_off(tid, half * 32 + kb * 8)) = q;
                     }
                 }
@@ -382,11 +432,10 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
                 }
 #pragma unroll
                 for (int kb = 0; kb < 2; kb++) {
-                    uint4 q;
-                    q.x = pack_bf16(gr[kb * 8 + 0], gr[kb * 8 + 1]);
-                    q.y = pack_bf16(gr[kb * 8 + 2], gr[kb * 8 + 3]);
-                    q.z = pack_bf16(gr[kb * 8 + 4], gr[kb * 8 + 5]);
-                    q.w = pack_bf16(gr[kb * 8 + 6], gr[kb * 8 + 7]);
+                    const uint4 q = make_uint4(pack2_bf16(gr[kb * 8 + 0], gr[kb * 8 + 1]),
+                                               pack2_bf16(gr[kb * 8 + 2], gr[kb * 8 + 3]),
+                                               pack2_bf16(gr[kb * 8 + 4], gr[kb * 8 + 5]),
+                                               pack2_bf16(gr[kb * 8 + 6], gr[kb * 8 + 7]));
                     *reinterpret_cast<uint4 *>(dtile + img_off(tid, kb * 8)) = q;
                 }
             }
@@ -428,7 +477,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
                         for (int e = 0; e < 4; e++) {
                             const float d0 = bf16_lo(hw[e]) > 0.0f ? v[kb * 8 + 2 * e] : 0.0f;
                             const float d1 = bf16_hi(hw[e]) > 0.0f ? v[kb * 8 + 2 * e + 1] : 0.0f;
-                            o[e] = pack_bf16(d0, d1);
+                            o[e] = pack2_bf16(d0, d1);
                         }
                         *reinterpret_cast<uint4 *>(dtile + off) = make_uint4(o[0], o[1], o[2], o[3]);
                     }
@@ -536,6 +585,7 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
                           cudaStream_t st) {
     TcArgs a;
     a.n = n;
+    a.plan = make_plan(n);
     a.wimg = img;
     a.count = count;
     a.input = input;
@@ -546,15 +596,16 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
         return STY_ERR_CUDA;
     }
     const size_t wbytes = nrc_tc_image_elems(n) * 2;
-    const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + kTileBytes + 1024;
+    const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + (size_t)kFwdWG * kTileBytes + 1024;
     STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "attr k_nrc_fwd_tc"));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t ntiles = (count + TM - 1) / TM;
-    const uint64_t grid = ntiles < (uint64_t)sms * 3 ? ntiles : (uint64_t)sms * 3;
-    k_nrc_fwd_tc<<<(unsigned)grid, 128, smem, st>>>(a);
+    const uint64_t ctas = (ntiles + kFwdWG - 1) / kFwdWG;
+    const uint64_t grid = ctas < (uint64_t)sms * 2 ? ctas : (uint64_t)sms * 2;
+    k_nrc_fwd_tc<<<(unsigned)grid, 128 * kFwdWG, smem, st>>>(a);
     return check_launch("k_nrc_fwd_tc");
 }
 
@@ -581,6 +632,7 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
     }
     TrainArgs a;
     a.n = n;
+    a.plan = make_plan(n);
     a.wimg = img;
     a.B = B;
     a.input = input;

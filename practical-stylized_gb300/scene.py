@@ -139,6 +139,57 @@ def furnace(albedo=0.5, le=1.0, width=32, height=32):
     return np.array(tris, dtype=np.float32), np.zeros(len(tris), dtype=np.uint32), mats, cam
 
 
+def icosphere(subdiv=3):
+    """Unit icosphere: the icosahedron with each face split into 4 `subdiv` times, vertices pushed
+    to the sphere (20 * 4^subdiv outward-facing triangles). Returns [n, 3, 3] float64."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+         (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+         (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+         (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    tris = np.array([[v[i] for i in face] for face in f], dtype=np.float64)
+    tris /= np.linalg.norm(tris, axis=2, keepdims=True)
+    for _ in range(subdiv):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab, bc, ca = a + b, b + c, c + a
+        ab /= np.linalg.norm(ab, axis=1, keepdims=True)
+        bc /= np.linalg.norm(bc, axis=1, keepdims=True)
+        ca /= np.linalg.norm(ca, axis=1, keepdims=True)
+        tris = np.concatenate([np.stack(q, 1) for q in ((a, ab, ca), (ab, b, bc), (ca, bc, c), (ab, bc, ca))])
+    return tris
+
+
+def icosphere_grid(width=1920, height=1080, n=10, subdiv=3, seed=0, camera_fov=40.0):
+    """Neural-cache workload scene: an n x n grid of subdivision-`subdiv` icospheres (radius 0.45,
+    spacing 1.2; 1280 triangles each at subdivision 3, 128 000 for the 10 x 10 grid) on a 16 x 16
+    ground quad (diffuse 0.5), each sphere GGX with alpha ~ U[0.05, 0.5] and albedo ~ U[0.2, 0.9]^3
+    (seeded), one 3 x 3 area light of radiance 12 at height 6. Returns (positions [n, 9], material
+    ids, materials, camera)."""
+    rng = np.random.default_rng(seed)
+    sph = icosphere(subdiv) * 0.45
+    tris, mids, mats = [], [], []
+    mats.append(material(MAT_DIFFUSE, (0.5, 0.5, 0.5)))
+    g = 8.0
+    ground = np.array(_quad([-g, 0, g], [g, 0, g], [g, 0, -g], [-g, 0, -g]), dtype=np.float64).reshape(-1, 3, 3)
+    tris.append(ground)
+    mids += [0, 0]
+    for i in range(n):
+        for j in range(n):
+            c = np.array([(i - (n - 1) / 2) * 1.2, 0.45, (j - (n - 1) / 2) * 1.2])
+            tris.append(sph + c)
+            mids += [len(mats)] * len(sph)
+            mats.append(material(MAT_GGX, tuple(rng.uniform(0.2, 0.9, 3)), alpha=float(rng.uniform(0.05, 0.5))))
+    L, y = 1.5, 6.0
+    light = np.array(_quad([-L, y, -L], [L, y, -L], [L, y, L], [-L, y, L]), dtype=np.float64).reshape(-1, 3, 3)
+    tris.append(light)
+    mids += [len(mats)] * 2
+    mats.append(material(MAT_DIFFUSE, (0.0, 0.0, 0.0), emission=(12.0, 12.0, 12.0)))
+    pos = np.concatenate(tris).reshape(-1, 9).astype(np.float32)
+    cam = camera((0.0, 6.5, 10.5), (0.0, 0.3, 0.0), fov_y=camera_fov, width=width, height=height)
+    return pos, np.array(mids, dtype=np.uint32), mats, cam
+
+
 class Scene:
     def __init__(self, positions: np.ndarray, mat_ids: np.ndarray, materials, cam: Camera):
         self.positions = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
