@@ -165,6 +165,47 @@ __device__ __forceinline__ void encode_row(const EncPlan &e, const float *x, uin
     }
 }
 
+// The same encoding with the frequency table of the neural-cache workload network (11 inputs,
+// octaves 4,4,4,3,3,3,3,2,2,2,2 -> 64 columns) fixed at compile time: every pair lands in a static
+// register, no per-pair branch or table lookup.
+constexpr int kC4Dims = 11;
+__device__ constexpr int kC4Freqs[kC4Dims] = {4, 4, 4, 3, 3, 3, 3, 2, 2, 2, 2};
+bool is_c4(const NrcNet &n) {
+    if (n.in_dims != kC4Dims) return false;
+    const int f[kC4Dims] = {4, 4, 4, 3, 3, 3, 3, 2, 2, 2, 2};
+    for (int d = 0; d < kC4Dims; d++)
+        if ((int)n.freqs[d] != f[d]) return false;
+    return true;
+}
+__device__ __forceinline__ void encode_row_c4(const float *x, uint8_t *img, uint32_t row) {
+    float xin[kC4Dims];
+#pragma unroll
+    for (int d = 0; d < kC4Dims; d++) xin[d] = x ? x[d] : 0.0f;
+    uint32_t q[kNrcWidth / 2];
+    int o = 0;
+#pragma unroll
+    for (int d = 0; d < kC4Dims; d++) {
+        float s, c;
+        sincospif(xin[d], &s, &c);
+#pragma unroll
+        for (int k = 0; k < kC4Freqs[d]; k++) {
+            q[o++] = x ? pack2_bf16(s, c) : 0u;
+            const float s2 = 2.0f * s * c;
+            c = fmaf(-2.0f * s, s, 1.0f);
+            s = s2;
+        }
+    }
+#pragma unroll
+    for (int kb = 0; kb < 8; kb++)
+        *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) =
+            make_uint4(q[kb * 4], q[kb * 4 + 1], q[kb * 4 + 2], q[kb * 4 + 3]);
+}
+__device__ __forceinline__ void encode_any(const NrcNet &n, const EncPlan &e, bool c4, const float *x, uint8_t *img,
+                                           uint32_t row) {
+    if (c4) encode_row_c4(x, img, row);
+    else encode_row(e, x, img, row);
+}
+
 // per-warpgroup named barriers (id 1 + warpgroup; id 0 is __syncthreads)
 __device__ __forceinline__ void wg_sync(uint32_t id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
 __device__ __forceinline__ bool wg_sync_and(uint32_t id, bool p) {
@@ -181,6 +222,7 @@ __device__ __forceinline__ bool wg_sync_and(uint32_t id, bool p) {
 struct TcArgs {
     NrcNet n;
     EncPlan plan;
+    int c4;  // the workload's frequency table: use encode_row_c4
     const uint16_t *wimg;  // global weight image
     uint64_t count;
     const float *input;
@@ -235,7 +277,7 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
     for (uint64_t tile = (uint64_t)blockIdx.x * kFwdWG + wg; tile < ntiles && !failed;
          tile += (uint64_t)gridDim.x * kFwdWG) {
         const uint64_t row = tile * TM + t;
-        encode_row(a.plan, row < a.count ? a.input + row * a.n.in_dims : nullptr, act, t);
+        encode_any(a.n, a.plan, a.c4 != 0, row < a.count ? a.input + row * a.n.in_dims : nullptr, act, t);
         fence_async_smem();
         fence_before();
         wg_sync(bar_id);
@@ -312,6 +354,7 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
 struct TrainArgs {
     NrcNet n;
     EncPlan plan;
+    int c4;
     const uint16_t *wimg;
     uint32_t B;
     const float *input, *target;
@@ -380,7 +423,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
     for (uint32_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const uint32_t row = tile * TM + tid;
         const bool valid = row < a.B;
-        encode_row(a.plan, valid ? a.input + (size_t)row * a.n.in_dims : nullptr, acts, tid);
+        encode_any(a.n, a.plan, a.c4 != 0, valid ? a.input + (size_t)row * a.n.in_dims : nullptr, acts, tid);
         publish();
         // ---- forward
         for (int l = 0; l <= L && !failed; l++) {
@@ -586,6 +629,7 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
     TcArgs a;
     a.n = n;
     a.plan = make_plan(n);
+    a.c4 = is_c4(n) ? 1 : 0;
     a.wimg = img;
     a.count = count;
     a.input = input;
@@ -633,6 +677,7 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
     TrainArgs a;
     a.n = n;
     a.plan = make_plan(n);
+    a.c4 = is_c4(n) ? 1 : 0;
     a.wimg = img;
     a.B = B;
     a.input = input;

@@ -122,6 +122,28 @@ def test_bf16_tensor_core_inference(sty, cuda, layers):
 
 
 @pytest.mark.gpu
+def test_bf16_generic_frequency_table(sty, cuda):
+    """An encoding table other than the workload's (which has a compile-time path) goes through the
+    table-driven encoder: inference and gradient against the oracle's BF16 emulation."""
+    freqs = (5, 1, 3, 0, 6, 2)
+    net = sty.nrc.NRC(sty.nrc.config(freqs, 3, 1024, 3, sty.nrc.STY_NRC_BF16, seed=9))
+    p = net.save_params().astype(np.float64)
+    rng = np.random.default_rng(12)
+    x = rng.random((128 * 9 + 3, 6)) * 1.5 - 0.25
+    out = net.inference(_dev(x)).cpu().numpy()
+    emu, _ = onrc.forward(p, x, freqs, 3, 3, bf16=True)
+    scale = np.abs(emu).max()
+    err = np.abs(out - emu)
+    assert np.mean(err <= 1e-4 * scale) >= 0.99 and err.max() <= 1e-2 * scale
+    t = rng.random((x.shape[0], 3)) + 0.1
+    g, _ = net.gradient(_dev(x), _dev(t))
+    _, eg = onrc.loss_and_grad(p, x, t, freqs, 3, 3, bf16=True)
+    g = g.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(g - eg) <= 3e-3 * np.linalg.norm(eg)
+    assert sty.abi.device_status() == 0
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("layers,batch", [(5, 128 * 300 + 77), (1, 200), (6, 1024)])
 def test_bf16_tensor_core_gradient(sty, cuda, layers, batch):
     """Fused tcgen05 training step (forward, loss gradient, backward, weight gradient) against the
