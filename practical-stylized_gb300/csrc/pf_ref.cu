@@ -7,10 +7,11 @@
 //      order, the fixed replacement of the reference's CAS-built linked lists (:230-255);
 //   4. bucket -> [start, end) table;
 //   5. (cluster) deterministic clustering rounds (:533-623, :1675-1710): claim / propose / accept;
-//   6. filter: one thread per active vertex (evaluate_filtered_radiance, :758-972).
+//   6. filter: one warp per active vertex (evaluate_filtered_radiance, :758-972).
 #include <cub/cub.cuh>
 #include <thrust/iterator/counting_iterator.h>
 
+#include <algorithm>
 #include <cmath>
 
 #include "common.cuh"
@@ -29,6 +30,7 @@ struct Geo {
     uint32_t res[3];
     uint32_t table;
     float r;
+    float r2max;  // largest f32 s with sqrt_rn(s) <= r: dist_f(..) <= r  <=>  dist2_f(..) <= r2max
 };
 
 struct VArgs {  // device views of sty_pf_vertices
@@ -63,6 +65,14 @@ __device__ __forceinline__ float dist_f(float ax, float ay, float az, float bx, 
     return __fsqrt_rn(s);
 }
 
+// the radicand of dist_f, rounded the same way
+__device__ __forceinline__ float dist2_f(float ax, float ay, float az, float bx, float by, float bz) {
+    const float dx = __fsub_rn(ax, bx), dy = __fsub_rn(ay, by), dz = __fsub_rn(az, bz);
+    float s = __fmul_rn(dx, dx);
+    s = __fadd_rn(s, __fmul_rn(dy, dy));
+    return __fadd_rn(s, __fmul_rn(dz, dz));
+}
+
 // 27-cell walk (:61-123): dz outer, dy, dx inner; f(u) returns false to stop.
 template <class F>
 __device__ __forceinline__ void walk(const Geo &g, const uint2 *__restrict__ ranges, const uint32_t *__restrict__ sorted,
@@ -80,14 +90,6 @@ __device__ __forceinline__ void walk(const Geo &g, const uint2 *__restrict__ ran
                 for (uint32_t k = rg.x; k < rg.y; k++)
                     if (!f(sorted[k])) return;
             }
-}
-
-__device__ __forceinline__ uint32_t pcg_next(sty_pcg32 &s) {
-    const uint64_t old = s.state;
-    s.state = old * 0x5851f42d4c957f2dULL + s.inc;
-    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
-    const uint32_t rot = (uint32_t)(old >> 59);
-    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
 }
 
 struct V3 {
@@ -177,6 +179,16 @@ __global__ void k_ranges(const uint32_t *keys, const uint32_t *num, uint2 *range
     if (i == 0 || keys[i - 1] != k) ranges[k].x = (uint32_t)i;
     if (i + 1 == m || keys[i + 1] != k) ranges[k].y = (uint32_t)i + 1;
 }
+// bucket-ordered copies of what the walk reads per candidate: position + flags (16 B), cluster id
+__global__ void k_sorted_view(VArgs v, const uint32_t *num, const uint32_t *sorted, const uint32_t *cid, int cluster,
+                              float4 *spos, uint32_t *scid) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= *num) return;
+    const uint32_t u = sorted[k];
+    spos[k] = make_float4(v.p[0][u], v.p[1][u], v.p[2][u], __uint_as_float(v.flags[u] & 15u));
+    if (cluster) scid[k] = cid[u];
+}
+
 // clustering: claim
 __global__ void k_cl_claim_reset(VArgs v, Geo g, const uint32_t *act, const uint32_t *num, const uint32_t *cid,
                                  uint32_t *winner) {
@@ -253,90 +265,266 @@ __global__ void k_cl_count(const uint32_t *act, const uint32_t *num, const uint3
     if (cid[act[i]] == NONE) atomicAdd(counter, 1u);
 }
 
-template <int MAXK>
-__global__ void __launch_bounds__(128) k_ref_filter(VArgs v, Geo g, const uint32_t *act, const uint32_t *num,
-                                                    const uint2 *ranges, const uint32_t *sorted, const uint32_t *cid,
-                                                    const float *in_next, sty_pf_ref_params prm,
+__device__ __forceinline__ uint32_t pcg_output(uint64_t old) {
+    const uint32_t xs = (uint32_t)(((old >> 18) ^ old) >> 27);
+    const uint32_t rot = (uint32_t)(old >> 59);
+    return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
+}
+
+// Per-warp shared scratch for a reservoir of R neighbours: 64-bit (candidate index, vertex) keys,
+// the neighbour list, and each neighbour's BSDF frame with its wo-side terms precomputed for the
+// SMIS pdf sums.
+struct __align__(16) NbFrame {  // 64 bytes: four 16-byte shared-memory reads
+    float ns[3], ng[3], wo[3];
+    float fl;      // sign(ng . ns)
+    float co;      // wo . ns
+    float alpha;   // GGX: max(alpha, 1e-4)
+    float g1;      // GGX: 1 / (1 + Lambda(co))
+    uint32_t bits; // bit 0: the wo half of check_wo_wi_valid holds; bit 1: GGX
+    uint32_t pad[2];
+};
+// rounded up to 16 bytes so that every warp's scratch starts 16-byte aligned for any R
+__host__ __device__ constexpr size_t warp_scratch_bytes(uint32_t R) {
+    return ((size_t)R * (sizeof(unsigned long long) + sizeof(uint32_t) + sizeof(NbFrame)) + 15u) & ~(size_t)15u;
+}
+__device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, V3 ns, V3 ng, V3 wo) {
+    auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
+    NbFrame f;
+    f.ns[0] = ns.x, f.ns[1] = ns.y, f.ns[2] = ns.z;
+    f.ng[0] = ng.x, f.ng[1] = ng.y, f.ng[2] = ng.z;
+    f.wo[0] = wo.x, f.wo[1] = wo.y, f.wo[2] = wo.z;
+    f.fl = sgn(dot3(ng, ns));
+    f.co = dot3(wo, ns);
+    const bool ok = sgn(f.fl * f.co) * sgn(dot3(wo, ng)) > 0.0f;
+    const bool ggx = m.kind != STY_MAT_DIFFUSE;
+    f.alpha = fmaxf(m.alpha, 1e-4f);
+    f.g1 = ggx ? 1.0f / (1.0f + tr_lambda(f.co, f.alpha)) : 0.0f;
+    f.bits = (ok ? 1u : 0u) | (ggx ? 2u : 0u);
+    return f;
+}
+// the pdf of bsdf_eval for a precomputed frame (same arithmetic; the lane-dependent validity tests
+// become selects, only the frame's lobe -- the same on every lane -- branches)
+__device__ __forceinline__ float frame_pdf(const NbFrame &f, V3 wi) {
+    auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
+    const V3 ns = {f.ns[0], f.ns[1], f.ns[2]}, ng = {f.ng[0], f.ng[1], f.ng[2]};
+    const float ci = dot3(wi, ns), co = f.co;
+    const bool ok = (f.bits & 1u) && sgn(f.fl * ci) * sgn(dot3(wi, ng)) > 0.0f && co * ci >= 0.0f;
+    if (!(f.bits & 2u)) return ok ? fabsf(ci) / kPi : 0.0f;
+    const V3 wo = {f.wo[0], f.wo[1], f.wo[2]};
+    V3 wh = {wo.x + wi.x, wo.y + wi.y, wo.z + wi.z};
+    const bool ok2 = ok && !(dot3(wh, wo) * dot3(wi, wh) < 0.0f) && !(wh.x == 0.0f && wh.y == 0.0f && wh.z == 0.0f) &&
+                     ci != 0.0f && co != 0.0f;
+    if (!ok2) wh = {0.0f, 0.0f, 1.0f};  // any unit vector: the result is discarded
+    const float l = sqrtf(dot3(wh, wh));
+    wh = {wh.x / l, wh.y / l, wh.z / l};
+    const float d = tr_d(dot3(wh, ns), f.alpha);
+    const float owh = fabsf(dot3(wo, wh));
+    const float p = d * f.g1 * owh / fabsf(co) / (4.0f * owh);
+    return ok2 ? p : 0.0f;
+}
+
+// One warp per active vertex (evaluate_filtered_radiance, :758-972); persistent warps take the
+// vertices in bucket order from a work counter, so that warps running together walk the same cells.
+// Gather: the 27-cell walk in the sequential order (cells dz, dy, dx; bucket entries ascending),
+// 32 candidates at a time from the bucket-ordered positions; a passing candidate's index c in that
+// order comes from a ballot prefix count. The reservoir (:806-829) keeps the first R candidates and
+// lets candidate c >= R replace slot j = pcg32() % (c + 1) when j < R, the draw being the
+// (c - R)-th of the vertex's stream. The replacing candidates of one chunk take consecutive draws,
+// so lane r's state is A^r s + inc * (1 + A + ... + A^(r-1)) from the chunk's starting state s,
+// with (A^r, sum) held by lane r; slot j keeps the largest replacing c (64-bit atomicMax of
+// (c, vertex)), which is what the sequential loop leaves there. Neighbour counts, lists and the
+// final RNG state are therefore bit-identical to the sequential walk.
+// Evaluate: lanes take neighbours t = lane, lane + 32, ...; the SMIS pdf sums (:886-939) read the
+// reservoir's frames from shared memory (warp-wide broadcasts); lane sums are combined by a
+// shuffle tree, then lane 0 applies the style node and writes the vertex's radiance.
+__device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
+    const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)x, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(x >> 32), src);
+    return ((uint64_t)hi << 32) | lo;
+}
+__global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uint32_t *num, uint32_t *next,
+                                                    const uint2 *ranges,
+                                                    const uint32_t *sorted, const float4 *spos, const uint32_t *scid,
+                                                    const uint32_t *cid, const float *in_next, sty_pf_ref_params prm,
                                                     const sty_pf_material *mats, uint32_t n_mats,
                                                     const sty_style_program *progs, uint32_t n_progs, sty_pcg32 *rng,
                                                     float *out, uint32_t *neighbours) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= *num) return;
-    const uint32_t vi = act[i];
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    static_assert(sizeof(NbFrame) == 64 && alignof(NbFrame) == 16, "frame layout");
+    const uint32_t R = prm.reuse;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint8_t *ws = smem_raw + (size_t)wib * warp_scratch_bytes(R);
+    // frames first (16-byte aligned), then the 8-byte keys, then the list
+    NbFrame *frames = reinterpret_cast<NbFrame *>(ws);
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(ws + (size_t)R * sizeof(NbFrame));
+    uint32_t *list = reinterpret_cast<uint32_t *>(ws + (size_t)R * (sizeof(NbFrame) + sizeof(unsigned long long)));
+    const unsigned lt_mask = (1u << lane) - 1u;
+    // lane r: A^r and 1 + A + ... + A^(r-1) (mod 2^64), for the reservoir draws
+    uint64_t a_pow = 1u, a_sum = 0u;
+    for (int r = 0; r < lane; r++) {
+        a_sum += a_pow;
+        a_pow *= 0x5851f42d4c957f2dULL;
+    }
+    const uint32_t nact = *num;
+    for (;;) {
+    // next vertex in bucket order from the launch's work counter (dynamic balance: vertices in
+    // dense regions cost far more than others)
+    uint32_t i = 0;
+    if (lane == 0) i = atomicAdd(next, 1u);
+    i = __shfl_sync(0xffffffffu, i, 0);
+    if (i >= nact) break;
+    const uint32_t vi = sorted[i];
     const uint64_t n = v.n;
     const uint32_t qs = prm.cluster ? cid[vi] : vi;
     const float qx = v.p[0][qs], qy = v.p[1][qs], qz = v.p[2][qs];
     const uint32_t my_cluster = prm.cluster ? cid[vi] : NONE;
     const uint32_t my_flags = v.flags[vi] & 15u;
-    const uint32_t reuse = prm.reuse;
-    uint32_t list[MAXK];
-    uint32_t cnt = 0;
-    sty_pcg32 st = rng[vi];
-    walk(g, ranges, sorted, qx, qy, qz, [&](uint32_t u) {
-        if (!(dist_f(v.p[0][u], v.p[1][u], v.p[2][u], qx, qy, qz) <= g.r)) return true;
-        if (prm.cluster && cid[u] != my_cluster) return true;
-        if (!prm.disable_flag_check && (v.flags[u] & 15u) != my_flags) return true;
-        if (cnt < reuse) {
-            list[cnt] = u;
-        } else {
-            const uint32_t j = pcg_next(st) % (cnt + 1);
-            if (j < reuse) list[j] = u;
+    const sty_pcg32 st0 = rng[vi];
+    uint64_t s_cur = st0.state;  // state before the next draw (warp-uniform)
+    // lane l < 27 looks up cell l of the walk order (dz outer, dy, dx inner)
+    uint2 my_rg = make_uint2(0u, 0u);
+    {
+        int32_t c0[3];
+        get_cell(g, qx, qy, qz, c0);
+        if (lane < 27) {
+            const int32_t nx = c0[0] + lane % 3 - 1, ny = c0[1] + (lane / 3) % 3 - 1, nz = c0[2] + lane / 9 - 1;
+            if (nx >= 0 && ny >= 0 && nz >= 0 && nx < (int32_t)g.res[0] && ny < (int32_t)g.res[1] &&
+                nz < (int32_t)g.res[2])
+                my_rg = ranges[bucket_of(g, nx, ny, nz)];
         }
-        cnt++;
-        return true;
-    });
-    rng[vi] = st;
-    if (neighbours) neighbours[vi] = cnt;
-    const uint32_t k = min(cnt, reuse);
+    }
+    // ---- gather
+    uint32_t cnt = 0;  // warp-uniform
+    for (int cell = 0; cell < 27; cell++) {
+                const uint2 rg = make_uint2(__shfl_sync(0xffffffffu, my_rg.x, cell), __shfl_sync(0xffffffffu, my_rg.y, cell));
+                // four chunks of 32 candidates per step: their loads are issued together
+                for (uint32_t base = rg.x; base < rg.y; base += 128) {
+                    float4 e[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        const uint32_t kk = base + q * 32 + lane;
+                        e[q] = kk < rg.y ? spos[kk] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        if (base + q * 32 >= rg.y) break;  // warp-uniform
+                        const uint32_t kk = base + q * 32 + lane;
+                        bool pass = false;
+                        if (kk < rg.y) {
+                            pass = dist2_f(e[q].x, e[q].y, e[q].z, qx, qy, qz) <= g.r2max;
+                            if (pass && prm.cluster && scid[kk] != my_cluster) pass = false;
+                            if (pass && !prm.disable_flag_check && __float_as_uint(e[q].w) != my_flags) pass = false;
+                        }
+                        const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                        if (bal == 0u) continue;
+                        const uint32_t c = cnt + __popc(bal & lt_mask);
+                        const uint32_t u = pass ? sorted[kk] : 0u;
+                        if (pass && c < R) keys[c] = ((unsigned long long)c << 32) | u;
+                        __syncwarp();
+                        const bool rep = pass && c >= R;
+                        const unsigned balr = __ballot_sync(0xffffffffu, rep);
+                        if (balr) {
+                            const int r = __popc(balr & lt_mask);
+                            const uint64_t ap = shfl64(a_pow, r), as = shfl64(a_sum, r);
+                            const uint64_t s_m = ap * s_cur + st0.inc * as;
+                            if (rep) {
+                                const uint32_t j = pcg_output(s_m) % (c + 1u);
+                                if (j < R) atomicMax(&keys[j], ((unsigned long long)c << 32) | u);
+                            }
+                            const int last = 31 - __clz((int)balr);
+                            s_cur = shfl64(s_m * 0x5851f42d4c957f2dULL + st0.inc, last);
+                        }
+                        __syncwarp();
+                        cnt += __popc(bal);
+                    }
+                }
+            }
+    if (lane == 0) {
+        sty_pcg32 st = st0;
+        st.state = s_cur;
+        rng[vi] = st;
+        if (neighbours) neighbours[vi] = cnt;
+    }
+    const uint32_t k = min(cnt, R);
+    for (uint32_t t = lane; t < k; t += 32) {
+        const uint32_t u = (uint32_t)keys[t];
+        list[t] = u;
+        frames[t] = make_frame(mats[min(v.material[u], n_mats - 1)], ld3(v.ns, u), ld3(v.ng, u), ld3(v.wo, u));
+    }
+    __syncwarp();
+
+    // ---- evaluate
     const sty_pf_material mv = mats[min(v.material[vi], n_mats - 1)];
     const V3 wo = ld3(v.wo, vi), ns = ld3(v.ns, vi), ng = ld3(v.ng, vi);
     float direct[3] = {0.f, 0.f, 0.f}, indirect[3] = {0.f, 0.f, 0.f};
-    const float invk = 1.0f / (float)k;
-    for (uint32_t t = 0; t < k; t++) {
-        const uint32_t u = list[t];
-        const float dpdf = v.dir_pdf[u];
-        if (dpdf > 0.0f) {  // :839-863
-            float f[3], pdf;
-            bsdf_eval(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf);
-            const float w = dpdf / (dpdf + pdf);
+    const float invk = k ? 1.0f / (float)k : 0.0f;
+    const uint32_t rounds = (k + 31u) / 32u;  // every lane runs the SMIS loop the same number of times
+    for (uint32_t r = 0; r < rounds; r++) {
+        const uint32_t t = r * 32u + lane;
+        const bool have = t < k;
+        const uint32_t u = have ? list[t] : 0u;
+        V3 wi = {0.f, 0.f, 0.f};
+        float reused[3] = {0.f, 0.f, 0.f}, pdf_v = 0.0f;
+        bool ind = false;
+        if (have) {
+            const float dpdf = v.dir_pdf[u];
+            if (dpdf > 0.0f) {  // :839-863
+                float f[3], pdf;
+                bsdf_eval(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf);
+                const float w = dpdf / (dpdf + pdf);
 #pragma unroll
-            for (int c = 0; c < 3; c++) direct[c] += f[c] * v.dir_l[c][u] * w / dpdf * invk;
-        }
-        const V3 wi = ld3(v.ind_wi, u);
-        if (dot3(wi, wi) == 0.0f) continue;
-        float f[3], pdf;
-        bsdf_eval(mv, ns, ng, wo, wi, f, &pdf);
-        const float mis = v.ind_mis[u];
-        float reused[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) reused[c] = f[c] * (in_next ? in_next[c * n + u] : 0.0f) * mis;
-        if (prm.smis) {  // :886-939
-            float sum_pdf = 0.0f;
-            for (uint32_t jj = 0; jj < k; jj++) {
-                const uint32_t a = list[jj];
-                const sty_pf_material ma = mats[min(v.material[a], n_mats - 1)];
-                float fa[3], pa;
-                bsdf_eval(ma, ld3(v.ns, a), ld3(v.ng, a), ld3(v.wo, a), wi, fa, &pa);
-                sum_pdf += pa;
+                for (int c = 0; c < 3; c++) direct[c] += f[c] * v.dir_l[c][u] * w / dpdf * invk;
             }
-            if (sum_pdf > 0.0f)
+            wi = ld3(v.ind_wi, u);
+            if (dot3(wi, wi) != 0.0f) {
+                ind = true;
+                float f[3];
+                bsdf_eval(mv, ns, ng, wo, wi, f, &pdf_v);
+                const float mis = v.ind_mis[u];
+#pragma unroll
+                for (int c = 0; c < 3; c++) reused[c] = f[c] * (in_next ? in_next[c * n + u] : 0.0f) * mis;
+            }
+        }
+        if (prm.smis) {
+            float sum_pdf = 0.0f;
+            uint32_t a = 0;
+            for (; a + 4 <= k; a += 4) {
+                const float p0 = frame_pdf(frames[a], wi), p1 = frame_pdf(frames[a + 1], wi);
+                const float p2 = frame_pdf(frames[a + 2], wi), p3 = frame_pdf(frames[a + 3], wi);
+                sum_pdf += p0;  // in list order, as the sequential sum
+                sum_pdf += p1;
+                sum_pdf += p2;
+                sum_pdf += p3;
+            }
+            for (; a < k; a++) sum_pdf += frame_pdf(frames[a], wi);
+            if (ind && sum_pdf > 0.0f)
 #pragma unroll
                 for (int c = 0; c < 3; c++) indirect[c] += reused[c] / sum_pdf;
-        } else if (pdf > 0.0f) {
+        } else if (ind && pdf_v > 0.0f) {
 #pragma unroll
-            for (int c = 0; c < 3; c++) indirect[c] += reused[c] / pdf * invk;
+            for (int c = 0; c < 3; c++) indirect[c] += reused[c] / pdf_v * invk;
         }
     }
-    f3 rad = {v.le[0][vi] + direct[0] + indirect[0], v.le[1][vi] + direct[1] + indirect[1],
-              v.le[2][vi] + direct[2] + indirect[2]};
-    const uint32_t fl = v.flags[vi];
-    if ((prm.depth > 0 || !prm.no_first_hit_stylization) && !(fl & 1u)) {
-        const int32_t pi = mv.style[style_index(fl)];
-        if (pi >= 0 && (uint32_t)pi < n_progs) rad = style_apply(progs[pi], prm.depth, rad);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            direct[c] += __shfl_xor_sync(0xffffffffu, direct[c], o);
+            indirect[c] += __shfl_xor_sync(0xffffffffu, indirect[c], o);
+        }
+    if (lane == 0) {
+        f3 rad = {v.le[0][vi] + direct[0] + indirect[0], v.le[1][vi] + direct[1] + indirect[1],
+                  v.le[2][vi] + direct[2] + indirect[2]};
+        const uint32_t fl = v.flags[vi];
+        if ((prm.depth > 0 || !prm.no_first_hit_stylization) && !(fl & 1u)) {
+            const int32_t pi = mv.style[style_index(fl)];
+            if (pi >= 0 && (uint32_t)pi < n_progs) rad = style_apply(progs[pi], prm.depth, rad);
+        }
+        out[vi] = rad.x;
+        out[n + vi] = rad.y;
+        out[2 * n + vi] = rad.z;
     }
-    out[vi] = rad.x;
-    out[n + vi] = rad.y;
-    out[2 * n + vi] = rad.z;
+    __syncwarp();  // the next vertex reuses the warp's scratch
+    }
 }
 
 }  // namespace
@@ -349,6 +537,8 @@ struct sty_pf_ref_ctx {
     uint2 *ranges = nullptr;
     uint32_t *cid = nullptr, *csize = nullptr, *size0 = nullptr, *prop = nullptr, *winner = nullptr;
     uint32_t *counter = nullptr;
+    float4 *spos = nullptr;  // bucket-ordered position + flags
+    uint32_t *scid = nullptr;  // bucket-ordered cluster id
     sty_pf_material *mats = nullptr;      // device copies of the host tables
     sty_style_program *progs = nullptr;
     void *tmp = nullptr;
@@ -361,7 +551,8 @@ using namespace sty;
 namespace {
 void free_ctx(sty_pf_ref_ctx *c) {
     void *ptrs[] = {c->act,   c->num,    c->keys,  c->vals,    c->keys_s,  c->vals_s, c->ranges, c->cid,
-                    c->csize, c->size0,  c->prop,  c->winner,  c->counter, c->mats,   c->progs,  c->tmp};
+                    c->csize, c->size0,  c->prop,  c->winner,  c->counter, c->mats,   c->progs,  c->tmp,
+                    c->spos,  c->scid};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -426,6 +617,8 @@ sty_status sty_pf_ref_create(uint64_t max_vertices, uint32_t table_size, sty_pf_
     alloc((void **)&c->prop, n * 4, "alloc prop");
     alloc((void **)&c->winner, (size_t)table_size * 4, "alloc winner");
     alloc((void **)&c->counter, 4, "alloc counter");
+    alloc((void **)&c->spos, n * sizeof(float4), "alloc sorted positions");
+    alloc((void **)&c->scid, n * 4, "alloc sorted cluster ids");
     alloc((void **)&c->mats, kMaxMaterials * sizeof(sty_pf_material), "alloc materials");
     alloc((void **)&c->progs, kMaxPrograms * sizeof(sty_style_program), "alloc programs");
     if (st == STY_OK) {
@@ -486,6 +679,17 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     }
     g.table = prm->table_size;
     g.r = prm->radius;
+    {
+        // f32 sqrt is correctly rounded on host and device: find the largest s with sqrt(s) <= r
+        float t = prm->radius * prm->radius;
+        while (std::sqrt(t) > prm->radius) t = std::nextafter(t, 0.0f);
+        for (;;) {
+            const float nx = std::nextafter(t, INFINITY);
+            if (!(std::sqrt(nx) <= prm->radius)) break;
+            t = nx;
+        }
+        g.r2max = t;
+    }
     const int bs = 256;
     const unsigned nb = (unsigned)((n + bs - 1) / bs);
     STY_TRY(check_cuda(cudaMemcpyAsync(ctx->mats, materials, n_materials * sizeof(sty_pf_material),
@@ -552,14 +756,29 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     // 6. filter
     STY_TRY(check_cuda(cudaMemsetAsync(out, 0, 3 * n * sizeof(float), st), "reset out"));
     if (neighbours) STY_TRY(check_cuda(cudaMemsetAsync(neighbours, 0, n * 4, st), "reset neighbours"));
-    const unsigned nbf = (unsigned)((n + 127) / 128);
-    if (prm->reuse <= 128)
-        k_ref_filter<128><<<nbf, 128, 0, st>>>(va, g, ctx->act, ctx->num, ctx->ranges, ctx->vals_s, ctx->cid, in_next,
-                                               *prm, ctx->mats, n_materials, ctx->progs, n_programs, rng, out, neighbours);
-    else
-        k_ref_filter<1024><<<nbf, 128, 0, st>>>(va, g, ctx->act, ctx->num, ctx->ranges, ctx->vals_s, ctx->cid, in_next,
-                                                *prm, ctx->mats, n_materials, ctx->progs, n_programs, rng, out,
-                                                neighbours);
+    // one warp per active vertex; warps per block as the reservoir's shared scratch allows
+    const size_t wsb = warp_scratch_bytes(prm->reuse);
+    uint32_t wpb = (uint32_t)std::min<size_t>(8, (96u * 1024u) / wsb);
+    if (wpb < 1) wpb = 1;
+    const size_t smem = wpb * wsb;
+    if (smem > 48u * 1024u)
+        STY_TRY(check_cuda(cudaFuncSetAttribute(k_ref_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                           "attr k_ref_filter"));
+    // persistent warps: as many blocks as stay resident, each warp looping over vertices
+    int per_sm = 0, dev = 0, sms = 0;
+    STY_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ref_filter, 32 * wpb, smem),
+                       "occupancy k_ref_filter"));
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const uint64_t want = (n + wpb - 1) / wpb, cap_blocks = (uint64_t)std::max(per_sm, 1) * (uint64_t)std::max(sms, 1);
+    const unsigned nbf = (unsigned)std::min(want, cap_blocks);
+    k_sorted_view<<<nb, bs, 0, st>>>(va, ctx->num, ctx->vals_s, ctx->cid, prm->cluster, ctx->spos, ctx->scid);
+    STY_TRY(check_launch("k_sorted_view"));
+    STY_TRY(check_cuda(cudaMemsetAsync(ctx->counter, 0, 4, st), "reset work counter"));
+    k_ref_filter<<<nbf, 32 * wpb, smem, st>>>(va, g, ctx->num, ctx->counter, ctx->ranges, ctx->vals_s, ctx->spos,
+                                              ctx->scid, ctx->cid,
+                                              in_next, *prm, ctx->mats, n_materials, ctx->progs, n_programs, rng, out,
+                                              neighbours);
     STY_TRY(check_launch("k_ref_filter"));
     if (cluster_id)
         STY_TRY(check_cuda(cudaMemcpyAsync(cluster_id, ctx->cid, n * 4, cudaMemcpyDeviceToDevice, st), "copy cid"));

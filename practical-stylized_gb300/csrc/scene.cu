@@ -21,6 +21,7 @@ struct sty_scene {
     sty_scene_material *materials = nullptr;
     uint32_t *light_tris = nullptr;
     float *light_cdf = nullptr;
+    void *render_cache = nullptr;  // device buffers of the last render, reused by the next (trace.cu)
 };
 
 namespace sty {
@@ -170,6 +171,7 @@ struct Builder {
 };
 
 void free_scene(sty_scene *s) {
+    render_cache_free(s->render_cache);
     void *ptrs[] = {s->nodes, s->tris, s->tri_material, s->tri_normal, s->tri_area,
                     s->tri_pos, s->materials, s->light_tris, s->light_cdf};
     for (void *p : ptrs)
@@ -300,6 +302,7 @@ sty_status sty_scene_closest_hit(sty_scene *s, const float *rays, uint64_t n, ui
 // accessors used by the render driver
 namespace sty {
 const sty_camera &scene_camera(const sty_scene *s) { return s->camera; }
+void *&scene_render_cache(sty_scene *s) { return s->render_cache; }
 void scene_bounds(const sty_scene *s, float mn[3], float mx[3]) {
     for (int a = 0; a < 3; a++) {
         mn[a] = s->bmin[a];

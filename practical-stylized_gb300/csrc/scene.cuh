@@ -226,5 +226,7 @@ __device__ inline bool trace_any(const SceneView &s, const float o[3], const flo
 }
 
 SceneView scene_view(const sty_scene *s);
+// device buffers kept by a scene between renders (defined in trace.cu)
+void render_cache_free(void *cache);
 
 }  // namespace sty

@@ -25,6 +25,7 @@ namespace sty {
 const sty_camera &scene_camera(const sty_scene *s);
 void scene_bounds(const sty_scene *s, float mn[3], float mx[3]);
 const std::vector<sty_scene_material> &scene_materials(const sty_scene *s);
+void *&scene_render_cache(sty_scene *s);
 }  // namespace sty
 
 namespace sty {
@@ -602,14 +603,34 @@ CamArgs make_camera(const sty_camera &cam) {
     return ca;
 }
 
-// Device buffers of one wavefront trace: per-depth vertex planes, path state, per-path Pcg32,
-// per-depth radiance planes; freed with the job.
+// Device buffers a scene keeps between renders (grown on demand, freed with the scene): renders
+// of one scene reuse them, so calls on one scene are serialised by the caller.
+enum CacheSlot { kVerts, kOuts, kPathState, kRng, kPrograms, kVertexCount, kRowCount, kRowIndex, kScanTmp, kSlots };
+struct RenderCache {
+    void *p[kSlots] = {};
+    size_t bytes[kSlots] = {};
+    sty_pf_ref_ctx *ctx = nullptr;
+    uint64_t ctx_cap = 0;
+    ~RenderCache() {
+        for (void *q : p)
+            if (q) cudaFree(q);
+        if (ctx) sty_pf_ref_destroy(ctx);
+    }
+};
+RenderCache &render_cache(sty_scene *scene) {
+    void *&c = scene_render_cache(scene);
+    if (!c) c = new RenderCache();
+    return *static_cast<RenderCache *>(c);
+}
+
+// Per-depth vertex planes, path state, per-path Pcg32 and per-depth radiance planes of one
+// wavefront trace, in the scene's cached buffers.
 struct TraceJob {
     static constexpr size_t kPlanes = 30;  // per depth: active, 27 float planes, flags, material
     uint32_t npx = 0, n = 0, D = 0, max_depth = 0, n_programs = 0;
     CamArgs ca;
     SceneView sv;
-    std::vector<void *> owned;
+    RenderCache *cache = nullptr;
     float *verts = nullptr, *outs = nullptr, *psb = nullptr;
     sty_pcg32 *rng = nullptr;
     sty_style_program *dprog = nullptr;
@@ -620,14 +641,17 @@ struct TraceJob {
     float bmin[3], bmax[3];
     sty_status s = STY_OK;
 
-    ~TraceJob() {
-        for (void *p : owned) cudaFree(p);
-    }
-    void *alloc(size_t bytes, const char *what) {
-        void *p = nullptr;
-        if (s == STY_OK) s = check_cuda(cudaMalloc(&p, bytes), what);
-        if (p) owned.push_back(p);
-        return p;
+    void *alloc(CacheSlot k, size_t bytes, const char *what) {
+        if (s != STY_OK) return nullptr;
+        if (cache->bytes[k] < bytes) {
+            if (cache->p[k]) cudaFree(cache->p[k]);
+            cache->p[k] = nullptr;
+            cache->bytes[k] = 0;
+            s = check_cuda(cudaMalloc(&cache->p[k], bytes), what);
+            if (s != STY_OK) return nullptr;
+            cache->bytes[k] = bytes;
+        }
+        return cache->p[k];
     }
     sty_status init(sty_scene *scene, uint32_t branch, uint32_t maxd, const sty_style_program *programs,
                     uint32_t nprog, uint64_t seed, cudaStream_t st) {
@@ -642,15 +666,16 @@ struct TraceJob {
         max_depth = maxd;
         D = maxd + 1;
         n_programs = nprog;
+        cache = &render_cache(scene);
         ca = make_camera(cam);
         sv = scene_view(scene);
         scene_bounds(scene, bmin, bmax);
-        verts = (float *)alloc((size_t)D * kPlanes * n * 4, "alloc vertices");
-        outs = (float *)alloc((size_t)D * 3 * n * 4, "alloc outputs");
-        psb = (float *)alloc((size_t)13 * n * 4, "alloc path state");
-        rng = (sty_pcg32 *)alloc((size_t)n * sizeof(sty_pcg32), "alloc rng");
-        dprog = (sty_style_program *)alloc(64 * sizeof(sty_style_program), "alloc programs");
-        vc = (unsigned long long *)alloc(8, "alloc counter");
+        verts = (float *)alloc(kVerts, (size_t)D * kPlanes * n * 4, "alloc vertices");
+        outs = (float *)alloc(kOuts, (size_t)D * 3 * n * 4, "alloc outputs");
+        psb = (float *)alloc(kPathState, (size_t)13 * n * 4, "alloc path state");
+        rng = (sty_pcg32 *)alloc(kRng, (size_t)n * sizeof(sty_pcg32), "alloc rng");
+        dprog = (sty_style_program *)alloc(kPrograms, 64 * sizeof(sty_style_program), "alloc programs");
+        vc = (unsigned long long *)alloc(kVertexCount, 8, "alloc counter");
         if (s != STY_OK) return s;
         if (nprog)
             STY_TRY(check_cuda(cudaMemcpyAsync(dprog, programs, nprog * sizeof(sty_style_program),
@@ -723,6 +748,10 @@ struct TraceJob {
 
 }  // namespace
 
+namespace sty {
+void render_cache_free(void *cache) { delete static_cast<RenderCache *>(cache); }
+}  // namespace sty
+
 extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *cfg,
                                     const sty_style_program *programs, uint32_t n_programs, double *film,
                                     uint64_t *vertex_count, void *stream) {
@@ -737,8 +766,15 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
     TraceJob job;
     STY_TRY(job.init(scene, cfg->branch, cfg->max_depth, programs, n_programs, cfg->seed, st));
     const uint32_t n = job.n, D = job.D, npx = job.npx;
-    sty_pf_ref_ctx *ctx = nullptr;
-    STY_TRY(sty_pf_ref_create(n, 1u << 26, &ctx));
+    RenderCache &rc = *job.cache;
+    if (!rc.ctx || rc.ctx_cap < n) {
+        if (rc.ctx) sty_pf_ref_destroy(rc.ctx);
+        rc.ctx = nullptr;
+        rc.ctx_cap = 0;
+        STY_TRY(sty_pf_ref_create(n, 1u << 26, &rc.ctx));
+        rc.ctx_cap = n;
+    }
+    sty_pf_ref_ctx *ctx = rc.ctx;
     const auto &mh = scene_materials(scene);
     std::vector<sty_pf_material> pm(mh.size());
     for (size_t i = 0; i < mh.size(); i++) {
@@ -791,7 +827,6 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
         *vertex_count = h;
     }
     if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
-    sty_pf_ref_destroy(ctx);
     return s;
 }
 
@@ -831,14 +866,14 @@ extern "C" sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t 
                                             job.out(d));
         STY_TRY(check_launch("k_self_radiance"));
     }
-    unsigned long long *cnt = (unsigned long long *)job.alloc(8, "alloc row counter");
-    uint32_t *idx = (uint32_t *)job.alloc((size_t)job.n * 4, "alloc row index");
+    unsigned long long *cnt = (unsigned long long *)job.alloc(kRowCount, 8, "alloc row counter");
+    uint32_t *idx = (uint32_t *)job.alloc(kRowIndex, (size_t)job.n * 4, "alloc row index");
     size_t tmp_bytes = 0;
     STY_TRY(job.s);
     STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, (const uint32_t *)job.vo[0].active, idx,
                                                       (int)job.n, st),
                        "scan size"));
-    void *tmp = job.alloc(tmp_bytes, "alloc scan scratch");
+    void *tmp = job.alloc(kScanTmp, tmp_bytes, "alloc scan scratch");
     STY_TRY(job.s);
     STY_TRY(check_cuda(cudaMemsetAsync(cnt, 0, 8, st), "zero rows"));
     for (uint32_t d = 0; d < job.D; d++) {

@@ -128,7 +128,7 @@ def _gpu(sty, arr, mats, progs, rng, prm, n_progs=2):
 @pytest.mark.gpu
 @pytest.mark.parametrize("cluster", [False, True])
 @pytest.mark.parametrize("smis", [True, False])
-@pytest.mark.parametrize("reuse", [4, 64])
+@pytest.mark.parametrize("reuse", [1, 3, 4, 64])
 def test_ref_filter_matches_oracle(sty, orc, cuda, cluster, smis, reuse):
     arr, mats, progs, rng = _setup(sty, n=6000, seed=11 + reuse)
     prm = sty.pf_ref.RefParams(depth=1, radius=0.08, reuse=reuse, smis=smis, cluster=cluster)
