@@ -262,6 +262,53 @@ def c1_bench(sty, repeats: int = 3):
             "image_mean": float(film.mean())}
 
 
+def c3_bench(sty, reps: int = 20):
+    """Adjoint of the screen-space filter + smoothed ramp (36 parameters: sharpness 50, 8
+    thresholds, 8 RGB ramp colours, sigma_pixel / sigma_pos / sigma_nrm) on 512 x 512 x 4 spp
+    synthetic records (the filter workload's distributions), radius 16, one depth with a child
+    input: one gradient = forward + loss + backward (weights recomputed, two sweeps), timed with
+    CUDA events over `reps` gradients. The loss target is a seeded image (the time does not
+    depend on it); gradient correctness is checked against FP64 central differences in the tests."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    W, H, S, R = 512, 512, 4, 16
+    planes, valid = sty.synth.records(W, H, S, 1, seed=3)
+    rs = sty.RecordSet.from_numpy(planes, valid, W, H, S, 1)
+    rng = np.random.default_rng(4)
+    p = np.zeros(36, np.float32)
+    p[0] = 50.0
+    p[1:9] = np.sort(rng.uniform(0.05, 1.2, 8))
+    p[9:33] = np.sort(rng.uniform(0.0, 1.0, 24))
+    p[33:36] = [8.0, 0.5, 0.2]
+    prm = (C.c_float * 36)(*p)
+    child = torch.rand((3, W * H * S), device="cuda")
+    target = torch.rand((H, W, 3), device="cuda")
+    grad = torch.zeros(36, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def one():
+        sty.check(sty.lib().sty_pf_adjoint(C.byref(rs.c()), 0, R, prm, 8, C.c_void_p(child.data_ptr()),
+                                           C.c_void_p(target.data_ptr()), C.c_void_p(grad.data_ptr()), None,
+                                           C.c_void_p(sp)))
+
+    for _ in range(3):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nrec = W * H * S
+    return {"workload": "adjoint 512x512 x 4 spp, radius 16, 36 parameters (filter + smoothed ramp)",
+            "ms_per_gradient": ms, "gradients_per_s": 1e3 / ms, "mrecords_per_s": nrec / ms / 1e3,
+            "grad_finite": bool(torch.isfinite(grad).all().item())}
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -303,6 +350,9 @@ def run(args):
     lib = sty.abi.lib()
     if args.nrc_only:  # profiling case: the NL-NRC frames alone
         print(json.dumps({"nrc": nrc_bench(sty, args.nrc_frames, max(3, args.warmup), dev, 1943.8)}), flush=True)
+        return
+    if args.c1_only:  # profiling case: the end-to-end render alone
+        print(json.dumps({"c1_render": c1_bench(sty, repeats=max(1, args.steps))}), flush=True)
         return
 
     D_ = args.depths
@@ -437,6 +487,7 @@ def run(args):
     }
     if world == 1 and not args.no_c1:
         line["c1_render"] = c1_bench(sty)
+        line["c3_adjoint"] = c3_bench(sty)
     if world == 1 and not args.no_nrc:
         bf16_peak = 1943.8
         p = ROOT / "MEASURED_PEAKS.json"
@@ -465,6 +516,7 @@ def main():
     ap.add_argument("--nrc-frames", type=int, default=256)
     ap.add_argument("--no-c1", action="store_true", help="skip the end-to-end Cornell box render")
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
+    ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
