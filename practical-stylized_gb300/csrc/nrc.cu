@@ -194,7 +194,15 @@ __global__ void k_sum_chunks(size_t np, uint32_t chunks, const float *__restrict
     const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= np) return;
     float s = 0.0f;
-    for (uint32_t c = 0; c < chunks; c++) s += part[c * np + p];
+    uint32_t c = 0;
+    for (; c + 8 <= chunks; c += 8) {  // eight loads in flight, added in chunk order
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) v[j] = part[(c + j) * np + p];
+#pragma unroll
+        for (int j = 0; j < 8; j++) s += v[j];
+    }
+    for (; c < chunks; c++) s += part[c * np + p];
     grad[p] = s;
 }
 
@@ -313,7 +321,7 @@ sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t s
     dim3 grid(chunks, n.layers + 1);
     k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->np, nr->gpart);
     STY_TRY(check_launch("k_wgrad_f32"));
-    k_sum_chunks<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, chunks, nr->gpart, nr->g);
+    k_sum_chunks<<<(unsigned)((nr->np + 127) / 128), 128, 0, st>>>(nr->np, chunks, nr->gpart, nr->g);
     return check_launch("k_sum_chunks");
 }
 
@@ -337,7 +345,7 @@ sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float 
     nr->img_dirty = true;  // nr->img now holds w, which the optimiser step is about to change
     const uint32_t ctas = nrc_tc_train_ctas(B);
     STY_TRY(nrc_tc_train(nr->net, nr->img, B, in, target, nr->gpart, nr->np, nr->loss, ctas, st));
-    k_sum_chunks<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, ctas, nr->gpart, nr->g);
+    k_sum_chunks<<<(unsigned)((nr->np + 127) / 128), 128, 0, st>>>(nr->np, ctas, nr->gpart, nr->g);
     return check_launch("k_sum_chunks");
 }
 
