@@ -154,6 +154,62 @@ __device__ __forceinline__ void row_pass(const float *__restrict__ rowp, int pla
     }
 }
 
+// Packed FP32: d = a * b + c on both lanes (fma.rn.f32x2; each lane rounds exactly like fmaf),
+// one issue slot for two FMAs.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// The expanded-form row pass on pairs of queries (spp samples 2p, 2p+1 of one pixel) with packed
+// FMAs: each lane performs exactly the operation sequence of row_pass<true, ..>, so the sums are
+// bit-identical; the candidate's fields are duplicated once per candidate for the four pairs.
+template <bool DA, bool DB>
+__device__ __forceinline__ void row_pass2(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
+                                          const float2 (&qa2)[4][3], const float2 (&qn2)[4][3], float rbA, float rbB,
+                                          float2 (&part2)[4][4]) {
+#pragma unroll 1
+    for (int dx = -R; dx <= R; dx++) {
+        const float cx = -pix2 * (float)(dx * dx);
+        const float *cp = rowp + (lx + R + dx) * S;
+        float c[NF][S];
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            const float4 v = *reinterpret_cast<const float4 *>(cp + f * plane);
+            c[f][0] = v.x;
+            c[f][1] = v.y;
+            c[f][2] = v.z;
+            c[f][3] = v.w;
+        }
+        const float bA = rbA + cx, bB = rbB + cx;
+#pragma unroll
+        for (int t = 0; t < S; t++) {
+            float2 cd[NF];
+#pragma unroll
+            for (int f = 0; f < NF; f++) cd[f] = make_float2(c[f][t], c[f][t]);
+#pragma unroll
+            for (int qp = 0; qp < 4; qp++) {
+                if ((qp < 2 && !DA) || (qp >= 2 && !DB)) continue;
+                const float base = qp < 2 ? bA : bB;
+                float2 arg = ffma2(qa2[qp][0], cd[0], make_float2(base, base));
+                arg = ffma2(qa2[qp][1], cd[1], arg);
+                arg = ffma2(qa2[qp][2], cd[2], arg);
+                arg = ffma2(qn2[qp][0], cd[3], arg);
+                arg = ffma2(qn2[qp][1], cd[4], arg);
+                arg = ffma2(qn2[qp][2], cd[5], arg);
+                const float2 e = make_float2(ex2_approx(arg.x), ex2_approx(arg.y));
+                part2[qp][0] = ffma2(e, cd[6], part2[qp][0]);
+                part2[qp][1] = ffma2(e, cd[7], part2[qp][1]);
+                part2[qp][2] = ffma2(e, cd[8], part2[qp][2]);
+                part2[qp][3] = ffma2(e, cd[9], part2[qp][3]);
+            }
+        }
+    }
+}
+
 // Kahan totals: kst[(q * NC + ctid) * 2 + 0] = sums (w, r, g, b), [.. + 1] = compensations.
 template <bool EXP>
 __device__ __forceinline__ void consume_chunk(const float *__restrict__ buf, int plane, int cy0, int row_hi, int yA,
@@ -169,17 +225,44 @@ __device__ __forceinline__ void consume_chunk(const float *__restrict__ buf, int
         const float rbA = -pix2 * (float)(dyA * dyA) - nscale;
         const float rbB = -pix2 * (float)(dyB * dyB) - nscale;
         float part[8][4];
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-#pragma unroll
-            for (int k = 0; k < 4; k++) part[q][k] = 0.0f;
         const float *rowp = buf + r * (plane / CH);
-        if (ia && ib)
-            row_pass<EXP, true, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
-        else if (ia)
-            row_pass<EXP, true, false>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
-        else
-            row_pass<EXP, false, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
+        if (EXP) {
+            float2 part2[4][4], qa2[4][3], qn2[4][3];
+#pragma unroll
+            for (int qp = 0; qp < 4; qp++) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) part2[qp][k] = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    qa2[qp][k] = make_float2(qa[2 * qp][k], qa[2 * qp + 1][k]);
+                    qn2[qp][k] = make_float2(qn[2 * qp][k], qn[2 * qp + 1][k]);
+                }
+            }
+            if (ia && ib)
+                row_pass2<true, true>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
+            else if (ia)
+                row_pass2<true, false>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
+            else
+                row_pass2<false, true>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
+#pragma unroll
+            for (int qp = 0; qp < 4; qp++)
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    part[2 * qp][k] = part2[qp][k].x;
+                    part[2 * qp + 1][k] = part2[qp][k].y;
+                }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+#pragma unroll
+                for (int k = 0; k < 4; k++) part[q][k] = 0.0f;
+            if (ia && ib)
+                row_pass<false, true, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
+            else if (ia)
+                row_pass<false, true, false>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
+            else
+                row_pass<false, false, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
+        }
 #pragma unroll
         for (int q = 0; q < 8; q++) {
             if ((q < 4 && !ia) || (q >= 4 && !ib)) continue;
