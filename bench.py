@@ -6,7 +6,9 @@ One step = one full NL-PF pass: the 5 depths filtered deepest-first through the 
           second; 41.47 M records, ~90 % valid, per step). Inputs (2.2 GB) exceed the 129 MB L2,
           so no explicit flush is needed between steps.
   e2e   : the same metric through the public API with HOST buffers: every step copies the
-          records from pinned host memory, runs the pass and reads back the depth-0 result.
+          records from pinned host memory (per depth, deepest first, on a copy stream so that a
+          depth's upload overlaps the filter of the depth below it), runs the pass and reads back
+          the depth-0 result.
   roofline: the dominant kernel (k_pf_screen) against measured HBM bandwidth, from CUDA events
           around each launch on the launching stream; `alu_roofline` gives the binding FP32 roof.
   cpu_baseline: the FP32 CPU restatement (oracle, all host cores) on a bounded band of rows.
@@ -410,10 +412,27 @@ def run(args):
     h_out = torch.empty((3, n), dtype=torch.float32).pin_memory()
     d_planes, d_valid = rs.planes, rs.valid
 
+    # per depth (deepest first, the order of the backward loop) the depth's 13 record slices go up on
+    # a copy stream; the filter of a depth waits only for its own records, so the upload of depth
+    # d-1 overlaps the filter of depth d
+    copy_stream = torch.cuda.Stream(dev)
+    ev_free = torch.cuda.Event()
+    ev_copied = [torch.cuda.Event() for _ in range(D_)]
+
     def e2e_step():
-        d_planes.copy_(h_planes, non_blocking=True)
-        d_valid.copy_(h_valid, non_blocking=True)
-        one_pass()
+        ev_free.record(stream)  # the previous step's filters are done with the record buffers
+        copy_stream.wait_event(ev_free)
+        with torch.cuda.stream(copy_stream):
+            for d in range(D_ - 1, -1, -1):
+                sl = slice(d * n, (d + 1) * n)
+                for f in range(d_planes.shape[0]):
+                    d_planes[f, sl].copy_(h_planes[f, sl], non_blocking=True)
+                d_valid[sl].copy_(h_valid[sl], non_blocking=True)
+                ev_copied[d].record(copy_stream)
+        for d in range(D_ - 1, -1, -1):
+            stream.wait_event(ev_copied[d])
+            nxt = out[d + 1] if d + 1 < D_ else None
+            sty.pf_screen_filter_depth(rs, d, prm, style, out_next=nxt, out=out[d], stream=stream)
         h_out.copy_(out[0], non_blocking=True)
 
     e2e_ms = float("nan")
