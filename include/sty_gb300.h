@@ -447,6 +447,42 @@ STY_API sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t lay
                                    uint32_t max_depth, uint64_t seed, float *inputs, float *targets,
                                    uint64_t capacity, uint64_t *count_out, void *stream);
 
+/* The NL-NRC render (NRCPathTracer::render without final gathering, nrc_pt.rs:1519-1690) on the
+ * scene and a cache created with sty_nrc_create (11 inputs: rows in STY_NRC_ROWS_SPHERICAL).
+ * Training, `training_iters` times: `training_paths` paths (0: batches_per_iter x the cache's batch
+ * size / (max_depth + 1), clamped to the pixel count, :1126-1128), each from a pixel drawn from its
+ * own Pcg32 stream (:1394), traced to max_depth; the cache (training weights) predicts the
+ * radiance leaving every vertex of depth >= 1 (:667-703); each vertex of depth >= training_level
+ * gets the target Le + NEE (balance MIS) + f * L_next * mis_next / pdf with L_next the prediction
+ * at the next vertex, styled at that depth unless learn_stylized_radiance (:704-842); then
+ * sty_nrc_train(rows, batches_per_iter). With per_level_training > 0 the training level starts at
+ * max_depth and drops by one every per_level_training iterations (:1538-1545), else it is 0.
+ * Rendering, `repeats` times: one first hit per pixel, the cache's EMA prediction there, styled at
+ * depth 0 unless no_first_hit_stylization, added with weight 1/repeats to `film` (device,
+ * width*height*3 doubles, rgb; the caller zeroes it) (:844-965). `programs` is a HOST array.
+ * Calls on one scene are serialised by the caller (the scene keeps the render's buffers).
+ * Reference flags are taken after the vertex's own set_style update (as in sty_pf_render). */
+typedef struct sty_nrc_render_config {
+    uint32_t max_depth;
+    uint32_t training_iters;
+    uint32_t batches_per_iter;
+    uint32_t training_paths;
+    uint32_t repeats;
+    uint32_t per_level_training;
+    int32_t no_first_hit_stylization;
+    int32_t learn_stylized_radiance;
+    uint64_t seed;
+} sty_nrc_render_config;
+typedef struct sty_nrc_render_stats {
+    uint64_t training_rows;      /* training rows over all iterations */
+    uint64_t inference_queries;  /* cache queries over training and rendering */
+    float last_loss;             /* mean loss of the last training call */
+    uint32_t reserved;
+} sty_nrc_render_stats;
+STY_API sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_render_config *config,
+                                  const sty_style_program *programs, uint32_t n_programs, double *film,
+                                  sty_nrc_render_stats *stats, void *stream);
+
 /* ----------------------------------------------------------------------------------------
  * Integer helpers (bit-exact with the reference)
  * -------------------------------------------------------------------------------------- */

@@ -276,6 +276,11 @@ struct sty_nrc {
     bool img_dirty = true;
 };
 
+namespace sty {
+uint32_t nrc_batch_size(const sty_nrc *nr) { return nr->cfg.batch_size; }
+uint32_t nrc_input_dims(const sty_nrc *nr) { return nr->cfg.input_dims; }
+}  // namespace sty
+
 namespace {
 
 sty_status ensure_batch(sty_nrc *nr, uint32_t B) {

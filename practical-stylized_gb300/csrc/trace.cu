@@ -26,6 +26,8 @@ const sty_camera &scene_camera(const sty_scene *s);
 void scene_bounds(const sty_scene *s, float mn[3], float mx[3]);
 const std::vector<sty_scene_material> &scene_materials(const sty_scene *s);
 void *&scene_render_cache(sty_scene *s);
+uint32_t nrc_batch_size(const sty_nrc *nr);
+uint32_t nrc_input_dims(const sty_nrc *nr);
 }  // namespace sty
 
 namespace sty {
@@ -193,6 +195,7 @@ struct CamArgs {
     float eye[3], fwd[3], right[3], up[3];
     float tan_half, aspect, radius;
     uint32_t W, H;
+    uint32_t random_px;  // 1: path tid starts at pixel pcg32() % (W*H) (training paths, nrc_pt.rs:1394)
 };
 
 __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t depth, uint32_t max_depth,
@@ -206,7 +209,8 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
     float prev_pdf;
     F3 prev_p;
     if (depth == 0) {
-        const uint32_t npx = cam.W * cam.H, px = tid % npx;
+        const uint32_t npx = cam.W * cam.H;
+        const uint32_t px = cam.random_px ? pcg_next(st) % npx : tid % npx;
         const float fx = (float)(px % cam.W) + 0.5f, fy = (float)(px / cam.W) + 0.5f;
         const float u0 = next_1d(st), u1 = next_1d(st);
         const float ox = (u0 - 0.5f) * cam.radius, oy = (u1 - 0.5f) * cam.radius;
@@ -568,6 +572,50 @@ __global__ void k_nrc_query_rows(SceneView sc, FeatArgs fa, uint32_t n, VertOut 
     for (int c = 0; c < 3; c++) targets[(size_t)i * 3 + c] = le[c];
 }
 
+// The cache's predictions for the vertices of one depth (rows [n][3], dense in path order) as
+// radiance planes [3][n], styled at that depth by the vertex's material and flags unless the cache
+// learns styled radiance (nrc_pt.rs:748-775); inactive slots give 0.
+__global__ void k_nrc_style_pred(SceneView sc, uint32_t n, VertOut v, const float *pred, const sty_style_program *progs,
+                                 uint32_t n_progs, uint32_t depth, int stylize, float *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 c = {0.0f, 0.0f, 0.0f};
+    if (v.active[i]) {
+        c = {pred[3 * (size_t)i], pred[3 * (size_t)i + 1], pred[3 * (size_t)i + 2]};
+        const uint32_t fl = v.flags[i];
+        if (stylize && !(fl & 1u)) {
+            const int32_t pi = sc.materials[v.material[i]].style[style_index(fl)];
+            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], depth, c);
+        }
+    }
+    out[i] = c.x;
+    out[n + i] = c.y;
+    out[2 * (size_t)n + i] = c.z;
+}
+// Rendering pass: one first hit per pixel (path i = pixel i); the cache's prediction there, styled
+// at depth 0 unless no_first_hit_stylization, into the FP64 film (kernel_inference_stage_gathering,
+// nrc_pt.rs:877-965).
+__global__ void k_nrc_splat_pred(uint32_t npx, VertOut v0, const float *pred, const sty_scene_material *mats,
+                                 const sty_style_program *progs, uint32_t n_progs, int no_first_hit, double weight,
+                                 double *film) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npx || !v0.active[px]) return;
+    f3 c = {pred[3 * (size_t)px], pred[3 * (size_t)px + 1], pred[3 * (size_t)px + 2]};
+    const uint32_t fl = v0.flags[px];
+    if (!no_first_hit && !(fl & 1u)) {
+        const int32_t pi = mats[v0.material[px]].style[style_index(fl)];
+        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c);
+    }
+    film[3 * (size_t)px] += weight * c.x;
+    film[3 * (size_t)px + 1] += weight * c.y;
+    film[3 * (size_t)px + 2] += weight * c.z;
+}
+// zero the targets that are not finite (the reference drops such rows, :790-793)
+__global__ void k_finite_targets(size_t n3, float *t) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n3 && !isfinite(t[i])) t[i] = 0.0f;
+}
+
 }  // namespace
 }  // namespace sty
 
@@ -600,12 +648,16 @@ CamArgs make_camera(const sty_camera &cam) {
     ca.radius = cam.filter_radius;
     ca.W = cam.width;
     ca.H = cam.height;
+    ca.random_px = 0;
     return ca;
 }
 
 // Device buffers a scene keeps between renders (grown on demand, freed with the scene): renders
 // of one scene reuse them, so calls on one scene are serialised by the caller.
-enum CacheSlot { kVerts, kOuts, kPathState, kRng, kPrograms, kVertexCount, kRowCount, kRowIndex, kScanTmp, kSlots };
+enum CacheSlot {
+    kVerts, kOuts, kPathState, kRng, kPrograms, kVertexCount, kRowCount, kRowIndex, kScanTmp,
+    kQueryIn, kQueryPred, kQueryScratch, kTargets, kRowsIn, kRowsTgt, kSlots
+};
 struct RenderCache {
     void *p[kSlots] = {};
     size_t bytes[kSlots] = {};
@@ -654,10 +706,10 @@ struct TraceJob {
         return cache->p[k];
     }
     sty_status init(sty_scene *scene, uint32_t branch, uint32_t maxd, const sty_style_program *programs,
-                    uint32_t nprog, uint64_t seed, cudaStream_t st) {
+                    uint32_t nprog, uint64_t seed, cudaStream_t st, uint32_t paths = 0) {
         const sty_camera &cam = scene_camera(scene);
         npx = cam.width * cam.height;
-        const uint64_t np64 = (uint64_t)npx * branch;
+        const uint64_t np64 = paths ? (uint64_t)paths : (uint64_t)npx * branch;
         if (np64 >= (1ull << 31)) {
             set_error("too many paths (%llu)", (unsigned long long)np64);
             return STY_ERR_ARG;
@@ -889,5 +941,130 @@ extern "C" sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t 
     STY_TRY(check_cuda(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, st), "read rows"));
     STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync samples"));
     *count_out = h < capacity ? h : capacity;
+    return STY_OK;
+}
+
+extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_render_config *cfg,
+                                     const sty_style_program *programs, uint32_t n_programs, double *film,
+                                     sty_nrc_render_stats *stats, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && nrc && cfg && film, "sty_nrc_render: null argument");
+    STY_ARG_CHECK(cfg->max_depth >= 1 && cfg->max_depth <= 30 && cfg->repeats >= 1 && cfg->batches_per_iter >= 1,
+                  "bad max_depth / repeats / batches_per_iter");
+    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
+    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
+    STY_ARG_CHECK(nrc_input_dims(nrc) == 11, "the cache must take the 11-input rows (STY_NRC_ROWS_SPHERICAL)");
+    cudaStream_t st = as_stream(stream);
+    const sty_camera &cam = scene_camera(scene);
+    const uint32_t npx = cam.width * cam.height, D = cfg->max_depth;
+    uint64_t tp = cfg->training_paths;
+    if (!tp) tp = (uint64_t)cfg->batches_per_iter * nrc_batch_size(nrc) / (D + 1);
+    tp = std::min<uint64_t>(std::max<uint64_t>(tp, 1), npx);
+    STY_ARG_CHECK(tp * (D + 1) < (1ull << 31), "too many training rows");
+    const uint32_t n = (uint32_t)tp;
+    sty_nrc_render_stats acc = {0, 0, 0.0f, 0};
+
+    FeatArgs fa;
+    {
+        float bmin[3], bmax[3];
+        scene_bounds(scene, bmin, bmax);
+        for (int a = 0; a < 3; a++) {
+            fa.bmin[a] = bmin[a];
+            fa.bext[a] = std::max(bmax[a] - bmin[a], 1e-6f);
+        }
+        fa.max_depth = D;
+        fa.layout = STY_NRC_ROWS_SPHERICAL;
+        fa.dims = 11;
+    }
+    // ---- training
+    for (uint32_t it = 0; it < cfg->training_iters; it++) {
+        TraceJob job;
+        STY_TRY(job.init(scene, 1, D, programs, n_programs, cfg->seed * 0x9e3779b97f4a7c15ull + it, st, n));
+        job.ca.random_px = 1;
+        RenderCache &rc = *job.cache;
+        const size_t rows = (size_t)D * n;
+        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>(rows, npx) * 11 * 4, "alloc query rows");
+        float *qpred = (float *)job.alloc(kQueryPred, std::max<size_t>(rows, npx) * 3 * 4, "alloc predictions");
+        float *qscr = (float *)job.alloc(kQueryScratch, std::max<size_t>(rows, npx) * 3 * 4, "alloc query scratch");
+        float *tgt = (float *)job.alloc(kTargets, (size_t)(D + 1) * 3 * n * 4, "alloc targets");
+        float *rin = (float *)job.alloc(kRowsIn, (size_t)(D + 1) * n * 11 * 4, "alloc training rows");
+        float *rtg = (float *)job.alloc(kRowsTgt, (size_t)(D + 1) * n * 3 * 4, "alloc training targets");
+        unsigned long long *cnt = (unsigned long long *)job.alloc(kRowCount, 8, "alloc row counter");
+        uint32_t *idx = (uint32_t *)job.alloc(kRowIndex, (size_t)n * 4, "alloc row index");
+        STY_TRY(job.s);
+        (void)rc;
+        STY_TRY(job.trace(st));
+        const unsigned nb = (n + 255) / 256;
+        // predictions (training weights) at depths 1..D
+        for (uint32_t d = 1; d <= D; d++) {
+            k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, n, job.vo[d], qin + (size_t)(d - 1) * n * 11,
+                                                 qscr + (size_t)(d - 1) * n * 3);
+            STY_TRY(check_launch("k_nrc_query_rows"));
+        }
+        STY_TRY(sty_nrc_train_inference(nrc, rows, qin, qpred, stream));
+        acc.inference_queries += rows;
+        for (uint32_t d = 1; d <= D; d++) {
+            k_nrc_style_pred<<<nb, 256, 0, st>>>(job.sv, n, job.vo[d], qpred + (size_t)(d - 1) * n * 3, job.dprog,
+                                                 n_programs, d, cfg->learn_stylized_radiance ? 0 : 1, job.out(d));
+            STY_TRY(check_launch("k_nrc_style_pred"));
+        }
+        // targets: Le + NEE + continuation with the styled prediction at the next vertex
+        for (uint32_t d = 0; d <= D; d++) {
+            k_self_radiance<<<nb, 256, 0, st>>>(job.sv, n, job.vo[d], d < D ? job.out(d + 1) : nullptr,
+                                                tgt + (size_t)d * 3 * n);
+            STY_TRY(check_launch("k_self_radiance"));
+        }
+        k_finite_targets<<<(unsigned)(((size_t)(D + 1) * 3 * n + 255) / 256), 256, 0, st>>>((size_t)(D + 1) * 3 * n,
+                                                                                          tgt);
+        STY_TRY(check_launch("k_finite_targets"));
+        // rows of the depths >= the training level, depth-major in path order
+        const uint32_t level =
+            cfg->per_level_training ? (it / cfg->per_level_training >= D ? 0u : D - it / cfg->per_level_training) : 0u;
+        size_t tmp_bytes = 0;
+        STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, (const uint32_t *)job.vo[0].active, idx,
+                                                          (int)n, st),
+                           "scan size"));
+        void *tmp = job.alloc(kScanTmp, tmp_bytes, "alloc scan scratch");
+        STY_TRY(job.s);
+        STY_TRY(check_cuda(cudaMemsetAsync(cnt, 0, 8, st), "zero rows"));
+        for (uint32_t d = level; d <= D; d++) {
+            STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, (const uint32_t *)job.vo[d].active, idx,
+                                                              (int)n, st),
+                               "scan rows"));
+            k_nrc_train_rows<<<nb, 256, 0, st>>>(job.sv, fa, n, d, job.vo[d], tgt + (size_t)d * 3 * n, idx, cnt, rin,
+                                                 rtg, (uint64_t)(D + 1) * n);
+            STY_TRY(check_launch("k_nrc_train_rows"));
+            k_advance_rows<<<1, 1, 0, st>>>(n, idx, job.vo[d].active, cnt);
+            STY_TRY(check_launch("k_advance_rows"));
+        }
+        unsigned long long h = 0;
+        STY_TRY(check_cuda(cudaMemcpyAsync(&h, cnt, 8, cudaMemcpyDeviceToHost, st), "read rows"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync rows"));
+        if (h) {
+            const bool last = it + 1 == cfg->training_iters;
+            STY_TRY(sty_nrc_train(nrc, h, cfg->batches_per_iter, rin, rtg, last ? &acc.last_loss : nullptr, stream));
+            acc.training_rows += h;
+        }
+    }
+    // ---- rendering
+    for (uint32_t r = 0; r < cfg->repeats; r++) {
+        TraceJob job;
+        STY_TRY(job.init(scene, 1, 0, programs, n_programs, cfg->seed * 0x9e3779b97f4a7c15ull + 0x5bd1e995ull + r, st));
+        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>((size_t)D * n, npx) * 11 * 4, "alloc query rows");
+        float *qpred = (float *)job.alloc(kQueryPred, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc predictions");
+        float *qscr = (float *)job.alloc(kQueryScratch, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc scratch");
+        STY_TRY(job.s);
+        STY_TRY(job.trace(st));
+        const unsigned nb = (npx + 255) / 256;
+        k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, npx, job.vo[0], qin, qscr);
+        STY_TRY(check_launch("k_nrc_query_rows"));
+        STY_TRY(sty_nrc_inference(nrc, npx, qin, qpred, stream));
+        acc.inference_queries += npx;
+        k_nrc_splat_pred<<<nb, 256, 0, st>>>(npx, job.vo[0], qpred, job.sv.materials, job.dprog, n_programs,
+                                             cfg->no_first_hit_stylization, 1.0 / cfg->repeats, film);
+        STY_TRY(check_launch("k_nrc_splat_pred"));
+    }
+    STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync nrc render"));
+    if (stats) *stats = acc;
     return STY_OK;
 }

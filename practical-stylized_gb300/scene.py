@@ -40,6 +40,28 @@ class RenderConfig(C.Structure):
                 ("has_scene_bounds", C.c_int32), ("scene_bounds", C.c_float * 6), ("seed", C.c_uint64)]
 
 
+class NrcRenderConfig(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("training_iters", C.c_uint32), ("batches_per_iter", C.c_uint32),
+                ("training_paths", C.c_uint32), ("repeats", C.c_uint32), ("per_level_training", C.c_uint32),
+                ("no_first_hit_stylization", C.c_int32), ("learn_stylized_radiance", C.c_int32), ("seed", C.c_uint64)]
+
+
+class NrcRenderStats(C.Structure):
+    _fields_ = [("training_rows", C.c_uint64), ("inference_queries", C.c_uint64), ("last_loss", C.c_float),
+                ("reserved", C.c_uint32)]
+
+
+def nrc_render_config(max_depth=5, training_iters=64, batches_per_iter=16, training_paths=0, repeats=1,
+                      per_level_training=0, no_first_hit_stylization=False, learn_stylized_radiance=False,
+                      seed=0) -> NrcRenderConfig:
+    c = NrcRenderConfig()
+    c.max_depth, c.training_iters, c.batches_per_iter = max_depth, training_iters, batches_per_iter
+    c.training_paths, c.repeats, c.per_level_training = training_paths, repeats, per_level_training
+    c.no_first_hit_stylization, c.learn_stylized_radiance = int(no_first_hit_stylization), int(learn_stylized_radiance)
+    c.seed = seed
+    return c
+
+
 def material(kind=MAT_DIFFUSE, albedo=(0.75, 0.75, 0.75), alpha=0.3, emission=(0, 0, 0), style=(-1, -1, -1, -1),
              set_style=-1) -> SceneMaterial:
     m = SceneMaterial()
@@ -253,3 +275,18 @@ class Scene:
         check(lib().sty_nrc_samples(self.h, mode, layout, spp, max_depth, seed, x.data_ptr(), y.data_ptr(), capacity,
                                     C.byref(cnt), _stream_ptr(stream)))
         return x[:cnt.value], y[:cnt.value]
+
+    def nrc_render(self, net, cfg: NrcRenderConfig, programs=(), film=None, stream=None):
+        """The NL-NRC render (sty_nrc_render): trains `net` online on the scene's own paths and
+        renders the cache at the first hit. Returns (film [H, W, 3] float64 device tensor, stats)."""
+        import torch
+        from .pf import _stream_ptr
+        W, H = self.camera.width, self.camera.height
+        if film is None:
+            film = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+        progs = list(programs)
+        arr = (abi.StyleProgram * max(1, len(progs)))(*progs) if progs else None
+        st = NrcRenderStats()
+        check(lib().sty_nrc_render(self.h, net.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(st),
+                                   _stream_ptr(stream)))
+        return film, st
