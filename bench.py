@@ -311,6 +311,60 @@ def c3_bench(sty, reps: int = 20):
             "grad_finite": bool(torch.isfinite(grad).all().item())}
 
 
+def c5_bench(sty, W: int = 160, H: int = 90):
+    """Full stylized render of the interior workload (6 x 3 x 4 m room of ~377 k triangles, door
+    open 20 degrees, the only emitter behind it; GGX + diffuse; toon (band 0.2) and a 3-colour
+    luminance ramp at bounces 0 and 1; max depth 8) at a reduced scale: W x H px. Methods, each
+    timed (CUDA-synchronised wall time) and scored by image MSE against a 1024-spp
+    FP64-accumulated NL-PF render of the same view:
+      nl_pf      reference-mode NL-PF at 64 spp (16 paths x 4 repeats, radius 1 % of the scene
+                 extent, reuse 32, SMIS);
+      nl_nrc_*   the NL-NRC loop (128 training iterations of 4 batches of 2^14, 16 first-hit
+                 passes) with the BF16 tcgen05 cache and with the FP32 cache."""
+    import numpy as np
+    import torch
+    a = sty.abi
+    pos, mids, mats, cam = sty.scene.room_with_door(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    progs = [a.style_program([a.toon(0.2, depth_mask=0b11),
+                              a.ramp_smooth(30.0, [0.02, 0.15, 0.6],
+                                            [(0.08, 0.1, 0.2), (0.55, 0.45, 0.35), (1.3, 1.2, 1.0)],
+                                            depth_mask=0b11)])]
+
+    def pf(branch, repeats, seed):
+        cfg = sty.scene.render_config(max_depth=8, branch=branch, repeats=repeats, radius_scale=(1.0,),
+                                      reuse=(32,), seed=seed)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        film, nv = sc.render(cfg, progs)
+        torch.cuda.synchronize()
+        return film.cpu().numpy(), time.perf_counter() - t0, nv
+
+    pf(4, 1, 99)  # warm-up
+    ref, t_ref, nv_ref = pf(64, 16, 4242)
+    res = {"workload": f"interior room {pos.shape[0]} tris, door 20 deg, {W}x{H}, max depth 8, toon + "
+                       "3-colour ramp at bounces 0-1",
+           "reference": {"spp": 1024, "seconds": t_ref, "vertices": nv_ref}}
+    img, t, nv = pf(16, 4, 7)
+    res["nl_pf"] = {"spp": 64, "seconds": t, "mpath_vertices_per_s": nv / t / 1e6,
+                    "image_mse": float(((img - ref) ** 2).mean())}
+    for name, prec in (("nl_nrc_bf16", sty.nrc.STY_NRC_BF16), ("nl_nrc_fp32", sty.nrc.STY_NRC_FP32)):
+        net = sty.nrc.NRC(sty.nrc.config(sty.nrc.C4_FREQS, 3, 1 << 14, 5, prec, learning_rate=1e-2, seed=1))
+        cfg = sty.scene.nrc_render_config(max_depth=8, training_iters=128, batches_per_iter=4, repeats=16, seed=3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        film, st = sc.nrc_render(net, cfg, progs)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        img = film.cpu().numpy()
+        res[name] = {"seconds": t, "training_rows": int(st.training_rows), "queries": int(st.inference_queries),
+                     "image_mse": float(((img - ref) ** 2).mean())}
+        net.close()
+    res["reference_mean"] = float(ref.mean())
+    sc.close()
+    return res
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -355,6 +409,9 @@ def run(args):
         return
     if args.c1_only:  # profiling case: the end-to-end render alone
         print(json.dumps({"c1_render": c1_bench(sty, repeats=max(1, args.steps))}), flush=True)
+        return
+    if args.c5_only:  # the full stylized render alone
+        print(json.dumps({"c5_render": c5_bench(sty)}), flush=True)
         return
 
     D_ = args.depths
@@ -507,6 +564,7 @@ def run(args):
     if world == 1 and not args.no_c1:
         line["c1_render"] = c1_bench(sty)
         line["c3_adjoint"] = c3_bench(sty)
+        line["c5_render"] = c5_bench(sty)
     if world == 1 and not args.no_nrc:
         bf16_peak = 1943.8
         p = ROOT / "MEASURED_PEAKS.json"
@@ -536,6 +594,7 @@ def main():
     ap.add_argument("--no-c1", action="store_true", help="skip the end-to-end Cornell box render")
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
+    ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

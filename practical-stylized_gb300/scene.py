@@ -212,6 +212,94 @@ def icosphere_grid(width=1920, height=1080, n=10, subdiv=3, seed=0, camera_fov=4
     return pos, np.array(mids, dtype=np.uint32), mats, cam
 
 
+def _grid_quad(o, u, v, nu, nv):
+    """A planar quad o + s*u + t*v (s, t in [0, 1]) tessellated into nu x nv cells (2 triangles
+    each), counter-clockwise seen from the side u x v points to."""
+    o, u, v = (np.asarray(x, dtype=np.float64) for x in (o, u, v))
+    s = np.linspace(0.0, 1.0, nu + 1)
+    t = np.linspace(0.0, 1.0, nv + 1)
+    P = o[None, None] + s[:, None, None] * u[None, None] + t[None, :, None] * v[None, None]
+    a, b, c, d = P[:-1, :-1], P[1:, :-1], P[1:, 1:], P[:-1, 1:]
+    return np.concatenate([np.stack([a, b, c], 2).reshape(-1, 3, 3), np.stack([a, c, d], 2).reshape(-1, 3, 3)])
+
+
+def _box_tris(lo, hi, inward=False):
+    t = np.array(_box(lo, hi), dtype=np.float64).reshape(-1, 3, 3)
+    return t[:, [0, 2, 1]] if inward else t
+
+
+def room_with_door(width=320, height=180, cell=0.028, door_angle=20.0, seed=0):
+    """Full-render workload scene: a 6 x 3 x 4 m room (x: 0..6, y: 0..3 up, z: 0..4) whose walls,
+    floor and ceiling are tessellated into `cell`-sized quads (~125 k triangles at 5 cm, ~400 k at
+    2.8 cm); a 1 x 2.1 m doorway in the wall x = 6 with a door panel turned `door_angle` degrees about
+    its hinge; behind it a 2 m deep corridor whose ceiling holds the only emitter (1 x 2 m, radiance
+    40), so most light reaches the room indirectly through the door gap. Furniture: 6 diffuse
+    boxes and 8 GGX icospheres (alpha ~ U[0.05, 0.5], albedo ~ U[0.2, 0.9]^3, seeded); walls
+    diffuse 0.7, floor GGX alpha 0.3. Style indices: every surface uses program slot 0.
+    Returns (positions [n, 9], material ids, materials, camera)."""
+    rng = np.random.default_rng(seed)
+    tris, mids, mats = [], [], []
+
+    def add(t, m):
+        tris.append(np.asarray(t, dtype=np.float64).reshape(-1, 3, 3))
+        mids.extend([m] * len(tris[-1]))
+
+    sty0 = (0, -1, -1, -1)
+    mats.append(material(MAT_DIFFUSE, (0.7, 0.7, 0.68), style=sty0))            # 0 walls
+    mats.append(material(MAT_GGX, (0.55, 0.45, 0.35), alpha=0.3, style=sty0))  # 1 floor
+    mats.append(material(MAT_DIFFUSE, (0.6, 0.35, 0.2), style=sty0))           # 2 door / boxes
+    mats.append(material(MAT_DIFFUSE, (0.0, 0.0, 0.0), emission=(40.0, 40.0, 40.0), style=sty0))  # 3 light
+    n = lambda L: max(1, int(round(L / cell)))  # noqa: E731
+    X, Y, Z = 6.0, 3.0, 4.0
+    # floor (normal +y) and ceiling (normal -y), room and corridor
+    add(_grid_quad([0, 0, 0], [0, 0, Z], [X, 0, 0], n(Z), n(X)), 1)
+    add(_grid_quad([0, Y, 0], [X, 0, 0], [0, 0, Z], n(X), n(Z)), 0)
+    add(_grid_quad([X, 0, 0], [0, 0, Z], [2, 0, 0], n(Z), n(2)), 1)
+    # corridor ceiling with the light in its middle
+    add(_grid_quad([X, Y, 0], [2, 0, 0], [0, 0, 1], n(2), n(1)), 0)
+    add(_grid_quad([X, Y, 3], [2, 0, 0], [0, 0, 1], n(2), n(1)), 0)
+    add(_grid_quad([X, Y, 1], [0.5, 0, 0], [0, 0, 2], n(0.5), n(2)), 0)
+    add(_grid_quad([X + 1.5, Y, 1], [0.5, 0, 0], [0, 0, 2], n(0.5), n(2)), 0)
+    ly = Y - 1e-3
+    add(_quad([X + 0.5, ly, 1], [X + 1.5, ly, 1], [X + 1.5, ly, 3], [X + 0.5, ly, 3]), 3)
+    # room walls (inward): z = 0 (normal +z), z = Z (normal -z), x = 0 (normal +x)
+    add(_grid_quad([0, 0, 0], [X, 0, 0], [0, Y, 0], n(X), n(Y)), 0)
+    add(_grid_quad([X, 0, Z], [-X, 0, 0], [0, Y, 0], n(X), n(Y)), 0)
+    add(_grid_quad([0, 0, Z], [0, 0, -Z], [0, Y, 0], n(Z), n(Y)), 0)
+    # corridor walls: z = 0, z = Z, x = X + 2 (back)
+    add(_grid_quad([X, 0, 0], [2, 0, 0], [0, Y, 0], n(2), n(Y)), 0)
+    add(_grid_quad([X + 2, 0, Z], [-2, 0, 0], [0, Y, 0], n(2), n(Y)), 0)
+    add(_grid_quad([X + 2, 0, 0], [0, 0, Z], [0, Y, 0], n(Z), n(Y)), 0)
+    # the wall x = X around the doorway z in [1.5, 2.5], y in [0, 2.1], one face towards the room (the
+    # BSDFs are two-sided, so the corridor sees the same triangles from behind)
+    dz0, dz1, dh = 1.5, 2.5, 2.1
+    for o, u, v, nu, nv in (([X, 0, 0], [0, 0, dz0], [0, Y, 0], n(dz0), n(Y)),
+                            ([X, 0, dz1], [0, 0, Z - dz1], [0, Y, 0], n(Z - dz1), n(Y)),
+                            ([X, dh, dz0], [0, 0, dz1 - dz0], [0, Y - dh, 0], n(dz1 - dz0), n(Y - dh))):
+        add(_grid_quad(o, u, v, nu, nv), 0)
+    # door panel: 1 x 2.1 x 0.04 m, hinged at (X, z = dz0), turned into the room by door_angle
+    door = _box_tris((0.0, 0.0, 0.0), (0.04, dh, dz1 - dz0))
+    th = np.radians(door_angle)
+    R = np.array([[np.cos(th), 0, np.sin(th)], [0, 1, 0], [-np.sin(th), 0, np.cos(th)]])
+    door = door @ R.T + np.array([X - 0.04, 0, dz0])
+    add(door, 2)
+    # furniture
+    for k in range(6):
+        cx, cz = rng.uniform(0.6, X - 1.2), rng.uniform(0.5, Z - 0.5)
+        sx, sy, sz = rng.uniform(0.3, 0.8), rng.uniform(0.3, 1.2), rng.uniform(0.3, 0.8)
+        add(_box_tris((cx, 0.0, cz), (cx + sx, sy, cz + sz)), 2)
+    sph = icosphere(3)
+    for k in range(8):
+        r = rng.uniform(0.15, 0.4)
+        c = np.array([rng.uniform(0.5, X - 0.8), r, rng.uniform(0.5, Z - 0.5)])
+        mats.append(material(MAT_GGX, tuple(rng.uniform(0.2, 0.9, 3)), alpha=float(rng.uniform(0.05, 0.5)),
+                             style=sty0))
+        add(sph * r + c, len(mats) - 1)
+    pos = np.concatenate(tris).reshape(-1, 9).astype(np.float32)
+    cam = camera((0.6, 1.6, 2.0), (6.0, 1.1, 2.0), fov_y=60.0, width=width, height=height)
+    return pos, np.array(mids, dtype=np.uint32), mats, cam
+
+
 class Scene:
     def __init__(self, positions: np.ndarray, mat_ids: np.ndarray, materials, cam: Camera):
         self.positions = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)

@@ -101,3 +101,25 @@ def test_cornell_render_deterministic(sty, cuda):
         assert np.isfinite(i1).all() and (i1 == i2).all()
         assert 0.05 < i1.mean() < 5.0
     assert sty.abi.device_status() == 0
+
+
+def test_room_scene_renders(sty, cuda):
+    """The interior workload scene: light from the corridor emitter reaches the room only through
+    the door gap; the NL-PF and NL-NRC renders of it are finite, lit, and deterministic."""
+    pos, mids, mats, cam = sty.scene.room_with_door(48, 27, cell=0.2)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    a = sty.abi
+    progs = [a.style_program([a.toon(0.2, depth_mask=0b11)])]
+    cfg = sty.scene.render_config(max_depth=6, branch=8, radius_scale=(1.0,), reuse=(16,), seed=2)
+    f1, nv = sc.render(cfg, progs)
+    f2, _ = sc.render(cfg, progs)
+    img = f1.cpu().numpy()
+    assert nv > 0 and np.isfinite(img).all() and img.mean() > 1e-3
+    assert (f1 == f2).all()
+    net = sty.nrc.NRC(sty.nrc.config(batch_size=1 << 12, seed=2))
+    film, st = sc.nrc_render(net, sty.scene.nrc_render_config(max_depth=6, training_iters=8, batches_per_iter=2),
+                             progs)
+    im = film.cpu().numpy()
+    assert np.isfinite(im).all() and st.training_rows > 0
+    net.close()
+    assert sty.abi.device_status() == 0
