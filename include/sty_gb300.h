@@ -457,9 +457,17 @@ STY_API sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t lay
  * at the next vertex, styled at that depth unless learn_stylized_radiance (:704-842); then
  * sty_nrc_train(rows, batches_per_iter). With per_level_training > 0 the training level starts at
  * max_depth and drops by one every per_level_training iterations (:1538-1545), else it is 0.
- * Rendering, `repeats` times: one first hit per pixel, the cache's EMA prediction there, styled at
- * depth 0 unless no_first_hit_stylization, added with weight 1/repeats to `film` (device,
- * width*height*3 doubles, rgb; the caller zeroes it) (:844-965). `programs` is a HOST array.
+ * Rendering, `repeats` times, added with weight 1/repeats to `film` (device, width*height*3
+ * doubles, rgb; the caller zeroes it):
+ *   final_gather == 0: one first hit per pixel, the cache's EMA prediction there, styled at depth 0
+ *     unless no_first_hit_stylization (:844-965);
+ *   final_gather > 0: each pixel's path continues through vertices of roughness <= 0.05 up to
+ *     max_depth and splits at the first rougher one (:372-375); final_gather times, the split
+ *     vertex takes another light sample and one BSDF-sampled ray whose hit the EMA cache predicts
+ *     (styled at that depth) (:436-582, 877-965); the split vertex's radiance is Le +
+ *     direct / (n + 1) + indirect / n, propagated to the camera with the style node at every
+ *     depth (:969-1047). Paths that never split are path traced without the cache.
+ * `programs` is a HOST array.
  * Calls on one scene are serialised by the caller (the scene keeps the render's buffers).
  * Reference flags are taken after the vertex's own set_style update (as in sty_pf_render). */
 typedef struct sty_nrc_render_config {
@@ -471,6 +479,8 @@ typedef struct sty_nrc_render_config {
     uint32_t per_level_training;
     int32_t no_first_hit_stylization;
     int32_t learn_stylized_radiance;
+    uint32_t final_gather;
+    uint32_t reserved;
     uint64_t seed;
 } sty_nrc_render_config;
 typedef struct sty_nrc_render_stats {

@@ -185,6 +185,7 @@ struct PathState {
     float *prev_p[3];
     float *prev_pdf;
     uint32_t *flags, *exclude, *terminated;
+    uint32_t *split;  // depth of the vertex a final-gathering render stopped at, NONE otherwise
 };
 struct VertOut {  // mutable view of one depth's sty_pf_vertices planes
     int32_t *active;
@@ -198,9 +199,57 @@ struct CamArgs {
     uint32_t random_px;  // 1: path tid starts at pixel pcg32() % (W*H) (training paths, nrc_pt.rs:1394)
 };
 
+// One light sample for a vertex at p (sample_light, lm_path_filtering.rs:1261-1316): emitter chosen
+// by the area x luminance CDF, uniform point on it, Li styled at depth + 1 by the emitter's program
+// (flags = the vertex's updated flags), shadow ray. Returns false when the sample carries nothing.
+__device__ bool nee_sample(const SceneView &sc, F3 p, F3 ng, uint32_t prim, uint32_t new_flags, uint32_t depth,
+                           const sty_style_program *progs, uint32_t n_progs, sty_pcg32 &st, F3 *wi_out, f3 *li_out,
+                           float *pdf_out) {
+    const float ux = next_1d(st), uy = next_1d(st), uz = next_1d(st);
+    if (sc.n_lights == 0) return false;
+    uint32_t lo = 0, hi = sc.n_lights - 1;
+    while (lo < hi) {  // first k with cdf[k+1] > ux
+        const uint32_t mid = (lo + hi) >> 1;
+        if (sc.light_cdf[mid + 1] > ux) hi = mid;
+        else lo = mid + 1;
+    }
+    const uint32_t lt = sc.light_tris[lo];
+    const float sel = sc.light_cdf[lo + 1] - sc.light_cdf[lo];
+    const float2 bb = uniform_sample_triangle(uy, uz);
+    const float *lp = sc.tri_pos + 9 * (size_t)lt;
+    const float c0 = 1.0f - bb.x - bb.y;
+    const F3 q = f3m(c0 * lp[0] + bb.x * lp[3] + bb.y * lp[6], c0 * lp[1] + bb.x * lp[4] + bb.y * lp[7],
+                     c0 * lp[2] + bb.x * lp[5] + bb.y * lp[8]);
+    const F3 ln = f3m(sc.tri_normal[3 * lt], sc.tri_normal[3 * lt + 1], sc.tri_normal[3 * lt + 2]);
+    F3 wi = q - p;
+    const float dist2 = dot(wi, wi);
+    if (!(dist2 > 0.0f)) return false;
+    const float dist = sqrtf(dist2);
+    wi = wi * (1.0f / dist);
+    const sty_scene_material lm = sc.materials[sc.tri_material[lt]];
+    f3 li = {0.0f, 0.0f, 0.0f};
+    if (dot(wi, ln) < 0.0f) li = {lm.emission[0], lm.emission[1], lm.emission[2]};
+    const float lpdf = sel / sc.tri_area[lt] * dist2 / fabsf(dot(ln, wi));
+    if (!(isfinite(lpdf) && lpdf > 0.0f)) return false;
+    if (!(new_flags & 1u)) {  // the light's style node at the next depth (sample_light :1286-1305)
+        const int32_t pi = lm.style[style_index(new_flags)];
+        if (pi >= 0 && (uint32_t)pi < n_progs) li = style_apply(progs[pi], depth + 1, li);
+    }
+    const F3 so = offset_ray_origin(p, face_forward(ng, wi));
+    const float s3[3] = {so.x, so.y, so.z}, w3[3] = {wi.x, wi.y, wi.z};
+    if (trace_any(sc, s3, w3, 0.0f, dist * (1.0f - 1e-3f), prim, lt)) return false;
+    *wi_out = wi;
+    *li_out = li;
+    *pdf_out = lpdf;
+    return true;
+}
+__device__ __forceinline__ float lobe_roughness(const sty_scene_material &m) {  // avg_roughness
+    return m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
+}
+
 __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t depth, uint32_t max_depth,
                         PathState ps, VertOut v, VertOut parent, sty_pcg32 *rng, const sty_style_program *progs,
-                        uint32_t n_progs, unsigned long long *vcount) {
+                        uint32_t n_progs, unsigned long long *vcount, float split_rough) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= n_paths) return;
     sty_pcg32 st = rng[tid];
@@ -225,6 +274,7 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
         prev_pdf = 0.0f;
         prev_p = ro;
         ps.terminated[tid] = 0;
+        ps.split[tid] = NONE;
     } else {
         if (ps.terminated[tid]) return;
         ro = f3m(ps.o[0][tid], ps.o[1][tid], ps.o[2][tid]);
@@ -309,51 +359,26 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
     }
     // NEE (sample_light)
     {
-        const float ux = next_1d(st), uy = next_1d(st), uz = next_1d(st);
-        if (sc.n_lights > 0) {
-            uint32_t lo = 0, hi = sc.n_lights - 1;
-            while (lo < hi) {  // first k with cdf[k+1] > ux
-                const uint32_t mid = (lo + hi) >> 1;
-                if (sc.light_cdf[mid + 1] > ux) hi = mid;
-                else lo = mid + 1;
-            }
-            const uint32_t lt = sc.light_tris[lo];
-            const float sel = sc.light_cdf[lo + 1] - sc.light_cdf[lo];
-            const float2 bb = uniform_sample_triangle(uy, uz);
-            const float *lp = sc.tri_pos + 9 * (size_t)lt;
-            const float c0 = 1.0f - bb.x - bb.y;
-            const F3 q = f3m(c0 * lp[0] + bb.x * lp[3] + bb.y * lp[6], c0 * lp[1] + bb.x * lp[4] + bb.y * lp[7],
-                             c0 * lp[2] + bb.x * lp[5] + bb.y * lp[8]);
-            const F3 ln = f3m(sc.tri_normal[3 * lt], sc.tri_normal[3 * lt + 1], sc.tri_normal[3 * lt + 2]);
-            F3 wi = q - p;
-            const float dist2 = dot(wi, wi);
-            if (dist2 > 0.0f) {
-                const float dist = sqrtf(dist2);
-                wi = wi * (1.0f / dist);
-                const sty_scene_material lm = sc.materials[sc.tri_material[lt]];
-                f3 li = {0.0f, 0.0f, 0.0f};
-                if (dot(wi, ln) < 0.0f) li = {lm.emission[0], lm.emission[1], lm.emission[2]};
-                const float lpdf = sel / sc.tri_area[lt] * dist2 / fabsf(dot(ln, wi));
-                if (isfinite(lpdf) && lpdf > 0.0f) {
-                    // the light's style node at the next depth (sample_light :1286-1305)
-                    if (!(new_flags & 1u)) {
-                        const int32_t pi = lm.style[style_index(new_flags)];
-                        if (pi >= 0 && (uint32_t)pi < n_progs) li = style_apply(progs[pi], depth + 1, li);
-                    }
-                    const F3 so = offset_ray_origin(p, face_forward(ng, wi));
-                    const float s3[3] = {so.x, so.y, so.z}, w3[3] = {wi.x, wi.y, wi.z};
-                    if (!trace_any(sc, s3, w3, 0.0f, dist * (1.0f - 1e-3f), prim, lt)) {
-                        v.dir_wi[0][tid] = wi.x;
-                        v.dir_wi[1][tid] = wi.y;
-                        v.dir_wi[2][tid] = wi.z;
-                        v.dir_l[0][tid] = li.x;
-                        v.dir_l[1][tid] = li.y;
-                        v.dir_l[2][tid] = li.z;
-                        v.dir_pdf[tid] = lpdf;
-                    }
-                }
-            }
+        F3 lwi;
+        f3 li;
+        float lpdf;
+        if (nee_sample(sc, p, ng, prim, new_flags, depth, progs, n_progs, st, &lwi, &li, &lpdf)) {
+            v.dir_wi[0][tid] = lwi.x;
+            v.dir_wi[1][tid] = lwi.y;
+            v.dir_wi[2][tid] = lwi.z;
+            v.dir_l[0][tid] = li.x;
+            v.dir_l[1][tid] = li.y;
+            v.dir_l[2][tid] = li.z;
+            v.dir_pdf[tid] = lpdf;
         }
+    }
+    // final-gathering renders stop at the first rough vertex (splitting, nrc_pt.rs:372-375)
+    if (split_rough > 0.0f && lobe_roughness(m) > split_rough) {
+        ps.split[tid] = depth;
+        ps.exclude[tid] = prim;  // the split vertex's triangle, skipped by its gather rays
+        ps.terminated[tid] = 1;
+        rng[tid] = st;
+        return;
     }
     // BSDF sample and continuation
     const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
@@ -616,6 +641,183 @@ __global__ void k_finite_targets(size_t n3, float *t) {
     if (i < n3 && !isfinite(t[i])) t[i] = 0.0f;
 }
 
+// ---- final gathering (nrc_pt.rs:436-582, 877-965, 969-1047) -------------------------------------
+// The split vertex of every path, gathered from the per-depth planes into per-path planes.
+struct SplitPlanes {
+    float *p[3], *wo[3], *ns[3], *ng[3];
+    uint32_t *material, *flags, *prim;
+};
+__global__ void k_split_collect(uint32_t n, uint32_t d, VertOut v, const uint32_t *split, const uint32_t *prim_of,
+                                SplitPlanes sp) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || split[i] != d) return;
+    for (int a = 0; a < 3; a++) {
+        sp.p[a][i] = v.p[a][i];
+        sp.wo[a][i] = v.wo[a][i];
+        sp.ns[a][i] = v.ns[a][i];
+        sp.ng[a][i] = v.ng[a][i];
+    }
+    sp.material[i] = v.material[i];
+    sp.flags[i] = v.flags[i];
+    sp.prim[i] = prim_of[i];
+}
+// One gather iteration for every split path: another light sample at the split vertex (added to
+// acc_direct) and one BSDF-sampled ray; its hit becomes a cache query row (zero row if none) with
+// the sample's throughput f |cos| / pdf and the hit's emission MIS weight.
+__global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t *split, SplitPlanes sp, sty_pcg32 *rng,
+                          const sty_style_program *progs, uint32_t n_progs, float *rows, float *thr, float *gmis,
+                          uint32_t *gmat, uint32_t *gflags, float *acc_direct) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float *row = rows + (size_t)i * fa.dims;
+    for (uint32_t c = 0; c < fa.dims; c++) row[c] = 0.0f;
+    thr[i] = thr[n + i] = thr[2 * (size_t)n + i] = 0.0f;
+    const uint32_t s = split[i];
+    if (s == NONE) return;
+    sty_pcg32 st = rng[i];
+    const sty_scene_material m = sc.materials[sp.material[i]];
+    const F3 p = f3m(sp.p[0][i], sp.p[1][i], sp.p[2][i]), wo = f3m(sp.wo[0][i], sp.wo[1][i], sp.wo[2][i]);
+    const F3 ns = f3m(sp.ns[0][i], sp.ns[1][i], sp.ns[2][i]), ng = f3m(sp.ng[0][i], sp.ng[1][i], sp.ng[2][i]);
+    const uint32_t fl = sp.flags[i], prim = sp.prim[i];
+    {
+        F3 lwi;
+        f3 li;
+        float lpdf;
+        if (nee_sample(sc, p, ng, prim, fl, s, progs, n_progs, st, &lwi, &li, &lpdf)) {
+            F3 f;
+            const float bp = bsdf_eval(m, ns, ng, wo, lwi, &f);
+            const float w = lpdf / (lpdf + bp) / lpdf;
+            acc_direct[i] += f.x * li.x * w;
+            acc_direct[n + i] += f.y * li.y * w;
+            acc_direct[2 * (size_t)n + i] += f.z * li.z * w;
+        }
+    }
+    const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
+    float pdf = 0.0f;
+    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf);
+    rng[i] = st;
+    if (!(pdf > 0.0f)) return;
+    const F3 o = offset_ray_origin(p, face_forward(ng, wi));
+    const float o3[3] = {o.x, o.y, o.z}, d3[3] = {wi.x, wi.y, wi.z};
+    const Hit h = trace_closest(sc, o3, d3, 0.0f, 1e20f, prim);
+    if (h.prim == NONE) return;
+    const float *tp = sc.tri_pos + 9 * (size_t)h.prim;
+    const float b0 = 1.0f - h.b1 - h.b2;
+    const F3 q = f3m(b0 * tp[0] + h.b1 * tp[3] + h.b2 * tp[6], b0 * tp[1] + h.b1 * tp[4] + h.b2 * tp[7],
+                     b0 * tp[2] + h.b1 * tp[5] + h.b2 * tp[8]);
+    const F3 qn = f3m(sc.tri_normal[3 * h.prim], sc.tri_normal[3 * h.prim + 1], sc.tri_normal[3 * h.prim + 2]);
+    const uint32_t qm = sc.tri_material[h.prim];
+    const sty_scene_material mq = sc.materials[qm];
+    float mis = 1.0f;
+    if (mq.emission[0] > 0.0f || mq.emission[1] > 0.0f || mq.emission[2] > 0.0f) {  // handle_surface_light
+        float sel = 0.0f;
+        for (uint32_t k = 0; k < sc.n_lights; k++)
+            if (sc.light_tris[k] == h.prim) sel = sc.light_cdf[k + 1] - sc.light_cdf[k];
+        const F3 w = q - p;
+        const float dist2 = dot(w, w);
+        const float lpdf = sel / sc.tri_area[h.prim] * dist2 / fmaxf(fabsf(dot(qn, w * (1.0f / sqrtf(dist2)))), 1e-6f);
+        mis = pdf / (pdf + lpdf);
+    }
+    uint32_t qf = fl;  // update_stylization_flags at the gather hit
+    if (mq.set_style >= 0) {
+        qf &= 1u;
+        if (mq.set_style == 1) qf |= 2u;
+        if (mq.set_style == 2) qf |= 4u;
+        if (mq.set_style == 3) qf |= 8u;
+    }
+    F3 f;
+    const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+    if (!(bp > 0.0f)) return;
+    thr[i] = f.x / bp;
+    thr[n + i] = f.y / bp;
+    thr[2 * (size_t)n + i] = f.z / bp;
+    gmis[i] = mis;
+    gmat[i] = qm;
+    gflags[i] = qf;
+    write_features(sc, fa, q, -wi, qn, qm, qf, s + 1, row);
+}
+// acc_indirect += style_{s+1}(cache prediction at the gather hit) * throughput * mis; every
+// iteration counts (a miss contributes 0)
+__global__ void k_fg_accumulate(SceneView sc, uint32_t n, const uint32_t *split, const float *pred, const float *thr,
+                                const float *gmis, const uint32_t *gmat, const uint32_t *gflags,
+                                const sty_style_program *progs, uint32_t n_progs, int stylize, float *acc_ind,
+                                float *ngath) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || split[i] == NONE) return;
+    ngath[i] += 1.0f;
+    if (thr[i] == 0.0f && thr[n + i] == 0.0f && thr[2 * (size_t)n + i] == 0.0f) return;
+    f3 c = {pred[3 * (size_t)i], pred[3 * (size_t)i + 1], pred[3 * (size_t)i + 2]};
+    const uint32_t fl = gflags[i];
+    if (stylize && !(fl & 1u)) {
+        const int32_t pi = sc.materials[gmat[i]].style[style_index(fl)];
+        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], split[i] + 1, c);
+    }
+    const float w = gmis[i];
+    if (!(isfinite(c.x) && isfinite(c.y) && isfinite(c.z))) return;
+    acc_ind[i] += c.x * thr[i] * w;
+    acc_ind[n + i] += c.y * thr[n + i] * w;
+    acc_ind[2 * (size_t)n + i] += c.z * thr[2 * (size_t)n + i] * w;
+}
+// Backward sweep over depth d (propagate_and_splat :969-1047): at the split vertex
+// Le + direct / (n + 1) + indirect / n, elsewhere Le + direct + f L_{d+1} mis / pdf; styled at
+// depth d when `stylize` (style applies at d > 0, and at 0 unless no_first_hit_stylization).
+__global__ void k_fg_sweep(SceneView sc, uint32_t n, uint32_t d, VertOut v, const float *next, const uint32_t *split,
+                           const float *acc_direct, const float *acc_ind, const float *ngath,
+                           const sty_style_program *progs, uint32_t n_progs, int stylize, float *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    f3 r = {0.0f, 0.0f, 0.0f};
+    if (v.active[i]) {
+        const sty_scene_material m = sc.materials[v.material[i]];
+        const F3 ns = f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), ng = f3m(v.ng[0][i], v.ng[1][i], v.ng[2][i]);
+        const F3 wo = f3m(v.wo[0][i], v.wo[1][i], v.wo[2][i]);
+        F3 dir = f3m(0.0f, 0.0f, 0.0f);
+        const float dpdf = v.dir_pdf[i];
+        if (dpdf > 0.0f) {
+            F3 f;
+            const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f);
+            const float w = dpdf / (dpdf + bp) / dpdf;
+            dir = f3m(f.x * v.dir_l[0][i] * w, f.y * v.dir_l[1][i] * w, f.z * v.dir_l[2][i] * w);
+        }
+        r = {v.le[0][i], v.le[1][i], v.le[2][i]};
+        if (split[i] == d) {
+            const float ng_ = ngath[i];
+            const float kd = 1.0f / (ng_ + 1.0f), ki = ng_ > 0.0f ? 1.0f / ng_ : 0.0f;
+            r.x += (dir.x + acc_direct[i]) * kd + acc_ind[i] * ki;
+            r.y += (dir.y + acc_direct[n + i]) * kd + acc_ind[n + i] * ki;
+            r.z += (dir.z + acc_direct[2 * (size_t)n + i]) * kd + acc_ind[2 * (size_t)n + i] * ki;
+        } else {
+            r.x += dir.x;
+            r.y += dir.y;
+            r.z += dir.z;
+            const F3 wi = f3m(v.ind_wi[0][i], v.ind_wi[1][i], v.ind_wi[2][i]);
+            if (next && dot(wi, wi) != 0.0f) {
+                F3 f;
+                const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+                if (bp > 0.0f) {
+                    const float k = v.ind_mis[i] / bp;
+                    r.x += f.x * next[i] * k;
+                    r.y += f.y * next[n + i] * k;
+                    r.z += f.z * next[2 * (size_t)n + i] * k;
+                }
+            }
+        }
+        const uint32_t fl = v.flags[i];
+        if (stylize && !(fl & 1u)) {
+            const int32_t pi = m.style[style_index(fl)];
+            if (pi >= 0 && (uint32_t)pi < n_progs) r = style_apply(progs[pi], d, r);
+        }
+    }
+    out[i] = r.x;
+    out[n + i] = r.y;
+    out[2 * (size_t)n + i] = r.z;
+}
+__global__ void k_fg_splat(uint32_t npx, const int32_t *active0, const float *rad0, double weight, double *film) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npx || !active0[px]) return;
+    for (int c = 0; c < 3; c++) film[3 * (size_t)px + c] += weight * rad0[(size_t)c * npx + px];
+}
+
 }  // namespace
 }  // namespace sty
 
@@ -656,7 +858,7 @@ CamArgs make_camera(const sty_camera &cam) {
 // of one scene reuse them, so calls on one scene are serialised by the caller.
 enum CacheSlot {
     kVerts, kOuts, kPathState, kRng, kPrograms, kVertexCount, kRowCount, kRowIndex, kScanTmp,
-    kQueryIn, kQueryPred, kQueryScratch, kTargets, kRowsIn, kRowsTgt, kSlots
+    kQueryIn, kQueryPred, kQueryScratch, kTargets, kRowsIn, kRowsTgt, kFinalGather, kSlots
 };
 struct RenderCache {
     void *p[kSlots] = {};
@@ -691,6 +893,7 @@ struct TraceJob {
     std::vector<sty_pf_vertices> vin;
     PathState ps;
     float bmin[3], bmax[3];
+    float split_rough = 0.0f;  // > 0: stop paths at the first vertex rougher than this
     sty_status s = STY_OK;
 
     void *alloc(CacheSlot k, size_t bytes, const char *what) {
@@ -724,7 +927,7 @@ struct TraceJob {
         scene_bounds(scene, bmin, bmax);
         verts = (float *)alloc(kVerts, (size_t)D * kPlanes * n * 4, "alloc vertices");
         outs = (float *)alloc(kOuts, (size_t)D * 3 * n * 4, "alloc outputs");
-        psb = (float *)alloc(kPathState, (size_t)13 * n * 4, "alloc path state");
+        psb = (float *)alloc(kPathState, (size_t)14 * n * 4, "alloc path state");
         rng = (sty_pcg32 *)alloc(kRng, (size_t)n * sizeof(sty_pcg32), "alloc rng");
         dprog = (sty_style_program *)alloc(kPrograms, 64 * sizeof(sty_style_program), "alloc programs");
         vc = (unsigned long long *)alloc(kVertexCount, 8, "alloc counter");
@@ -782,6 +985,7 @@ struct TraceJob {
         ps.flags = (uint32_t *)pl();
         ps.exclude = (uint32_t *)pl();
         ps.terminated = (uint32_t *)pl();
+        ps.split = (uint32_t *)pl();
         k_rng_init<<<(n + 255) / 256, 256, 0, st>>>(n, seed, rng);
         return check_launch("k_rng_init");
     }
@@ -790,7 +994,7 @@ struct TraceJob {
         STY_TRY(check_cuda(cudaMemsetAsync(verts, 0, (size_t)D * kPlanes * n * 4, st), "reset vertices"));
         for (uint32_t d = 0; d < D; d++) {
             k_trace<<<(n + 255) / 256, 256, 0, st>>>(sv, ca, n, d, max_depth, ps, vo[d], vo[d > 0 ? d - 1 : 0], rng,
-                                                     dprog, n_programs, vc);
+                                                     dprog, n_programs, vc, split_rough);
             STY_TRY(check_launch("k_trace"));
         }
         return STY_OK;
@@ -1047,22 +1251,90 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         }
     }
     // ---- rendering
+    const int style0 = cfg->no_first_hit_stylization ? 0 : 1;
+    const int stylize_pred = cfg->learn_stylized_radiance ? 0 : 1;
     for (uint32_t r = 0; r < cfg->repeats; r++) {
         TraceJob job;
-        STY_TRY(job.init(scene, 1, 0, programs, n_programs, cfg->seed * 0x9e3779b97f4a7c15ull + 0x5bd1e995ull + r, st));
+        const uint64_t rseed = cfg->seed * 0x9e3779b97f4a7c15ull + 0x5bd1e995ull + r;
+        const uint32_t fg = cfg->final_gather;
+        if (fg) job.split_rough = 0.05f;  // denoising roughness above which a path splits (:372)
+        STY_TRY(job.init(scene, 1, fg ? D : 0, programs, n_programs, rseed, st));
         float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>((size_t)D * n, npx) * 11 * 4, "alloc query rows");
         float *qpred = (float *)job.alloc(kQueryPred, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc predictions");
         float *qscr = (float *)job.alloc(kQueryScratch, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc scratch");
         STY_TRY(job.s);
         STY_TRY(job.trace(st));
         const unsigned nb = (npx + 255) / 256;
-        k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, npx, job.vo[0], qin, qscr);
-        STY_TRY(check_launch("k_nrc_query_rows"));
-        STY_TRY(sty_nrc_inference(nrc, npx, qin, qpred, stream));
-        acc.inference_queries += npx;
-        k_nrc_splat_pred<<<nb, 256, 0, st>>>(npx, job.vo[0], qpred, job.sv.materials, job.dprog, n_programs,
-                                             cfg->no_first_hit_stylization, 1.0 / cfg->repeats, film);
-        STY_TRY(check_launch("k_nrc_splat_pred"));
+        if (!fg) {
+            // the cache at each pixel's first hit (kernel_inference_stage_gathering, depth 0)
+            k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, npx, job.vo[0], qin, qscr);
+            STY_TRY(check_launch("k_nrc_query_rows"));
+            STY_TRY(sty_nrc_inference(nrc, npx, qin, qpred, stream));
+            acc.inference_queries += npx;
+            k_nrc_splat_pred<<<nb, 256, 0, st>>>(npx, job.vo[0], qpred, job.sv.materials, job.dprog, n_programs,
+                                                 cfg->no_first_hit_stylization, 1.0 / cfg->repeats, film);
+            STY_TRY(check_launch("k_nrc_splat_pred"));
+            continue;
+        }
+        // final gathering: per-path planes of the split vertex, accumulators, gather scratch
+        constexpr size_t kFgPlanes = 28;  // split vertex 15, accumulators 7, gather scratch 6
+        float *fgb = (float *)job.alloc(kFinalGather, kFgPlanes * npx * 4, "alloc final gather");
+        STY_TRY(job.s);
+        SplitPlanes sp;
+        float *acc_direct, *acc_ind, *ngath, *thr, *gmis;
+        uint32_t *gmat, *gflags;
+        {
+            int k = 0;
+            auto pl = [&]() { return fgb + (size_t)(k++) * npx; };
+            for (int a = 0; a < 3; a++) sp.p[a] = pl();
+            for (int a = 0; a < 3; a++) sp.wo[a] = pl();
+            for (int a = 0; a < 3; a++) sp.ns[a] = pl();
+            for (int a = 0; a < 3; a++) sp.ng[a] = pl();
+            sp.material = (uint32_t *)pl();
+            sp.flags = (uint32_t *)pl();
+            sp.prim = (uint32_t *)pl();
+            acc_direct = pl();
+            pl();
+            pl();
+            acc_ind = pl();
+            pl();
+            pl();
+            ngath = pl();
+            thr = pl();
+            pl();
+            pl();
+            gmis = pl();
+            gmat = (uint32_t *)pl();
+            gflags = (uint32_t *)pl();
+            if ((size_t)k != kFgPlanes) {
+                set_error("final gather planes: %d carved, %zu allocated", k, kFgPlanes);
+                return STY_ERR_ARG;
+            }
+        }
+        STY_TRY(check_cuda(cudaMemsetAsync(acc_direct, 0, (size_t)7 * npx * 4, st), "zero gather accumulators"));
+        for (uint32_t d = 0; d <= D; d++) {
+            k_split_collect<<<nb, 256, 0, st>>>(npx, d, job.vo[d], job.ps.split, job.ps.exclude, sp);
+            STY_TRY(check_launch("k_split_collect"));
+        }
+        for (uint32_t it = 0; it < fg; it++) {
+            k_fg_step<<<nb, 256, 0, st>>>(job.sv, fa, npx, job.ps.split, sp, job.rng, job.dprog, n_programs, qin, thr, gmis,
+                                          gmat, gflags, acc_direct);
+            STY_TRY(check_launch("k_fg_step"));
+            STY_TRY(sty_nrc_inference(nrc, npx, qin, qpred, stream));
+            acc.inference_queries += npx;
+            k_fg_accumulate<<<nb, 256, 0, st>>>(job.sv, npx, job.ps.split, qpred, thr, gmis, gmat, gflags, job.dprog,
+                                                n_programs, stylize_pred, acc_ind, ngath);
+            STY_TRY(check_launch("k_fg_accumulate"));
+        }
+        for (int d = (int)D; d >= 0; d--) {
+            const int sty_d = stylize_pred && (d > 0 || style0);
+            k_fg_sweep<<<nb, 256, 0, st>>>(job.sv, npx, (uint32_t)d, job.vo[d], d < (int)D ? job.out(d + 1) : nullptr,
+                                           job.ps.split, acc_direct, acc_ind, ngath, job.dprog, n_programs, sty_d,
+                                           job.out(d));
+            STY_TRY(check_launch("k_fg_sweep"));
+        }
+        k_fg_splat<<<nb, 256, 0, st>>>(npx, job.vo[0].active, job.out(0), 1.0 / cfg->repeats, film);
+        STY_TRY(check_launch("k_fg_splat"));
     }
     STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync nrc render"));
     if (stats) *stats = acc;

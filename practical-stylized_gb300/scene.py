@@ -43,7 +43,8 @@ class RenderConfig(C.Structure):
 class NrcRenderConfig(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("training_iters", C.c_uint32), ("batches_per_iter", C.c_uint32),
                 ("training_paths", C.c_uint32), ("repeats", C.c_uint32), ("per_level_training", C.c_uint32),
-                ("no_first_hit_stylization", C.c_int32), ("learn_stylized_radiance", C.c_int32), ("seed", C.c_uint64)]
+                ("no_first_hit_stylization", C.c_int32), ("learn_stylized_radiance", C.c_int32),
+                ("final_gather", C.c_uint32), ("reserved", C.c_uint32), ("seed", C.c_uint64)]
 
 
 class NrcRenderStats(C.Structure):
@@ -53,11 +54,12 @@ class NrcRenderStats(C.Structure):
 
 def nrc_render_config(max_depth=5, training_iters=64, batches_per_iter=16, training_paths=0, repeats=1,
                       per_level_training=0, no_first_hit_stylization=False, learn_stylized_radiance=False,
-                      seed=0) -> NrcRenderConfig:
+                      final_gather=0, seed=0) -> NrcRenderConfig:
     c = NrcRenderConfig()
     c.max_depth, c.training_iters, c.batches_per_iter = max_depth, training_iters, batches_per_iter
     c.training_paths, c.repeats, c.per_level_training = training_paths, repeats, per_level_training
     c.no_first_hit_stylization, c.learn_stylized_radiance = int(no_first_hit_stylization), int(learn_stylized_radiance)
+    c.final_gather = final_gather
     c.seed = seed
     return c
 
