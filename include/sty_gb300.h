@@ -332,6 +332,33 @@ typedef struct sty_nrc_config {
 typedef struct sty_nrc sty_nrc;
 
 STY_API sty_status sty_nrc_create(const sty_nrc_config *config, sty_nrc **out);       /* akr_create_nrc */
+
+/* The reference's own NL-NRC network (akr_create_nrc with the tiny-cuda-nn JSON of nrc_pt.rs:
+ * 1159-1352): a Composite encoding of `input_dims` = 20 + max_depth inputs in the
+ * STY_NRC_ROWS_REF layout -- multiresolution hash grid on inputs 0..2 (`grid_levels` levels of
+ * `grid_features` features, tables of at most 2^log2_table entries, base resolution
+ * `base_resolution`, `per_level_scale` growth; the reference uses 22 x 4, 2^19, 16, 2.0),
+ * one-blob (`blob_bins` bins) on the next `blob_dims` inputs (7 / 4), identity on the rest -- and
+ * a ReLU MLP of `hidden_units` (128) x `hidden_layers` (5) without biases, linear output. BF16
+ * GEMM operands with FP32 accumulation, FP32 master parameters (MLP weights, then the tables),
+ * relative L2, Adam + exponential decay, EMA for inference. The handle works with every other
+ * sty_nrc_* call; param_count covers the tables. Table gradients are accumulated with atomics,
+ * so training on this network is not bit-deterministic. No counterpart of the encodings' exact
+ * numerics exists here (tiny-cuda-nn is not vendored): they follow the published definitions. */
+typedef struct sty_nrc_grid_config {
+    uint32_t input_dims, output_dims, batch_size;
+    uint32_t hidden_layers, hidden_units;
+    uint32_t grid_levels, grid_features, log2_table, base_resolution;
+    float per_level_scale;
+    uint32_t blob_dims, blob_bins;
+    float learning_rate, beta1, beta2, epsilon;
+    float ema_decay;
+    float decay_base;
+    uint32_t decay_interval;
+    uint32_t reserved;
+    uint64_t seed;
+} sty_nrc_grid_config;
+STY_API sty_status sty_nrc_create_grid(const sty_nrc_grid_config *config, sty_nrc **out);
 STY_API sty_status sty_nrc_destroy(sty_nrc *nrc);                                      /* akr_destroy_nrc */
 STY_API sty_status sty_nrc_param_count(sty_nrc *nrc, uint64_t *count);                 /* akr_nrc_param_count */
 /* FP32 master weights to / from a HOST array of param_count floats (akr_nrc_save/load_params);
@@ -447,8 +474,9 @@ STY_API sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t lay
                                    uint32_t max_depth, uint64_t seed, float *inputs, float *targets,
                                    uint64_t capacity, uint64_t *count_out, void *stream);
 
-/* The NL-NRC render (NRCPathTracer::render without final gathering, nrc_pt.rs:1519-1690) on the
- * scene and a cache created with sty_nrc_create (11 inputs: rows in STY_NRC_ROWS_SPHERICAL).
+/* The NL-NRC render (NRCPathTracer::render, nrc_pt.rs:1519-1690) on the scene and a cache made by
+ * sty_nrc_create with 11 inputs (rows in STY_NRC_ROWS_SPHERICAL) or by sty_nrc_create_grid with
+ * 20 + max_depth inputs (rows in STY_NRC_ROWS_REF, the reference's own network).
  * Training, `training_iters` times: `training_paths` paths (0: batches_per_iter x the cache's batch
  * size / (max_depth + 1), clamped to the pixel count, :1126-1128), each from a pixel drawn from its
  * own Pcg32 stream (:1394), traced to max_depth; the cache (training weights) predicts the

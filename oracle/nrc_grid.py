@@ -1,0 +1,107 @@
+"""FP64 numpy restatement of the composite input encoding of the reference's NL-NRC network -- TEST
+INFRASTRUCTURE ONLY.
+
+The reference configures tiny-cuda-nn (crates/akari_integrator/src/nrc_pt.rs:1315-1349) with a
+Composite encoding of its 20 + max_depth inputs: a multiresolution hash grid on the 3 position
+dims, a one-blob encoding of the next 7 dims (normal, direction, roughness) and the identity on the
+rest. tiny-cuda-nn (git submodule shiinamiyuki/tiny-cuda-nn, branch `ema`, no commit pinned) is not
+available, so the encodings are restated from their published definitions:
+
+  hash grid (Mueller, Evans, Schied, Keller 2022, "Instant Neural Graphics Primitives"): level l of
+    L has scale s_l = N_min * b^l - 1 and resolution r_l = ceil(s_l) + 1; x in [0, 1]^3 maps to
+    u = x * s_l + 0.5, cell c = floor(u), weights w = u - c (trilinear over the 8 corners). A level
+    whose r_l^3 entries fit its table (T_l = min(r_l^3 rounded up to a multiple of 8, 2^log2T))
+    indexes densely (c.x + c.y r_l + c.z r_l^2), else by the spatial hash
+    (c.x * 1 ^ c.y * 2654435761 ^ c.z * 805459861, in 32-bit arithmetic) mod T_l; dense indices
+    are taken mod T_l too (the corner past the last cell). Inputs are clamped to [0, 1]. F features
+    per entry.
+  one-blob (Mueller, McWilliams, Rousselle, Gross, Novak 2019, "Neural Importance Sampling"): a
+    Gaussian of standard deviation 1/B centred at x, discretised into B equal bins of [0, 1]: bin k
+    gets the kernel's mass over [k/B, (k+1)/B].
+  identity: the value itself.
+Output order: hash-grid features (level-major), one-blob bins (dim-major), identity dims, zero
+padding up to `out_width`.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+P1, P2 = 2654435761, 805459861
+
+
+def level_geometry(levels, log2_table, base_res, per_level_scale):
+    """Per level: (scale, resolution, table size, dense?) and the table offsets."""
+    geo, offs, off = [], [], 0
+    for l in range(levels):
+        scale = base_res * (per_level_scale ** l) - 1.0
+        res = int(math.ceil(scale)) + 1
+        full = res ** 3
+        size = min((full + 7) // 8 * 8, 1 << log2_table)
+        geo.append((scale, res, size, full <= size))
+        offs.append(off)
+        off += size
+    return geo, offs, off
+
+
+def corner_index(c, res, size, dense):
+    c = c.astype(np.uint64)
+    if dense:
+        return (c[..., 0] + c[..., 1] * np.uint64(res) + c[..., 2] * np.uint64(res * res)) % np.uint64(size)
+    h = (c[..., 0] * np.uint64(1)) ^ (c[..., 1] * np.uint64(P1)) ^ (c[..., 2] * np.uint64(P2))
+    return (h & np.uint64(0xFFFFFFFF)) % np.uint64(size)
+
+
+def grid_forward(x3, tables, levels, feats, log2_table, base_res, per_level_scale):
+    """x3 [n, 3] (clamped to [0, 1]); tables [total_entries, feats] -> features [n, levels * feats]."""
+    x3 = np.clip(x3, 0.0, 1.0)
+    geo, offs, _ = level_geometry(levels, log2_table, base_res, per_level_scale)
+    n = x3.shape[0]
+    out = np.zeros((n, levels * feats))
+    for l, (scale, res, size, dense) in enumerate(geo):
+        u = x3 * scale + 0.5
+        c0 = np.floor(u)
+        w = u - c0
+        for k in range(8):
+            o = np.array([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1], dtype=np.float64)
+            wt = np.prod(np.where(o == 1, w, 1.0 - w), axis=1)
+            idx = corner_index(c0 + o, res, size, dense).astype(np.int64) + offs[l]
+            out[:, l * feats:(l + 1) * feats] += wt[:, None] * tables[idx]
+    return out
+
+
+def grid_backward(x3, dfeat, levels, feats, log2_table, base_res, per_level_scale, total):
+    """Gradient of sum(dfeat * features) with respect to the tables."""
+    x3 = np.clip(x3, 0.0, 1.0)
+    geo, offs, _ = level_geometry(levels, log2_table, base_res, per_level_scale)
+    g = np.zeros((total, feats))
+    for l, (scale, res, size, dense) in enumerate(geo):
+        u = x3 * scale + 0.5
+        c0 = np.floor(u)
+        w = u - c0
+        for k in range(8):
+            o = np.array([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1], dtype=np.float64)
+            wt = np.prod(np.where(o == 1, w, 1.0 - w), axis=1)
+            idx = corner_index(c0 + o, res, size, dense).astype(np.int64) + offs[l]
+            np.add.at(g, idx, wt[:, None] * dfeat[:, l * feats:(l + 1) * feats])
+    return g
+
+
+def oneblob(x, bins):
+    """x [n, d] -> [n, d * bins]: Gaussian (sigma = 1 / bins) mass over each bin of [0, 1]."""
+    from scipy.special import erf
+    sig = 1.0 / bins
+    edges = np.arange(bins + 1) / bins
+    cdf = 0.5 * (1.0 + erf((edges[None, None, :] - x[:, :, None]) / (sig * math.sqrt(2.0))))
+    return (cdf[:, :, 1:] - cdf[:, :, :-1]).reshape(x.shape[0], -1)
+
+
+def encode(x, tables, levels, feats, log2_table, base_res, per_level_scale, blob_dims, bins, out_width):
+    g = grid_forward(x[:, :3], tables, levels, feats, log2_table, base_res, per_level_scale)
+    b = oneblob(x[:, 3:3 + blob_dims], bins)
+    ident = x[:, 3 + blob_dims:]
+    e = np.concatenate([g, b, ident], axis=1)
+    out = np.zeros((x.shape[0], out_width))
+    out[:, :e.shape[1]] = e
+    return out

@@ -270,6 +270,7 @@ struct sty_nrc {
     uint16_t *img = nullptr, *img_ema = nullptr;  // BF16 tensor-core images of w / ema
     float *bin = nullptr, *btg = nullptr, *bpred = nullptr, *acts = nullptr, *dpre = nullptr, *loss = nullptr;
     float *gpart = nullptr;  // per-chunk weight-gradient partials
+    GridModel *grid = nullptr;  // the composite-encoding network (sty_nrc_create_grid), else null
     uint32_t bcap = 0;
     uint64_t step = 0;  // optimiser steps taken (Adam t, EMA iteration)
     float lr = 0.0f;
@@ -295,9 +296,11 @@ sty_status ensure_batch(sty_nrc *nr, uint32_t B) {
     STY_TRY(check_cuda(cudaMalloc(&nr->bpred, (size_t)B * n.out_dims * 4), "alloc batch pred"));
     STY_TRY(check_cuda(cudaMalloc(&nr->acts, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc activations"));
     STY_TRY(check_cuda(cudaMalloc(&nr->dpre, (size_t)(n.layers + 1) * B * kNrcWidth * 4), "alloc gradients"));
-    size_t chunks = (B + kWgChunk - 1) / kWgChunk;
-    if (nr->cfg.precision == STY_NRC_BF16) chunks = std::max<size_t>(chunks, nrc_tc_train_ctas(B));
-    STY_TRY(check_cuda(cudaMalloc(&nr->gpart, chunks * nr->np * 4), "alloc gradient partials"));
+    if (!nr->grid) {  // the composite-encoding network computes its gradient without partials
+        size_t chunks = (B + kWgChunk - 1) / kWgChunk;
+        if (nr->cfg.precision == STY_NRC_BF16) chunks = std::max<size_t>(chunks, nrc_tc_train_ctas(B));
+        STY_TRY(check_cuda(cudaMalloc(&nr->gpart, chunks * nr->np * 4), "alloc gradient partials"));
+    }
     nr->bcap = B;
     return STY_OK;
 }
@@ -336,12 +339,17 @@ sty_status forward_batch(sty_nrc *nr, uint32_t B, const float *in, cudaStream_t 
 }
 
 bool tc_training(const sty_nrc *nr) {
-    return nr->cfg.precision == STY_NRC_BF16 && nr->net.layers <= kNrcTcTrainMaxLayers;
+    return !nr->grid && nr->cfg.precision == STY_NRC_BF16 && nr->net.layers <= kNrcTcTrainMaxLayers;
 }
 
 // Weight gradient of one batch into nr->g (loss added to nr->loss): the fused BF16 tensor-core
 // step for BF16 caches, else the FP32 forward / backward / weight-gradient kernels.
 sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float *target, cudaStream_t st) {
+    if (nr->grid) {
+        STY_TRY(grid_pack(nr->grid, nr->w, nullptr, st));
+        nr->img_dirty = true;
+        return grid_gradient(nr->grid, B, in, target, nr->w, nr->g, nr->loss, st);
+    }
     if (!tc_training(nr)) {
         STY_TRY(forward_batch(nr, B, in, st));
         return backward(nr, B, target, st);
@@ -355,6 +363,11 @@ sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float 
 }
 
 sty_status refresh_images(sty_nrc *nr, cudaStream_t st) {
+    if (nr->grid) {
+        if (nr->img_dirty) STY_TRY(grid_pack(nr->grid, nr->w, nr->ema, st));
+        nr->img_dirty = false;
+        return STY_OK;
+    }
     if (nr->cfg.precision != STY_NRC_BF16 || !nr->img_dirty) return STY_OK;
     STY_TRY(nrc_tc_pack(nr->net, nr->w, nr->img, st));
     STY_TRY(nrc_tc_pack(nr->net, nr->ema, nr->img_ema, st));
@@ -364,6 +377,10 @@ sty_status refresh_images(sty_nrc *nr, cudaStream_t st) {
 
 sty_status infer(sty_nrc *nr, bool ema, uint64_t count, const float *in, float *out, cudaStream_t st) {
     if (count == 0) return STY_OK;
+    if (nr->grid) {
+        STY_TRY(refresh_images(nr, st));
+        return grid_infer(nr->grid, ema, ema ? nr->ema : nr->w, count, in, out, st);
+    }
     if (nr->cfg.precision == STY_NRC_BF16) {
         STY_TRY(refresh_images(nr, st));
         return nrc_tc_forward(nr->net, ema ? nr->img_ema : nr->img, count, in, out, st);
@@ -372,6 +389,7 @@ sty_status infer(sty_nrc *nr, bool ema, uint64_t count, const float *in, float *
 }
 
 void free_nrc(sty_nrc *nr) {
+    grid_destroy(nr->grid);
     void *ptrs[] = {nr->w, nr->m, nr->v, nr->g, nr->ema, nr->img, nr->img_ema, nr->bin,
                     nr->btg, nr->bpred, nr->acts, nr->dpre, nr->loss, nr->gpart};
     for (void *p : ptrs)
@@ -427,6 +445,62 @@ sty_status sty_nrc_create(const sty_nrc_config *cfg, sty_nrc **out) {
     if (s == STY_OK) s = check_cuda(cudaMemset(nr->m, 0, nr->np * 4), "zero m");
     if (s == STY_OK) s = check_cuda(cudaMemset(nr->v, 0, nr->np * 4), "zero v");
     if (s == STY_OK) s = check_cuda(cudaDeviceSynchronize(), "sty_nrc_create");
+    if (s != STY_OK) {
+        free_nrc(nr);
+        return s;
+    }
+    *out = nr;
+    return STY_OK;
+}
+
+sty_status sty_nrc_create_grid(const sty_nrc_grid_config *gc, sty_nrc **out) {
+    clear_error();
+    STY_ARG_CHECK(gc && out, "sty_nrc_create_grid: null argument");
+    STY_ARG_CHECK(gc->batch_size >= 128 && gc->batch_size % 128 == 0, "batch_size must be a multiple of 128");
+    STY_ARG_CHECK(gc->decay_interval > 0 && gc->learning_rate > 0.0f, "decay_interval and learning_rate must be > 0");
+    sty_nrc *nr = new sty_nrc();
+    size_t np = 0, n_mlp = 0;
+    sty_status s = grid_create(gc, &nr->grid, &np, &n_mlp);
+    if (s != STY_OK) {
+        delete nr;
+        return s;
+    }
+    // the fields the shared training loop reads (batch sampling, Adam, decay, EMA)
+    sty_nrc_config &c = nr->cfg;
+    std::memset(&c, 0, sizeof(c));
+    c.input_dims = gc->input_dims;
+    c.output_dims = gc->output_dims;
+    c.batch_size = gc->batch_size;
+    c.hidden_layers = gc->hidden_layers;
+    c.precision = STY_NRC_BF16;
+    c.learning_rate = gc->learning_rate;
+    c.beta1 = gc->beta1;
+    c.beta2 = gc->beta2;
+    c.epsilon = gc->epsilon;
+    c.ema_decay = gc->ema_decay;
+    c.decay_base = gc->decay_base;
+    c.decay_interval = gc->decay_interval;
+    c.seed = gc->seed;
+    nr->net.in_dims = (int)gc->input_dims;
+    nr->net.out_dims = (int)gc->output_dims;
+    nr->net.layers = 1;
+    nr->np = np;
+    nr->lr = gc->learning_rate;
+    auto alloc = [&](void **p, size_t bytes, const char *what) {
+        if (s == STY_OK) s = check_cuda(cudaMalloc(p, bytes), what);
+    };
+    alloc((void **)&nr->w, np * 4, "alloc parameters");
+    alloc((void **)&nr->m, np * 4, "alloc adam m");
+    alloc((void **)&nr->v, np * 4, "alloc adam v");
+    alloc((void **)&nr->g, np * 4, "alloc grad");
+    alloc((void **)&nr->ema, np * 4, "alloc ema");
+    alloc((void **)&nr->loss, 4, "alloc loss");
+    if (s == STY_OK) s = ensure_batch(nr, gc->batch_size);
+    if (s == STY_OK) s = grid_init_params(nr->grid, gc->seed, nr->w, nullptr);
+    if (s == STY_OK) s = check_cuda(cudaMemcpy(nr->ema, nr->w, np * 4, cudaMemcpyDeviceToDevice), "init ema");
+    if (s == STY_OK) s = check_cuda(cudaMemset(nr->m, 0, np * 4), "zero m");
+    if (s == STY_OK) s = check_cuda(cudaMemset(nr->v, 0, np * 4), "zero v");
+    if (s == STY_OK) s = check_cuda(cudaDeviceSynchronize(), "sty_nrc_create_grid");
     if (s != STY_OK) {
         free_nrc(nr);
         return s;

@@ -55,4 +55,15 @@ uint32_t nrc_tc_train_ctas(uint32_t B);
 sty_status nrc_tc_train(const NrcNet &n, const uint16_t *w_img, uint32_t B, const float *input, const float *target,
                         float *part, size_t np, float *loss, uint32_t ctas, cudaStream_t st);
 
+// The reference's composite-encoding network (nrc_grid.cu)
+struct GridModel;
+sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_params, size_t *n_mlp);
+void grid_destroy(GridModel *g);
+sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t st);
+sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_t st);
+sty_status grid_infer(GridModel *g, bool ema, const float *params, uint64_t count, const float *in, float *out,
+                      cudaStream_t st);
+sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, const float *params,
+                         float *grad, float *loss, cudaStream_t st);
+
 }  // namespace sty

@@ -580,14 +580,15 @@ __global__ void k_nrc_train_rows(SceneView sc, FeatArgs fa, uint32_t n, uint32_t
 __global__ void k_advance_rows(uint32_t n, const uint32_t *idx, const int32_t *active, unsigned long long *base) {
     *base += (unsigned long long)idx[n - 1] + (active[n - 1] ? 1u : 0u);
 }
-__global__ void k_nrc_query_rows(SceneView sc, FeatArgs fa, uint32_t n, VertOut v, float *inputs, float *targets) {
+__global__ void k_nrc_query_rows(SceneView sc, FeatArgs fa, uint32_t n, VertOut v, float *inputs, float *targets,
+                                 uint32_t depth = 0) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float *row = inputs + (size_t)i * fa.dims;
     float le[3] = {0.0f, 0.0f, 0.0f};
     if (v.active[i]) {
         write_features(sc, fa, f3m(v.p[0][i], v.p[1][i], v.p[2][i]), f3m(v.wo[0][i], v.wo[1][i], v.wo[2][i]),
-                       f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), v.material[i], v.flags[i], 0, row);
+                       f3m(v.ns[0][i], v.ns[1][i], v.ns[2][i]), v.material[i], v.flags[i], depth, row);
         le[0] = v.le[0][i];
         le[1] = v.le[1][i];
         le[2] = v.le[2][i];
@@ -1157,7 +1158,9 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
                   "bad max_depth / repeats / batches_per_iter");
     STY_ARG_CHECK(programs || n_programs == 0, "null programs");
     STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
-    STY_ARG_CHECK(nrc_input_dims(nrc) == 11, "the cache must take the 11-input rows (STY_NRC_ROWS_SPHERICAL)");
+    const uint32_t in_dims = nrc_input_dims(nrc);
+    STY_ARG_CHECK(in_dims == 11 || in_dims == 20 + cfg->max_depth,
+                  "the cache must take 11-input rows (STY_NRC_ROWS_SPHERICAL) or 20 + max_depth (STY_NRC_ROWS_REF)");
     cudaStream_t st = as_stream(stream);
     const sty_camera &cam = scene_camera(scene);
     const uint32_t npx = cam.width * cam.height, D = cfg->max_depth;
@@ -1177,8 +1180,8 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
             fa.bext[a] = std::max(bmax[a] - bmin[a], 1e-6f);
         }
         fa.max_depth = D;
-        fa.layout = STY_NRC_ROWS_SPHERICAL;
-        fa.dims = 11;
+        fa.layout = in_dims == 11 ? STY_NRC_ROWS_SPHERICAL : STY_NRC_ROWS_REF;
+        fa.dims = in_dims;
     }
     // ---- training
     for (uint32_t it = 0; it < cfg->training_iters; it++) {
@@ -1187,11 +1190,11 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         job.ca.random_px = 1;
         RenderCache &rc = *job.cache;
         const size_t rows = (size_t)D * n;
-        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>(rows, npx) * 11 * 4, "alloc query rows");
+        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>(rows, npx) * fa.dims * 4, "alloc query rows");
         float *qpred = (float *)job.alloc(kQueryPred, std::max<size_t>(rows, npx) * 3 * 4, "alloc predictions");
         float *qscr = (float *)job.alloc(kQueryScratch, std::max<size_t>(rows, npx) * 3 * 4, "alloc query scratch");
         float *tgt = (float *)job.alloc(kTargets, (size_t)(D + 1) * 3 * n * 4, "alloc targets");
-        float *rin = (float *)job.alloc(kRowsIn, (size_t)(D + 1) * n * 11 * 4, "alloc training rows");
+        float *rin = (float *)job.alloc(kRowsIn, (size_t)(D + 1) * n * fa.dims * 4, "alloc training rows");
         float *rtg = (float *)job.alloc(kRowsTgt, (size_t)(D + 1) * n * 3 * 4, "alloc training targets");
         unsigned long long *cnt = (unsigned long long *)job.alloc(kRowCount, 8, "alloc row counter");
         uint32_t *idx = (uint32_t *)job.alloc(kRowIndex, (size_t)n * 4, "alloc row index");
@@ -1201,8 +1204,8 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         const unsigned nb = (n + 255) / 256;
         // predictions (training weights) at depths 1..D
         for (uint32_t d = 1; d <= D; d++) {
-            k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, n, job.vo[d], qin + (size_t)(d - 1) * n * 11,
-                                                 qscr + (size_t)(d - 1) * n * 3);
+            k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, n, job.vo[d], qin + (size_t)(d - 1) * n * fa.dims,
+                                                 qscr + (size_t)(d - 1) * n * 3, d);
             STY_TRY(check_launch("k_nrc_query_rows"));
         }
         STY_TRY(sty_nrc_train_inference(nrc, rows, qin, qpred, stream));
@@ -1259,7 +1262,7 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         const uint32_t fg = cfg->final_gather;
         if (fg) job.split_rough = 0.05f;  // denoising roughness above which a path splits (:372)
         STY_TRY(job.init(scene, 1, fg ? D : 0, programs, n_programs, rseed, st));
-        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>((size_t)D * n, npx) * 11 * 4, "alloc query rows");
+        float *qin = (float *)job.alloc(kQueryIn, std::max<size_t>((size_t)D * n, npx) * fa.dims * 4, "alloc query rows");
         float *qpred = (float *)job.alloc(kQueryPred, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc predictions");
         float *qscr = (float *)job.alloc(kQueryScratch, std::max<size_t>((size_t)D * n, npx) * 3 * 4, "alloc scratch");
         STY_TRY(job.s);

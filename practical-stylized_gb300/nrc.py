@@ -40,6 +40,33 @@ def config(freqs=C4_FREQS, output_dims=3, batch_size=1 << 16, hidden_layers=5, p
     return c
 
 
+class NrcGridConfig(C.Structure):
+    _fields_ = [("input_dims", C.c_uint32), ("output_dims", C.c_uint32), ("batch_size", C.c_uint32),
+                ("hidden_layers", C.c_uint32), ("hidden_units", C.c_uint32), ("grid_levels", C.c_uint32),
+                ("grid_features", C.c_uint32), ("log2_table", C.c_uint32), ("base_resolution", C.c_uint32),
+                ("per_level_scale", C.c_float), ("blob_dims", C.c_uint32), ("blob_bins", C.c_uint32),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("ema_decay", C.c_float), ("decay_base", C.c_float), ("decay_interval", C.c_uint32),
+                ("reserved", C.c_uint32), ("seed", C.c_uint64)]
+
+
+def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5, hidden_units=128, grid_levels=22,
+                grid_features=4, log2_table=19, base_resolution=16, per_level_scale=2.0, blob_dims=7, blob_bins=4,
+                learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8, ema_decay=0.95, decay_base=1.0,
+                decay_interval=100, seed=1337) -> NrcGridConfig:
+    """The reference's NL-NRC network (nrc_pt.rs:1159-1352; defaults of configs/teaser/nl-nrc.json):
+    rows of 20 + max_depth inputs in the reference layout."""
+    c = NrcGridConfig()
+    c.input_dims, c.output_dims, c.batch_size = 20 + max_depth, output_dims, batch_size
+    c.hidden_layers, c.hidden_units = hidden_layers, hidden_units
+    c.grid_levels, c.grid_features, c.log2_table = grid_levels, grid_features, log2_table
+    c.base_resolution, c.per_level_scale = base_resolution, per_level_scale
+    c.blob_dims, c.blob_bins = blob_dims, blob_bins
+    c.learning_rate, c.beta1, c.beta2, c.epsilon = learning_rate, beta1, beta2, epsilon
+    c.ema_decay, c.decay_base, c.decay_interval, c.seed = ema_decay, decay_base, decay_interval, seed
+    return c
+
+
 def _sp(stream):
     from .pf import _stream_ptr
     return _stream_ptr(stream)
@@ -49,10 +76,13 @@ class NRC:
     """Mirror of TinyCudaNRC: train / inference / train_inference on device matrices (torch
     tensors, sample-major rows)."""
 
-    def __init__(self, cfg: NrcConfig):
+    def __init__(self, cfg):
         self.cfg = cfg
         self.h = C.c_void_p()
-        check(lib().sty_nrc_create(C.byref(cfg), C.byref(self.h)))
+        if isinstance(cfg, NrcGridConfig):
+            check(lib().sty_nrc_create_grid(C.byref(cfg), C.byref(self.h)))
+        else:
+            check(lib().sty_nrc_create(C.byref(cfg), C.byref(self.h)))
 
     def close(self):
         if self.h:

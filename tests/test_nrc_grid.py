@@ -1,0 +1,207 @@
+"""The reference's NL-NRC network (sty_nrc_create_grid): composite encoding (hash grid + one-blob +
+identity) and a ReLU MLP, against the FP64 oracle (oracle/nrc_grid.py + a BF16 emulation of the
+GEMM operands).
+
+Tolerances: GPU grid features accumulate in FP32 and are rounded to BF16 like every GEMM operand,
+so outputs are compared to the emulation statistically (98 % within 2e-3 of the output scale, all
+within 3e-2); gradients in norm (MLP 1e-2, tables 2e-2 relative)."""
+import numpy as np
+import pytest
+
+import oracle.nrc as onrc
+import oracle.nrc_grid as og
+
+# a small network with dense and hashed levels
+SMALL = dict(max_depth=5, hidden_layers=2, hidden_units=32, grid_levels=6, grid_features=2, log2_table=12,
+             base_resolution=4, per_level_scale=2.0, blob_dims=7, blob_bins=4)
+
+
+def _geo(c):
+    return og.level_geometry(c["grid_levels"], c["log2_table"], c["base_resolution"], c["per_level_scale"])
+
+
+def test_oracle_geometry_teaser():
+    geo, offs, total = og.level_geometry(22, 19, 16, 2.0)
+    assert [g[3] for g in geo[:4]] == [True, True, True, False]
+    assert [g[2] for g in geo[:4]] == [16 ** 3, 32 ** 3, 64 ** 3, 1 << 19]
+    assert total == 16 ** 3 + 32 ** 3 + 64 ** 3 + 19 * (1 << 19)
+
+
+def test_oracle_grid_backward_is_the_gradient():
+    c = SMALL
+    _, _, total = _geo(c)
+    rng = np.random.default_rng(0)
+    x = rng.random((40, 3))
+    t = rng.uniform(-1, 1, (total, c["grid_features"]))
+    d = rng.normal(size=(40, c["grid_levels"] * c["grid_features"]))
+    args = (c["grid_levels"], c["grid_features"], c["log2_table"], c["base_resolution"], c["per_level_scale"])
+    g = og.grid_backward(x, d, *args, total)
+    f0 = float((og.grid_forward(x, t, *args) * d).sum())
+    for idx in rng.choice(np.flatnonzero(np.abs(g).sum(1)), 10, replace=False):
+        e = np.zeros_like(t)
+        e[idx, 1] = 1.0
+        f1 = float((og.grid_forward(x, t + e, *args) * d).sum())  # the features are linear in the tables
+        assert f1 - f0 == pytest.approx(g[idx, 1], rel=1e-9, abs=1e-12)
+
+
+def test_oracle_oneblob():
+    b = og.oneblob(np.array([[0.5, 0.3, 0.0]]), 4).reshape(3, 4)
+    assert b[0].sum() == pytest.approx(0.9545, abs=1e-3)  # +-2 sigma inside [0, 1]
+    assert b[0][1] == pytest.approx(b[0][2]) and b[0][0] == pytest.approx(b[0][3])
+    assert b[2][0] > b[2][1] > b[2][2]
+
+
+def _net(sty, seed=3, batch=1024, **kw):
+    c = dict(SMALL)
+    c.update(kw)
+    return sty.nrc.NRC(sty.nrc.grid_config(batch_size=batch, seed=seed, **c)), c
+
+
+def _split(p, c):
+    """MLP weights (list of [out, in] matrices) and tables from the flat parameters."""
+    E = c["grid_levels"] * c["grid_features"] + c["blob_dims"] * c["blob_bins"] + (20 + c["max_depth"] - 3 - c["blob_dims"])
+    Ep = (E + 15) // 16 * 16
+    H, L = c["hidden_units"], c["hidden_layers"]
+    mats, o = [], 0
+    for l in range(L):
+        k = Ep if l == 0 else H
+        mats.append(p[o:o + H * k].reshape(H, k))
+        o += H * k
+    mats.append(p[o:o + 3 * H].reshape(3, H))
+    o += 3 * H
+    return mats, p[o:].reshape(-1, c["grid_features"]), Ep
+
+
+def _emulate(p, c, x):
+    mats, tables, Ep = _split(p.astype(np.float64), c)
+    enc = og.encode(x, tables, c["grid_levels"], c["grid_features"], c["log2_table"], c["base_resolution"],
+                    c["per_level_scale"], c["blob_dims"], c["blob_bins"], Ep)
+    mb = [onrc.bf16_round(m) for m in mats]
+    acts = [onrc.bf16_round(enc)]
+    h = acts[0]
+    for l in range(c["hidden_layers"]):
+        h = onrc.bf16_round(np.maximum(h @ mb[l].T, 0.0))
+        acts.append(h)
+    return h @ mb[-1].T, acts, mb, enc
+
+
+def _rows(rng, n, c):
+    x = rng.random((n, 20 + c["max_depth"]))
+    x[:, 10:] = (x[:, 10:] > 0.5)  # one-hot-like flag / depth columns
+    return x
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()
+
+
+@pytest.mark.gpu
+def test_grid_inference_matches_emulation(sty, cuda):
+    net, c = _net(sty)
+    p = net.save_params().astype(np.float64)
+    # spread the tables so the encoding matters
+    mats, tables, _ = _split(p, c)
+    rng = np.random.default_rng(1)
+    p[len(p) - tables.size:] = rng.uniform(-0.5, 0.5, tables.size)
+    net.load_params(p.astype(np.float32))
+    p = p.astype(np.float32).astype(np.float64)
+    x = _rows(rng, 3000, c)
+    out = net.inference(_dev(x)).cpu().numpy()
+    ref, _, _, _ = _emulate(p, c, x)
+    scale = np.abs(ref).max()
+    err = np.abs(out - ref)
+    assert np.isfinite(out).all()
+    assert np.mean(err <= 2e-3 * scale) >= 0.98, np.mean(err > 2e-3 * scale)
+    assert err.max() <= 3e-2 * scale
+    assert sty.abi.device_status() == 0
+
+
+@pytest.mark.gpu
+def test_grid_gradient_matches_emulation(sty, cuda):
+    net, c = _net(sty, seed=5)
+    p = net.save_params().astype(np.float64)
+    rng = np.random.default_rng(2)
+    mats, tables, Ep = _split(p, c)
+    p[len(p) - tables.size:] = rng.uniform(-0.5, 0.5, tables.size)
+    net.load_params(p.astype(np.float32))
+    p = p.astype(np.float32).astype(np.float64)
+    B = 512
+    x = _rows(rng, B, c)
+    t = rng.random((B, 3)) + 0.1
+    g, loss = net.gradient(_dev(x), _dev(t))
+    g = g.cpu().numpy().astype(np.float64)
+    # emulated backward: BF16 loss gradient and layer gradients, FP32-like sums in FP64
+    pred, acts, mb, enc = _emulate(p, c, x)
+    den = pred * pred + 0.01
+    gp = onrc.bf16_round(2.0 * (pred - t) / den / (B * 3))
+    grads = [None] * (c["hidden_layers"] + 1)
+    grads[-1] = gp.T @ acts[-1]
+    dh = gp @ mb[-1]
+    for l in range(c["hidden_layers"] - 1, -1, -1):
+        dp = onrc.bf16_round(dh * (acts[l + 1] > 0))
+        grads[l] = dp.T @ acts[l]
+        dh = dp @ mb[l]
+    ng = c["grid_levels"] * c["grid_features"]
+    _, _, total = _geo(c)
+    gt = og.grid_backward(x[:, :3], dh[:, :ng], c["grid_levels"], c["grid_features"], c["log2_table"],
+                          c["base_resolution"], c["per_level_scale"], total)
+    ref_mlp = np.concatenate([m.reshape(-1) for m in grads])
+    n_mlp = ref_mlp.size
+    assert np.linalg.norm(g[:n_mlp] - ref_mlp) <= 1e-2 * np.linalg.norm(ref_mlp)
+    assert np.linalg.norm(g[n_mlp:] - gt.reshape(-1)) <= 2e-2 * np.linalg.norm(gt)
+    assert loss == pytest.approx(float(((pred - t) ** 2 / den).mean()), rel=1e-2)
+
+
+@pytest.mark.gpu
+def test_grid_training_reduces_loss(sty, cuda):
+    net, c = _net(sty, seed=7, batch=4096, learning_rate=1e-2)
+    rng = np.random.default_rng(4)
+    x = _rows(rng, 1 << 15, c)
+    tgt = np.stack([0.5 + 0.4 * np.sin(4 * x[:, 0] + 3 * x[:, 1]), 0.3 + 0.3 * x[:, 2] * x[:, 4],
+                    0.2 + 0.2 * np.cos(5 * x[:, 1]) + 0.1 * x[:, 12]], 1)
+    xd, td = _dev(x), _dev(tgt)
+    first = net.train(xd, td, 1)
+    for _ in range(6):
+        last = net.train(xd, td, 50)
+    assert last < 0.1 * first, (first, last)
+
+
+@pytest.mark.gpu
+def test_grid_teaser_network(sty, cuda):
+    """The teaser's configuration (configs/teaser/nl-nrc.json): 22 x 4 hash grid on 2^19-entry
+    tables, 5 x 128 MLP, max depth 12 (32 inputs), batch 2^16."""
+    net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=12, seed=11))
+    assert net.param_count() == 144 * 128 + 4 * 128 * 128 + 3 * 128 + 4 * (16 ** 3 + 32 ** 3 + 64 ** 3 + 19 * (1 << 19))
+    rng = np.random.default_rng(6)
+    x = _dev(_rows(rng, 1 << 17, dict(max_depth=12)))
+    t = _dev(rng.random((1 << 17, 3)))
+    l0 = net.train(x, t, 2)
+    y = net.inference(x).cpu().numpy()
+    assert np.isfinite(l0) and np.isfinite(y).all()
+    assert sty.abi.device_status() == 0
+    net.close()
+
+
+@pytest.mark.gpu
+def test_grid_network_in_the_nrc_render(sty, cuda):
+    """The reference's network inside the NL-NRC loop (rows in the reference layout): the cache
+    render of the Cornell box beats the 1-spp cache-free render against a 2048-spp render."""
+    W = H = 32
+    D = 4
+    pos, mids, mats, cam = sty.scene.cornell_box(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    so = lambda seed, b, r=1: sty.scene.render_config(max_depth=D, branch=b, repeats=r, radius_scale=(1e-4,),  # noqa: E731
+                                                       reuse=(8,), smis=False, seed=seed)
+    gt = sc.render(so(4242, 256, 8))[0].cpu().numpy()
+    mse_pt = np.mean([np.mean((sc.render(so(10 + s, 1))[0].cpu().numpy() - gt) ** 2) for s in range(4)])
+    net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=D, batch_size=1 << 12, hidden_units=64, grid_levels=8,
+                                          grid_features=2, log2_table=16, learning_rate=1e-2, seed=2))
+    film, st = sc.nrc_render(net, sty.scene.nrc_render_config(max_depth=D, training_iters=200, batches_per_iter=4,
+                                                               repeats=4, seed=7))
+    img = film.cpu().numpy()
+    mse = float(np.mean((img - gt) ** 2))
+    print(f"grid-network nrc render mse {mse:.5f} vs 1spp {mse_pt:.5f}")
+    assert np.isfinite(img).all() and st.training_rows > 0
+    assert mse < 0.5 * mse_pt
+    net.close()
