@@ -344,7 +344,14 @@ STY_API sty_status sty_nrc_create(const sty_nrc_config *config, sty_nrc **out); 
  * relative L2, Adam + exponential decay, EMA for inference. The handle works with every other
  * sty_nrc_* call; param_count covers the tables. Table gradients are accumulated with atomics,
  * so training on this network is not bit-deterministic. No counterpart of the encodings' exact
- * numerics exists here (tiny-cuda-nn is not vendored): they follow the published definitions. */
+ * numerics exists here (tiny-cuda-nn is not vendored): they follow the published definitions.
+ * The forward reads FP16 copies of the tables (as tiny-cuda-nn's half-precision forward does).
+ * Inference runs on the tensor cores in two launches per chunk -- the encoding written as 128-row
+ * MMA operand tiles, then one kernel running every layer on chip -- when hidden_units is 32, 64 or
+ * 128, the encoded width is at most 160 and the weights fit in shared memory (the reference's
+ * 144 -> 128 x 5 -> 3 network does); otherwise, or with STY_NRC_GRID_LAYERED in `flags`, it runs
+ * the layer-by-layer path (one BF16 GEMM per layer). */
+#define STY_NRC_GRID_LAYERED 1u
 typedef struct sty_nrc_grid_config {
     uint32_t input_dims, output_dims, batch_size;
     uint32_t hidden_layers, hidden_units;
@@ -355,7 +362,7 @@ typedef struct sty_nrc_grid_config {
     float ema_decay;
     float decay_base;
     uint32_t decay_interval;
-    uint32_t reserved;
+    uint32_t flags;        /* STY_NRC_GRID_* bits */
     uint64_t seed;
 } sty_nrc_grid_config;
 STY_API sty_status sty_nrc_create_grid(const sty_nrc_grid_config *config, sty_nrc **out);

@@ -9,7 +9,10 @@ available, so the encodings are restated from their published definitions:
 
   hash grid (Mueller, Evans, Schied, Keller 2022, "Instant Neural Graphics Primitives"): level l of
     L has scale s_l = N_min * b^l - 1 and resolution r_l = ceil(s_l) + 1; x in [0, 1]^3 maps to
-    u = x * s_l + 0.5, cell c = floor(u), weights w = u - c (trilinear over the 8 corners). A level
+    u = x * s_l + 0.5, cell c = floor(u), weights w = u - c (trilinear over the 8 corners). As in
+    tiny-cuda-nn the cell arithmetic is FP32: s_l = exp2(l log2 b) N_min - 1 in FP32, r_l from that
+    FP32 value, u = fma(x, s_l, 0.5) rounded once to FP32 (at the finest levels of deep grids s_l
+    exceeds 2^24, so the FP32 cell differs from the exact one); the interpolation itself is FP64. A level
     whose r_l^3 entries fit its table (T_l = min(r_l^3 rounded up to a multiple of 8, 2^log2T))
     indexes densely (c.x + c.y r_l + c.z r_l^2), else by the spatial hash
     (c.x * 1 ^ c.y * 2654435761 ^ c.z * 805459861, in 32-bit arithmetic) mod T_l; dense indices
@@ -31,11 +34,17 @@ import numpy as np
 P1, P2 = 2654435761, 805459861
 
 
+def level_scale(l, base_res, per_level_scale):
+    """s_l as the FP32 evaluation exp2(l * log2(b)) * N_min - 1 (exact for b = 2)."""
+    f = np.float32
+    return float(f(f(np.exp2(f(l) * f(np.log2(f(per_level_scale))))) * f(base_res)) - f(1.0))
+
+
 def level_geometry(levels, log2_table, base_res, per_level_scale):
     """Per level: (scale, resolution, table size, dense?) and the table offsets."""
     geo, offs, off = [], [], 0
     for l in range(levels):
-        scale = base_res * (per_level_scale ** l) - 1.0
+        scale = level_scale(l, base_res, per_level_scale)
         res = int(math.ceil(scale)) + 1
         full = res ** 3
         size = min((full + 7) // 8 * 8, 1 << log2_table)
@@ -53,16 +62,21 @@ def corner_index(c, res, size, dense):
     return (h & np.uint64(0xFFFFFFFF)) % np.uint64(size)
 
 
+def cells(x3, scale):
+    """Cell corner and FP32 fractional weights of positions x3 at one level's scale."""
+    x32 = np.clip(np.asarray(x3, dtype=np.float32), np.float32(0.0), np.float32(1.0))
+    u = (x32.astype(np.float64) * scale + 0.5).astype(np.float32)  # exact product + 0.5, one rounding
+    c0 = np.floor(u)
+    return c0.astype(np.float64), (u - c0).astype(np.float64)
+
+
 def grid_forward(x3, tables, levels, feats, log2_table, base_res, per_level_scale):
     """x3 [n, 3] (clamped to [0, 1]); tables [total_entries, feats] -> features [n, levels * feats]."""
-    x3 = np.clip(x3, 0.0, 1.0)
     geo, offs, _ = level_geometry(levels, log2_table, base_res, per_level_scale)
     n = x3.shape[0]
     out = np.zeros((n, levels * feats))
     for l, (scale, res, size, dense) in enumerate(geo):
-        u = x3 * scale + 0.5
-        c0 = np.floor(u)
-        w = u - c0
+        c0, w = cells(x3, scale)
         for k in range(8):
             o = np.array([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1], dtype=np.float64)
             wt = np.prod(np.where(o == 1, w, 1.0 - w), axis=1)
@@ -73,13 +87,10 @@ def grid_forward(x3, tables, levels, feats, log2_table, base_res, per_level_scal
 
 def grid_backward(x3, dfeat, levels, feats, log2_table, base_res, per_level_scale, total):
     """Gradient of sum(dfeat * features) with respect to the tables."""
-    x3 = np.clip(x3, 0.0, 1.0)
     geo, offs, _ = level_geometry(levels, log2_table, base_res, per_level_scale)
     g = np.zeros((total, feats))
     for l, (scale, res, size, dense) in enumerate(geo):
-        u = x3 * scale + 0.5
-        c0 = np.floor(u)
-        w = u - c0
+        c0, w = cells(x3, scale)
         for k in range(8):
             o = np.array([(k >> 0) & 1, (k >> 1) & 1, (k >> 2) & 1], dtype=np.float64)
             wt = np.prod(np.where(o == 1, w, 1.0 - w), axis=1)

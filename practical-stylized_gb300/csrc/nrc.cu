@@ -271,6 +271,7 @@ struct sty_nrc {
     float *bin = nullptr, *btg = nullptr, *bpred = nullptr, *acts = nullptr, *dpre = nullptr, *loss = nullptr;
     float *gpart = nullptr;  // per-chunk weight-gradient partials
     GridModel *grid = nullptr;  // the composite-encoding network (sty_nrc_create_grid), else null
+    bool layered = false;       // grid network: STY_NRC_GRID_LAYERED (no tensor-core inference)
     uint32_t bcap = 0;
     uint64_t step = 0;  // optimiser steps taken (Adam t, EMA iteration)
     float lr = 0.0f;
@@ -348,7 +349,7 @@ sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float 
     if (nr->grid) {
         STY_TRY(grid_pack(nr->grid, nr->w, nullptr, st));
         nr->img_dirty = true;
-        return grid_gradient(nr->grid, B, in, target, nr->w, nr->g, nr->loss, st);
+        return grid_gradient(nr->grid, B, in, target, nr->g, nr->loss, st);
     }
     if (!tc_training(nr)) {
         STY_TRY(forward_batch(nr, B, in, st));
@@ -379,7 +380,7 @@ sty_status infer(sty_nrc *nr, bool ema, uint64_t count, const float *in, float *
     if (count == 0) return STY_OK;
     if (nr->grid) {
         STY_TRY(refresh_images(nr, st));
-        return grid_infer(nr->grid, ema, ema ? nr->ema : nr->w, count, in, out, st);
+        return grid_infer(nr->grid, ema, !nr->layered, count, in, out, st);
     }
     if (nr->cfg.precision == STY_NRC_BF16) {
         STY_TRY(refresh_images(nr, st));
@@ -458,7 +459,9 @@ sty_status sty_nrc_create_grid(const sty_nrc_grid_config *gc, sty_nrc **out) {
     STY_ARG_CHECK(gc && out, "sty_nrc_create_grid: null argument");
     STY_ARG_CHECK(gc->batch_size >= 128 && gc->batch_size % 128 == 0, "batch_size must be a multiple of 128");
     STY_ARG_CHECK(gc->decay_interval > 0 && gc->learning_rate > 0.0f, "decay_interval and learning_rate must be > 0");
+    STY_ARG_CHECK((gc->flags & ~STY_NRC_GRID_LAYERED) == 0, "unknown flags 0x%x", gc->flags);
     sty_nrc *nr = new sty_nrc();
+    nr->layered = (gc->flags & STY_NRC_GRID_LAYERED) != 0;
     size_t np = 0, n_mlp = 0;
     sty_status s = grid_create(gc, &nr->grid, &np, &n_mlp);
     if (s != STY_OK) {

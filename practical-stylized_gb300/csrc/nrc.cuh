@@ -61,9 +61,13 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
 void grid_destroy(GridModel *g);
 sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t st);
 sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_t st);
-sty_status grid_infer(GridModel *g, bool ema, const float *params, uint64_t count, const float *in, float *out,
+// inference with the EMA or the current parameters (packed by grid_pack with both sets); the
+// tensor-core path (tile encoder + MMA kernel) when the network fits it and allow_tc, else the
+// cuBLAS layer-by-layer path
+sty_status grid_infer(GridModel *g, bool ema, bool allow_tc, uint64_t count, const float *in, float *out,
                       cudaStream_t st);
-sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, const float *params,
-                         float *grad, float *loss, cudaStream_t st);
+// loss and full parameter gradient of B rows with the current parameters (packed by grid_pack)
+sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, float *grad, float *loss,
+                         cudaStream_t st);
 
 }  // namespace sty

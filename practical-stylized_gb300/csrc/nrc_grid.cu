@@ -5,7 +5,8 @@
 //
 // Encoding (definitions restated from the published papers: tiny-cuda-nn is not available):
 //   hash grid: level l: s_l = N_min b^l - 1, r_l = ceil(s_l) + 1, u = clamp(x, 0, 1) s_l + 0.5,
-//     trilinear over the 8 corners of floor(u); table T_l = min(roundup8(r_l^3), 2^log2T) entries
+//     trilinear over the 8 corners of floor(u); as in tiny-cuda-nn, s_l is the FP32 evaluation
+//     exp2(l log2 b) N_min - 1 and u = fma(x, s_l, 0.5) in FP32; table T_l = min(roundup8(r_l^3), 2^log2T) entries
 //     of F features, dense index when r_l^3 <= T_l else (c.x ^ c.y 2654435761 ^ c.z 805459861) in
 //     32-bit arithmetic, both mod T_l. One thread per (sample, level); the backward scatters
 //     w * dL/dfeature into the FP32 table gradient with atomics.
@@ -15,6 +16,7 @@
 // backward. Layout: rows are samples; encoded width padded to a multiple of 16, output padded to 8.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <algorithm>
 #include <cmath>
@@ -22,9 +24,11 @@
 
 #include "common.cuh"
 #include "nrc.cuh"
+#include "tc.cuh"
 
 namespace sty {
 namespace {
+using namespace tc;
 
 constexpr int kMaxLevels = 32;
 constexpr int kOpad = 8;
@@ -36,38 +40,115 @@ struct GridGeo {
     int dense[kMaxLevels];
 };
 
+// Table entry of corner (cx, cy, cz) of level l. Hashed levels have power-of-two tables, so the
+// modulo is a mask; a dense index is at most r + r^2 + r^3 < 2 T_l (corners reach r = the
+// resolution), so one conditional subtraction is the modulo.
 __device__ __forceinline__ uint32_t grid_index(const GridGeo &g, int l, uint32_t cx, uint32_t cy, uint32_t cz) {
+    const uint32_t size = g.size[l];
     uint32_t h;
-    if (g.dense[l]) h = cx + cy * g.res[l] + cz * g.res[l] * g.res[l];
-    else h = cx ^ (cy * 2654435761u) ^ (cz * 805459861u);
-    return g.off[l] + h % g.size[l];
+    if (g.dense[l]) {
+        h = cx + cy * g.res[l] + cz * g.res[l] * g.res[l];
+        h = h >= size ? h - size : h;
+    } else {
+        h = (cx ^ (cy * 2654435761u) ^ (cz * 805459861u)) & (size - 1u);
+    }
+    return g.off[l] + h;
+}
+
+// F FP16 features of one table entry, as raw 32-bit words (F = 1: the low half)
+template <int F>
+struct RawEntry {
+    uint32_t w[F >= 2 ? F / 2 : 1];
+};
+template <int F>
+__device__ __forceinline__ RawEntry<F> load_entry(const __half *p) {
+    RawEntry<F> r;
+    if constexpr (F == 1) {
+        r.w[0] = __ldg(reinterpret_cast<const unsigned short *>(p));
+    } else if constexpr (F == 2) {
+        r.w[0] = __ldg(reinterpret_cast<const unsigned int *>(p));
+    } else if constexpr (F == 4) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(p));
+        r.w[0] = v.x;
+        r.w[1] = v.y;
+    } else {
+        const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+        r.w[0] = v.x;
+        r.w[1] = v.y;
+        r.w[2] = v.z;
+        r.w[3] = v.w;
+    }
+    return r;
+}
+__device__ __forceinline__ float half_lo(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w & 0xffffu))); }
+__device__ __forceinline__ float half_hi(uint32_t w) { return __half2float(__ushort_as_half((unsigned short)(w >> 16))); }
+
+// Trilinear interpolation of level l at x (clamped to [0, 1]) from the FP16 tables, in three parts
+// so that callers can keep several levels' loads in flight: the cell and FP32 weights, the 8
+// corner loads, and acc[f] = sum_k w_k t_k[f] in corner order k = 0..7 (FMA).
+__device__ __forceinline__ void level_cell(const GridGeo &g, int l, float x0, float x1, float x2, uint32_t (&c)[3],
+                                           float (&w)[3]) {
+    const float xs[3] = {x0, x1, x2};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const float u = fmaf(fminf(fmaxf(xs[a], 0.0f), 1.0f), g.scale[l], 0.5f);
+        const float f = floorf(u);
+        c[a] = (uint32_t)f;
+        w[a] = u - f;
+    }
+}
+template <int F>
+__device__ __forceinline__ void level_loads(const GridGeo &g, int l, const uint32_t (&c)[3],
+                                            const __half *__restrict__ tab, RawEntry<F> (&e)[8]) {
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+        e[k] = load_entry<F>(tab + (size_t)grid_index(g, l, c[0] + (k & 1), c[1] + ((k >> 1) & 1), c[2] + (k >> 2)) * F);
+}
+template <int F>
+__device__ __forceinline__ void level_sum(const RawEntry<F> (&e)[8], const float (&w)[3], float (&acc)[F]) {
+#pragma unroll
+    for (int f = 0; f < F; f++) acc[f] = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float wt = ((k & 1) ? w[0] : 1.0f - w[0]) * (((k >> 1) & 1) ? w[1] : 1.0f - w[1]) *
+                         ((k >> 2) ? w[2] : 1.0f - w[2]);
+#pragma unroll
+        for (int f = 0; f < F; f++) {
+            const uint32_t word = e[k].w[f / 2];
+            acc[f] = fmaf(wt, (f & 1) ? half_hi(word) : half_lo(word), acc[f]);
+        }
+    }
+}
+template <int F>
+__device__ __forceinline__ void gather_level(const GridGeo &g, int l, float x0, float x1, float x2,
+                                             const __half *__restrict__ tab, float (&acc)[F]) {
+    uint32_t c[3];
+    float w[3];
+    level_cell(g, l, x0, x1, x2, c, w);
+    RawEntry<F> e[8];
+    level_loads<F>(g, l, c, tab, e);
+    level_sum<F>(e, w, acc);
+}
+// one-blob: mass of N(v, (1 / bins)^2) below bin edge k / bins
+__device__ __forceinline__ float blob_cdf(int k, int bins, float v) {
+    const float inv = 1.0f / ((1.0f / bins) * 1.41421356237f);
+    return 0.5f * (1.0f + erff(((float)k / bins - v) * inv));
 }
 
 // one thread per (sample, level): the level's F features into enc[s][l F ..]
-__global__ void k_grid_enc(uint64_t n, const float *__restrict__ x, GridGeo g, const float *__restrict__ tab,
+template <int F>
+__global__ void k_grid_enc(uint64_t n, const float *__restrict__ x, GridGeo g, const __half *__restrict__ tab,
                            __nv_bfloat16 *__restrict__ enc) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= n * (uint64_t)g.levels) return;
     const uint64_t s = t / g.levels;
     const int l = (int)(t % g.levels);
     const float *xs = x + s * g.in_dims;
-    float u[3], w[3];
-    uint32_t c[3];
-    for (int a = 0; a < 3; a++) {
-        u[a] = fminf(fmaxf(xs[a], 0.0f), 1.0f) * g.scale[l] + 0.5f;
-        const float f = floorf(u[a]);
-        c[a] = (uint32_t)f;
-        w[a] = u[a] - f;
-    }
-    float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = 0; k < 8; k++) {
-        const uint32_t ox = k & 1, oy = (k >> 1) & 1, oz = (k >> 2) & 1;
-        const float wt = (ox ? w[0] : 1.0f - w[0]) * (oy ? w[1] : 1.0f - w[1]) * (oz ? w[2] : 1.0f - w[2]);
-        const float *e = tab + (size_t)grid_index(g, l, c[0] + ox, c[1] + oy, c[2] + oz) * g.feats;
-        for (int f = 0; f < g.feats; f++) acc[f] = fmaf(wt, e[f], acc[f]);
-    }
-    __nv_bfloat16 *o = enc + s * g.out_w + (size_t)l * g.feats;
-    for (int f = 0; f < g.feats; f++) o[f] = __float2bfloat16_rn(acc[f]);
+    float acc[F];
+    gather_level<F>(g, l, xs[0], xs[1], xs[2], tab, acc);
+    __nv_bfloat16 *o = enc + s * g.out_w + (size_t)l * F;
+#pragma unroll
+    for (int f = 0; f < F; f++) o[f] = __float2bfloat16_rn(acc[f]);
 }
 // one thread per sample: one-blob bins, identity dims, zero padding
 __global__ void k_blob_ident(uint64_t n, const float *__restrict__ x, GridGeo g, __nv_bfloat16 *__restrict__ enc) {
@@ -76,12 +157,11 @@ __global__ void k_blob_ident(uint64_t n, const float *__restrict__ x, GridGeo g,
     const float *xs = x + s * g.in_dims;
     __nv_bfloat16 *o = enc + s * g.out_w;
     int k = g.levels * g.feats;
-    const float inv = 1.0f / ((1.0f / g.bins) * 1.41421356237f);
     for (int d = 0; d < g.blob_dims; d++) {
         const float v = xs[3 + d];
-        float prev = 0.5f * (1.0f + erff((0.0f - v) * inv));
+        float prev = blob_cdf(0, g.bins, v);
         for (int b = 0; b < g.bins; b++) {
-            const float cdf = 0.5f * (1.0f + erff(((float)(b + 1) / g.bins - v) * inv));
+            const float cdf = blob_cdf(b + 1, g.bins, v);
             o[k++] = __float2bfloat16_rn(cdf - prev);
             prev = cdf;
         }
@@ -100,7 +180,7 @@ __global__ void k_grid_bwd(uint64_t n, const float *__restrict__ x, GridGeo g, c
     float w[3];
     uint32_t c[3];
     for (int a = 0; a < 3; a++) {
-        const float u = fminf(fmaxf(xs[a], 0.0f), 1.0f) * g.scale[l] + 0.5f;
+        const float u = fmaf(fminf(fmaxf(xs[a], 0.0f), 1.0f), g.scale[l], 0.5f);
         const float f = floorf(u);
         c[a] = (uint32_t)f;
         w[a] = u - f;
@@ -185,6 +265,252 @@ __global__ void k_grid_init(size_t n_mlp, size_t n_total, const int *fan_in, con
     while (l + 1 < n_layers && i >= layer_off[l + 1]) l++;
     w[i] = u * sqrtf(6.0f / (float)(fan_in[l] + fan_out[l]));
 }
+__global__ void k_tab_half(size_t n, const float *__restrict__ t, __half *__restrict__ h) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) h[i] = __float2half_rn(t[i]);
+}
+
+// ---- tensor-core inference --------------------------------------------------------------------------
+// Two launches per chunk of rows:
+//   k_grid_tiles   the encoding, written straight into 128-row tile images in the MMA A-operand
+//                  layout (K-major core matrices, K = E columns). One thread per (row, unit):
+//                  unit v < levels gathers hash-grid level v, unit levels + k writes columns
+//                  G + 8k .. G + 8k + 7 (one-blob / identity / zero padding). A gather-bound kernel
+//                  wants every warp slot of the SM for loads in flight, so it is kept apart from
+//                  the MMA kernel, whose weights fill shared memory.
+//   k_grid_mlp_tc  one persistent CTA per SM holding every layer's weights as BF16 operand images
+//                  (W_0: H x E, W_1..W_{L-1}: H x H, W_out: 16 x H with rows >= O zero) and one
+//                  activation image. Warps 0-3: per layer thread 0 issues K/16 x tcgen05.mma (M=128,
+//                  N=H or 16, K=16) and commits to `bar_mma`; the warpgroup waits (bounded),
+//                  tcgen05.ld's its rows, applies ReLU, converts to BF16 and writes them back as the
+//                  next layer's A operand; after the output layer's MMA the image is released
+//                  (`bar_free`) and the output columns are read. Warps 4-11 copy the next tile's
+//                  image from global memory into registers while the current tile's layers run, then
+//                  store it once `bar_free` completes and arrive on `bar_full`.
+// Every wait is bounded: on a timeout the kernel sets STY_DEV_WAIT_TIMEOUT, waits once more for an
+// MMA still in flight, frees its TMEM columns and returns.
+constexpr int kTM = 128;
+constexpr int kCopyThreads = 256;
+constexpr int kMlpThreads = 128 + kCopyThreads;
+constexpr int kMaxE = 160;  // encoded width the copy warps stage (10 x 16 bytes per thread)
+constexpr int kCopyChunks = kTM * kMaxE * 2 / 16 / kCopyThreads;
+constexpr int kOutN = 16;
+constexpr uint64_t kInferChunk = 1ull << 18;  // rows per encode + MLP launch pair
+
+// byte offset of (row, k) in a K-major no-swizzle image of K columns (core matrices of one 8-row
+// group adjacent along K: LBO 128 bytes, SBO K * 16 bytes)
+__host__ __device__ __forceinline__ uint32_t kimg_off(uint32_t row, uint32_t k, uint32_t K) {
+    return ((row >> 3) * (K >> 3) + (k >> 3)) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+// element offset of layer l's image (l = L: the output layer)
+__host__ __device__ __forceinline__ size_t img_layer(int l, int H, int E) {
+    return l == 0 ? 0 : (size_t)H * E + (size_t)(l - 1) * H * H;
+}
+// FP32 parameters -> the MMA kernel's BF16 weight images; grid (rows * K / 256, L + 1)
+__global__ void k_grid_img(int H, int L, int E, int O, const float *__restrict__ w, uint16_t *__restrict__ img) {
+    const int l = blockIdx.y;
+    const uint32_t K = l == 0 ? (uint32_t)E : (uint32_t)H, R = l == L ? (uint32_t)kOutN : (uint32_t)H;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= R * K) return;
+    const uint32_t n = i / K, k = i % K;
+    const size_t base = img_layer(l, H, E);  // also the layer's offset in the flat parameters
+    const float v = (l < L || n < (uint32_t)O) ? w[base + (size_t)n * K + k] : 0.0f;
+    img[base + kimg_off(n, k, K) / 2] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+
+// encoded value of non-grid column G + r of input row xs: one-blob bin, identity or padding
+__device__ __forceinline__ float extra_column(const GridGeo &g, int r, const float *xs) {
+    const int nblob = g.blob_dims * g.bins, nident = g.in_dims - 3 - g.blob_dims;
+    if (r < nblob) {
+        const float v = xs[3 + r / g.bins];
+        const int b = r % g.bins;
+        return blob_cdf(b + 1, g.bins, v) - blob_cdf(b, g.bins, v);
+    }
+    if (r < nblob + nident) return xs[3 + g.blob_dims + (r - nblob)];
+    return 0.0f;
+}
+// block = one tile x one unit (blockIdx.x = tile * units + unit, so a tile's units run together
+// and its input rows are read while they are cached); rows >= count are written as zeros
+template <int F>
+__global__ void __launch_bounds__(kTM) k_grid_tiles(uint64_t count, const float *__restrict__ x, GridGeo g,
+                                                    int units, const __half *__restrict__ tab, uint8_t *__restrict__ img) {
+    const uint32_t m = threadIdx.x;
+    const uint64_t tile = blockIdx.x / (uint32_t)units;
+    const int v = (int)(blockIdx.x % (uint32_t)units);
+    const uint64_t row = tile * kTM + m;
+    const bool valid = row < count;
+    const uint32_t E = (uint32_t)g.out_w;
+    uint8_t *t = img + tile * (uint64_t)(kTM * E * 2u);
+    const float *xs = x + (valid ? row : 0) * (uint64_t)g.in_dims;
+    if (v < g.levels) {
+        float acc[F];
+#pragma unroll
+        for (int f = 0; f < F; f++) acc[f] = 0.0f;
+        if (valid) gather_level<F>(g, v, xs[0], xs[1], xs[2], tab, acc);
+        uint8_t *p = t + kimg_off(m, (uint32_t)(v * F), E);
+        if constexpr (F == 1) {
+            *reinterpret_cast<unsigned short *>(p) = __bfloat16_as_ushort(__float2bfloat16_rn(acc[0]));
+        } else if constexpr (F == 2) {
+            *reinterpret_cast<uint32_t *>(p) = pack2_bf16(acc[0], acc[1]);
+        } else if constexpr (F == 4) {
+            *reinterpret_cast<uint2 *>(p) = make_uint2(pack2_bf16(acc[0], acc[1]), pack2_bf16(acc[2], acc[3]));
+        } else {
+            *reinterpret_cast<uint4 *>(p) = make_uint4(pack2_bf16(acc[0], acc[1]), pack2_bf16(acc[2], acc[3]),
+                                                       pack2_bf16(acc[4], acc[5]), pack2_bf16(acc[6], acc[7]));
+        }
+        return;
+    }
+    const int G = g.levels * F, c0 = G + (v - g.levels) * 8;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int c = c0 + i;
+        if (c < (int)E) {
+            const float val = valid ? extra_column(g, c - G, xs) : 0.0f;
+            *reinterpret_cast<unsigned short *>(t + kimg_off(m, (uint32_t)c, E)) =
+                __bfloat16_as_ushort(__float2bfloat16_rn(val));
+        }
+    }
+}
+
+struct GridTcArgs {
+    int E, H, L, O;
+    const uint8_t *enc;  // tile images of the chunk (k_grid_tiles)
+    const uint16_t *wimg;
+    uint64_t count;
+    float *output;
+    uint32_t *status;
+};
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t bar_mma, bar_full, bar_free;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int H = a.H, L = a.L, E = a.E;
+    const uint32_t wbytes = (uint32_t)(img_layer(L, H, E) + (size_t)kOutN * H) * 2u;
+    uint8_t *act = smem + ((wbytes + 1023u) & ~1023u);
+    for (uint32_t o = tid * 16u; o < wbytes; o += kMlpThreads * 16u)
+        *reinterpret_cast<uint4 *>(smem + o) =
+            *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
+    if (tid == 0) {
+        mbar_init(&bar_mma, 1);
+        mbar_init(&bar_full, kCopyThreads);
+        mbar_init(&bar_free, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"((uint32_t)H)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint64_t ntiles = (a.count + kTM - 1) / kTM;
+
+    if (warp < 4) {
+        // ---- MMA issue + epilogue ----
+        const uint32_t t = (uint32_t)tid;
+        const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
+        const uint32_t wbase = smem_u32(smem), abase = smem_u32(act);
+        uint32_t phase = 0, it = 0;
+        bool failed = false, pending = false;
+        for (uint64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x, it++) {
+            const bool got = mbar_wait(&bar_full, it & 1u, a.status);
+            if (!wg_sync_and(1, got)) {
+                failed = true;
+                break;
+            }
+            const uint64_t row = tile * kTM + t;
+            for (int l = 0; l <= L; l++) {
+                const bool out_layer = l == L;
+                const uint32_t K = l == 0 ? (uint32_t)E : (uint32_t)H;
+                if (t == 0) {
+                    fence_after();
+                    const uint32_t wl = wbase + (uint32_t)img_layer(l, H, E) * 2u;
+                    const uint32_t idesc = out_layer ? idesc_bf16(kTM, kOutN) : idesc_bf16(kTM, (uint32_t)H);
+                    for (uint32_t kk = 0; kk < K / 16u; kk++)
+                        mma_bf16(tmem, make_desc(abase + kk * 256u, 128u, K * 16u),
+                                 make_desc(wl + kk * 256u, 128u, K * 16u), idesc, kk > 0 ? 1u : 0u);
+                    mma_commit(&bar_mma);
+                }
+                pending = true;
+                const bool ok = mbar_wait(&bar_mma, phase, a.status);
+                if (!wg_sync_and(1, ok)) {
+                    failed = true;
+                    break;
+                }
+                pending = false;
+                phase ^= 1u;
+                fence_after();
+                if (!out_layer) {
+                    for (uint32_t c = 0; c < (uint32_t)H; c += 32u) {
+                        float v[32];
+                        tmem_ld32(lane_base + c, v);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int kb = 0; kb < 4; kb++) {
+                            const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
+                                                       pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
+                                                       pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
+                                                       pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
+                            *reinterpret_cast<uint4 *>(act + kimg_off(t, c + kb * 8u, (uint32_t)H)) = q;
+                        }
+                    }
+                    fence_async_smem();
+                } else {
+                    if (t == 0) mbar_arrive(&bar_free);  // the output MMA has read the last activations
+                    float v[16];
+                    tmem_ld16(lane_base, v);
+                    tmem_wait_ld();
+                    if (row < a.count)
+                        for (int c = 0; c < a.O; c++) a.output[row * a.O + c] = v[c];
+                }
+                fence_before();
+                wg_sync(1);
+            }
+        }
+        if (failed && pending) mbar_wait(&bar_mma, phase, a.status);
+    } else {
+        // ---- copy warps: the next tile's image through registers ----
+        const uint32_t e = (uint32_t)(tid - 128);
+        const uint32_t chunks = (uint32_t)(kTM * E * 2) / 16u;  // 16-byte chunks per tile image
+        uint32_t it = 0;
+        for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
+            const uint4 *src = reinterpret_cast<const uint4 *>(a.enc + tile * (uint64_t)(kTM * E * 2));
+            uint4 r[kCopyChunks];
+#pragma unroll
+            for (int i = 0; i < kCopyChunks; i++) {
+                const uint32_t c = e + (uint32_t)i * kCopyThreads;
+                if (c < chunks) r[i] = __ldcs(src + c);  // read once: evict first
+            }
+            if (!mbar_wait(&bar_free, (it & 1u) ^ 1u, a.status)) break;
+#pragma unroll
+            for (int i = 0; i < kCopyChunks; i++) {
+                const uint32_t c = e + (uint32_t)i * kCopyThreads;
+                if (c < chunks) reinterpret_cast<uint4 *>(act)[c] = r[i];
+            }
+            fence_async_smem();
+            mbar_arrive(&bar_full);
+        }
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"((uint32_t)H)
+                     : "memory");
+}
 
 }  // namespace
 
@@ -195,7 +521,14 @@ struct GridModel {
     size_t n_mlp, n_tab, out_off;
     std::vector<size_t> loff;  // FP32 offsets of W_0 .. W_L (W_L = output layer)
     __nv_bfloat16 *wb = nullptr, *wb_ema = nullptr;
-    bool wb_dirty = true;
+    __half *tab16 = nullptr, *tab16_ema = nullptr;  // FP16 copies of the tables the forward reads
+    // tensor-core inference (k_grid_tiles + k_grid_mlp_tc): BF16 weight images, the MMA kernel's
+    // shared memory, the chunk's tile images
+    bool tc = false;
+    size_t img_elems = 0, tc_smem = 0;
+    uint16_t *img = nullptr, *img_ema = nullptr;
+    uint8_t *tiles = nullptr;
+    uint64_t tiles_cap = 0;
     cublasHandle_t h = nullptr;
     // batch scratch
     uint64_t cap = 0;
@@ -253,11 +586,17 @@ sty_status ensure_cap(GridModel *g, uint64_t B) {
 
 // forward of B rows with the given BF16 weights and FP32 tables: leaves enc, acts (for the backward)
 // and the padded output (B x kOpad) in g->z
-sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const float *tables, const __nv_bfloat16 *wb,
+sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const __half *tables, const __nv_bfloat16 *wb,
                         cudaStream_t st) {
     STY_TRY(cublas_ok(cublasSetStream(g->h, st), "cublasSetStream"));
     const uint64_t nl = B * (uint64_t)g->geo.levels;
-    k_grid_enc<<<(unsigned)((nl + 255) / 256), 256, 0, st>>>(B, x, g->geo, tables, g->enc);
+    const unsigned blocks = (unsigned)((nl + 255) / 256);
+    switch (g->geo.feats) {
+        case 1: k_grid_enc<1><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
+        case 2: k_grid_enc<2><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
+        case 4: k_grid_enc<4><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
+        default: k_grid_enc<8><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
+    }
     STY_TRY(check_launch("k_grid_enc"));
     k_blob_ident<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->enc);
     STY_TRY(check_launch("k_blob_ident"));
@@ -277,12 +616,65 @@ sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const float *t
     return STY_OK;
 }
 
+// the two tensor-core launches per chunk of kInferChunk rows (tile images in g->tiles)
+sty_status grid_tc_forward(GridModel *g, bool ema, uint64_t count, const float *in, float *out, cudaStream_t st) {
+    const uint64_t chunk = std::min<uint64_t>(count, kInferChunk);
+    const uint64_t tile_bytes = (uint64_t)kTM * g->E * 2;
+    const uint64_t need = (chunk + kTM - 1) / kTM * tile_bytes;
+    if (need > g->tiles_cap) {
+        if (g->tiles) cudaFree(g->tiles);
+        g->tiles = nullptr;
+        g->tiles_cap = 0;
+        STY_TRY(check_cuda(cudaMalloc(&g->tiles, need), "alloc tile images"));
+        g->tiles_cap = need;
+    }
+    GridTcArgs a;
+    a.E = g->E;
+    a.H = g->H;
+    a.L = g->L;
+    a.O = g->O;
+    a.enc = g->tiles;
+    a.wimg = ema ? g->img_ema : g->img;
+    a.status = device_status_ptr();
+    if (!a.status) {
+        set_error("device status word unavailable");
+        return STY_ERR_CUDA;
+    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int smem = (int)g->tc_smem;
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_grid_mlp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                       "attr k_grid_mlp_tc"));
+    const int units = g->geo.levels + (g->E - g->geo.levels * g->geo.feats + 7) / 8;
+    const __half *tab = ema ? g->tab16_ema : g->tab16;
+    for (uint64_t b0 = 0; b0 < count; b0 += chunk) {
+        const uint64_t B = std::min<uint64_t>(chunk, count - b0);
+        const uint64_t ntiles = (B + kTM - 1) / kTM;
+        const float *x = in + b0 * g->geo.in_dims;
+        const unsigned blocks = (unsigned)(ntiles * (uint64_t)units);
+        switch (g->geo.feats) {
+            case 1: k_grid_tiles<1><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
+            case 2: k_grid_tiles<2><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
+            case 4: k_grid_tiles<4><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
+            default: k_grid_tiles<8><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
+        }
+        STY_TRY(check_launch("k_grid_tiles"));
+        a.count = B;
+        a.output = out + b0 * g->O;
+        k_grid_mlp_tc<<<(unsigned)std::min<uint64_t>(ntiles, (uint64_t)sms), kMlpThreads, smem, st>>>(a);
+        STY_TRY(check_launch("k_grid_mlp_tc"));
+    }
+    return STY_OK;
+}
+
 }  // namespace
 
 // ---- interface used by nrc.cu ----------------------------------------------------------------------
 sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_params, size_t *n_mlp) {
     STY_ARG_CHECK(c->grid_levels >= 1 && c->grid_levels <= kMaxLevels, "grid_levels must be in [1, %d]", kMaxLevels);
-    STY_ARG_CHECK(c->grid_features >= 1 && c->grid_features <= 8, "grid_features must be in [1, 8]");
+    STY_ARG_CHECK(c->grid_features == 1 || c->grid_features == 2 || c->grid_features == 4 || c->grid_features == 8,
+                  "grid_features must be 1, 2, 4 or 8");
     STY_ARG_CHECK(c->log2_table >= 4 && c->log2_table <= 24, "log2_table must be in [4, 24]");
     STY_ARG_CHECK(c->input_dims >= 3 + c->blob_dims && c->input_dims <= 64, "input_dims must cover 3 + blob_dims");
     STY_ARG_CHECK(c->blob_bins >= 1 && c->blob_bins <= 16, "blob_bins must be in [1, 16]");
@@ -301,14 +693,16 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     geo.bins = (int)c->blob_bins;
     uint64_t off = 0;
     for (int l = 0; l < geo.levels; l++) {
-        const double scale = (double)c->base_resolution * std::pow((double)c->per_level_scale, l) - 1.0;
+        // FP32 like tiny-cuda-nn's grid_scale / grid_resolution
+        const float scale = std::exp2((float)l * std::log2(c->per_level_scale)) * (float)c->base_resolution - 1.0f;
+        STY_ARG_CHECK(std::isfinite(scale) && scale < 2147483648.0f, "grid level %d resolution overflows", l);
         const uint64_t res = (uint64_t)std::ceil(scale) + 1;
         STY_ARG_CHECK(res < (1ull << 31), "grid level %d resolution overflows", l);
         // r^3 exceeds 64 bits at the finest levels of deep grids: compare in double first
         const uint64_t cap = 1ull << c->log2_table;
         const bool fits = (double)res * (double)res * (double)res <= (double)cap;
         const uint64_t size = fits ? std::min<uint64_t>((res * res * res + 7) / 8 * 8, cap) : cap;
-        geo.scale[l] = (float)scale;
+        geo.scale[l] = scale;
         geo.res[l] = (uint32_t)res;
         geo.size[l] = (uint32_t)size;
         geo.dense[l] = fits && res * res * res <= size;
@@ -332,9 +726,21 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     g->n_tab = off * geo.feats;
     *n_params = g->n_mlp + g->n_tab;
     *n_mlp = g->n_mlp;
+    // the tensor-core path: H in {32, 64, 128} (one TMEM column per unit), E <= kMaxE (what the copy
+    // warps stage), weight images + one 128-row activation image within the opt-in shared memory
+    int dev = 0, smem_optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    g->img_elems = img_layer(g->L, g->H, g->E) + (size_t)kOutN * g->H;
+    g->tc_smem = ((g->img_elems * 2 + 1023) & ~(size_t)1023) + (size_t)kTM * std::max(g->E, g->H) * 2 + 1024;
+    g->tc = (g->H == 32 || g->H == 64 || g->H == 128) && g->E <= kMaxE && g->tc_smem + 64 <= (size_t)smem_optin;
     sty_status s = cublas_ok(cublasCreate(&g->h), "cublasCreate");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc bf16 weights");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb_ema, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc bf16 ema");
+    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16, g->n_tab * 2), "alloc fp16 tables");
+    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16_ema, g->n_tab * 2), "alloc fp16 ema tables");
+    if (s == STY_OK && g->tc) s = check_cuda(cudaMalloc(&g->img, g->img_elems * 2), "alloc weight images");
+    if (s == STY_OK && g->tc) s = check_cuda(cudaMalloc(&g->img_ema, g->img_elems * 2), "alloc ema images");
     if (s != STY_OK) {
         grid_destroy(g);
         return s;
@@ -345,7 +751,8 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
 
 void grid_destroy(GridModel *g) {
     if (!g) return;
-    void *ptrs[] = {g->wb, g->wb_ema, g->enc, g->acts, g->dp, g->z, g->dh, g->d_fan_in, g->d_fan_out, g->d_loff};
+    void *ptrs[] = {g->wb, g->wb_ema, g->tab16, g->tab16_ema, g->img, g->img_ema, g->tiles, g->enc,
+                    g->acts, g->dp, g->z, g->dh, g->d_fan_in, g->d_fan_out, g->d_loff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (g->h) cublasDestroy(g->h);
@@ -378,24 +785,37 @@ sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t 
 
 sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_t st) {
     const size_t total = g->out_off + (size_t)kOpad * g->H;
+    const unsigned tblocks = (unsigned)((g->n_tab + 255) / 256);
     k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, w, g->wb);
     STY_TRY(check_launch("k_weights_bf16"));
-    if (ema) {
-        k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema,
-                                                                         g->wb_ema);
-        STY_TRY(check_launch("k_weights_bf16"));
+    k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, w + g->n_mlp, g->tab16);
+    STY_TRY(check_launch("k_tab_half"));
+    if (!ema) return STY_OK;
+    // the inference set: EMA copies and the tensor-core weight images of both parameter sets
+    k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema,
+                                                                     g->wb_ema);
+    STY_TRY(check_launch("k_weights_bf16"));
+    k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, ema + g->n_mlp, g->tab16_ema);
+    STY_TRY(check_launch("k_tab_half"));
+    if (g->tc) {
+        const dim3 grid((unsigned)(((size_t)g->H * std::max(g->E, g->H) + 255) / 256), (unsigned)(g->L + 1));
+        k_grid_img<<<grid, 256, 0, st>>>(g->H, g->L, g->E, g->O, w, g->img);
+        STY_TRY(check_launch("k_grid_img"));
+        k_grid_img<<<grid, 256, 0, st>>>(g->H, g->L, g->E, g->O, ema, g->img_ema);
+        STY_TRY(check_launch("k_grid_img"));
     }
     return STY_OK;
 }
 
-sty_status grid_infer(GridModel *g, bool ema, const float *params, uint64_t count, const float *in, float *out,
+sty_status grid_infer(GridModel *g, bool ema, bool allow_tc, uint64_t count, const float *in, float *out,
                       cudaStream_t st) {
+    if (g->tc && allow_tc) return grid_tc_forward(g, ema, count, in, out, st);
     const uint64_t chunk = 1ull << 18;
     STY_TRY(ensure_cap(g, std::min<uint64_t>(count, chunk)));
-    const float *tables = params + g->n_mlp;
     for (uint64_t b0 = 0; b0 < count; b0 += chunk) {
         const uint64_t B = std::min<uint64_t>(chunk, count - b0);
-        STY_TRY(grid_forward(g, B, in + b0 * g->geo.in_dims, tables, ema ? g->wb_ema : g->wb, st));
+        STY_TRY(grid_forward(g, B, in + b0 * g->geo.in_dims, ema ? g->tab16_ema : g->tab16, ema ? g->wb_ema : g->wb,
+                             st));
         k_out_rows<<<(unsigned)((B * g->O + 255) / 256), 256, 0, st>>>(B, g->O, g->z, out + b0 * g->O);
         STY_TRY(check_launch("k_out_rows"));
     }
@@ -403,10 +823,10 @@ sty_status grid_infer(GridModel *g, bool ema, const float *params, uint64_t coun
 }
 
 // loss gradient, backward and the full parameter gradient (MLP weights and tables) of B rows
-sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, const float *params,
-                         float *grad, float *loss, cudaStream_t st) {
+sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, float *grad, float *loss,
+                         cudaStream_t st) {
     STY_TRY(ensure_cap(g, B));
-    STY_TRY(grid_forward(g, B, x, params + g->n_mlp, g->wb, st));
+    STY_TRY(grid_forward(g, B, x, g->tab16, g->wb, st));
     // dP_out = dLoss/dpred (B x kOpad) in g->dp
     k_rel_l2_grad<<<(B + 255) / 256, 256, 0, st>>>(B, g->O, g->z, target, g->dp, loss);
     STY_TRY(check_launch("k_rel_l2_grad"));

@@ -11,8 +11,10 @@ from .abi import check, lib
 
 STY_NRC_FP32 = 0
 STY_NRC_BF16 = 1
+GRID_LAYERED = 1  # STY_NRC_GRID_LAYERED
 
-# BASELINE NL-NRC layout: pos 3, dir 2, normal 2, roughness 1, albedo 3 -> 3*8 + 4*6 + 4*4 = 64
+# the spherical row layout's frequency table: pos 3, dir 2, normal 2, roughness 1, albedo 3
+# -> 3*8 + 4*6 + 4*4 = 64 encoded columns
 C4_FREQS = (4, 4, 4, 3, 3, 3, 3, 2, 2, 2, 2)
 
 
@@ -47,15 +49,16 @@ class NrcGridConfig(C.Structure):
                 ("per_level_scale", C.c_float), ("blob_dims", C.c_uint32), ("blob_bins", C.c_uint32),
                 ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("ema_decay", C.c_float), ("decay_base", C.c_float), ("decay_interval", C.c_uint32),
-                ("reserved", C.c_uint32), ("seed", C.c_uint64)]
+                ("flags", C.c_uint32), ("seed", C.c_uint64)]
 
 
 def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5, hidden_units=128, grid_levels=22,
                 grid_features=4, log2_table=19, base_resolution=16, per_level_scale=2.0, blob_dims=7, blob_bins=4,
                 learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8, ema_decay=0.95, decay_base=1.0,
-                decay_interval=100, seed=1337) -> NrcGridConfig:
+                decay_interval=100, seed=1337, layered=False) -> NrcGridConfig:
     """The reference's NL-NRC network (nrc_pt.rs:1159-1352; defaults of configs/teaser/nl-nrc.json):
-    rows of 20 + max_depth inputs in the reference layout."""
+    rows of 20 + max_depth inputs in the reference layout. `layered` forces the layer-by-layer
+    inference path instead of the tensor-core path (tile encoder + on-chip MLP kernel)."""
     c = NrcGridConfig()
     c.input_dims, c.output_dims, c.batch_size = 20 + max_depth, output_dims, batch_size
     c.hidden_layers, c.hidden_units = hidden_layers, hidden_units
@@ -64,6 +67,7 @@ def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5
     c.blob_dims, c.blob_bins = blob_dims, blob_bins
     c.learning_rate, c.beta1, c.beta2, c.epsilon = learning_rate, beta1, beta2, epsilon
     c.ema_decay, c.decay_base, c.decay_interval, c.seed = ema_decay, decay_base, decay_interval, seed
+    c.flags = GRID_LAYERED if layered else 0
     return c
 
 

@@ -2,9 +2,11 @@
 identity) and a ReLU MLP, against the FP64 oracle (oracle/nrc_grid.py + a BF16 emulation of the
 GEMM operands).
 
-Tolerances: GPU grid features accumulate in FP32 and are rounded to BF16 like every GEMM operand,
-so outputs are compared to the emulation statistically (98 % within 2e-3 of the output scale, all
-within 3e-2); gradients in norm (MLP 1e-2, tables 2e-2 relative)."""
+The forward reads FP16 copies of the tables (the emulation rounds them the same way); grid features
+accumulate in FP32 and are rounded to BF16 like every GEMM operand, so outputs are compared to the
+emulation statistically (98 % within 2e-3 of the output scale, all within 3e-2); gradients in norm
+(MLP 1e-2, tables 2e-2 relative). Networks with 32, 64 or 128 hidden units run tensor-core
+inference (tile encoder + on-chip MLP kernel); `layered=True` forces the layer-by-layer GEMM path."""
 import numpy as np
 import pytest
 
@@ -74,6 +76,7 @@ def _split(p, c):
 
 def _emulate(p, c, x):
     mats, tables, Ep = _split(p.astype(np.float64), c)
+    tables = tables.astype(np.float16).astype(np.float64)
     enc = og.encode(x, tables, c["grid_levels"], c["grid_features"], c["log2_table"], c["base_resolution"],
                     c["per_level_scale"], c["blob_dims"], c["blob_bins"], Ep)
     mb = [onrc.bf16_round(m) for m in mats]
@@ -115,6 +118,43 @@ def test_grid_inference_matches_emulation(sty, cuda):
     assert np.mean(err <= 2e-3 * scale) >= 0.98, np.mean(err > 2e-3 * scale)
     assert err.max() <= 3e-2 * scale
     assert sty.abi.device_status() == 0
+
+
+TEASER_SHAPE = dict(max_depth=12, hidden_units=128, hidden_layers=5, grid_levels=22, grid_features=4,
+                    log2_table=14, base_resolution=16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kw", [dict(), dict(hidden_units=64, hidden_layers=3, grid_levels=8, grid_features=4),
+                                dict(hidden_units=128, hidden_layers=2, grid_levels=5, grid_features=8),
+                                TEASER_SHAPE], ids=["h32f2", "h64f4", "h128f8", "teaser-shape"])
+def test_grid_tc_matches_layered(sty, cuda, kw):
+    """Tensor-core inference (tile encoder + every layer on chip) against the layer-by-layer GEMM
+    path and the emulation, on ragged row counts (partial tiles, fewer rows than one tile)."""
+    fused, c = _net(sty, seed=9, **kw)
+    layered, _ = _net(sty, seed=9, layered=True, **kw)
+    p = fused.save_params().astype(np.float64)
+    rng = np.random.default_rng(3)
+    _, tables, _ = _split(p, c)
+    p[len(p) - tables.size:] = rng.uniform(-0.5, 0.5, tables.size)
+    p32 = p.astype(np.float32)
+    fused.load_params(p32)
+    layered.load_params(p32)
+    for n in (1, 127, 128, 1000, 5000):
+        x = _rows(rng, n, c)
+        a = fused.inference(_dev(x)).cpu().numpy()
+        b = layered.inference(_dev(x)).cpu().numpy()
+        ref, _, _, _ = _emulate(p32.astype(np.float64), c, x)
+        scale = np.abs(ref).max()
+        assert a.shape == (n, 3) and np.isfinite(a).all()
+        for out in (a, b):
+            err = np.abs(out - ref)
+            assert np.mean(err <= 2e-3 * scale) >= 0.98, (n, np.mean(err > 2e-3 * scale))
+            assert err.max() <= 3e-2 * scale, (n, err.max() / scale)
+        assert np.abs(a - b).max() <= 3e-2 * scale
+    assert sty.abi.device_status() == 0
+    fused.close()
+    layered.close()
 
 
 @pytest.mark.gpu
