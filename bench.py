@@ -237,6 +237,71 @@ def nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
     return res
 
 
+def grid_nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
+    """The reference's NL-NRC network (hash grid 22 x 4 levels on 2^19-entry FP16 tables, one-blob 7 x
+    4, identity; 144 -> 5 x 128 ReLU -> 3; the teaser's configuration with max depth 12, so 32 inputs
+    per row in the reference's row layout) on the interior workload scene. Per frame: one training
+    step on a 2^16 batch from that frame's tracer rows (1 path per pixel of a 192 x 108 view) and
+    inference of the 1920 x 1080 first-hit queries (2 073 600 rows), as in the NL-NRC frames of the
+    spherical network. Inference runs the tensor-core path (k_grid_tiles + k_grid_mlp_tc); the
+    layer-by-layer cuBLAS path is timed beside it on the same rows."""
+    import numpy as np
+    import torch
+    D, nt = 12, 1 << 16
+    stream = torch.cuda.current_stream(dev)
+    pos, mids, mats, cam = sty.scene.room_with_door(1920, 1080)
+    view = sty.scene.camera(tuple(cam.eye), tuple(cam.target), fov_y=cam.fov_y, width=192, height=108)
+    q_scene = sty.scene.Scene(pos, mids, mats, cam)
+    t_scene = sty.scene.Scene(pos, mids, mats, view)
+    ref_rows = sty.scene.NRC_ROWS_REF
+    qx, _ = q_scene.nrc_samples(sty.scene.NRC_SAMPLES_QUERY, 1, D, layout=ref_rows, seed=99)
+    rows = [t_scene.nrc_samples(sty.scene.NRC_SAMPLES_TRAIN, 1, D, layout=ref_rows, seed=1000 + f)
+            for f in range(frames + warmup)]
+    nq = qx.shape[0]
+    out = torch.empty((nq, 3), device=dev)
+    res = {}
+    for name, layered in (("tensor_core", False), ("layered", True)):
+        net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=D, batch_size=nt, learning_rate=1e-2, seed=1,
+                                              layered=layered))
+        for f in range(warmup):
+            net.train(rows[frames + f][0], rows[frames + f][1], 1, stream=stream, want_loss=False)
+            net.inference(qx, out, stream=stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for f in range(frames):
+            net.train(rows[f][0], rows[f][1], 1, stream=stream, want_loss=False)
+            net.inference(qx, out, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / frames
+        i0, i1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        i0.record(stream)
+        for _ in range(frames):
+            net.inference(qx, out, stream=stream)
+        i1.record(stream)
+        torch.cuda.synchronize()
+        inf_ms = i0.elapsed_time(i1) / frames
+        res[name] = {"ms_per_frame": ms, "msamples_per_s": (nq + nt) / ms / 1e3, "inference_ms": inf_ms,
+                     "inference_mqueries_per_s": nq / inf_ms / 1e3, "train_ms": ms - inf_ms,
+                     "params": net.param_count(), "frames": frames}
+        net.close()
+    mlp_flops = 2.0 * (144 * 128 + 4 * 128 * 128 + 16 * 128)  # MMA work per query incl. the padded output rows
+    tc = res["tensor_core"]
+    res["inference_speedup_tc_over_layered"] = res["layered"]["inference_ms"] / tc["inference_ms"]
+    res["inference_mlp_tflops"] = nq * mlp_flops / (tc["inference_ms"] / 1e3) / 1e12
+    res["inference_mlp_frac_of_bf16_peak"] = res["inference_mlp_tflops"] / bf16_peak
+    res["config"] = {"workload": "interior room (~377k tris), 1920x1080 first-hit queries, rows in the reference layout",
+                     "queries_per_frame": nq, "train_batch_per_frame": nt,
+                     "train_rows_per_frame": int(np.mean([r[0].shape[0] for r in rows[:frames]])),
+                     "network": "hash grid 22x4 (2^19, FP16) + one-blob 7x4 + identity -> 144, 5x128 ReLU, 3",
+                     "lr": 1e-2, "loss": "relative L2",
+                     "note": "inference is bound by the encoder's random table gathers (L2 sectors)"}
+    q_scene.close()
+    t_scene.close()
+    return res
+
+
 def c1_bench(sty, repeats: int = 3):
     """End-to-end NL-PF render of the Cornell box workload: 256x256 px, 16 paths per pixel, vertex
     depths 0..5, reference-mode filter (radius 0.05 = 1 % of the box x 5, reuse 64, SMIS, clusters
@@ -320,7 +385,9 @@ def c5_bench(sty, W: int = 160, H: int = 90):
       nl_pf      reference-mode NL-PF at 64 spp (16 paths x 4 repeats, radius 1 % of the scene
                  extent, reuse 32, SMIS);
       nl_nrc_*   the NL-NRC loop (128 training iterations of 4 batches of 2^14, 16 first-hit
-                 passes) with the BF16 tcgen05 cache and with the FP32 cache."""
+                 passes) with the BF16 tcgen05 cache and with the FP32 cache (spherical-frequency
+                 network), and with the reference's own network (hash grid 22 x 4 on 2^19 tables +
+                 one-blob + identity, 5 x 128; rows in the reference layout)."""
     import numpy as np
     import torch
     a = sty.abi
@@ -360,6 +427,18 @@ def c5_bench(sty, W: int = 160, H: int = 90):
         res[name] = {"seconds": t, "training_rows": int(st.training_rows), "queries": int(st.inference_queries),
                      "image_mse": float(((img - ref) ** 2).mean())}
         net.close()
+    net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=8, batch_size=1 << 14, learning_rate=1e-2, seed=1))
+    cfg = sty.scene.nrc_render_config(max_depth=8, training_iters=128, batches_per_iter=4, repeats=16, seed=3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    film, st = sc.nrc_render(net, cfg, progs)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    img = film.cpu().numpy()
+    res["nl_nrc_ref_network"] = {"seconds": t, "training_rows": int(st.training_rows),
+                                 "queries": int(st.inference_queries), "params": net.param_count(),
+                                 "image_mse": float(((img - ref) ** 2).mean())}
+    net.close()
     res["reference_mean"] = float(ref.mean())
     sc.close()
     return res
@@ -409,6 +488,9 @@ def run(args):
         return
     if args.c1_only:  # profiling case: the end-to-end render alone
         print(json.dumps({"c1_render": c1_bench(sty, repeats=max(1, args.steps))}), flush=True)
+        return
+    if args.grid_only:  # the reference's NL-NRC network alone
+        print(json.dumps({"nrc_ref_network": grid_nrc_bench(sty, 32, max(3, args.warmup), dev, 1943.8)}), flush=True)
         return
     if args.c5_only:  # the full stylized render alone
         print(json.dumps({"c5_render": c5_bench(sty)}), flush=True)
@@ -571,6 +653,7 @@ def run(args):
         if p.exists():
             bf16_peak = float(json.loads(p.read_text())["bf16_tflops"])
         line["nrc"] = nrc_bench(sty, args.nrc_frames, max(3, args.warmup), dev, bf16_peak)
+        line["nrc_ref_network"] = grid_nrc_bench(sty, 32, max(3, args.warmup), dev, bf16_peak)
     if world == 1 and not args.no_cpu_baseline:
         import oracle as orc
         line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid, D_)
@@ -595,6 +678,7 @@ def main():
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
     ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
+    ap.add_argument("--grid-only", action="store_true", help="only the reference's NL-NRC network frames")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

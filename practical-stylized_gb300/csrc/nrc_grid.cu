@@ -6,14 +6,16 @@
 // Encoding (definitions restated from the published papers: tiny-cuda-nn is not available):
 //   hash grid: level l: s_l = N_min b^l - 1, r_l = ceil(s_l) + 1, u = clamp(x, 0, 1) s_l + 0.5,
 //     trilinear over the 8 corners of floor(u); as in tiny-cuda-nn, s_l is the FP32 evaluation
-//     exp2(l log2 b) N_min - 1 and u = fma(x, s_l, 0.5) in FP32; table T_l = min(roundup8(r_l^3), 2^log2T) entries
-//     of F features, dense index when r_l^3 <= T_l else (c.x ^ c.y 2654435761 ^ c.z 805459861) in
-//     32-bit arithmetic, both mod T_l. One thread per (sample, level); the backward scatters
-//     w * dL/dfeature into the FP32 table gradient with atomics.
+//     exp2(l log2 b) N_min - 1 and u = fma(x, s_l, 0.5) in FP32; table T_l = min(roundup8(r_l^3),
+//     2^log2T) entries of F features, dense index when r_l^3 <= T_l else (c.x ^ c.y 2654435761 ^
+//     c.z 805459861) in 32-bit arithmetic, both mod T_l. The forward reads FP16 copies of the
+//     tables; the backward scatters w * dL/dfeature into the FP32 table gradient with atomics.
 //   one-blob: bin k of B gets the mass of N(x, (1/B)^2) over [k/B, (k+1)/B] (erf).
-// MLP layers are plain BF16 GEMMs with FP32 accumulation (cuBLAS); ReLU, the ReLU mask, the loss
-// gradient and the BF16 packing are the kernels below. Activations are kept in BF16 for the
-// backward. Layout: rows are samples; encoded width padded to a multiple of 16, output padded to 8.
+// Inference (networks with H in {32, 64, 128}): k_grid_tiles writes the encoding as 128-row MMA
+// operand tiles, k_grid_mlp_tc runs every layer on the tensor cores with the weights in shared
+// memory. Training and other widths: the layer-by-layer path -- the encoding as row-major BF16
+// [rows][E] (k_grid_enc, k_blob_ident), each layer a BF16 GEMM with FP32 accumulation (cuBLAS),
+// ReLU / mask / loss-gradient kernels, BF16 activations kept for the backward; output padded to 8.
 #include <cublas_v2.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -97,12 +99,35 @@ __device__ __forceinline__ void level_cell(const GridGeo &g, int l, float x0, fl
         w[a] = u - f;
     }
 }
+// For F = 2 and 4 the two x-neighbours k, k + 1 are fetched as one aligned two-entry load whenever
+// they form such a pair (entries 2i and 2i + 1: a hashed level with c.x even always does, a dense
+// level half the time; level offsets are multiples of 8 entries), else as two loads. The gathers
+// are bound by L2 sector throughput, and this saves about a quarter of the sectors.
 template <int F>
 __device__ __forceinline__ void level_loads(const GridGeo &g, int l, const uint32_t (&c)[3],
                                             const __half *__restrict__ tab, RawEntry<F> (&e)[8]) {
+    if constexpr (F == 2 || F == 4) {
+        constexpr int kW = F / 2;
 #pragma unroll
-    for (int k = 0; k < 8; k++)
-        e[k] = load_entry<F>(tab + (size_t)grid_index(g, l, c[0] + (k & 1), c[1] + ((k >> 1) & 1), c[2] + (k >> 2)) * F);
+        for (int k = 0; k < 8; k += 2) {
+            const uint32_t cy = c[1] + ((k >> 1) & 1), cz = c[2] + (k >> 2);
+            const uint32_t i0 = grid_index(g, l, c[0], cy, cz), i1 = grid_index(g, l, c[0] + 1u, cy, cz);
+            const RawEntry<2 * F> p = load_entry<2 * F>(tab + (size_t)(i0 & ~1u) * F);
+            const bool hi = (i0 & 1u) != 0;  // i0 is the upper entry of the pair
+#pragma unroll
+            for (int w = 0; w < kW; w++) e[k].w[w] = hi ? p.w[kW + w] : p.w[w];
+            if ((i0 ^ i1) == 1u) {
+#pragma unroll
+                for (int w = 0; w < kW; w++) e[k + 1].w[w] = hi ? p.w[w] : p.w[kW + w];
+            } else {
+                e[k + 1] = load_entry<F>(tab + (size_t)i1 * F);
+            }
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            e[k] = load_entry<F>(tab + (size_t)grid_index(g, l, c[0] + (k & 1), c[1] + ((k >> 1) & 1), c[2] + (k >> 2)) * F);
+    }
 }
 template <int F>
 __device__ __forceinline__ void level_sum(const RawEntry<F> (&e)[8], const float (&w)[3], float (&acc)[F]) {
