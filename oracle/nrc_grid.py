@@ -116,3 +116,27 @@ def encode(x, tables, levels, feats, log2_table, base_res, per_level_scale, blob
     out = np.zeros((x.shape[0], out_width))
     out[:, :e.shape[1]] = e
     return out
+
+
+def adam_step(w, m, v, g, tsteps, n_mlp, t, lr, b1=0.9, b2=0.99, eps=1e-8):
+    """One optimiser step of the grid network, FP64: tiny-cuda-nn's Adam as the reference configures it
+    (nrc_pt.rs:1195-1213: Adam nested in ExponentialDecay; tiny-cuda-nn is the git submodule
+    shiinamiyuki/tiny-cuda-nn, branch `ema`, no commit pinned). Matrix parameters (the MLP weights,
+    p < n_mlp) take the step with the global step count t; a non-matrix parameter (table entry)
+    whose gradient is exactly zero is left as it is -- weight, moments and its own step count -- and
+    the others advance their own count t_p, which sets their bias correction:
+        m = b1 m + (1 - b1) g,  v = b2 v + (1 - b2) g^2,
+        w -= lr (m / (1 - b1^t)) / (sqrt(v / (1 - b2^t)) + eps).
+    Returns new (w, m, v, tsteps); tsteps covers the table entries only."""
+    w, m, v, g = (np.asarray(a, dtype=np.float64).copy() for a in (w, m, v, g))
+    tsteps = np.asarray(tsteps, dtype=np.int64).copy()
+    tp = np.full(w.shape, float(t))
+    upd = np.ones(w.shape, dtype=bool)
+    upd[n_mlp:] = g[n_mlp:] != 0.0
+    tsteps[upd[n_mlp:]] += 1
+    tp[n_mlp:] = tsteps
+    m[upd] = b1 * m[upd] + (1 - b1) * g[upd]
+    v[upd] = b2 * v[upd] + (1 - b2) * g[upd] ** 2
+    c1, c2 = 1 - b1 ** tp[upd], 1 - b2 ** tp[upd]
+    w[upd] -= lr * (m[upd] / c1) / (np.sqrt(v[upd] / c2) + eps)
+    return w, m, v, tsteps

@@ -541,6 +541,7 @@ sty_status sty_nrc_load_params(sty_nrc *nr, const float *host) {
     STY_TRY(check_cuda(cudaMemcpy(nr->w, host, nr->np * 4, cudaMemcpyHostToDevice), "load params"));
     STY_TRY(check_cuda(cudaMemcpy(nr->ema, host, nr->np * 4, cudaMemcpyHostToDevice), "load ema"));
     nr->img_dirty = true;
+    if (nr->grid) grid_params_changed(nr->grid);
     return STY_OK;
 }
 
@@ -563,6 +564,7 @@ sty_status sty_nrc_reset_optimizer(sty_nrc *nr) {
     STY_ARG_CHECK(nr, "sty_nrc_reset_optimizer: null nrc");
     STY_TRY(check_cuda(cudaMemset(nr->m, 0, nr->np * 4), "zero m"));
     STY_TRY(check_cuda(cudaMemset(nr->v, 0, nr->np * 4), "zero v"));
+    if (nr->grid) STY_TRY(grid_reset_steps(nr->grid));
     nr->step = 0;
     return STY_OK;
 }
@@ -615,10 +617,15 @@ sty_status sty_nrc_train(sty_nrc *nr, uint64_t count, uint64_t n_iters, const fl
         const float bc2 = (float)(1.0 - std::pow((double)c.beta2, t));
         const float ema_old = (float)(1.0 - std::pow((double)c.ema_decay, t - 1.0));
         const float ema_new = (float)(1.0 / (1.0 - std::pow((double)c.ema_decay, t)));
-        k_adam<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, nr->w, nr->m, nr->v, nr->g, nr->ema, lr_t,
-                                                                 c.beta1, c.beta2, c.epsilon, bc1, bc2, c.ema_decay,
-                                                                 ema_old, ema_new);
-        STY_TRY(check_launch("k_adam"));
+        if (nr->grid) {
+            STY_TRY(grid_adam(nr->grid, nr->w, nr->m, nr->v, nr->g, nr->ema, lr_t, c.beta1, c.beta2, c.epsilon, bc1,
+                              bc2, c.ema_decay, ema_old, ema_new, st));
+        } else {
+            k_adam<<<(unsigned)((nr->np + 255) / 256), 256, 0, st>>>(nr->np, nr->w, nr->m, nr->v, nr->g, nr->ema,
+                                                                     lr_t, c.beta1, c.beta2, c.epsilon, bc1, bc2,
+                                                                     c.ema_decay, ema_old, ema_new);
+            STY_TRY(check_launch("k_adam"));
+        }
         nr->img_dirty = true;
     }
     if (loss_out) {

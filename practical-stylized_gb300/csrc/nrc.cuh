@@ -66,6 +66,15 @@ sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_
 // cuBLAS layer-by-layer path
 sty_status grid_infer(GridModel *g, bool ema, bool allow_tc, uint64_t count, const float *in, float *out,
                       cudaStream_t st);
+// the optimiser step (tiny-cuda-nn's Adam: sparse over the tables, per-entry step counts) and the EMA;
+// keeps the FP16 table copy current
+sty_status grid_adam(GridModel *g, float *w, float *m, float *v, const float *grad, float *ema, float lr, float b1,
+                     float b2, float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new,
+                     cudaStream_t st);
+// the parameters were overwritten outside the optimiser (load): the FP16 table copy is stale
+void grid_params_changed(GridModel *g);
+// zero the tables' per-entry Adam step counts (optimiser reset)
+sty_status grid_reset_steps(GridModel *g);
 // loss and full parameter gradient of B rows with the current parameters (packed by grid_pack)
 sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, float *grad, float *loss,
                          cudaStream_t st);

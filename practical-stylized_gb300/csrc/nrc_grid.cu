@@ -159,6 +159,17 @@ __device__ __forceinline__ float blob_cdf(int k, int bins, float v) {
     const float inv = 1.0f / ((1.0f / bins) * 1.41421356237f);
     return 0.5f * (1.0f + erff(((float)k / bins - v) * inv));
 }
+// encoded value of non-grid column G + r of input row xs: one-blob bin, identity or padding
+__device__ __forceinline__ float extra_column(const GridGeo &g, int r, const float *xs) {
+    const int nblob = g.blob_dims * g.bins, nident = g.in_dims - 3 - g.blob_dims;
+    if (r < nblob) {
+        const float v = xs[3 + r / g.bins];
+        const int b = r % g.bins;
+        return blob_cdf(b + 1, g.bins, v) - blob_cdf(b, g.bins, v);
+    }
+    if (r < nblob + nident) return xs[3 + g.blob_dims + (r - nblob)];
+    return 0.0f;
+}
 
 // one thread per (sample, level): the level's F features into enc[s][l F ..]
 template <int F>
@@ -175,26 +186,19 @@ __global__ void k_grid_enc(uint64_t n, const float *__restrict__ x, GridGeo g, c
 #pragma unroll
     for (int f = 0; f < F; f++) o[f] = __float2bfloat16_rn(acc[f]);
 }
-// one thread per sample: one-blob bins, identity dims, zero padding
+// one thread per (row, non-grid column): one-blob bins, identity dims, zero padding; consecutive
+// threads write consecutive columns of a row
 __global__ void k_blob_ident(uint64_t n, const float *__restrict__ x, GridGeo g, __nv_bfloat16 *__restrict__ enc) {
-    const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const float *xs = x + s * g.in_dims;
-    __nv_bfloat16 *o = enc + s * g.out_w;
-    int k = g.levels * g.feats;
-    for (int d = 0; d < g.blob_dims; d++) {
-        const float v = xs[3 + d];
-        float prev = blob_cdf(0, g.bins, v);
-        for (int b = 0; b < g.bins; b++) {
-            const float cdf = blob_cdf(b + 1, g.bins, v);
-            o[k++] = __float2bfloat16_rn(cdf - prev);
-            prev = cdf;
-        }
-    }
-    for (int d = 3 + g.blob_dims; d < g.in_dims; d++) o[k++] = __float2bfloat16_rn(xs[d]);
-    for (; k < g.out_w; k++) o[k] = __float2bfloat16_rn(0.0f);
+    const int G = g.levels * g.feats, nx = g.out_w - G;
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t >= n * (uint64_t)nx) return;
+    const uint64_t s = t / (uint64_t)nx;
+    const int r = (int)(t % (uint64_t)nx);
+    enc[s * g.out_w + G + r] = __float2bfloat16_rn(extra_column(g, r, x + s * g.in_dims));
 }
-// the hash-grid part of the backward: gtab[entry][f] += w * denc[s][l F + f]
+// the hash-grid part of the backward: gtab[entry][f] += w * denc[s][l F + f], one vector atomic per
+// corner for F >= 2 (the table gradient starts at a multiple of 16 floats: n_mlp = H (E + ...))
+template <int F>
 __global__ void k_grid_bwd(uint64_t n, const float *__restrict__ x, GridGeo g, const float *__restrict__ denc,
                            float *__restrict__ gtab) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -204,28 +208,48 @@ __global__ void k_grid_bwd(uint64_t n, const float *__restrict__ x, GridGeo g, c
     const float *xs = x + s * g.in_dims;
     float w[3];
     uint32_t c[3];
-    for (int a = 0; a < 3; a++) {
-        const float u = fmaf(fminf(fmaxf(xs[a], 0.0f), 1.0f), g.scale[l], 0.5f);
-        const float f = floorf(u);
-        c[a] = (uint32_t)f;
-        w[a] = u - f;
-    }
-    const float *d = denc + s * g.out_w + (size_t)l * g.feats;
+    level_cell(g, l, xs[0], xs[1], xs[2], c, w);
+    float d[F];
+#pragma unroll
+    for (int f = 0; f < F; f++) d[f] = denc[s * g.out_w + (size_t)l * F + f];
+#pragma unroll
     for (int k = 0; k < 8; k++) {
-        const uint32_t ox = k & 1, oy = (k >> 1) & 1, oz = (k >> 2) & 1;
-        const float wt = (ox ? w[0] : 1.0f - w[0]) * (oy ? w[1] : 1.0f - w[1]) * (oz ? w[2] : 1.0f - w[2]);
-        float *e = gtab + (size_t)grid_index(g, l, c[0] + ox, c[1] + oy, c[2] + oz) * g.feats;
-        for (int f = 0; f < g.feats; f++) atomicAdd(e + f, wt * d[f]);
+        const float wt = ((k & 1) ? w[0] : 1.0f - w[0]) * (((k >> 1) & 1) ? w[1] : 1.0f - w[1]) *
+                         ((k >> 2) ? w[2] : 1.0f - w[2]);
+        float *e = gtab + (size_t)grid_index(g, l, c[0] + (k & 1), c[1] + ((k >> 1) & 1), c[2] + (k >> 2)) * F;
+        if constexpr (F == 4 || F == 8) {
+#pragma unroll
+            for (int h = 0; h < F / 4; h++)
+                atomicAdd(reinterpret_cast<float4 *>(e) + h,
+                          make_float4(wt * d[4 * h], wt * d[4 * h + 1], wt * d[4 * h + 2], wt * d[4 * h + 3]));
+        } else if constexpr (F == 2) {
+            atomicAdd(reinterpret_cast<float2 *>(e), make_float2(wt * d[0], wt * d[1]));
+        } else {
+            atomicAdd(e, wt * d[0]);
+        }
     }
 }
-__global__ void k_relu_bf16(size_t n, const float *__restrict__ z, __nv_bfloat16 *__restrict__ a) {
+// element-wise kernels, 8 elements per thread (n = rows x H, a multiple of 16)
+__global__ void k_relu_bf16(size_t n8, const float4 *__restrict__ z, uint4 *__restrict__ a) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = __float2bfloat16_rn(fmaxf(z[i], 0.0f));
+    if (i >= n8) return;
+    const float4 p = z[2 * i], q = z[2 * i + 1];
+    a[i] = make_uint4(pack2_relu_bf16(p.x, p.y), pack2_relu_bf16(p.z, p.w), pack2_relu_bf16(q.x, q.y),
+                      pack2_relu_bf16(q.z, q.w));
 }
-__global__ void k_mask_bf16(size_t n, const float *__restrict__ dh, const __nv_bfloat16 *__restrict__ act,
-                            __nv_bfloat16 *__restrict__ dp) {
+__device__ __forceinline__ float bf16_pos_sel(uint32_t act_half, float v) {  // v where the BF16 act > 0
+    return (act_half & 0x8000u) == 0u && (act_half & 0x7fffu) != 0u ? v : 0.0f;
+}
+__global__ void k_mask_bf16(size_t n8, const float4 *__restrict__ dh, const uint4 *__restrict__ act,
+                            uint4 *__restrict__ dp) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dp[i] = __float2bfloat16_rn(__bfloat162float(act[i]) > 0.0f ? dh[i] : 0.0f);
+    if (i >= n8) return;
+    const float4 p = dh[2 * i], q = dh[2 * i + 1];
+    const uint4 a = act[i];
+    dp[i] = make_uint4(pack2_bf16(bf16_pos_sel(a.x & 0xffffu, p.x), bf16_pos_sel(a.x >> 16, p.y)),
+                       pack2_bf16(bf16_pos_sel(a.y & 0xffffu, p.z), bf16_pos_sel(a.y >> 16, p.w)),
+                       pack2_bf16(bf16_pos_sel(a.z & 0xffffu, q.x), bf16_pos_sel(a.z >> 16, q.y)),
+                       pack2_bf16(bf16_pos_sel(a.w & 0xffffu, q.z), bf16_pos_sel(a.w >> 16, q.w)));
 }
 // relative L2 (prediction constant in the denominator): dP = 2 (p - t) / (p^2 + 0.01) / (B O)
 __global__ void k_rel_l2_grad(uint32_t B, int O, const float *__restrict__ pred, const float *__restrict__ tgt,
@@ -295,6 +319,45 @@ __global__ void k_tab_half(size_t n, const float *__restrict__ t, __half *__rest
     if (i < n) h[i] = __float2half_rn(t[i]);
 }
 
+// Optimiser step of the grid network: tiny-cuda-nn's Adam (the reference's "Adam" nested in
+// "ExponentialDecay", nrc_pt.rs:1195-1213) and the reference's EMA (akari_tcnn.cu:42-83).
+//   MLP weights (p < n_mlp): Adam with the global step t (bias corrections bc1 = 1 - b1^t,
+//     bc2 = 1 - b2^t).
+//   table entries: an entry whose gradient is exactly 0 this step keeps its weight, moments and
+//     step count (tiny-cuda-nn's rule for non-matrix parameters); the others advance their own step
+//     count t_p and use it in the bias correction. Updated entries refresh their FP16 copy.
+//   EMA over every parameter: ema = (ema d (1 - d^(t-1)) + w (1 - d)) / (1 - d^t).
+__global__ void k_adam_grid(size_t n_mlp, size_t np, float *__restrict__ w, float *__restrict__ m,
+                            float *__restrict__ v, const float *__restrict__ g, float *__restrict__ ema,
+                            uint32_t *__restrict__ tsteps, __half *__restrict__ tab16, float lr, float b1, float b2,
+                            float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new) {
+    const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (p >= np) return;
+    const float gr = g[p];
+    float wn = w[p];
+    float c1 = bc1, c2 = bc2;
+    bool step = true;
+    if (p >= n_mlp) {
+        step = gr != 0.0f;
+        if (step) {
+            const uint32_t tp = tsteps[p - n_mlp] + 1u;
+            tsteps[p - n_mlp] = tp;
+            c1 = 1.0f - powf(b1, (float)tp);
+            c2 = 1.0f - powf(b2, (float)tp);
+        }
+    }
+    if (step) {
+        const float mm = b1 * m[p] + (1.0f - b1) * gr;
+        const float vv = b2 * v[p] + (1.0f - b2) * gr * gr;
+        m[p] = mm;
+        v[p] = vv;
+        wn -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
+        w[p] = wn;
+        if (p >= n_mlp) tab16[p - n_mlp] = __float2half_rn(wn);
+    }
+    ema[p] = (ema[p] * ema_decay * ema_old + wn * (1.0f - ema_decay)) * ema_new;
+}
+
 // ---- tensor-core inference --------------------------------------------------------------------------
 // Two launches per chunk of rows:
 //   k_grid_tiles   the encoding, written straight into 128-row tile images in the MMA A-operand
@@ -343,17 +406,6 @@ __global__ void k_grid_img(int H, int L, int E, int O, const float *__restrict__
     img[base + kimg_off(n, k, K) / 2] = __bfloat16_as_ushort(__float2bfloat16_rn(v));
 }
 
-// encoded value of non-grid column G + r of input row xs: one-blob bin, identity or padding
-__device__ __forceinline__ float extra_column(const GridGeo &g, int r, const float *xs) {
-    const int nblob = g.blob_dims * g.bins, nident = g.in_dims - 3 - g.blob_dims;
-    if (r < nblob) {
-        const float v = xs[3 + r / g.bins];
-        const int b = r % g.bins;
-        return blob_cdf(b + 1, g.bins, v) - blob_cdf(b, g.bins, v);
-    }
-    if (r < nblob + nident) return xs[3 + g.blob_dims + (r - nblob)];
-    return 0.0f;
-}
 // block = one tile x one unit (blockIdx.x = tile * units + unit, so a tile's units run together
 // and its input rows are read while they are cached); rows >= count are written as zeros
 template <int F>
@@ -547,6 +599,8 @@ struct GridModel {
     std::vector<size_t> loff;  // FP32 offsets of W_0 .. W_L (W_L = output layer)
     __nv_bfloat16 *wb = nullptr, *wb_ema = nullptr;
     __half *tab16 = nullptr, *tab16_ema = nullptr;  // FP16 copies of the tables the forward reads
+    bool tab16_valid = false;     // tab16 == fp16(current tables) (kept by k_adam_grid)
+    uint32_t *tsteps = nullptr;   // per-entry Adam step counts of the tables
     // tensor-core inference (k_grid_tiles + k_grid_mlp_tc): BF16 weight images, the MMA kernel's
     // shared memory, the chunk's tile images
     bool tc = false;
@@ -623,7 +677,8 @@ sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const __half *
         default: k_grid_enc<8><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
     }
     STY_TRY(check_launch("k_grid_enc"));
-    k_blob_ident<<<(unsigned)((B + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->enc);
+    const uint64_t nx = B * (uint64_t)(g->E - g->geo.levels * g->geo.feats);
+    k_blob_ident<<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->enc);
     STY_TRY(check_launch("k_blob_ident"));
     const __nv_bfloat16 *a = g->enc;
     int K = g->E;
@@ -631,7 +686,9 @@ sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const __half *
         STY_TRY(gemm_fwd(g, (int)B, g->H, K, a, wb + g->loff[l], g->z));
         count_launch();
         __nv_bfloat16 *nx = g->acts + (size_t)l * B * g->H;
-        k_relu_bf16<<<(unsigned)((B * g->H + 255) / 256), 256, 0, st>>>(B * g->H, g->z, nx);
+        const size_t n8 = (size_t)B * g->H / 8;
+        k_relu_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->z),
+                                                                  reinterpret_cast<uint4 *>(nx));
         STY_TRY(check_launch("k_relu_bf16"));
         a = nx;
         K = g->H;
@@ -764,6 +821,8 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb_ema, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc bf16 ema");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16, g->n_tab * 2), "alloc fp16 tables");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16_ema, g->n_tab * 2), "alloc fp16 ema tables");
+    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tsteps, g->n_tab * 4), "alloc table step counts");
+    if (s == STY_OK) s = check_cuda(cudaMemset(g->tsteps, 0, g->n_tab * 4), "zero table step counts");
     if (s == STY_OK && g->tc) s = check_cuda(cudaMalloc(&g->img, g->img_elems * 2), "alloc weight images");
     if (s == STY_OK && g->tc) s = check_cuda(cudaMalloc(&g->img_ema, g->img_elems * 2), "alloc ema images");
     if (s != STY_OK) {
@@ -776,7 +835,7 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
 
 void grid_destroy(GridModel *g) {
     if (!g) return;
-    void *ptrs[] = {g->wb, g->wb_ema, g->tab16, g->tab16_ema, g->img, g->img_ema, g->tiles, g->enc,
+    void *ptrs[] = {g->wb, g->wb_ema, g->tab16, g->tab16_ema, g->tsteps, g->img, g->img_ema, g->tiles, g->enc,
                     g->acts, g->dp, g->z, g->dh, g->d_fan_in, g->d_fan_out, g->d_loff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -803,6 +862,7 @@ sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t 
                                        cudaMemcpyHostToDevice, st),
                        "upload offsets"));
     const size_t n = g->n_mlp + g->n_tab;
+    g->tab16_valid = false;
     k_grid_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->n_mlp, n, g->d_fan_in, g->d_fan_out, g->d_loff,
                                                              g->L + 1, seed, w);
     return check_launch("k_grid_init");
@@ -813,8 +873,11 @@ sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_
     const unsigned tblocks = (unsigned)((g->n_tab + 255) / 256);
     k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, w, g->wb);
     STY_TRY(check_launch("k_weights_bf16"));
-    k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, w + g->n_mlp, g->tab16);
-    STY_TRY(check_launch("k_tab_half"));
+    if (!g->tab16_valid) {
+        k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, w + g->n_mlp, g->tab16);
+        STY_TRY(check_launch("k_tab_half"));
+        g->tab16_valid = true;
+    }
     if (!ema) return STY_OK;
     // the inference set: EMA copies and the tensor-core weight images of both parameter sets
     k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema,
@@ -866,7 +929,10 @@ sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *
     STY_TRY(gemm_dx(g, (int)B, kOpad, g->H, g->dp, g->wb + g->out_off, g->dh));
     count_launch();
     __nv_bfloat16 *dp = g->dp;
-    k_mask_bf16<<<(unsigned)(((size_t)B * g->H + 255) / 256), 256, 0, st>>>((size_t)B * g->H, g->dh, aL, dp);
+    const size_t n8 = (size_t)B * g->H / 8;
+    k_mask_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->dh),
+                                                              reinterpret_cast<const uint4 *>(aL),
+                                                              reinterpret_cast<uint4 *>(dp));
     STY_TRY(check_launch("k_mask_bf16"));
     for (int l = g->L - 1; l >= 0; l--) {
         const __nv_bfloat16 *al = l == 0 ? g->enc : g->acts + (size_t)(l - 1) * B * g->H;
@@ -876,15 +942,39 @@ sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *
         STY_TRY(gemm_dx(g, (int)B, g->H, K, dp, g->wb + g->loff[l], g->dh));
         count_launch();
         if (l > 0) {
-            k_mask_bf16<<<(unsigned)(((size_t)B * g->H + 255) / 256), 256, 0, st>>>((size_t)B * g->H, g->dh, al, dp);
+            k_mask_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->dh),
+                                                                      reinterpret_cast<const uint4 *>(al),
+                                                                      reinterpret_cast<uint4 *>(dp));
             STY_TRY(check_launch("k_mask_bf16"));
         }
     }
     // g->dh now holds dLoss/dencoding (B x E): the tables' gradient
     STY_TRY(check_cuda(cudaMemsetAsync(grad + g->n_mlp, 0, g->n_tab * 4, st), "zero table gradient"));
     const uint64_t nl = (uint64_t)B * g->geo.levels;
-    k_grid_bwd<<<(unsigned)((nl + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->dh, grad + g->n_mlp);
+    const unsigned blocks = (unsigned)((nl + 255) / 256);
+    float *gtab = grad + g->n_mlp;
+    switch (g->geo.feats) {
+        case 1: k_grid_bwd<1><<<blocks, 256, 0, st>>>(B, x, g->geo, g->dh, gtab); break;
+        case 2: k_grid_bwd<2><<<blocks, 256, 0, st>>>(B, x, g->geo, g->dh, gtab); break;
+        case 4: k_grid_bwd<4><<<blocks, 256, 0, st>>>(B, x, g->geo, g->dh, gtab); break;
+        default: k_grid_bwd<8><<<blocks, 256, 0, st>>>(B, x, g->geo, g->dh, gtab); break;
+    }
     return check_launch("k_grid_bwd");
+}
+
+void grid_params_changed(GridModel *g) { g->tab16_valid = false; }
+
+sty_status grid_reset_steps(GridModel *g) {
+    return check_cuda(cudaMemset(g->tsteps, 0, g->n_tab * 4), "zero table step counts");
+}
+
+sty_status grid_adam(GridModel *g, float *w, float *m, float *v, const float *grad, float *ema, float lr, float b1,
+                     float b2, float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new,
+                     cudaStream_t st) {
+    const size_t np = g->n_mlp + g->n_tab;
+    k_adam_grid<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(g->n_mlp, np, w, m, v, grad, ema, g->tsteps, g->tab16,
+                                                              lr, b1, b2, eps, bc1, bc2, ema_decay, ema_old, ema_new);
+    return check_launch("k_adam_grid");
 }
 
 }  // namespace sty

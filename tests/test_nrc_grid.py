@@ -193,6 +193,58 @@ def test_grid_gradient_matches_emulation(sty, cuda):
     assert loss == pytest.approx(float(((pred - t) ** 2 / den).mean()), rel=1e-2)
 
 
+def test_oracle_adam_sparse_rule():
+    """Table entries with a zero gradient keep weight, moments and step count; the others use their
+    own step count in the bias correction."""
+    n_mlp = 2
+    w = np.array([1.0, 2.0, 3.0, 4.0, 5.0])
+    z = np.zeros(5)
+    g = np.array([0.5, 0.0, 0.25, 0.0, -1.0])
+    w1, m1, v1, ts = og.adam_step(w, z, z, g, np.zeros(3), n_mlp, t=1, lr=0.1)
+    assert w1[1] == 2.0 - 0.0 and m1[1] == 0.0  # MLP weight with a zero gradient still steps (by 0)
+    assert w1[3] == 4.0 and m1[3] == 0.0 and list(ts) == [1, 0, 1]
+    assert w1[0] == pytest.approx(1.0 - 0.1) and w1[4] == pytest.approx(5.0 + 0.1)  # |step| = lr at t = 1
+    # second step: entry 3 gets its first update (t_p = 1) while the MLP is at t = 2
+    g2 = np.array([0.5, 0.0, 0.0, 2.0, 0.0])
+    w2, m2, v2, ts2 = og.adam_step(w1, m1, v1, g2, ts, n_mlp, t=2, lr=0.1)
+    assert w2[3] == pytest.approx(4.0 - 0.1) and w2[2] == w1[2] and w2[4] == w1[4] and list(ts2) == [1, 1, 1]
+
+
+@pytest.mark.gpu
+def test_grid_optimiser_matches_oracle(sty, cuda):
+    """One training step on a batch of identical rows (so batch sampling cannot matter) against the
+    oracle's Adam on the same gradient; then a step on another row, after which the table entries
+    only the first row touched are bit-identical (a dense Adam would move them by momentum)."""
+    c = dict(SMALL)
+    lr = 1e-2
+    net = sty.nrc.NRC(sty.nrc.grid_config(batch_size=128, seed=4, learning_rate=lr, **c))
+    rng = np.random.default_rng(8)
+    xa, xb = _rows(rng, 1, c), _rows(rng, 1, c)
+    ta, tb = rng.random((1, 3)) + 0.2, rng.random((1, 3)) + 0.2
+    XA, TA = _dev(np.repeat(xa, 128, 0)), _dev(np.repeat(ta, 128, 0))
+    XB, TB = _dev(np.repeat(xb, 128, 0)), _dev(np.repeat(tb, 128, 0))
+    p0 = net.save_params().astype(np.float64)
+    n_tab = _split(p0, c)[1].size
+    n_mlp = p0.size - n_tab
+    ga = net.gradient(XA, TA)[0].cpu().numpy().astype(np.float64)
+    net.train(XA, TA, 1)
+    p1 = net.save_params().astype(np.float64)
+    z = np.zeros_like(p0)
+    w1, m1, v1, ts1 = og.adam_step(p0, z, z, ga, np.zeros(n_tab), n_mlp, t=1, lr=lr)
+    touched_a = ga[n_mlp:] != 0
+    assert touched_a.sum() > 0 and (~touched_a).sum() > 0
+    np.testing.assert_allclose(p1, w1, rtol=2e-5, atol=1e-7)
+    gb = net.gradient(XB, TB)[0].cpu().numpy().astype(np.float64)
+    net.train(XB, TB, 1)
+    p2 = net.save_params().astype(np.float64)
+    w2, _, _, _ = og.adam_step(w1, m1, v1, gb, ts1, n_mlp, t=2, lr=lr)
+    only_a = touched_a & (gb[n_mlp:] == 0)
+    assert only_a.sum() > 0
+    assert np.array_equal(p2[n_mlp:][only_a], p1[n_mlp:][only_a])
+    np.testing.assert_allclose(p2, w2, rtol=5e-5, atol=1e-7)
+    net.close()
+
+
 @pytest.mark.gpu
 def test_grid_training_reduces_loss(sty, cuda):
     net, c = _net(sty, seed=7, batch=4096, learning_rate=1e-2)
