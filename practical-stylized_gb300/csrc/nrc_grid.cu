@@ -368,18 +368,20 @@ __global__ void k_adam_grid(size_t n_mlp, size_t np, float *__restrict__ w, floa
 //                  the MMA kernel, whose weights fill shared memory.
 //   k_grid_mlp_tc  one persistent CTA per SM holding every layer's weights as BF16 operand images
 //                  (W_0: H x E, W_1..W_{L-1}: H x H, W_out: 16 x H with rows >= O zero) and one
-//                  activation image. Warps 0-3: per layer thread 0 issues K/16 x tcgen05.mma (M=128,
-//                  N=H or 16, K=16) and commits to `bar_mma`; the warpgroup waits (bounded),
-//                  tcgen05.ld's its rows, applies ReLU, converts to BF16 and writes them back as the
-//                  next layer's A operand; after the output layer's MMA the image is released
-//                  (`bar_free`) and the output columns are read. Warps 4-11 copy the next tile's
-//                  image from global memory into registers while the current tile's layers run, then
-//                  store it once `bar_free` completes and arrive on `bar_full`.
+//                  activation image. Warps 0-7: per layer thread 0 issues K/16 x tcgen05.mma (M=128,
+//                  N=H or 16, K=16) and commits to `bar_mma`; the warps wait (bounded), tcgen05.ld
+//                  their rows (TMEM lane quarter warp % 4) and column half (warp / 4), apply ReLU,
+//                  convert to BF16 and write them back as the next layer's A operand; after the
+//                  output layer's MMA the image is released (`bar_free`) and warps 0-3 read the
+//                  output columns. Warps 8-15 copy the next tile's image from global memory into
+//                  registers while the current tile's layers run, then store it once `bar_free`
+//                  completes and arrive on `bar_full`.
 // Every wait is bounded: on a timeout the kernel sets STY_DEV_WAIT_TIMEOUT, waits once more for an
 // MMA still in flight, frees its TMEM columns and returns.
 constexpr int kTM = 128;
+constexpr int kEpiThreads = 256;  // two warpgroups: TMEM lane quarter = warp % 4, column half = warp / 4
 constexpr int kCopyThreads = 256;
-constexpr int kMlpThreads = 128 + kCopyThreads;
+constexpr int kMlpThreads = kEpiThreads + kCopyThreads;
 constexpr int kMaxE = 160;  // encoded width the copy warps stage (10 x 16 bytes per thread)
 constexpr int kCopyChunks = kTM * kMaxE * 2 / 16 / kCopyThreads;
 constexpr int kOutN = 16;
@@ -408,9 +410,11 @@ __global__ void k_grid_img(int H, int L, int E, int O, const float *__restrict__
 
 // block = one tile x one unit (blockIdx.x = tile * units + unit, so a tile's units run together
 // and its input rows are read while they are cached); rows >= count are written as zeros
+// vec_x: every row starts 16-byte aligned (the host checks the pointer and in_dims % 4)
 template <int F>
 __global__ void __launch_bounds__(kTM) k_grid_tiles(uint64_t count, const float *__restrict__ x, GridGeo g,
-                                                    int units, const __half *__restrict__ tab, uint8_t *__restrict__ img) {
+                                                    int units, int vec_x, const __half *__restrict__ tab,
+                                                    uint8_t *__restrict__ img) {
     const uint32_t m = threadIdx.x;
     const uint64_t tile = blockIdx.x / (uint32_t)units;
     const int v = (int)(blockIdx.x % (uint32_t)units);
@@ -423,7 +427,22 @@ __global__ void __launch_bounds__(kTM) k_grid_tiles(uint64_t count, const float 
         float acc[F];
 #pragma unroll
         for (int f = 0; f < F; f++) acc[f] = 0.0f;
-        if (valid) gather_level<F>(g, v, xs[0], xs[1], xs[2], tab, acc);
+        if (valid) {
+            // the divergent loads are what bound this kernel (L1): the position in one request
+            // when rows are 16-byte aligned
+            float p0, p1, p2;
+            if (vec_x) {
+                const float4 p = __ldg(reinterpret_cast<const float4 *>(xs));
+                p0 = p.x;
+                p1 = p.y;
+                p2 = p.z;
+            } else {
+                p0 = xs[0];
+                p1 = xs[1];
+                p2 = xs[2];
+            }
+            gather_level<F>(g, v, p0, p1, p2, tab, acc);
+        }
         uint8_t *p = t + kimg_off(m, (uint32_t)(v * F), E);
         if constexpr (F == 1) {
             *reinterpret_cast<unsigned short *>(p) = __bfloat16_as_ushort(__float2bfloat16_rn(acc[0]));
@@ -495,16 +514,17 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs
     const uint32_t tmem = tmem_slot;
     const uint64_t ntiles = (a.count + kTM - 1) / kTM;
 
-    if (warp < 4) {
+    if (tid < kEpiThreads) {
         // ---- MMA issue + epilogue ----
-        const uint32_t t = (uint32_t)tid;
-        const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
+        const uint32_t t = (uint32_t)(tid & 127), half = (uint32_t)(warp >> 2);
+        const uint32_t lane_base = tmem + (((uint32_t)(warp & 3) * 32u) << 16);
         const uint32_t wbase = smem_u32(smem), abase = smem_u32(act);
+        const uint32_t hc = (uint32_t)H / 2u, c_lo = half * hc;  // this warp's columns
         uint32_t phase = 0, it = 0;
         bool failed = false, pending = false;
         for (uint64_t tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x, it++) {
             const bool got = mbar_wait(&bar_full, it & 1u, a.status);
-            if (!wg_sync_and(1, got)) {
+            if (!bar_and_n(1, kEpiThreads, got)) {
                 failed = true;
                 break;
             }
@@ -512,7 +532,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs
             for (int l = 0; l <= L; l++) {
                 const bool out_layer = l == L;
                 const uint32_t K = l == 0 ? (uint32_t)E : (uint32_t)H;
-                if (t == 0) {
+                if (tid == 0) {
                     fence_after();
                     const uint32_t wl = wbase + (uint32_t)img_layer(l, H, E) * 2u;
                     const uint32_t idesc = out_layer ? idesc_bf16(kTM, kOutN) : idesc_bf16(kTM, (uint32_t)H);
@@ -523,7 +543,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs
                 }
                 pending = true;
                 const bool ok = mbar_wait(&bar_mma, phase, a.status);
-                if (!wg_sync_and(1, ok)) {
+                if (!bar_and_n(1, kEpiThreads, ok)) {
                     failed = true;
                     break;
                 }
@@ -531,12 +551,12 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs
                 phase ^= 1u;
                 fence_after();
                 if (!out_layer) {
-                    for (uint32_t c = 0; c < (uint32_t)H; c += 32u) {
-                        float v[32];
-                        tmem_ld32(lane_base + c, v);
+                    for (uint32_t c = c_lo; c < c_lo + hc; c += 16u) {
+                        float v[16];
+                        tmem_ld16(lane_base + c, v);
                         tmem_wait_ld();
 #pragma unroll
-                        for (int kb = 0; kb < 4; kb++) {
+                        for (int kb = 0; kb < 2; kb++) {
                             const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
                                                        pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
                                                        pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
@@ -546,21 +566,23 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_grid_mlp_tc(const GridTcArgs
                     }
                     fence_async_smem();
                 } else {
-                    if (t == 0) mbar_arrive(&bar_free);  // the output MMA has read the last activations
-                    float v[16];
-                    tmem_ld16(lane_base, v);
-                    tmem_wait_ld();
-                    if (row < a.count)
-                        for (int c = 0; c < a.O; c++) a.output[row * a.O + c] = v[c];
+                    if (tid == 0) mbar_arrive(&bar_free);  // the output MMA has read the last activations
+                    if (half == 0) {
+                        float v[16];
+                        tmem_ld16(lane_base, v);
+                        tmem_wait_ld();
+                        if (row < a.count)
+                            for (int c = 0; c < a.O; c++) a.output[row * a.O + c] = v[c];
+                    }
                 }
                 fence_before();
-                wg_sync(1);
+                bar_sync_n(1, kEpiThreads);
             }
         }
         if (failed && pending) mbar_wait(&bar_mma, phase, a.status);
     } else {
         // ---- copy warps: the next tile's image through registers ----
-        const uint32_t e = (uint32_t)(tid - 128);
+        const uint32_t e = (uint32_t)(tid - kEpiThreads);
         const uint32_t chunks = (uint32_t)(kTM * E * 2) / 16u;  // 16-byte chunks per tile image
         uint32_t it = 0;
         for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++) {
@@ -735,11 +757,12 @@ sty_status grid_tc_forward(GridModel *g, bool ema, uint64_t count, const float *
         const uint64_t ntiles = (B + kTM - 1) / kTM;
         const float *x = in + b0 * g->geo.in_dims;
         const unsigned blocks = (unsigned)(ntiles * (uint64_t)units);
+        const int vx = (g->geo.in_dims % 4 == 0 && reinterpret_cast<uintptr_t>(x) % 16 == 0) ? 1 : 0;
         switch (g->geo.feats) {
-            case 1: k_grid_tiles<1><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
-            case 2: k_grid_tiles<2><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
-            case 4: k_grid_tiles<4><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
-            default: k_grid_tiles<8><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, tab, g->tiles); break;
+            case 1: k_grid_tiles<1><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, vx, tab, g->tiles); break;
+            case 2: k_grid_tiles<2><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, vx, tab, g->tiles); break;
+            case 4: k_grid_tiles<4><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, vx, tab, g->tiles); break;
+            default: k_grid_tiles<8><<<blocks, kTM, 0, st>>>(B, x, g->geo, units, vx, tab, g->tiles); break;
         }
         STY_TRY(check_launch("k_grid_tiles"));
         a.count = B;

@@ -104,6 +104,20 @@ __device__ __forceinline__ uint32_t pack2_relu_bf16(float lo, float hi) {  // ma
     asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
     return r;
 }
+// named barrier over n threads (id 0 is __syncthreads), and its AND-reduction form
+__device__ __forceinline__ void bar_sync_n(uint32_t id, uint32_t n) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+__device__ __forceinline__ bool bar_and_n(uint32_t id, uint32_t n, bool p) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred pi, po;\n\tsetp.ne.u32 pi, %1, 0;\n\tbar.red.and.pred po, %2, %3, pi;\n\t"
+        "selp.u32 %0, 1, 0, po;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)p), "r"(id), "r"(n)
+        : "memory");
+    return r != 0;
+}
 // per-warpgroup named barriers (id 1 + warpgroup; id 0 is __syncthreads)
 __device__ __forceinline__ void wg_sync(uint32_t id) { asm volatile("bar.sync %0, 128;" ::"r"(id) : "memory"); }
 __device__ __forceinline__ bool wg_sync_and(uint32_t id, bool p) {
