@@ -490,7 +490,8 @@ def run(args):
         print(json.dumps({"c1_render": c1_bench(sty, repeats=max(1, args.steps))}), flush=True)
         return
     if args.grid_only:  # the reference's NL-NRC network alone
-        print(json.dumps({"nrc_ref_network": grid_nrc_bench(sty, 32, max(3, args.warmup), dev, 1943.8)}), flush=True)
+        print(json.dumps({"nrc_ref_network": grid_nrc_bench(sty, args.grid_frames, max(3, args.warmup), dev, 1943.8)}),
+              flush=True)
         return
     if args.c5_only:  # the full stylized render alone
         print(json.dumps({"c5_render": c5_bench(sty)}), flush=True)
@@ -653,7 +654,7 @@ def run(args):
         if p.exists():
             bf16_peak = float(json.loads(p.read_text())["bf16_tflops"])
         line["nrc"] = nrc_bench(sty, args.nrc_frames, max(3, args.warmup), dev, bf16_peak)
-        line["nrc_ref_network"] = grid_nrc_bench(sty, 32, max(3, args.warmup), dev, bf16_peak)
+        line["nrc_ref_network"] = grid_nrc_bench(sty, args.grid_frames, max(3, args.warmup), dev, bf16_peak)
     if world == 1 and not args.no_cpu_baseline:
         import oracle as orc
         line["cpu_baseline"] = cpu_baseline(sty, orc, planes, valid, D_)
@@ -679,6 +680,7 @@ def main():
     ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
     ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
     ap.add_argument("--grid-only", action="store_true", help="only the reference's NL-NRC network frames")
+    ap.add_argument("--grid-frames", type=int, default=32, help="frames of the reference's NL-NRC network")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -326,11 +326,13 @@ __global__ void k_tab_half(size_t n, const float *__restrict__ t, __half *__rest
 //   table entries: an entry whose gradient is exactly 0 this step keeps its weight, moments and
 //     step count (tiny-cuda-nn's rule for non-matrix parameters); the others advance their own step
 //     count t_p and use it in the bias correction. Updated entries refresh their FP16 copy.
-//   EMA over every parameter: ema = (ema d (1 - d^(t-1)) + w (1 - d)) / (1 - d^t).
+//   EMA over every parameter: ema = (ema d (1 - d^(t-1)) + w (1 - d)) / (1 - d^t), with the FP16
+//     copy of the EMA tables written in place.
 __global__ void k_adam_grid(size_t n_mlp, size_t np, float *__restrict__ w, float *__restrict__ m,
                             float *__restrict__ v, const float *__restrict__ g, float *__restrict__ ema,
-                            uint32_t *__restrict__ tsteps, __half *__restrict__ tab16, float lr, float b1, float b2,
-                            float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new) {
+                            uint32_t *__restrict__ tsteps, __half *__restrict__ tab16, __half *__restrict__ tab16_ema,
+                            float lr, float b1, float b2, float eps, float bc1, float bc2, float ema_decay,
+                            float ema_old, float ema_new) {
     const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (p >= np) return;
     const float gr = g[p];
@@ -355,7 +357,9 @@ __global__ void k_adam_grid(size_t n_mlp, size_t np, float *__restrict__ w, floa
         w[p] = wn;
         if (p >= n_mlp) tab16[p - n_mlp] = __float2half_rn(wn);
     }
-    ema[p] = (ema[p] * ema_decay * ema_old + wn * (1.0f - ema_decay)) * ema_new;
+    const float e = (ema[p] * ema_decay * ema_old + wn * (1.0f - ema_decay)) * ema_new;
+    ema[p] = e;
+    if (p >= n_mlp) tab16_ema[p - n_mlp] = __float2half_rn(e);
 }
 
 // ---- tensor-core inference --------------------------------------------------------------------------
@@ -622,6 +626,7 @@ struct GridModel {
     __nv_bfloat16 *wb = nullptr, *wb_ema = nullptr;
     __half *tab16 = nullptr, *tab16_ema = nullptr;  // FP16 copies of the tables the forward reads
     bool tab16_valid = false;     // tab16 == fp16(current tables) (kept by k_adam_grid)
+    bool tab16_ema_valid = false; // tab16_ema == fp16(EMA tables) (kept by k_adam_grid)
     uint32_t *tsteps = nullptr;   // per-entry Adam step counts of the tables
     // tensor-core inference (k_grid_tiles + k_grid_mlp_tc): BF16 weight images, the MMA kernel's
     // shared memory, the chunk's tile images
@@ -885,7 +890,7 @@ sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t 
                                        cudaMemcpyHostToDevice, st),
                        "upload offsets"));
     const size_t n = g->n_mlp + g->n_tab;
-    g->tab16_valid = false;
+    g->tab16_valid = g->tab16_ema_valid = false;
     k_grid_init<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(g->n_mlp, n, g->d_fan_in, g->d_fan_out, g->d_loff,
                                                              g->L + 1, seed, w);
     return check_launch("k_grid_init");
@@ -906,8 +911,11 @@ sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_
     k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema,
                                                                      g->wb_ema);
     STY_TRY(check_launch("k_weights_bf16"));
-    k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, ema + g->n_mlp, g->tab16_ema);
-    STY_TRY(check_launch("k_tab_half"));
+    if (!g->tab16_ema_valid) {
+        k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, ema + g->n_mlp, g->tab16_ema);
+        STY_TRY(check_launch("k_tab_half"));
+        g->tab16_ema_valid = true;
+    }
     if (g->tc) {
         const dim3 grid((unsigned)(((size_t)g->H * std::max(g->E, g->H) + 255) / 256), (unsigned)(g->L + 1));
         k_grid_img<<<grid, 256, 0, st>>>(g->H, g->L, g->E, g->O, w, g->img);
@@ -985,7 +993,7 @@ sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *
     return check_launch("k_grid_bwd");
 }
 
-void grid_params_changed(GridModel *g) { g->tab16_valid = false; }
+void grid_params_changed(GridModel *g) { g->tab16_valid = g->tab16_ema_valid = false; }
 
 sty_status grid_reset_steps(GridModel *g) {
     return check_cuda(cudaMemset(g->tsteps, 0, g->n_tab * 4), "zero table step counts");
@@ -996,7 +1004,8 @@ sty_status grid_adam(GridModel *g, float *w, float *m, float *v, const float *gr
                      cudaStream_t st) {
     const size_t np = g->n_mlp + g->n_tab;
     k_adam_grid<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(g->n_mlp, np, w, m, v, grad, ema, g->tsteps, g->tab16,
-                                                              lr, b1, b2, eps, bc1, bc2, ema_decay, ema_old, ema_new);
+                                                              g->tab16_ema, lr, b1, b2, eps, bc1, bc2, ema_decay,
+                                                              ema_old, ema_new);
     return check_launch("k_adam_grid");
 }
 
