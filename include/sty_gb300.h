@@ -528,6 +528,38 @@ STY_API sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_
                                   const sty_style_program *programs, uint32_t n_programs, double *film,
                                   sty_nrc_render_stats *stats, void *stream);
 
+/* Branching path tracer (crates/akari_integrator/src/branching_pt.rs, Config :77-100): the paper's
+ * BrPT baseline, and with inner_samples = {1} the plain stylized path tracer of
+ * configs/teaser/pt.json. Per pixel a tree of vertices: the k-th rough vertex (average roughness
+ * > 0.01) of a path takes inner_samples[k] branches (1 beyond n_levels, 1 at smooth vertices, none
+ * at max_depth), each one light sample + one BSDF-sampled child; bottom-up a vertex's radiance is
+ * style(Le + mean over branches of (direct + throughput * child radiance * child emission MIS)),
+ * the depth-0 radiance is the pixel sample (the non-debiased estimator; the jackknife / Russian-
+ * roulette debiasing option is not built). Pixels go through in passes whose worst-case vertex
+ * trees fit vram_mb (100 bytes per vertex slot). Adds (1/repeats) of each pixel's sample into
+ * `film` (device, width*height*3 doubles; the caller zeroes it). `programs` is a HOST array.
+ * Sampling keys on (seed, repeat, pixel) and, per child, on (parent, branch index): the image does
+ * not depend on vram_mb. Deterministic. */
+#define STY_BRPT_MAX_LEVELS 8
+typedef struct sty_brpt_config {
+    uint32_t max_depth;                          /* Config::max_depth (reference default 7) */
+    uint32_t n_levels;                           /* entries of inner_samples used, 1..8 */
+    uint32_t inner_samples[STY_BRPT_MAX_LEVELS]; /* Config::inner_samples (default 256, 32, 8, 1) */
+    uint32_t repeats;                            /* Config::repeats */
+    uint32_t vram_mb;                            /* Config::vram: vertex-tree budget per pass, MB */
+    uint64_t seed;
+} sty_brpt_config;
+typedef struct sty_brpt_stats {
+    uint64_t vertices;        /* surface hits (tree vertices) over all passes and repeats */
+    uint64_t slots;           /* vertex slots (hits + branches whose ray missed) */
+    uint64_t passes;          /* pixel passes over all repeats */
+    uint64_t pixels_per_pass;
+    uint64_t max_pass_slots;
+} sty_brpt_stats;
+STY_API sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *config,
+                                   const sty_style_program *programs, uint32_t n_programs, double *film,
+                                   sty_brpt_stats *stats, void *stream);
+
 /* ----------------------------------------------------------------------------------------
  * Integer helpers (bit-exact with the reference)
  * -------------------------------------------------------------------------------------- */

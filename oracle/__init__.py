@@ -40,6 +40,8 @@ def lib() -> C.CDLL:
         L.orc_pf_adjoint_image_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
         L.orc_closest_hit.argtypes = [vp, C.c_uint32, vp, C.c_uint64, vp, vp, vp]
         L.orc_path_trace.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, vp]
+        L.orc_brpt.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint32, C.c_uint32,
+                               C.c_uint64, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
@@ -171,6 +173,26 @@ def path_trace(tri_pos, mat_ids, albedo, emission, cam, spp: int, max_depth: int
     W, H = int(c[10]), int(c[11])
     img = np.zeros((H, W, 3), dtype=np.float64)
     lib().orc_path_trace(_p(pos), _p(m), m.size, _p(alb), _p(em), _p(c), spp, max_depth, seed, _p(img))
+    return img
+
+
+def brpt(tri_pos, mat_ids, materials, cam, programs, max_depth: int, inner_samples, repeats: int = 1,
+         seed: int = 0):
+    """Recursive FP64 branching path tracer on the same sampling keys as sty_brpt_render (diffuse
+    surfaces) -> image [H, W, 3]. `materials` is a ctypes array of sty_scene_material, `programs` a
+    sequence of sty_style_program, cam = (eye3, target3, up3, fov_y, W, H, filter_radius)."""
+    pos = np.ascontiguousarray(tri_pos, dtype=np.float32).reshape(-1)
+    m = np.ascontiguousarray(mat_ids, dtype=np.uint32)
+    c = np.ascontiguousarray(cam, dtype=np.float32)
+    inner = np.ascontiguousarray(inner_samples, dtype=np.uint32)
+    progs = list(programs)
+    parr = None
+    if progs:
+        parr = (type(progs[0]) * len(progs))(*progs)
+    W, H = int(c[10]), int(c[11])
+    img = np.zeros((H, W, 3), dtype=np.float64)
+    lib().orc_brpt(_p(pos), _p(m), m.size, C.addressof(materials), _p(c), None if parr is None else C.addressof(parr),
+                   len(progs), max_depth, _p(inner), inner.size, repeats, seed, _p(img))
     return img
 
 

@@ -929,3 +929,267 @@ extern "C" void orc_path_trace(const float *pos, const uint32_t *mat, uint32_t n
             for (int c = 0; c < 3; c++) img[3 * ((size_t)py * W + px) + c] = acc[c] / spp;
         }
 }
+
+// ---- branching path tracer (branching_pt.rs), recursive FP64 restatement -------------------------
+// Test infrastructure for sty_brpt_render: the same tree (inner_samples at the k-th rough vertex,
+// 1 at smooth vertices, none at max_depth), the same estimator (style(Le + mean over branches of
+// (direct + throughput * child radiance * child emission MIS))), the same sampling keys (camera on
+// (seed, repeat, pixel), children on (parent key, branch)) and draws (2 camera; per branch 3 light
+// + 3 BSDF, float u = u32 * 2^-32 as IndependentSampler::next_1d), the same light CDF (FP32
+// luminance x area) and sampling maps (uniform_sample_triangle, polar disk -> cosine hemisphere in
+// the frame of frame_from_n). Diffuse surfaces only; FP64 geometry and brute-force FP64 hits, so a
+// ray grazing an edge can hit differently than the GPU's FP32 BVH.
+namespace {
+inline uint64_t smix64(uint64_t x) {
+    x += 0x9e3779b97f4a7c15ull;
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
+inline sty_pcg32 key_stream(uint64_t key) {
+    sty_pcg32 g;
+    g.state = 0;
+    g.inc = (key << 1) | 1ull;
+    pcg_next(g);
+    g.state += smix64(key);
+    pcg_next(g);
+    return g;
+}
+inline uint32_t style_idx(uint32_t f) { return (f & 8u) ? 3u : (f & 4u) ? 2u : (f & 2u) ? 1u : 0u; }
+inline uint32_t flags_after(const sty_scene_material &m, uint32_t f) {
+    if (m.set_style < 0) return f;
+    return (f & 1u) | (m.set_style == 1 ? 2u : m.set_style == 2 ? 4u : m.set_style == 3 ? 8u : 0u);
+}
+struct BrScene {
+    PtScene pt;
+    const sty_scene_material *mats;
+    std::vector<float> cdf;  // FP32 like the GPU scene's
+    const sty_style_program *progs;
+    uint32_t n_progs, max_depth, n_levels;
+    const uint32_t *inner;
+};
+typedef std::array<double, 3> D3;
+inline double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// emitted radiance at a hit of triangle `prim` by direction d and its balance weight against the
+// light pdf seen from prev_p (handle_surface_light)
+inline bool br_emitter(const BrScene &s, uint32_t prim, const double *q, const double *d, uint32_t depth,
+                       const double *prev_p, double prev_pdf, D3 &le, double &mis) {
+    const sty_scene_material &m = s.mats[s.pt.mat[prim]];
+    le = {0, 0, 0};
+    mis = 1.0;
+    if (!(m.emission[0] > 0 || m.emission[1] > 0 || m.emission[2] > 0)) return false;
+    const auto &n = s.pt.nrm[prim];
+    if (n[0] * d[0] + n[1] * d[1] + n[2] * d[2] < 0) le = {m.emission[0], m.emission[1], m.emission[2]};
+    if (depth > 0) {
+        double sel = 0;
+        for (size_t k = 0; k < s.pt.lights.size(); k++)
+            if (s.pt.lights[k] == prim) sel = (double)s.cdf[k + 1] - (double)s.cdf[k];
+        const double w[3] = {q[0] - prev_p[0], q[1] - prev_p[1], q[2] - prev_p[2]};
+        const double d2 = dot3(w, w), dl = std::sqrt(d2);
+        const double cw = std::fabs((n[0] * w[0] + n[1] * w[1] + n[2] * w[2]) / dl);
+        const double lp = sel / s.pt.area[prim] * d2 / std::max(cw, 1e-6);
+        mis = prev_pdf / (prev_pdf + lp);
+    }
+    return true;
+}
+
+D3 br_radiance(const BrScene &s, uint32_t depth, const double *p, uint32_t prim, const double *wo, uint32_t flags,
+               uint32_t ab, uint64_t key, D3 le) {
+    const sty_scene_material &m = s.mats[s.pt.mat[prim]];
+    const auto &ngv = s.pt.nrm[prim];
+    const double ng[3] = {ngv[0], ngv[1], ngv[2]};
+    D3 li = le;
+    if (depth + 1 <= s.max_depth) {
+        const bool rough = (m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha) > 0.01f;
+        const uint32_t n = rough ? (ab < s.n_levels ? s.inner[ab] : 1u) : 1u;
+        const uint32_t nf = flags_after(m, flags), ab2 = ab + (rough ? 1u : 0u);
+        const double co = dot3(wo, ng);
+        D3 sum = {0, 0, 0};
+        for (uint32_t b = 0; b < n; b++) {
+            const uint64_t ck = smix64(key ^ (0x9e3779b97f4a7c15ull * (uint64_t)(b + 1u)));
+            sty_pcg32 g = key_stream(ck);
+            // NEE
+            const float ux = (float)pcg_next(g) * 2.3283064e-10f, uy = (float)pcg_next(g) * 2.3283064e-10f,
+                        uz = (float)pcg_next(g) * 2.3283064e-10f;
+            if (!s.pt.lights.empty()) {
+                uint32_t lo = 0, hi = (uint32_t)s.pt.lights.size() - 1;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (s.cdf[mid + 1] > ux) hi = mid;
+                    else lo = mid + 1;
+                }
+                const uint32_t lt = s.pt.lights[lo];
+                const double sel = (double)s.cdf[lo + 1] - (double)s.cdf[lo];
+                double bx, by;
+                if (uy < uz) {
+                    bx = uy / 2.0;
+                    by = uz - bx;
+                } else {
+                    by = uz / 2.0;
+                    bx = uy - by;
+                }
+                const float *lp = s.pt.pos + 9 * (size_t)lt;
+                double q[3], wi[3];
+                for (int a = 0; a < 3; a++) q[a] = (1 - bx - by) * lp[a] + bx * lp[3 + a] + by * lp[6 + a];
+                for (int a = 0; a < 3; a++) wi[a] = q[a] - p[a];
+                const double d2 = dot3(wi, wi);
+                if (d2 > 0) {
+                    const double dist = std::sqrt(d2);
+                    for (int a = 0; a < 3; a++) wi[a] /= dist;
+                    const auto &ln = s.pt.nrm[lt];
+                    const double lnw = ln[0] * wi[0] + ln[1] * wi[1] + ln[2] * wi[2];
+                    const double lpdf = sel / s.pt.area[lt] * d2 / std::fabs(lnw);
+                    const sty_scene_material &lm = s.mats[s.pt.mat[lt]];
+                    V3<double> lli = {0, 0, 0};
+                    if (lnw < 0) lli = {lm.emission[0], lm.emission[1], lm.emission[2]};
+                    if (std::isfinite(lpdf) && lpdf > 0) {
+                        if (!(nf & 1u)) {
+                            const int32_t pi = lm.style[style_idx(nf)];
+                            if (pi >= 0 && (uint32_t)pi < s.n_progs) lli = style_apply<double>(&s.progs[pi], depth + 1, lli);
+                        }
+                        double tt, c1, c2;
+                        const uint32_t blk = hit_bf(s.pt, p, wi, dist * (1 - 1e-3), prim, lt, &tt, &c1, &c2);
+                        const double ci = dot3(wi, ng);
+                        if (blk == 0xffffffffu && co * ci >= 0) {
+                            const double bp = std::fabs(ci) / M_PI, w = lpdf / (lpdf + bp) / lpdf;
+                            const double lv[3] = {lli.x, lli.y, lli.z};
+                            for (int c = 0; c < 3; c++) sum[c] += lv[c] * m.albedo[c] * bp * w;
+                        }
+                    }
+                }
+            }
+            // BSDF sample: cosine hemisphere (polar disk) in frame_from_n(ng), flipped to wo's side
+            const float usel = (float)pcg_next(g) * 2.3283064e-10f, u0 = (float)pcg_next(g) * 2.3283064e-10f,
+                        u1 = (float)pcg_next(g) * 2.3283064e-10f;
+            (void)usel;
+            const double r = std::sqrt((double)u0), ph = (double)u1 * 2.0 * M_PI;
+            const double lx = r * std::cos(ph), ly = r * std::sin(ph);
+            double lz = std::sqrt(std::max(0.0, 1 - lx * lx - ly * ly));
+            double t[3];
+            if (std::fabs(ng[0]) > std::fabs(ng[1])) {
+                const double il = 1.0 / std::sqrt(ng[0] * ng[0] + ng[2] * ng[2]);
+                t[0] = -ng[2] * il; t[1] = 0; t[2] = ng[0] * il;
+            } else {
+                const double il = 1.0 / std::sqrt(ng[1] * ng[1] + ng[2] * ng[2]);
+                t[0] = 0; t[1] = ng[2] * il; t[2] = -ng[1] * il;
+            }
+            const double sv[3] = {ng[1] * t[2] - ng[2] * t[1], ng[2] * t[0] - ng[0] * t[2], ng[0] * t[1] - ng[1] * t[0]};
+            if (!(co * lz >= 0)) lz = -lz;
+            double wi[3];
+            for (int a = 0; a < 3; a++) wi[a] = t[a] * lx + sv[a] * ly + ng[a] * lz;
+            const double pdf = std::fabs(lz) / M_PI;
+            if (!(pdf > 0)) continue;
+            double tt, b1, b2;
+            const uint32_t h = hit_bf(s.pt, p, wi, 1e30, prim, prim, &tt, &b1, &b2);
+            if (h == 0xffffffffu) continue;
+            double q[3];
+            for (int a = 0; a < 3; a++) q[a] = p[a] + tt * wi[a];
+            D3 cle;
+            double cmis;
+            br_emitter(s, h, q, wi, depth + 1, p, pdf, cle, cmis);
+            const double cwo[3] = {-wi[0], -wi[1], -wi[2]};
+            const D3 cl = br_radiance(s, depth + 1, q, h, cwo, nf, ab2, ck, cle);
+            for (int c = 0; c < 3; c++) sum[c] += m.albedo[c] * cl[c] * cmis;  // f cos / pdf = albedo
+        }
+        for (int c = 0; c < 3; c++) li[c] += sum[c] / n;
+    }
+    if (!(flags & 1u)) {
+        const int32_t pi = m.style[style_idx(flags)];
+        if (pi >= 0 && (uint32_t)pi < s.n_progs) {
+            const V3<double> o = style_apply<double>(&s.progs[pi], depth, v3(li[0], li[1], li[2]));
+            li = {o.x, o.y, o.z};
+        }
+    }
+    return li;
+}
+}  // namespace
+
+extern "C" void orc_brpt(const float *pos, const uint32_t *mat, uint32_t n_tris, const sty_scene_material *mats,
+                         const float *cam /* eye3 target3 up3 fov W H radius */, const sty_style_program *progs,
+                         uint32_t n_progs, uint32_t max_depth, const uint32_t *inner, uint32_t n_levels,
+                         uint32_t repeats, uint64_t seed, double *img) {
+    BrScene s;
+    s.pt.pos = pos;
+    s.pt.mat = mat;
+    s.pt.n = n_tris;
+    s.pt.area.resize(n_tris);
+    s.pt.nrm.resize(n_tris);
+    s.mats = mats;
+    s.progs = progs;
+    s.n_progs = n_progs;
+    s.max_depth = max_depth;
+    s.n_levels = n_levels;
+    s.inner = inner;
+    std::vector<double> lw;
+    for (uint32_t t = 0; t < n_tris; t++) {
+        const float *p = pos + 9 * (size_t)t;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; a++) {
+            e1[a] = (double)p[3 + a] - p[a];
+            e2[a] = (double)p[6 + a] - p[a];
+        }
+        const double c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const double l = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        s.pt.area[t] = (double)(float)(0.5 * l);
+        s.pt.nrm[t] = {c[0] / l, c[1] / l, c[2] / l};
+        const float *em = mats[mat[t]].emission;
+        const double lum = 0.2126 * em[0] + 0.7152 * em[1] + 0.0722 * em[2];
+        if (lum > 0 && s.pt.area[t] > 0) {
+            s.pt.lights.push_back(t);
+            lw.push_back(lum * s.pt.area[t]);
+        }
+    }
+    s.cdf.assign(lw.size() + 1, 0.0f);
+    double tot = 0, acc = 0;
+    for (double w : lw) tot += w;
+    for (size_t k = 0; k < lw.size(); k++) {
+        acc += lw[k];
+        s.cdf[k + 1] = (float)(acc / tot);
+    }
+    if (!lw.empty()) s.cdf.back() = 1.0f;
+    const uint32_t W = (uint32_t)cam[10], H = (uint32_t)cam[11];
+    double f[3], r[3], u[3];
+    for (int a = 0; a < 3; a++) f[a] = cam[3 + a] - cam[a];
+    double l = std::sqrt(dot3(f, f));
+    for (int a = 0; a < 3; a++) f[a] /= l;
+    r[0] = f[1] * cam[8] - f[2] * cam[7];
+    r[1] = f[2] * cam[6] - f[0] * cam[8];
+    r[2] = f[0] * cam[7] - f[1] * cam[6];
+    l = std::sqrt(dot3(r, r));
+    for (int a = 0; a < 3; a++) r[a] /= l;
+    u[0] = r[1] * f[2] - r[2] * f[1];
+    u[1] = r[2] * f[0] - r[0] * f[2];
+    u[2] = r[0] * f[1] - r[1] * f[0];
+    const double th = std::tan(cam[9] * 0.5 * M_PI / 180.0), asp = (double)W / H, rad = cam[12];
+    std::fill(img, img + 3 * (size_t)W * H, 0.0);
+    for (uint32_t rep = 0; rep < repeats; rep++) {
+        const uint64_t rkey = smix64(smix64(seed ^ 0x4252505400000000ull) + rep);
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int py = 0; py < (int)H; py++)
+            for (uint32_t px = 0; px < W; px++) {
+                const uint32_t pid = (uint32_t)py * W + px;
+                const uint64_t key = smix64(rkey + pid);
+                sty_pcg32 g = key_stream(key);
+                const double u0 = (float)pcg_next(g) * 2.3283064e-10f, u1 = (float)pcg_next(g) * 2.3283064e-10f;
+                const double fx = px + 0.5 + (u0 - 0.5) * rad, fy = py + 0.5 + (u1 - 0.5) * rad;
+                const double sx = (2 * fx / W - 1) * th * asp, sy = (1 - 2 * fy / H) * th;
+                double d[3];
+                for (int a = 0; a < 3; a++) d[a] = f[a] + r[a] * sx + u[a] * sy;
+                const double dl = std::sqrt(dot3(d, d));
+                for (int a = 0; a < 3; a++) d[a] /= dl;
+                const double o[3] = {cam[0], cam[1], cam[2]};
+                double tt, b1, b2;
+                const uint32_t h = hit_bf(s.pt, o, d, 1e30, 0xffffffffu, 0xffffffffu, &tt, &b1, &b2);
+                if (h == 0xffffffffu) continue;
+                double q[3];
+                for (int a = 0; a < 3; a++) q[a] = o[a] + tt * d[a];
+                D3 le;
+                double mis;
+                br_emitter(s, h, q, d, 0, o, 0.0, le, mis);
+                const double wo[3] = {-d[0], -d[1], -d[2]};
+                const D3 c = br_radiance(s, 0, q, h, wo, 0u, 0u, key, le);
+                for (int k = 0; k < 3; k++) img[3 * (size_t)pid + k] += c[k] / repeats;
+            }
+    }
+}

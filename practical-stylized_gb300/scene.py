@@ -52,6 +52,27 @@ class NrcRenderStats(C.Structure):
                 ("reserved", C.c_uint32)]
 
 
+class BrptConfig(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("n_levels", C.c_uint32), ("inner_samples", C.c_uint32 * 8),
+                ("repeats", C.c_uint32), ("vram_mb", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class BrptStats(C.Structure):
+    _fields_ = [("vertices", C.c_uint64), ("slots", C.c_uint64), ("passes", C.c_uint64),
+                ("pixels_per_pass", C.c_uint64), ("max_pass_slots", C.c_uint64)]
+
+
+def brpt_config(max_depth=7, inner_samples=(256, 32, 8, 1), repeats=1, vram_mb=8192, seed=0) -> BrptConfig:
+    """The branching path tracer's configuration (branching_pt.rs Config :77-100; the defaults are
+    the reference's)."""
+    c = BrptConfig()
+    c.max_depth, c.repeats, c.vram_mb, c.seed = max_depth, repeats, vram_mb, seed
+    c.n_levels = len(inner_samples)
+    for i, v in enumerate(inner_samples):
+        c.inner_samples[i] = v
+    return c
+
+
 def nrc_render_config(max_depth=5, training_iters=64, batches_per_iter=16, training_paths=0, repeats=1,
                       per_level_training=0, no_first_hit_stylization=False, learn_stylized_radiance=False,
                       final_gather=0, seed=0) -> NrcRenderConfig:
@@ -379,4 +400,19 @@ class Scene:
         st = NrcRenderStats()
         check(lib().sty_nrc_render(self.h, net.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(st),
                                    _stream_ptr(stream)))
+        return film, st
+
+    def brpt_render(self, cfg: BrptConfig, programs=(), film=None, stream=None):
+        """The branching path tracer (sty_brpt_render): returns (film [H, W, 3] float64 device
+        tensor, stats)."""
+        import torch
+        from .pf import _stream_ptr
+        W, H = self.camera.width, self.camera.height
+        if film is None:
+            film = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+        progs = list(programs)
+        arr = (abi.StyleProgram * max(1, len(progs)))(*progs) if progs else None
+        st = BrptStats()
+        check(lib().sty_brpt_render(self.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(st),
+                                    _stream_ptr(stream)))
         return film, st
