@@ -387,7 +387,9 @@ def c5_bench(sty, W: int = 160, H: int = 90):
       nl_nrc_*   the NL-NRC loop (128 training iterations of 4 batches of 2^14, 16 first-hit
                  passes) with the BF16 tcgen05 cache and with the FP32 cache (spherical-frequency
                  network), and with the reference's own network (hash grid 22 x 4 on 2^19 tables +
-                 one-blob + identity, 5 x 128; rows in the reference layout)."""
+                 one-blob + identity, 5 x 128; rows in the reference layout);
+      brpt       the branching path tracer at the teaser's branching (32, 14, 8, 6), 1 repeat;
+      pt_64spp   the plain stylized path tracer (branching 1), 64 repeats."""
     import numpy as np
     import torch
     a = sty.abi
@@ -415,8 +417,20 @@ def c5_bench(sty, W: int = 160, H: int = 90):
     img, t, nv = pf(16, 4, 7)
     res["nl_pf"] = {"spp": 64, "seconds": t, "mpath_vertices_per_s": nv / t / 1e6,
                     "image_mse": float(((img - ref) ** 2).mean())}
+    def nrc_warmup(make):
+        # untimed short render: the first use of a code path in a process loads its kernels (and,
+        # on a fresh machine, cuBLAS from disk: seconds)
+        w = make()
+        sc.nrc_render(w, sty.scene.nrc_render_config(max_depth=8, training_iters=2, batches_per_iter=1, repeats=1,
+                                                     seed=1), progs)
+        torch.cuda.synchronize()
+        w.close()
+
     for name, prec in (("nl_nrc_bf16", sty.nrc.STY_NRC_BF16), ("nl_nrc_fp32", sty.nrc.STY_NRC_FP32)):
-        net = sty.nrc.NRC(sty.nrc.config(sty.nrc.C4_FREQS, 3, 1 << 14, 5, prec, learning_rate=1e-2, seed=1))
+        make = lambda: sty.nrc.NRC(sty.nrc.config(sty.nrc.C4_FREQS, 3, 1 << 14, 5, prec, learning_rate=1e-2,  # noqa: E731
+                                                  seed=1))
+        nrc_warmup(make)
+        net = make()
         cfg = sty.scene.nrc_render_config(max_depth=8, training_iters=128, batches_per_iter=4, repeats=16, seed=3)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -427,7 +441,9 @@ def c5_bench(sty, W: int = 160, H: int = 90):
         res[name] = {"seconds": t, "training_rows": int(st.training_rows), "queries": int(st.inference_queries),
                      "image_mse": float(((img - ref) ** 2).mean())}
         net.close()
-    net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=8, batch_size=1 << 14, learning_rate=1e-2, seed=1))
+    make = lambda: sty.nrc.NRC(sty.nrc.grid_config(max_depth=8, batch_size=1 << 14, learning_rate=1e-2, seed=1))  # noqa: E731
+    nrc_warmup(make)
+    net = make()
     cfg = sty.scene.nrc_render_config(max_depth=8, training_iters=128, batches_per_iter=4, repeats=16, seed=3)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -439,6 +455,20 @@ def c5_bench(sty, W: int = 160, H: int = 90):
                                  "queries": int(st.inference_queries), "params": net.param_count(),
                                  "image_mse": float(((img - ref) ** 2).mean())}
     net.close()
+    # the branching path tracer at the teaser's branching (configs/teaser/brpt.json: inner samples
+    # 32, 14, 8, 6) and the plain stylized path tracer of configs/teaser/pt.json (inner samples 1)
+    sc.brpt_render(sty.scene.brpt_config(max_depth=8, inner_samples=(2,), repeats=1, seed=1), progs)  # warm-up
+    for name, inner, reps in (("brpt", (32, 14, 8, 6), 1), ("pt_64spp", (1,), 64)):
+        cfg = sty.scene.brpt_config(max_depth=8, inner_samples=inner, repeats=reps, vram_mb=16384, seed=5)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        film, st = sc.brpt_render(cfg, progs)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        img = film.cpu().numpy()
+        res[name] = {"seconds": t, "inner_samples": list(inner), "repeats": reps, "vertices": int(st.vertices),
+                     "mvertices_per_s": st.vertices / t / 1e6, "passes": int(st.passes),
+                     "image_mse": float(((img - ref) ** 2).mean())}
     res["reference_mean"] = float(ref.mean())
     sc.close()
     return res

@@ -535,8 +535,8 @@ STY_API sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_
  * at max_depth), each one light sample + one BSDF-sampled child; bottom-up a vertex's radiance is
  * style(Le + mean over branches of (direct + throughput * child radiance * child emission MIS)),
  * the depth-0 radiance is the pixel sample (the non-debiased estimator; the jackknife / Russian-
- * roulette debiasing option is not built). Pixels go through in passes whose worst-case vertex
- * trees fit vram_mb (100 bytes per vertex slot). Adds (1/repeats) of each pixel's sample into
+ * roulette debiasing option is not built). Pixel samples (pixel x repeat) go through in passes
+ * whose worst-case vertex trees fit vram_mb (100 bytes per vertex slot). Adds (1/repeats) of each pixel's sample into
  * `film` (device, width*height*3 doubles; the caller zeroes it). `programs` is a HOST array.
  * Sampling keys on (seed, repeat, pixel) and, per child, on (parent, branch index): the image does
  * not depend on vram_mb. Deterministic. */
@@ -553,7 +553,7 @@ typedef struct sty_brpt_stats {
     uint64_t vertices;        /* surface hits (tree vertices) over all passes and repeats */
     uint64_t slots;           /* vertex slots (hits + branches whose ray missed) */
     uint64_t passes;          /* pixel passes over all repeats */
-    uint64_t pixels_per_pass;
+    uint64_t pixels_per_pass; /* pixel samples (pixel x repeat) per pass */
     uint64_t max_pass_slots;
 } sty_brpt_stats;
 STY_API sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *config,

@@ -82,13 +82,19 @@ __device__ __forceinline__ void put3(float *const (&pl)[3], size_t i, F3 v) {
 }
 __device__ __forceinline__ F3 get3(float *const (&pl)[3], size_t i) { return f3m(pl[0][i], pl[1][i], pl[2][i]); }
 
-// depth 0: the camera slot of pixels px0 .. px0 + n (kernel_init :501-541)
-__global__ void k_br_camera(SceneView sc, CamArgs cam, uint32_t n, uint32_t px0, uint64_t rkey, BrSlots s,
-                            unsigned long long *hits) {
+// key of repeat r: every pixel sample of that repeat keys on it
+__host__ __device__ __forceinline__ uint64_t repeat_key(uint64_t seed, uint64_t r) {
+    return splitmix64(splitmix64(seed ^ 0x4252505400000000ull) + r);
+}
+// depth 0: the camera slots of samples q0 .. q0 + n, sample q = repeat * npx + pixel (kernel_init
+// :501-541)
+__global__ void k_br_camera(SceneView sc, CamArgs cam, uint32_t n, uint64_t q0, uint32_t npx, uint64_t seed,
+                            BrSlots s, unsigned long long *hits) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t px = px0 + i;
-    const uint64_t key = splitmix64(rkey + px);
+    const uint64_t q = q0 + i;
+    const uint32_t px = (uint32_t)(q % npx);
+    const uint64_t key = splitmix64(repeat_key(seed, q / npx) + px);
     sty_pcg32 st = key_stream(key);
     F3 ro, rd;
     camera_ray(cam, px, st, &ro, &rd);
@@ -199,10 +205,9 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
     s.mis[cg] = mis;
 }
 
-// bottom-up radiance of one depth; depth 0 adds the pixel sample into the film (kernel_propagate)
+// bottom-up radiance of one depth (kernel_propagate); depth 0 leaves the pixel samples in `rad`
 __global__ void k_br_propagate(SceneView sc, uint32_t n, uint32_t base, uint32_t cbase0, uint32_t depth,
-                               const sty_style_program *progs, uint32_t n_progs, BrSlots s, uint32_t px0,
-                               double weight, double *film) {
+                               const sty_style_program *progs, uint32_t n_progs, BrSlots s) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t g = base + i;
@@ -231,12 +236,22 @@ __global__ void k_br_propagate(SceneView sc, uint32_t n, uint32_t base, uint32_t
             if (pi >= 0 && (uint32_t)pi < n_progs) out = style_apply(progs[pi], depth, out);
         }
         put3(s.rad, g, f3m(out.x, out.y, out.z));
+    } else if (depth == 0) {
+        put3(s.rad, g, f3m(0.0f, 0.0f, 0.0f));
     }
-    if (depth == 0) {
-        double *fp = film + 3 * (size_t)(px0 + i);
-        fp[0] += weight * out.x;
-        fp[1] += weight * out.y;
-        fp[2] += weight * out.z;
+}
+// film += weight * sample for every sample of the pass, per pixel in repeat order (film.add_sample):
+// the sequence of FP64 additions does not depend on how samples are grouped into passes
+__global__ void k_br_film(uint32_t npx, uint64_t q0, uint32_t n, BrSlots s, double weight, double *film) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= npx) return;
+    uint64_t q = q0 + (px + npx - (uint32_t)(q0 % npx)) % npx;  // the pass's first sample of px
+    double *fp = film + 3 * (size_t)px;
+    for (; q < q0 + n; q += npx) {
+        const size_t i = (size_t)(q - q0);
+        fp[0] += weight * s.rad[0][i];
+        fp[1] += weight * s.rad[1][i];
+        fp[2] += weight * s.rad[2][i];
     }
 }
 
@@ -274,7 +289,7 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
         set_error("vram_mb (%u) is below one pixel's worst-case vertex tree (%.0f vertices)", cfg->vram_mb, worst);
         return STY_ERR_ARG;
     }
-    ppp = std::min<uint64_t>(ppp, npx);
+    ppp = std::min<uint64_t>(ppp, (uint64_t)npx * cfg->repeats);
     ppp = std::min<uint64_t>(ppp, (uint64_t)(2147483647.0 / worst));
     STY_ARG_CHECK(ppp >= 1, "vertex tree of one pixel exceeds 2^31 slots");
     const uint64_t cap = (uint64_t)((double)ppp * worst) + 1;
@@ -335,13 +350,13 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
         uint64_t slots = 0, passes = 0, max_pass = 0;
         const double weight = 1.0 / cfg->repeats;
         std::vector<uint32_t> cnt, off;
-        for (uint32_t r = 0; r < cfg->repeats; r++) {
-            const uint64_t rkey = splitmix64(splitmix64(cfg->seed ^ 0x4252505400000000ull) + r);
-            for (uint32_t px0 = 0; px0 < npx; px0 += (uint32_t)ppp) {
-                const uint32_t P = (uint32_t)std::min<uint64_t>(ppp, npx - px0);
+        const uint64_t total = (uint64_t)npx * cfg->repeats;
+        {
+            for (uint64_t q0 = 0; q0 < total; q0 += ppp) {
+                const uint32_t P = (uint32_t)std::min<uint64_t>(ppp, total - q0);
                 cnt.assign(1, P);
                 off.assign(1, 0);
-                k_br_camera<<<(P + 255) / 256, 256, 0, st>>>(sv, ca, P, px0, rkey, sl, dhits);
+                k_br_camera<<<(P + 255) / 256, 256, 0, st>>>(sv, ca, P, q0, npx, cfg->seed, sl, dhits);
                 STY_TRY(check_launch("k_br_camera"));
                 for (uint32_t d = 0; d <= cfg->max_depth; d++) {
                     const uint32_t n = cnt[d], base = off[d];
@@ -376,9 +391,11 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
                 for (int d = (int)cnt.size() - 1; d >= 0; d--) {
                     const uint32_t cb = (size_t)d + 1 < off.size() ? off[d + 1] : 0u;
                     k_br_propagate<<<(cnt[d] + 255) / 256, 256, 0, st>>>(sv, cnt[d], off[d], cb, (uint32_t)d, dprog,
-                                                                         n_programs, sl, px0, weight, film);
+                                                                         n_programs, sl);
                     STY_TRY(check_launch("k_br_propagate"));
                 }
+                k_br_film<<<(npx + 255) / 256, 256, 0, st>>>(npx, q0, P, sl, weight, film);
+                STY_TRY(check_launch("k_br_film"));
                 uint64_t pass_slots = 0;
                 for (uint32_t c : cnt) pass_slots += c;
                 slots += pass_slots;

@@ -73,17 +73,19 @@ def test_brpt_matches_oracle_per_pixel(sty, cuda, styled):
 
 @pytest.mark.gpu
 def test_brpt_image_independent_of_pass_layout(sty, cuda):
-    """Sampling keys on (seed, repeat, pixel) and (parent, branch): a budget that splits the image
-    into many passes gives the bit-identical image of a single pass."""
+    """Sampling keys on (seed, repeat, pixel) and (parent, branch), and the film adds each pixel's
+    samples in repeat order: a budget that splits the samples into many passes gives the
+    bit-identical image of a single pass holding every repeat."""
     pos, mids, mats, cam = sty.scene.cornell_box(32, 24, style=(0, -1, -1, -1))
     sc = sty.scene.Scene(pos, mids, mats, cam)
     progs = [_ramp(sty)]
-    big, sb = _render(sty, sc, sty.scene.brpt_config(max_depth=5, inner_samples=(8, 4, 2), vram_mb=8192, seed=2), progs)
-    small, ss = _render(sty, sc, sty.scene.brpt_config(max_depth=5, inner_samples=(8, 4, 2), vram_mb=4, seed=2), progs)
-    assert sb.passes == 1 and ss.passes > 4
+    cfg = lambda mb: sty.scene.brpt_config(max_depth=5, inner_samples=(8, 4, 2), repeats=3, vram_mb=mb, seed=2)  # noqa: E731
+    big, sb = _render(sty, sc, cfg(8192), progs)   # all 3 repeats of every pixel in one pass
+    small, ss = _render(sty, sc, cfg(4), progs)    # dozens of passes
+    assert sb.passes == 1 and ss.passes > 12
     assert np.array_equal(big, small)
     assert sb.vertices == ss.vertices and sb.slots == ss.slots
-    again, _ = _render(sty, sc, sty.scene.brpt_config(max_depth=5, inner_samples=(8, 4, 2), vram_mb=4, seed=2), progs)
+    again, _ = _render(sty, sc, cfg(4), progs)
     assert np.array_equal(again, small)
     sc.close()
 
