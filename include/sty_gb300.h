@@ -203,13 +203,25 @@ STY_API sty_status sty_film_accumulate(const float *out0, int32_t width, int32_t
  * All per-vertex arrays below are device arrays of `n` elements indexed by path slot.
  * -------------------------------------------------------------------------------------- */
 #define STY_MAT_DIFFUSE 0 /* Lambert: f = albedo/pi |cos|, pdf = |cos|/pi (diffuse.rs:17-48)       */
-#define STY_MAT_GGX 1     /* microfacet reflection, Trowbridge-Reitz alpha, unit Fresnel,                                        visible-normal pdf (mod.rs:1877-1910, microfacet.rs:44-206)           */
+#define STY_MAT_GGX 1     /* microfacet reflection, Trowbridge-Reitz alpha, unit Fresnel,
+                             visible-normal pdf (mod.rs:1877-1910, microfacet.rs:44-206)           */
+#define STY_MAT_PRINCIPLED 2 /* the reference's principled BSDF (svm/surface/principled.rs:118-330):
+                             diffuse, dielectric reflection / transmission, a tinted specular layer
+                             weighted by the ggx_dielectric_s albedo table, a conductor
+                             (Gulbrandsen) and a clear coat; albedo = base colour, the
+                             roughness / metallic / ior / transmission / specular / coat fields
+                             below. Flat shading (normal maps are not supported). */
 
 typedef struct sty_pf_material {
     int32_t kind;        /* STY_MAT_* */
     float albedo[3];
     float alpha;         /* GGX roughness alpha (>= 1e-4) */
     int32_t style[4];    /* style program per style index 0..3 (flags bits 1..3), -1 = none */
+    /* STY_MAT_PRINCIPLED parameters (ignored by the other kinds) */
+    float roughness, metallic, ior, transmission, specular_ior_level;
+    float specular_tint[3];
+    float coat_weight, coat_roughness, coat_ior;
+    float coat_tint[3];
 } sty_pf_material;
 
 typedef struct sty_pf_vertices {
@@ -408,7 +420,25 @@ typedef struct sty_scene_material {
     float emission[3];   /* radiance leaving the front (geometric-normal) side; 0 = not a light */
     int32_t style[4];    /* style program per style index, -1 = none (applied by the filter) */
     int32_t set_style;   /* -1: hits keep the path's flags; k >= 0: hits set style index k (sty_set_idx) */
+    /* STY_MAT_PRINCIPLED parameters (Blender's Principled BSDF inputs as the reference reads them;
+     * ignored by the other kinds) */
+    float roughness, metallic, ior, transmission, specular_ior_level;
+    float specular_tint[3];
+    float coat_weight, coat_roughness, coat_ior;
+    float coat_tint[3];
 } sty_scene_material;
+
+/* The principled BSDF's pieces, for checking them against the oracle (shading frame: z = normal;
+ * device arrays of n 3-vectors). sty_bsdf_eval: f * |cos_i| (rgb) and pdf of `material` for (wo, wi)
+ * (Surface::evaluate). sty_bsdf_sample: SurfaceClosure::sample with u = (u_select, u0, u1) per
+ * sample: wi, f * |cos_i| and pdf at wi (pdf 0 = invalid sample). sty_principled_table: the 16^3
+ * ggx_dielectric_s albedo table of the current device (HOST output, x = roughness fastest, then
+ * mu, then z = sqrt(|ior - 1| / (ior + 1))). */
+STY_API sty_status sty_bsdf_eval(const sty_scene_material *material, uint64_t n, const float *wo, const float *wi,
+                                 float *f, float *pdf, void *stream);
+STY_API sty_status sty_bsdf_sample(const sty_scene_material *material, uint64_t n, const float *wo, const float *u,
+                                   float *wi, float *f, float *pdf, void *stream);
+STY_API sty_status sty_principled_table(float *host_table);
 
 typedef struct sty_camera {
     float eye[3], target[3], up[3];

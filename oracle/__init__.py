@@ -42,6 +42,9 @@ def lib() -> C.CDLL:
         L.orc_path_trace.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, vp]
         L.orc_brpt.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint32, C.c_uint32,
                                C.c_uint64, vp]
+        L.orc_principled_table.argtypes = [vp]
+        L.orc_principled_eval.argtypes = [vp, C.c_uint64, vp, vp, vp, vp]
+        L.orc_principled_sample.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
         _lib = L
@@ -194,6 +197,34 @@ def brpt(tri_pos, mat_ids, materials, cam, programs, max_depth: int, inner_sampl
     lib().orc_brpt(_p(pos), _p(m), m.size, C.addressof(materials), _p(c), None if parr is None else C.addressof(parr),
                    len(progs), max_depth, _p(inner), inner.size, repeats, seed, _p(img))
     return img
+
+
+def principled_table() -> np.ndarray:
+    """The FP64 ggx_dielectric_s table [z, mu, roughness] (16^3)."""
+    t = np.zeros(16 ** 3, dtype=np.float64)
+    lib().orc_principled_table(_p(t))
+    return t.reshape(16, 16, 16)
+
+
+def principled_eval(material, wo, wi):
+    """FP64 principled closure in the shading frame: (f * |cos_i| [n, 3], pdf [n])."""
+    wo = np.ascontiguousarray(wo, dtype=np.float64).reshape(-1, 3)
+    wi = np.ascontiguousarray(wi, dtype=np.float64).reshape(-1, 3)
+    f = np.zeros_like(wo)
+    pdf = np.zeros(wo.shape[0])
+    lib().orc_principled_eval(C.addressof(material), wo.shape[0], _p(wo), _p(wi), _p(f), _p(pdf))
+    return f, pdf
+
+
+def principled_sample(material, wo, u):
+    """FP64 SurfaceClosure::sample of the principled closure: (wi [n, 3], f [n, 3], pdf [n])."""
+    wo = np.ascontiguousarray(wo, dtype=np.float64).reshape(-1, 3)
+    u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1, 3)
+    wi = np.zeros_like(wo)
+    f = np.zeros_like(wo)
+    pdf = np.zeros(wo.shape[0])
+    lib().orc_principled_sample(C.addressof(material), wo.shape[0], _p(wo), _p(u), _p(wi), _p(f), _p(pdf))
+    return wi, f, pdf
 
 
 def num_threads() -> int:

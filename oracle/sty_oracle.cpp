@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <complex>
 #include <cstring>
 #include <vector>
 #ifdef _OPENMP
@@ -1191,5 +1192,328 @@ extern "C" void orc_brpt(const float *pos, const uint32_t *mat, uint32_t n_tris,
                 const D3 c = br_radiance(s, 0, q, h, wo, 0u, 0u, key, le);
                 for (int k = 0; k < 3; k++) img[3 * (size_t)pid + k] += c[k] / repeats;
             }
+    }
+}
+
+// ---- the principled BSDF (principled.rs:118-330), FP64 restatement -------------------------------
+// Test infrastructure for STY_MAT_PRINCIPLED: the same closure (layers, blend modes, lobe choice),
+// microfacet lobes, Fresnel terms and ggx_dielectric_s table (the mean of f/pdf of a unit-colour
+// dielectric GGX reflection over the visible-normal sample, by the same 256 x 256 midpoint rule in
+// u), all in FP64.
+namespace {
+typedef std::array<double, 3> P3;
+inline P3 p3(double x, double y, double z) { return {x, y, z}; }
+inline P3 padd(P3 a, P3 b) { return {a[0] + b[0], a[1] + b[1], a[2] + b[2]}; }
+inline P3 pmul(P3 a, double s) { return {a[0] * s, a[1] * s, a[2] * s}; }
+inline double pdot(P3 a, P3 b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+inline P3 pcross(P3 a, P3 b) { return {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]}; }
+inline P3 pnorm(P3 a) { return pmul(a, 1.0 / std::sqrt(pdot(a, a))); }
+inline bool psame(P3 a, P3 b) { return a[2] * b[2] > 0; }
+inline double plerp(double a, double b, double t) { return a + (b - a) * t; }
+const double kPiD = 3.14159265358979323846;
+
+double p_d(P3 wh, double a) {
+    const double c2 = wh[2] * wh[2], s2 = std::max(0.0, 1 - c2), tan2 = s2 / c2, e = tan2 / (a * a);
+    const double inv = kPiD * a * a * c2 * c2 * (1 + e) * (1 + e);
+    if (!std::isfinite(tan2) || !std::isfinite(inv) || inv == 0) return 0;
+    return 1 / inv;
+}
+double p_lambda(P3 w, double a) {
+    const double c2 = w[2] * w[2], s2 = std::max(0.0, 1 - c2);
+    const double at = std::fabs(std::sqrt(s2) / w[2]);
+    return std::isfinite(at) ? (-1 + std::sqrt(1 + a * a * at * at)) * 0.5 : 0.0;
+}
+double p_vpdf(P3 wo, P3 wh, double a) {
+    return p_d(wh, a) / (1 + p_lambda(wo, a)) * std::fabs(pdot(wo, wh)) / std::fabs(wo[2]);
+}
+P3 p_sample_wh(P3 w, double a, double u0, double u1) {
+    P3 wh = pnorm(p3(a * w[0], a * w[1], w[2]));
+    if (wh[2] < 0) wh = pmul(wh, -1);
+    const P3 t1 = wh[2] < 0.99999 ? pnorm(pcross(p3(0, 0, 1), wh)) : p3(1, 0, 0);
+    const P3 t2 = pnorm(pcross(wh, t1));
+    const double r = std::sqrt(u0), ph = u1 * 2 * kPiD;
+    double px = r * std::cos(ph), py = r * std::sin(ph);
+    const double h = std::sqrt(1 - px * px);
+    py = h + (py - h) * ((1 + wh[2]) * 0.5);
+    const double pz = std::sqrt(std::max(1 - (px * px + py * py), 0.0));
+    const P3 nh = padd(padd(pmul(t1, px), pmul(t2, py)), pmul(wh, pz));
+    return pnorm(p3(a * nh[0], a * nh[1], std::max(nh[2], 1e-6)));
+}
+inline P3 p_reflect(P3 w, P3 n) { return padd(pmul(n, 2 * pdot(w, n)), pmul(w, -1)); }
+bool p_refract(P3 w, P3 n, double eta, P3 *wt) {
+    double ci = pdot(w, n);
+    const double e = ci >= 0 ? eta : 1 / eta;
+    const P3 nn = ci >= 0 ? n : pmul(n, -1);
+    ci = std::fabs(ci);
+    const double s2t = std::max(1 - ci * ci, 0.0) / (e * e);
+    if (s2t >= 1) return false;
+    *wt = padd(pmul(w, -1 / e), pmul(nn, ci / e - std::sqrt(1 - s2t)));
+    return true;
+}
+double p_fr_diel(double ci, double eta) {
+    ci = std::min(std::max(ci, -1.0), 1.0);
+    const double e = ci > 0 ? eta : 1 / eta;
+    ci = std::fabs(ci);
+    const double s2t = (1 - ci * ci) / (e * e);
+    if (s2t >= 1) return 1;
+    const double ct = std::sqrt(std::max(1 - s2t, 0.0));
+    const double a = (e * ci - ct) / (e * ci + ct), b = (ci - e * ct) / (ci + e * ct);
+    return std::min(std::max((a * a + b * b) * 0.5, 0.0), 1.0);
+}
+double p_fr_cond(double ci, double n, double k) {
+    typedef std::complex<double> cd;
+    ci = std::min(std::max(ci, 0.0), 0.999);
+    const cd eta(n, k), s2t = cd(1 - ci * ci, 0) / (eta * eta), ct = std::sqrt(cd(1, 0) - s2t);
+    const cd a = (eta * ci - ct) / (eta * ci + ct), b = (cd(ci, 0) - eta * ct) / (cd(ci, 0) + eta * ct);
+    return (std::norm(a) + std::norm(b)) * 0.5;
+}
+inline double p_ior_from_f0(double f0) {
+    const double s = std::sqrt(std::min(std::max(f0, 0.0), 0.99));
+    return (1 + s) / (1 - s);
+}
+double p_albedo_sample(double rough, double mu, double ior, double u0, double u1) {
+    const double a = std::max(rough * rough, 1e-4);
+    const P3 wo = p3(std::sqrt(1 - mu * mu), 0, mu), wh = p_sample_wh(wo, a, u0, u1), wi = p_reflect(wo, wh);
+    if (!psame(wo, wi)) return 0;
+    P3 h = padd(wo, wi);
+    if (pdot(h, wo) * pdot(wi, h) < 0 || wi[2] == 0) return 0;
+    h = pnorm(h);
+    const double F = p_fr_diel(pdot(wi, h[2] < 0 ? pmul(h, -1) : h), ior);
+    const double G = 1 / (1 + p_lambda(wo, a) + p_lambda(wi, a));
+    const double f = F * std::fabs(0.25 * p_d(h, a) * G / (wi[2] * wo[2])) * std::fabs(wi[2]);
+    const double pdf = p_vpdf(wo, h, a) / (4 * std::fabs(pdot(wo, h)));
+    return pdf > 0 ? f / pdf : 0;
+}
+struct PTab {
+    std::vector<double> v;
+};
+const PTab &p_table() {
+    static PTab t;
+    static bool done = false;
+    if (done) return t;
+    const int N = 16, Q = 256;
+    t.v.assign(N * N * N, 0.0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int cell = 0; cell < N * N * N; cell++) {
+        auto coord = [&](int i) { return std::min(std::max((double)(float)((float)i / (float)(N - 1)), 1e-4), 0.9999); };
+        const double r = coord(cell % N), mu = coord((cell / N) % N), z = coord(cell / (N * N));
+        const double ior = p_ior_from_f0(z * z * z * z);
+        double s = 0;
+        for (int k = 0; k < Q * Q; k++) s += p_albedo_sample(r, mu, ior, (k % Q + 0.5) / Q, (k / Q + 0.5) / Q);
+        t.v[cell] = s / (Q * Q);
+    }
+    done = true;
+    return t;
+}
+double p_tab3(double x, double y, double z) {
+    const PTab &t = p_table();
+    const int N = 16;
+    auto idx = [&](double c, int &i, int &j, double &w) {
+        c = std::min(std::max(c, 0.0), 1.0) * (N - 1);
+        i = (int)std::floor(c);
+        j = std::min(i + 1, N - 1);
+        w = c - i;
+    };
+    int xi, xj, yi, yj, zi, zj;
+    double wx, wy, wz;
+    idx(x, xi, xj, wx);
+    idx(y, yi, yj, wy);
+    idx(z, zi, zj, wz);
+    auto at = [&](int a, int b, int c) { return t.v[a + N * b + N * N * c]; };
+    auto l2 = [&](int c) {
+        return (1 - wy) * ((1 - wx) * at(xi, yi, c) + wx * at(xj, yi, c)) + wy * ((1 - wx) * at(xi, yj, c) + wx * at(xj, yj, c));
+    };
+    return (1 - wz) * l2(zi) + wz * l2(zj);
+}
+double p_albedo(double rough, double mu, double eta) {
+    const double z = std::sqrt(std::fabs((eta - 1) / (eta + 1)));
+    return p_tab3(rough, std::fabs(std::min(std::max(mu, -0.999), 0.999)), z);
+}
+struct PCl {
+    double base[3], tcol[3], alpha, rough, rough_d, metallic, trans, ior, seta, sf0, stint[3], stl, cn[3], ck[3];
+    double cw, calpha, crough, crough_d, cior, ctint[3];
+};
+PCl p_closure(const sty_scene_material &m) {
+    PCl c;
+    for (int i = 0; i < 3; i++) {
+        c.base[i] = m.albedo[i];
+        c.tcol[i] = std::sqrt((double)m.albedo[i]);
+        c.stint[i] = m.specular_tint[i];
+        c.ctint[i] = m.coat_tint[i];
+    }
+    c.rough = m.roughness;
+    c.alpha = std::max(c.rough * c.rough, 1e-4);
+    c.rough_d = std::sqrt(c.alpha);
+    c.metallic = m.metallic;
+    c.trans = m.transmission;
+    c.ior = m.ior;
+    double f0 = (c.ior - 1) / (c.ior + 1);
+    f0 *= f0;
+    double es = c.ior;
+    if (m.specular_ior_level != 0.5f) {
+        f0 *= 2.0 * m.specular_ior_level;
+        es = p_ior_from_f0(f0);
+    }
+    c.sf0 = f0;
+    c.seta = es;
+    c.stl = c.stint[0] * 0.2126 + c.stint[1] * 0.7152 + c.stint[2] * 0.0722;
+    for (int i = 0; i < 3; i++) {
+        const double r = std::min(std::max(c.base[i], 0.0), 0.99), g = c.stint[i], rs = std::sqrt(r);
+        const double nmin = (1 - r) / (1 + r), nmax = (1 + rs) / (1 - rs), n = nmax + (nmin - nmax) * g;
+        c.cn[i] = n;
+        c.ck[i] = std::sqrt(std::max(((n + 1) * (n + 1) * r - (n - 1) * (n - 1)) / (1 - r), 0.0));
+    }
+    c.cw = m.coat_weight;
+    c.crough = m.coat_roughness;
+    c.calpha = std::max(c.crough * c.crough, 1e-4);
+    c.crough_d = std::sqrt(c.calpha);
+    c.cior = m.coat_ior;
+    return c;
+}
+double p_refl(P3 wo, P3 wi, double a, int fk, double eta, const double *n, const double *k, const double *col, double f[3]) {
+    f[0] = f[1] = f[2] = 0;
+    P3 wh = padd(wo, wi);
+    const double co = wo[2], ci = wi[2];
+    if (pdot(wh, wo) * pdot(wi, wh) < 0 || (wh[0] == 0 && wh[1] == 0 && wh[2] == 0) || ci == 0 || co == 0 || !psame(wo, wi))
+        return 0;
+    wh = pnorm(wh);
+    const double cf = pdot(wi, wh[2] < 0 ? pmul(wh, -1) : wh);
+    const double s = std::fabs(0.25 * p_d(wh, a) / (1 + p_lambda(wo, a) + p_lambda(wi, a)) / (ci * co)) * std::fabs(ci);
+    for (int i = 0; i < 3; i++) f[i] = col[i] * (fk == 0 ? p_fr_diel(cf, eta) : p_fr_cond(std::fabs(cf), n[i], k[i])) * s;
+    return p_vpdf(wo, wh, a) / (4 * std::fabs(pdot(wo, wh)));
+}
+double p_trans(P3 wo, P3 wi, double a, double eta, const double *col, double f[3]) {
+    f[0] = f[1] = f[2] = 0;
+    const double co = wo[2], ci = wi[2], e = co > 0 ? eta : 1 / eta;
+    P3 wh = pnorm(padd(wo, pmul(wi, e)));
+    if (wh[2] < 0) wh = pmul(wh, -1);
+    const bool back = pdot(wh, wi) * ci < 0 || pdot(wh, wo) * co < 0;
+    if (pdot(wh, wo) * pdot(wi, wh) > 0 || ci == 0 || co == 0 || back || psame(wo, wi)) return 0;
+    const double F = p_fr_diel(pdot(wo, wh), eta), q = pdot(wi, wh) + pdot(wo, wh) / e, den = q * q * ci * co;
+    const double G = 1 / (1 + p_lambda(wo, a) + p_lambda(wi, a));
+    if (den != 0) {
+        const double s = std::fabs(p_d(wh, a) * G / (e * e) * std::fabs(pdot(wi, wh)) * std::fabs(pdot(wo, wh)) / den) * std::fabs(ci);
+        for (int i = 0; i < 3; i++) f[i] = (1 - F) * col[i] * s;
+    }
+    return q * q == 0 ? 0 : p_vpdf(wo, wh, a) * std::fabs(pdot(wi, wh)) / (q * q);
+}
+double p_eval(const PCl &c, P3 wo, P3 wi, double f[3]) {
+    const double mu = std::fabs(wo[2]), E = 1e-4;
+    double f1[3], p1;
+    {
+        double fa[3] = {0, 0, 0}, fb[3] = {0, 0, 0}, pa = 0, pb = 0;
+        if (c.trans < 1 - E && psame(wo, wi)) {
+            const double k = std::fabs(wi[2]) / kPiD;
+            for (int i = 0; i < 3; i++) fa[i] = c.base[i] * k;
+            pa = k;
+        }
+        if (c.trans > E) {
+            double ft[3], fr[3];
+            const double pt = p_trans(wo, wi, c.alpha, c.ior, c.tcol, ft);
+            const double pr = p_refl(wo, wi, c.alpha, 0, c.ior, nullptr, nullptr, c.base, fr);
+            for (int i = 0; i < 3; i++) fb[i] = ft[i] + fr[i];
+            pb = plerp(pt, pr, p_fr_diel(wo[2], c.ior));
+        }
+        for (int i = 0; i < 3; i++) f1[i] = plerp(fa[i], fb[i], c.trans);
+        p1 = plerp(pa, pb, c.trans);
+    }
+    double f2[3], p2;
+    {
+        const double A = p_albedo(c.rough, mu, c.seta), frac = c.sf0 * c.stl * A;
+        const double col[3] = {c.stint[0] * c.sf0, c.stint[1] * c.sf0, c.stint[2] * c.sf0};
+        double fs[3];
+        const double ps = p_refl(wo, wi, c.alpha, 0, c.seta, nullptr, nullptr, col, fs);
+        for (int i = 0; i < 3; i++) f2[i] = f1[i] * (1 - c.stint[i] * c.sf0 * A) + fs[i];
+        p2 = plerp(p1, ps, frac);
+    }
+    double f3[3], p3v;
+    {
+        double fa[3] = {0, 0, 0}, fm[3] = {0, 0, 0}, pa = 0, pm = 0;
+        if (c.metallic < 1 - E) {
+            for (int i = 0; i < 3; i++) fa[i] = f2[i];
+            pa = p2;
+        }
+        if (c.metallic > E) {
+            const double one[3] = {1, 1, 1};
+            pm = p_refl(wo, wi, c.alpha, 1, 0, c.cn, c.ck, one, fm);
+        }
+        for (int i = 0; i < 3; i++) f3[i] = plerp(fa[i], fm[i], c.metallic);
+        p3v = plerp(pa, pm, c.metallic);
+    }
+    const double A = p_albedo(c.crough, mu, c.cior), frac = c.cw * A;
+    const double col[3] = {c.cw, c.cw, c.cw};
+    double fc[3];
+    const double pc = p_refl(wo, wi, c.calpha, 0, c.cior, nullptr, nullptr, col, fc);
+    for (int i = 0; i < 3; i++) f[i] = f3[i] * plerp(1, c.ctint[i] * (1 - A), c.cw) + fc[i];
+    return plerp(p3v, pc, frac);
+}
+inline bool p_choose_b(double frac, double &u) {
+    if (u < frac) {
+        u /= frac;
+        return true;
+    }
+    u = (u - frac) / (1 - frac);
+    return false;
+}
+bool p_sample(const PCl &c, P3 wo, double u, double u0, double u1, P3 *wi) {
+    const double mu = std::fabs(wo[2]);
+    if (p_choose_b(c.cw * p_albedo(c.crough, mu, c.cior), u)) {
+        *wi = p_reflect(wo, p_sample_wh(wo, c.calpha, u0, u1));
+        return psame(wo, *wi);
+    }
+    if (p_choose_b(c.metallic, u) || p_choose_b(c.sf0 * c.stl * p_albedo(c.rough, mu, c.seta), u)) {
+        *wi = p_reflect(wo, p_sample_wh(wo, c.alpha, u0, u1));
+        return psame(wo, *wi);
+    }
+    if (p_choose_b(c.trans, u)) {
+        const P3 wh = p_sample_wh(wo, c.alpha, u0, u1);
+        if (p_choose_b(p_fr_diel(wo[2], c.ior), u)) {
+            *wi = p_reflect(wo, wh);
+            return psame(wo, *wi);
+        }
+        if (!p_refract(wo, wh, c.ior, wi)) return false;
+        return !psame(wo, *wi);
+    }
+    const double r = std::sqrt(u0), ph = u1 * 2 * kPiD, x = r * std::cos(ph), y = r * std::sin(ph);
+    P3 w = p3(x, y, std::sqrt(std::max(1 - x * x - y * y, 0.0)));
+    if (!psame(wo, w)) w = pmul(w, -1);
+    *wi = w;
+    return true;
+}
+}  // namespace
+
+extern "C" void orc_principled_table(double *out) {
+    const PTab &t = p_table();
+    std::copy(t.v.begin(), t.v.end(), out);
+}
+// shading frame: n x 3 wo / wi; f n x 3 (f * |cos_i|), pdf n
+extern "C" void orc_principled_eval(const sty_scene_material *m, uint64_t n, const double *wo, const double *wi,
+                                    double *f, double *pdf) {
+    const PCl c = p_closure(*m);
+    p_table();
+#pragma omp parallel for
+    for (int64_t i = 0; i < (int64_t)n; i++)
+        pdf[i] = p_eval(c, p3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), p3(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]), f + 3 * i);
+}
+// u: n x 3 (u_select, u0, u1); outputs wi, f, pdf (pdf 0 = invalid), as SurfaceClosure::sample
+extern "C" void orc_principled_sample(const sty_scene_material *m, uint64_t n, const double *wo, const double *u,
+                                      double *wi, double *f, double *pdf) {
+    const PCl c = p_closure(*m);
+    p_table();
+#pragma omp parallel for
+    for (int64_t i = 0; i < (int64_t)n; i++) {
+        const P3 o = p3(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]);
+        P3 w = p3(0, 0, 0);
+        double p = 0, fv[3] = {0, 0, 0};
+        if (p_sample(c, o, u[3 * i], u[3 * i + 1], u[3 * i + 2], &w)) p = p_eval(c, o, w, fv);
+        if (!(p > 0)) {
+            p = 0;
+            fv[0] = fv[1] = fv[2] = 0;
+        }
+        for (int k = 0; k < 3; k++) {
+            wi[3 * i + k] = w[k];
+            f[3 * i + k] = fv[k];
+        }
+        pdf[i] = p;
     }
 }

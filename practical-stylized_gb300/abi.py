@@ -114,6 +114,9 @@ SIGNATURES = {
                                     C.c_uint64, C.POINTER(C.c_uint64), _VP]),
     "sty_nrc_render": (C.c_int32, [C.c_void_p, C.c_void_p, _VP, _VP, C.c_uint32, _VP, _VP, _VP]),
     "sty_brpt_render": (C.c_int32, [C.c_void_p, _VP, _VP, C.c_uint32, _VP, _VP, _VP]),
+    "sty_bsdf_eval": (C.c_int32, [_VP, C.c_uint64, _VP, _VP, _VP, _VP, _VP]),
+    "sty_bsdf_sample": (C.c_int32, [_VP, C.c_uint64, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "sty_principled_table": (C.c_int32, [_VP]),
     "sty_nrc_create": (C.c_int32, [_VP, C.POINTER(C.c_void_p)]),
     "sty_nrc_create_grid": (C.c_int32, [_VP, C.POINTER(C.c_void_p)]),
     "sty_nrc_destroy": (C.c_int32, [C.c_void_p]),

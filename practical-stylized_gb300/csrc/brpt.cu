@@ -133,7 +133,8 @@ __global__ void k_br_count(SceneView sc, uint32_t n, uint32_t base, uint32_t dep
     if (prim != NONE && depth + 1 <= max_depth) {
         const sty_scene_material m = sc.materials[sc.tri_material[prim]];
         const uint32_t ab = s.ab[g];
-        c = lobe_roughness(m) > 0.01f ? (ab < inner.n ? inner.v[ab] : 1u) : 1u;
+        const F3 ng = get3(s.ng, g), wo = get3(s.wo, g);
+        c = lobe_roughness(m, sc.ggx_tab, ng, wo) > 0.01f ? (ab < inner.n ? inner.v[ab] : 1u) : 1u;
     }
     s.nchild[g] = c;
 }
@@ -156,7 +157,7 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
     const F3 p = get3(s.p, pg), ng = get3(s.ng, pg), wo = get3(s.wo, pg);
     const sty_scene_material m = sc.materials[sc.tri_material[prim]];
     const uint32_t new_flags = update_flags(m, s.flags[pg]);
-    const uint32_t ab = s.ab[pg] + (lobe_roughness(m) > 0.01f ? 1u : 0u);
+    const uint32_t ab = s.ab[pg] + (lobe_roughness(m, sc.ggx_tab, ng, wo) > 0.01f ? 1u : 0u);
     const uint64_t key = child_key(s.key[pg], sidx);
     sty_pcg32 st = key_stream(key);
     // NEE (sample_light :727-783, shaded with balance MIS in sample_surface_and_shade_direct :170-197)
@@ -167,7 +168,7 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
         float lpdf;
         if (nee_sample(sc, p, ng, prim, new_flags, depth, progs, n_progs, st, &lwi, &li, &lpdf)) {
             F3 f;
-            const float bp = bsdf_eval(m, ng, ng, wo, lwi, &f);
+            const float bp = bsdf_eval(m, ng, ng, wo, lwi, &f, sc.ggx_tab);
             const float w = lpdf / (lpdf + bp) / lpdf;
             direct = f3m(li.x * f.x, li.y * f.y, li.z * f.z) * w;
         }
@@ -182,10 +183,10 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
     put3(s.thr, cg, f3m(0.0f, 0.0f, 0.0f));
     const float usel = next_1d(st), u0 = next_1d(st), u1 = next_1d(st);
     float pdf = 0.0f;
-    const F3 wi = bsdf_sample(m, ng, ng, wo, usel, u0, u1, &pdf);
+    const F3 wi = bsdf_sample(m, ng, ng, wo, usel, u0, u1, &pdf, sc.ggx_tab);
     if (!(pdf > 0.0f)) return;
     F3 f;
-    bsdf_eval(m, ng, ng, wo, wi, &f);
+    bsdf_eval(m, ng, ng, wo, wi, &f, sc.ggx_tab);
     const F3 ro = offset_ray_origin(p, face_forward(ng, wi));
     const float o3[3] = {ro.x, ro.y, ro.z}, d3[3] = {wi.x, wi.y, wi.z};
     const Hit h = trace_closest(sc, o3, d3, 0.0f, 1e20f, prim);

@@ -14,6 +14,9 @@
 #include <algorithm>
 #include <cmath>
 
+#include <vector>
+
+#include "bsdf.cuh"
 #include "common.cuh"
 #include "style.cuh"
 
@@ -118,8 +121,20 @@ __device__ __forceinline__ float tr_lambda(float cw, float a) {  // microfacet.r
     const float l = (-1.0f + sqrtf(1.0f + a * a * at * at)) * 0.5f;
     return isfinite(at) ? l : 0.0f;
 }
-// Surface::evaluate: f*|cos_i| and pdf (diffuse.rs:17-48; mod.rs:1877-1910 with unit Fresnel)
-__device__ void bsdf_eval(const sty_pf_material &m, V3 ns, V3 ng, V3 wo, V3 wi, float f[3], float *pdf) {
+__device__ __forceinline__ bsdf::B3 tob(V3 v) { return bsdf::b3(v.x, v.y, v.z); }
+// the principled closure (inlined: an out-of-line call costs the filter more spills than it saves)
+__device__ __forceinline__ float princ_eval(const bsdf::PClosure *pc, const float *tab, V3 ns, V3 ng, V3 wo, V3 wi,
+                                         float *f) {
+    return bsdf::eval_world(*pc, tab, tob(ns), tob(ng), tob(wo), tob(wi), f);
+}
+// Surface::evaluate: f*|cos_i| and pdf (diffuse.rs:17-48; mod.rs:1877-1910 with unit Fresnel; the
+// principled closure pc with the albedo table tab, bsdf.cuh)
+__device__ void bsdf_eval(const sty_pf_material &m, V3 ns, V3 ng, V3 wo, V3 wi, float f[3], float *pdf,
+                          const bsdf::PClosure *pc, const float *tab) {
+    if (m.kind == STY_MAT_PRINCIPLED) {
+        *pdf = princ_eval(pc, tab, ns, ng, wo, wi, f);
+        return;
+    }
     f[0] = f[1] = f[2] = 0.0f;
     *pdf = 0.0f;
     if (!wo_wi_valid(ns, ng, wo, wi)) return;
@@ -280,14 +295,15 @@ struct __align__(16) NbFrame {  // 64 bytes: four 16-byte shared-memory reads
     float co;      // wo . ns
     float alpha;   // GGX: max(alpha, 1e-4)
     float g1;      // GGX: 1 / (1 + Lambda(co))
-    uint32_t bits; // bit 0: the wo half of check_wo_wi_valid holds; bit 1: GGX
-    uint32_t pad[2];
+    uint32_t bits; // bit 0: the wo half of check_wo_wi_valid holds; bit 1: GGX; bit 2: principled
+    uint32_t mat;  // material index (the principled closure)
+    uint32_t pad;
 };
 // rounded up to 16 bytes so that every warp's scratch starts 16-byte aligned for any R
 __host__ __device__ constexpr size_t warp_scratch_bytes(uint32_t R) {
     return ((size_t)R * (sizeof(unsigned long long) + sizeof(uint32_t) + sizeof(NbFrame)) + 15u) & ~(size_t)15u;
 }
-__device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, V3 ns, V3 ng, V3 wo) {
+__device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, uint32_t mi, V3 ns, V3 ng, V3 wo) {
     auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
     NbFrame f;
     f.ns[0] = ns.x, f.ns[1] = ns.y, f.ns[2] = ns.z;
@@ -299,14 +315,20 @@ __device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, V3 ns, V
     const bool ggx = m.kind != STY_MAT_DIFFUSE;
     f.alpha = fmaxf(m.alpha, 1e-4f);
     f.g1 = ggx ? 1.0f / (1.0f + tr_lambda(f.co, f.alpha)) : 0.0f;
-    f.bits = (ok ? 1u : 0u) | (ggx ? 2u : 0u);
+    f.bits = (ok ? 1u : 0u) | (ggx ? 2u : 0u) | (m.kind == STY_MAT_PRINCIPLED ? 4u : 0u);
+    f.mat = mi;
+    f.pad = 0;
     return f;
 }
 // the pdf of bsdf_eval for a precomputed frame (same arithmetic; the lane-dependent validity tests
 // become selects, only the frame's lobe -- the same on every lane -- branches)
-__device__ __forceinline__ float frame_pdf(const NbFrame &f, V3 wi) {
+__device__ __forceinline__ float frame_pdf(const NbFrame &f, V3 wi, const bsdf::PClosure *cls, const float *tab) {
     auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
     const V3 ns = {f.ns[0], f.ns[1], f.ns[2]}, ng = {f.ng[0], f.ng[1], f.ng[2]};
+    if (f.bits & 4u) {  // principled: the closure's pdf (no precomputed terms)
+        float fv[3];
+        return princ_eval(cls + f.mat, tab, ns, ng, V3{f.wo[0], f.wo[1], f.wo[2]}, wi, fv);
+    }
     const float ci = dot3(wi, ns), co = f.co;
     const bool ok = (f.bits & 1u) && sgn(f.fl * ci) * sgn(dot3(wi, ng)) > 0.0f && co * ci >= 0.0f;
     if (!(f.bits & 2u)) return ok ? fabsf(ci) / kPi : 0.0f;
@@ -346,6 +368,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
                                                     const uint32_t *sorted, const float4 *spos, const uint32_t *scid,
                                                     const uint32_t *cid, const float *in_next, sty_pf_ref_params prm,
                                                     const sty_pf_material *mats, uint32_t n_mats,
+                                                    const bsdf::PClosure *cls, const float *tab,
                                                     const sty_style_program *progs, uint32_t n_progs, sty_pcg32 *rng,
                                                     float *out, uint32_t *neighbours) {
     extern __shared__ __align__(16) uint8_t smem_raw[];
@@ -448,12 +471,15 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
     for (uint32_t t = lane; t < k; t += 32) {
         const uint32_t u = (uint32_t)keys[t];
         list[t] = u;
-        frames[t] = make_frame(mats[min(v.material[u], n_mats - 1)], ld3(v.ns, u), ld3(v.ng, u), ld3(v.wo, u));
+        const uint32_t mu = min(v.material[u], n_mats - 1);
+        frames[t] = make_frame(mats[mu], mu, ld3(v.ns, u), ld3(v.ng, u), ld3(v.wo, u));
     }
     __syncwarp();
 
     // ---- evaluate
-    const sty_pf_material mv = mats[min(v.material[vi], n_mats - 1)];
+    const uint32_t mvi = min(v.material[vi], n_mats - 1);
+    const sty_pf_material mv = mats[mvi];
+    const bsdf::PClosure *pcv = cls + mvi;
     const V3 wo = ld3(v.wo, vi), ns = ld3(v.ns, vi), ng = ld3(v.ng, vi);
     float direct[3] = {0.f, 0.f, 0.f}, indirect[3] = {0.f, 0.f, 0.f};
     const float invk = k ? 1.0f / (float)k : 0.0f;
@@ -469,7 +495,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             const float dpdf = v.dir_pdf[u];
             if (dpdf > 0.0f) {  // :839-863
                 float f[3], pdf;
-                bsdf_eval(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf);
+                bsdf_eval(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf, pcv, tab);
                 const float w = dpdf / (dpdf + pdf);
 #pragma unroll
                 for (int c = 0; c < 3; c++) direct[c] += f[c] * v.dir_l[c][u] * w / dpdf * invk;
@@ -478,7 +504,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             if (dot3(wi, wi) != 0.0f) {
                 ind = true;
                 float f[3];
-                bsdf_eval(mv, ns, ng, wo, wi, f, &pdf_v);
+                bsdf_eval(mv, ns, ng, wo, wi, f, &pdf_v, pcv, tab);
                 const float mis = v.ind_mis[u];
 #pragma unroll
                 for (int c = 0; c < 3; c++) reused[c] = f[c] * (in_next ? in_next[c * n + u] : 0.0f) * mis;
@@ -488,14 +514,14 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             float sum_pdf = 0.0f;
             uint32_t a = 0;
             for (; a + 4 <= k; a += 4) {
-                const float p0 = frame_pdf(frames[a], wi), p1 = frame_pdf(frames[a + 1], wi);
-                const float p2 = frame_pdf(frames[a + 2], wi), p3 = frame_pdf(frames[a + 3], wi);
+                const float p0 = frame_pdf(frames[a], wi, cls, tab), p1 = frame_pdf(frames[a + 1], wi, cls, tab);
+                const float p2 = frame_pdf(frames[a + 2], wi, cls, tab), p3 = frame_pdf(frames[a + 3], wi, cls, tab);
                 sum_pdf += p0;  // in list order, as the sequential sum
                 sum_pdf += p1;
                 sum_pdf += p2;
                 sum_pdf += p3;
             }
-            for (; a < k; a++) sum_pdf += frame_pdf(frames[a], wi);
+            for (; a < k; a++) sum_pdf += frame_pdf(frames[a], wi, cls, tab);
             if (ind && sum_pdf > 0.0f)
 #pragma unroll
                 for (int c = 0; c < 3; c++) indirect[c] += reused[c] / sum_pdf;
@@ -540,6 +566,8 @@ struct sty_pf_ref_ctx {
     float4 *spos = nullptr;  // bucket-ordered position + flags
     uint32_t *scid = nullptr;  // bucket-ordered cluster id
     sty_pf_material *mats = nullptr;      // device copies of the host tables
+    sty::bsdf::PClosure *cls = nullptr;   // principled closures of the materials (host-built)
+    std::vector<sty::bsdf::PClosure> hcls;  // their host copy (the async upload's source)
     sty_style_program *progs = nullptr;
     void *tmp = nullptr;
     size_t tmp_bytes = 0;
@@ -552,7 +580,7 @@ namespace {
 void free_ctx(sty_pf_ref_ctx *c) {
     void *ptrs[] = {c->act,   c->num,    c->keys,  c->vals,    c->keys_s,  c->vals_s, c->ranges, c->cid,
                     c->csize, c->size0,  c->prop,  c->winner,  c->counter, c->mats,   c->progs,  c->tmp,
-                    c->spos,  c->scid};
+                    c->spos,  c->scid,   c->cls};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -620,6 +648,7 @@ sty_status sty_pf_ref_create(uint64_t max_vertices, uint32_t table_size, sty_pf_
     alloc((void **)&c->spos, n * sizeof(float4), "alloc sorted positions");
     alloc((void **)&c->scid, n * 4, "alloc sorted cluster ids");
     alloc((void **)&c->mats, kMaxMaterials * sizeof(sty_pf_material), "alloc materials");
+    alloc((void **)&c->cls, kMaxMaterials * sizeof(bsdf::PClosure), "alloc closures");
     alloc((void **)&c->progs, kMaxPrograms * sizeof(sty_style_program), "alloc programs");
     if (st == STY_OK) {
         size_t b1 = 0, b2 = 0;
@@ -694,6 +723,15 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     const unsigned nb = (unsigned)((n + bs - 1) / bs);
     STY_TRY(check_cuda(cudaMemcpyAsync(ctx->mats, materials, n_materials * sizeof(sty_pf_material),
                                        cudaMemcpyHostToDevice, st), "upload materials"));
+    ctx->hcls.resize(n_materials);
+    for (uint32_t i = 0; i < n_materials; i++) ctx->hcls[i] = bsdf::make_closure(materials[i]);
+    STY_TRY(check_cuda(cudaMemcpyAsync(ctx->cls, ctx->hcls.data(), n_materials * sizeof(bsdf::PClosure),
+                                       cudaMemcpyHostToDevice, st), "upload closures"));
+    const float *ggx_tab = principled_table();
+    if (!ggx_tab) {
+        set_error("principled albedo table unavailable");
+        return STY_ERR_CUDA;
+    }
     if (n_programs)
         STY_TRY(check_cuda(cudaMemcpyAsync(ctx->progs, programs, n_programs * sizeof(sty_style_program),
                                            cudaMemcpyHostToDevice, st), "upload programs"));
@@ -777,8 +815,8 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     STY_TRY(check_cuda(cudaMemsetAsync(ctx->counter, 0, 4, st), "reset work counter"));
     k_ref_filter<<<nbf, 32 * wpb, smem, st>>>(va, g, ctx->num, ctx->counter, ctx->ranges, ctx->vals_s, ctx->spos,
                                               ctx->scid, ctx->cid,
-                                              in_next, *prm, ctx->mats, n_materials, ctx->progs, n_programs, rng, out,
-                                              neighbours);
+                                              in_next, *prm, ctx->mats, n_materials, ctx->cls, ggx_tab, ctx->progs,
+                                              n_programs, rng, out, neighbours);
     STY_TRY(check_launch("k_ref_filter"));
     if (cluster_id)
         STY_TRY(check_cuda(cudaMemcpyAsync(cluster_id, ctx->cid, n * 4, cudaMemcpyDeviceToDevice, st), "copy cid"));

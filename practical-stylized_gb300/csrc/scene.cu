@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "bsdf.cuh"
 #include "scene.cuh"
 
 using namespace sty;
@@ -39,6 +40,7 @@ SceneView scene_view(const sty_scene *s) {
     v.light_cdf = s->light_cdf;
     v.n_lights = s->n_lights;
     v.tri_pos = s->tri_pos;
+    v.ggx_tab = principled_table();
     return v;
 }
 }  // namespace sty
@@ -205,7 +207,14 @@ sty_status sty_scene_create(const float *pos, const uint32_t *tmat, uint32_t n, 
     STY_ARG_CHECK(cam->width > 0 && cam->height > 0 && cam->fov_y > 0.0f && cam->fov_y < 180.0f, "bad camera");
     for (uint32_t i = 0; i < n; i++) STY_ARG_CHECK(tmat[i] < nm, "triangle %u has material %u >= %u", i, tmat[i], nm);
     for (uint32_t i = 0; i < nm; i++)
-        STY_ARG_CHECK(mats[i].kind == STY_MAT_DIFFUSE || mats[i].kind == STY_MAT_GGX, "material %u: unknown kind", i);
+        STY_ARG_CHECK(mats[i].kind == STY_MAT_DIFFUSE || mats[i].kind == STY_MAT_GGX ||
+                          mats[i].kind == STY_MAT_PRINCIPLED,
+                      "material %u: unknown kind", i);
+    for (uint32_t i = 0; i < nm; i++)
+        STY_ARG_CHECK(mats[i].kind != STY_MAT_PRINCIPLED ||
+                          (mats[i].ior > 0.0f && mats[i].coat_ior > 0.0f && mats[i].roughness >= 0.0f &&
+                           mats[i].coat_roughness >= 0.0f),
+                      "material %u: principled ior / coat_ior must be > 0 and roughness >= 0", i);
     sty_scene *s = new sty_scene();
     s->n_tris = n;
     s->n_materials = nm;

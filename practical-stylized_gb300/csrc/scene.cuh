@@ -31,6 +31,7 @@ struct SceneView {
     const float *light_cdf;         // n_lights + 1 entries, cdf[0] = 0, cdf[n] = 1
     uint32_t n_lights;
     const float *tri_pos;           // by original id, 9 per triangle
+    const float *ggx_tab;           // the principled BSDF's albedo table (bsdf.cuh)
 };
 
 struct Hit {

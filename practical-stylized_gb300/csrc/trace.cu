@@ -132,7 +132,7 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
         }
     }
     // final-gathering renders stop at the first rough vertex (splitting, nrc_pt.rs:372-375)
-    if (split_rough > 0.0f && lobe_roughness(m) > split_rough) {
+    if (split_rough > 0.0f && lobe_roughness(m, sc.ggx_tab, ns, wo) > split_rough) {
         ps.split[tid] = depth;
         ps.exclude[tid] = prim;  // the split vertex's triangle, skipped by its gather rays
         ps.terminated[tid] = 1;
@@ -142,7 +142,7 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
     // BSDF sample and continuation
     const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
     float pdf = 0.0f;
-    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf);
+    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf, sc.ggx_tab);
     if (pdf > 0.0f) {
         const F3 no = offset_ray_origin(p, face_forward(ng, wi));
         ps.o[0][tid] = no.x; ps.o[1][tid] = no.y; ps.o[2][tid] = no.z;
@@ -211,14 +211,14 @@ __global__ void k_self_radiance(SceneView sc, uint32_t n, VertOut v, const float
     const float dpdf = v.dir_pdf[i];
     if (dpdf > 0.0f) {
         F3 f;
-        const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f);
+        const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f, sc.ggx_tab);
         const float w = dpdf / (dpdf + bp) / dpdf;
         rad = rad + f3m(f.x * v.dir_l[0][i], f.y * v.dir_l[1][i], f.z * v.dir_l[2][i]) * w;
     }
     const F3 wi = f3m(v.ind_wi[0][i], v.ind_wi[1][i], v.ind_wi[2][i]);
     if (next && dot(wi, wi) != 0.0f) {
         F3 f;
-        const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+        const float bp = bsdf_eval(m, ns, ng, wo, wi, &f, sc.ggx_tab);
         if (bp > 0.0f) {
             const float s = v.ind_mis[i] / bp;
             rad = rad + f3m(f.x * next[i], f.y * next[n + i], f.z * next[2 * (size_t)n + i]) * s;
@@ -249,7 +249,7 @@ __device__ void write_features(const SceneView &sc, const FeatArgs &fa, F3 p, F3
     row[0] = (p.x - fa.bmin[0]) / fa.bext[0];
     row[1] = (p.y - fa.bmin[1]) / fa.bext[1];
     row[2] = (p.z - fa.bmin[2]) / fa.bext[2];
-    const float rough = m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
+    const float rough = lobe_roughness(m, sc.ggx_tab, ns, wo);
     if (fa.layout == STY_NRC_ROWS_SPHERICAL) {
         sph(ns, &row[3], &row[4]);
         sph(wo, &row[5], &row[6]);
@@ -400,7 +400,7 @@ __global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t 
         float lpdf;
         if (nee_sample(sc, p, ng, prim, fl, s, progs, n_progs, st, &lwi, &li, &lpdf)) {
             F3 f;
-            const float bp = bsdf_eval(m, ns, ng, wo, lwi, &f);
+            const float bp = bsdf_eval(m, ns, ng, wo, lwi, &f, sc.ggx_tab);
             const float w = lpdf / (lpdf + bp) / lpdf;
             acc_direct[i] += f.x * li.x * w;
             acc_direct[n + i] += f.y * li.y * w;
@@ -409,7 +409,7 @@ __global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t 
     }
     const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
     float pdf = 0.0f;
-    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf);
+    const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf, sc.ggx_tab);
     rng[i] = st;
     if (!(pdf > 0.0f)) return;
     const F3 o = offset_ray_origin(p, face_forward(ng, wi));
@@ -441,7 +441,7 @@ __global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t 
         if (mq.set_style == 3) qf |= 8u;
     }
     F3 f;
-    const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+    const float bp = bsdf_eval(m, ns, ng, wo, wi, &f, sc.ggx_tab);
     if (!(bp > 0.0f)) return;
     thr[i] = f.x / bp;
     thr[n + i] = f.y / bp;
@@ -490,7 +490,7 @@ __global__ void k_fg_sweep(SceneView sc, uint32_t n, uint32_t d, VertOut v, cons
         const float dpdf = v.dir_pdf[i];
         if (dpdf > 0.0f) {
             F3 f;
-            const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f);
+            const float bp = bsdf_eval(m, ns, ng, wo, f3m(v.dir_wi[0][i], v.dir_wi[1][i], v.dir_wi[2][i]), &f, sc.ggx_tab);
             const float w = dpdf / (dpdf + bp) / dpdf;
             dir = f3m(f.x * v.dir_l[0][i] * w, f.y * v.dir_l[1][i] * w, f.z * v.dir_l[2][i] * w);
         }
@@ -508,7 +508,7 @@ __global__ void k_fg_sweep(SceneView sc, uint32_t n, uint32_t d, VertOut v, cons
             const F3 wi = f3m(v.ind_wi[0][i], v.ind_wi[1][i], v.ind_wi[2][i]);
             if (next && dot(wi, wi) != 0.0f) {
                 F3 f;
-                const float bp = bsdf_eval(m, ns, ng, wo, wi, &f);
+                const float bp = bsdf_eval(m, ns, ng, wo, wi, &f, sc.ggx_tab);
                 if (bp > 0.0f) {
                     const float k = v.ind_mis[i] / bp;
                     r.x += f.x * next[i] * k;
@@ -725,6 +725,18 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
         for (int c = 0; c < 3; c++) pm[i].albedo[c] = mh[i].albedo[c];
         pm[i].alpha = mh[i].alpha;
         for (int c = 0; c < 4; c++) pm[i].style[c] = mh[i].style[c];
+        pm[i].roughness = mh[i].roughness;
+        pm[i].metallic = mh[i].metallic;
+        pm[i].ior = mh[i].ior;
+        pm[i].transmission = mh[i].transmission;
+        pm[i].specular_ior_level = mh[i].specular_ior_level;
+        pm[i].coat_weight = mh[i].coat_weight;
+        pm[i].coat_roughness = mh[i].coat_roughness;
+        pm[i].coat_ior = mh[i].coat_ior;
+        for (int c = 0; c < 3; c++) {
+            pm[i].specular_tint[c] = mh[i].specular_tint[c];
+            pm[i].coat_tint[c] = mh[i].coat_tint[c];
+        }
     }
     float bmin[3], bmax[3];
     for (int a = 0; a < 3; a++) {

@@ -6,6 +6,7 @@
 
 #include <cmath>
 
+#include "bsdf.cuh"
 #include "common.cuh"
 #include "scene.cuh"
 #include "style.cuh"
@@ -111,7 +112,20 @@ __device__ __forceinline__ float tr_lambda(float cw, float a) {
     const float l = (-1.0f + sqrtf(1.0f + a * a * at * at)) * 0.5f;
     return isfinite(at) ? l : 0.0f;
 }
-__device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi) {
+__device__ __forceinline__ bsdf::B3 tob(F3 v) { return bsdf::b3(v.x, v.y, v.z); }
+// STY_MAT_PRINCIPLED through the shared closure (bsdf.cuh); tab = the scene's albedo table
+__device__ __forceinline__ float princ_eval(const sty_scene_material &m, const float *tab, F3 ns, F3 ng, F3 wo, F3 wi,
+                                            F3 *f) {
+    float fv[3];
+    const float p = bsdf::eval_world(bsdf::make_closure(m), tab, tob(ns), tob(ng), tob(wo), tob(wi), fv);
+    *f = f3m(fv[0], fv[1], fv[2]);
+    return p;
+}
+__device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, const float *tab) {
+    if (m.kind == STY_MAT_PRINCIPLED) {
+        F3 f;
+        return princ_eval(m, tab, ns, ng, wo, wi, &f);
+    }
     if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
     const float co = dot(wo, ns), ci = dot(wi, ns);
     if (m.kind == STY_MAT_DIFFUSE) return co * ci >= 0.0f ? fabsf(ci) / kPi : 0.0f;
@@ -127,8 +141,13 @@ __device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 w
 }
 // Surface::sample: wi (world) and its pdf (0 = invalid)
 __device__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, float u_sel, float u0, float u1,
-                          float *pdf) {
-    (void)u_sel;
+                          float *pdf, const float *tab) {
+    if (m.kind == STY_MAT_PRINCIPLED) {
+        bsdf::B3 w = bsdf::b3(0.0f, 0.0f, 0.0f);
+        float fv[3];
+        bsdf::sample_world(bsdf::make_closure(m), tab, tob(ns), tob(ng), tob(wo), u_sel, u0, u1, &w, fv, pdf);
+        return f3m(w.x, w.y, w.z);
+    }
     const Frame fr = frame_from_n(ns);
     const F3 wol = to_local(fr, wo);
     F3 wil;
@@ -155,7 +174,7 @@ __device__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, floa
     }
     const F3 wi = to_world(fr, wil);
     valid = valid && wo_wi_valid(ns, ng, wo, wi);
-    *pdf = valid ? bsdf_pdf(m, ns, ng, wo, wi) : 0.0f;
+    *pdf = valid ? bsdf_pdf(m, ns, ng, wo, wi, tab) : 0.0f;
     return wi;
 }
 
@@ -223,7 +242,10 @@ __device__ bool nee_sample(const SceneView &sc, F3 p, F3 ng, uint32_t prim, uint
     *pdf_out = lpdf;
     return true;
 }
-__device__ __forceinline__ float lobe_roughness(const sty_scene_material &m) {  // avg_roughness
+// Surface::avg_roughness: diffuse 1, the GGX lobe its alpha (as the NL-PF paths have used it), the
+// principled closure the frac-weighted mean of its lobes' (which depends on wo)
+__device__ __forceinline__ float lobe_roughness(const sty_scene_material &m, const float *tab, F3 ns, F3 wo) {
+    if (m.kind == STY_MAT_PRINCIPLED) return bsdf::avg_roughness_world(bsdf::make_closure(m), tab, tob(ns), tob(wo));
     return m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
 }
 
@@ -249,7 +271,8 @@ __global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
 
 // f * |cos| (rgb) and pdf of a scene material (Surface::evaluate; diffuse.rs:17-48,
 // svm/surface/mod.rs:1877-1910 with unit Fresnel)
-__device__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f) {
+__device__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f, const float *tab) {
+    if (m.kind == STY_MAT_PRINCIPLED) return princ_eval(m, tab, ns, ng, wo, wi, f);
     *f = f3m(0.0f, 0.0f, 0.0f);
     if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
     const float co = dot(wo, ns), ci = dot(wi, ns);

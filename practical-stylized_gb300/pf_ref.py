@@ -20,7 +20,10 @@ STY_MAT_GGX = 1
 
 
 class PfMaterial(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("albedo", C.c_float * 3), ("alpha", C.c_float), ("style", C.c_int32 * 4)]
+    _fields_ = [("kind", C.c_int32), ("albedo", C.c_float * 3), ("alpha", C.c_float), ("style", C.c_int32 * 4),
+                ("roughness", C.c_float), ("metallic", C.c_float), ("ior", C.c_float), ("transmission", C.c_float),
+                ("specular_ior_level", C.c_float), ("specular_tint", C.c_float * 3), ("coat_weight", C.c_float),
+                ("coat_roughness", C.c_float), ("coat_ior", C.c_float), ("coat_tint", C.c_float * 3)]
 
 
 class PfVertices(C.Structure):

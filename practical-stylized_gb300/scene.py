@@ -16,6 +16,7 @@ from .abi import check, lib
 
 MAT_DIFFUSE = 0
 MAT_GGX = 1
+MAT_PRINCIPLED = 2
 NRC_SAMPLES_TRAIN = 0
 NRC_SAMPLES_QUERY = 1
 NRC_ROWS_REF = 0
@@ -24,7 +25,10 @@ NRC_ROWS_SPHERICAL = 1
 
 class SceneMaterial(C.Structure):
     _fields_ = [("kind", C.c_int32), ("albedo", C.c_float * 3), ("alpha", C.c_float), ("emission", C.c_float * 3),
-                ("style", C.c_int32 * 4), ("set_style", C.c_int32)]
+                ("style", C.c_int32 * 4), ("set_style", C.c_int32),
+                ("roughness", C.c_float), ("metallic", C.c_float), ("ior", C.c_float), ("transmission", C.c_float),
+                ("specular_ior_level", C.c_float), ("specular_tint", C.c_float * 3), ("coat_weight", C.c_float),
+                ("coat_roughness", C.c_float), ("coat_ior", C.c_float), ("coat_tint", C.c_float * 3)]
 
 
 class Camera(C.Structure):
@@ -94,6 +98,24 @@ def material(kind=MAT_DIFFUSE, albedo=(0.75, 0.75, 0.75), alpha=0.3, emission=(0
     m.emission[:] = list(emission)
     m.style[:] = list(style)
     m.set_style = set_style
+    m.ior, m.specular_ior_level, m.coat_ior = 1.5, 0.5, 1.5
+    m.specular_tint[:] = [1.0, 1.0, 1.0]
+    m.coat_tint[:] = [1.0, 1.0, 1.0]
+    return m
+
+
+def principled(base_color=(0.8, 0.8, 0.8), roughness=0.5, metallic=0.0, ior=1.5, transmission=0.0,
+               specular_ior_level=0.5, specular_tint=(1, 1, 1), coat_weight=0.0, coat_roughness=0.03, coat_ior=1.5,
+               coat_tint=(1, 1, 1), emission=(0, 0, 0), style=(-1, -1, -1, -1), set_style=-1) -> SceneMaterial:
+    """The reference's principled BSDF (svm/surface/principled.rs; Blender's Principled BSDF inputs;
+    emission = emission colour x strength)."""
+    m = material(MAT_PRINCIPLED, base_color, alpha=max(roughness * roughness, 1e-4), emission=emission,
+                 style=style, set_style=set_style)
+    m.roughness, m.metallic, m.ior, m.transmission = roughness, metallic, ior, transmission
+    m.specular_ior_level = specular_ior_level
+    m.specular_tint[:] = list(specular_tint)
+    m.coat_weight, m.coat_roughness, m.coat_ior = coat_weight, coat_roughness, coat_ior
+    m.coat_tint[:] = list(coat_tint)
     return m
 
 

@@ -8,10 +8,11 @@ What the GPU path needs from a scene is extracted here on the host:
     Akari / Blender coordinate systems, scene.rs:31-60);
   * the camera (perspective TRS; camera space looks down -z and `fov` spans the longer image side,
     camera/mod.rs:129-151) as a look-at sty_camera;
-  * materials: the surface under the style wrappers mapped onto the tracer's lobes (principled ->
-    GGX with alpha = roughness^2, microfacet.rs:39-41; diffuse -> Lambert; emission -> emitter, the
-    mesh lights of load.rs:95-128); constant inputs only -- textured inputs fall back to a grey 0.5
-    and are listed in `warnings`;
+  * materials: the surface under the style wrappers (principled -> STY_MAT_PRINCIPLED, the
+    reference's principled closure with the node's roughness, metallic, ior, transmission,
+    specular and coat inputs, principled.rs:118-330; diffuse -> Lambert; emission -> emitter, the
+    mesh lights of load.rs:95-128); constant inputs only -- textured inputs (and normal maps) fall
+    back to constants and are listed in `warnings`;
   * the style graphs: for each style index s = 0..3 the ordered list of style nodes the graph
     applies (every sty_* node applies its inner surface's stylization first, then its own:
     svm/surface/mod.rs:275-285, 573-585; sty_enable_if follows `surface` when the path's style
@@ -29,7 +30,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import abi
-from .scene import MAT_DIFFUSE, MAT_GGX, camera, material
+from .scene import MAT_DIFFUSE, MAT_PRINCIPLED, camera, material, principled
 
 
 class UnsupportedNode(ValueError):
@@ -163,6 +164,7 @@ class LoadedMaterial:
     ops: list  # per style index: list of StyleNode
     set_style: int
     warnings: list = field(default_factory=list)
+    params: dict = field(default_factory=dict)  # principled inputs (scene.principled keywords)
 
 
 def convert_material(name, mat) -> LoadedMaterial:
@@ -186,12 +188,21 @@ def convert_material(name, mat) -> LoadedMaterial:
             warn.append(f"{name}: {e}; using {default}")
             return default
 
-    kind, albedo, alpha, emission = MAT_DIFFUSE, (0.5, 0.5, 0.5), 1.0, (0.0, 0.0, 0.0)
+    kind, albedo, alpha, emission, params = MAT_DIFFUSE, (0.5, 0.5, 0.5), 1.0, (0.0, 0.0, 0.0), {}
     if t == "principled":
-        kind = MAT_GGX
+        kind = MAT_PRINCIPLED
         albedo = rgb(base.get("base_color"), (0.5, 0.5, 0.5))
         r = flt(base.get("roughness"), 0.5)
         alpha = max(r * r, 1e-4)
+        params = dict(roughness=r, metallic=flt(base.get("metallic"), 0.0), ior=flt(base.get("ior"), 1.45),
+                      transmission=flt(base.get("transmission_weight"), 0.0),
+                      specular_ior_level=flt(base.get("specular_ior_level"), 0.5),
+                      specular_tint=rgb(base.get("specular_tint"), (1.0, 1.0, 1.0)),
+                      coat_weight=flt(base.get("coat_weight"), 0.0), coat_roughness=flt(base.get("coat_roughness"), 0.03),
+                      coat_ior=flt(base.get("coat_ior"), 1.5), coat_tint=rgb(base.get("coat_tint"), (1.0, 1.0, 1.0)))
+        if base.get("normal") is not None and _node(nodes, base.get("normal")) is not None and \
+                _node(nodes, base.get("normal")).get("type") == "normal_map":
+            warn.append(f"{name}: normal map ignored (flat shading)")
         strength = flt(base.get("emission_strength"), 0.0)
         if strength and strength > 0:
             e = rgb(base.get("emission_color"), (0.0, 0.0, 0.0))
@@ -210,7 +221,7 @@ def convert_material(name, mat) -> LoadedMaterial:
     for s, o in enumerate(ops):
         if len(o) > abi.STY_STYLE_MAX_NODES:
             raise UnsupportedNode(f"{name}: style index {s} applies {len(o)} nodes (max {abi.STY_STYLE_MAX_NODES})")
-    return LoadedMaterial(name, kind, albedo, alpha, emission, ops, set_style_index(nodes, out), warn)
+    return LoadedMaterial(name, kind, albedo, alpha, emission, ops, set_style_index(nodes, out), warn, params)
 
 
 def _program_key(nodes):
@@ -334,7 +345,9 @@ def load(path, bin_paths=None, width=None, height=None):
     names = list(graph["materials"].keys())
     loaded = [convert_material(k, graph["materials"][k]) for k in names]
     table, slots = build_style_table(loaded)
-    mats = [material(m.kind, m.albedo, m.alpha, m.emission, slots[i], m.set_style) for i, m in enumerate(loaded)]
+    mats = [principled(m.albedo, emission=m.emission, style=slots[i], set_style=m.set_style, **m.params)
+            if m.kind == MAT_PRINCIPLED else material(m.kind, m.albedo, m.alpha, m.emission, slots[i], m.set_style)
+            for i, m in enumerate(loaded)]
     mindex = {k: i for i, k in enumerate(names)}
     tris, mids = [], []
     for iname, inst in graph["instances"].items():

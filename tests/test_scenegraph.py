@@ -136,7 +136,8 @@ def test_synthetic_scene_load(sty, tmp_path):
     assert [names[m] for m in mids] == ["Grey", "Metal", "Metal", "Grey", "Lamp", "Lamp"]
     np.testing.assert_allclose(pos[2, 0], [0, 0.5, 0], atol=1e-6)  # Akari TRS translation
     grey, metal, lamp = (mats[names.index(k)] for k in ("Grey", "Metal", "Lamp"))
-    assert metal.kind == sty.scene.MAT_GGX and metal.alpha == pytest.approx(0.25)
+    assert metal.kind == sty.scene.MAT_PRINCIPLED and metal.roughness == pytest.approx(0.5)
+    assert metal.alpha == pytest.approx(0.25) and metal.ior == pytest.approx(1.45) and metal.metallic == 0.0
     assert list(lamp.emission) == pytest.approx([5.0, 4.5, 4.0])
     assert grey.style[0] >= 0 and list(grey.style)[1:] == [-1, -1, -1]
     assert sc["programs"][grey.style[0]].nodes[0].kind == sty.abi.STY_STYLE_TOON
