@@ -129,11 +129,32 @@ __device__ __forceinline__ float princ_eval(const bsdf::PClosure *pc, const floa
 }
 // Surface::evaluate: f*|cos_i| and pdf (diffuse.rs:17-48; mod.rs:1877-1910 with unit Fresnel; the
 // principled closure pc with the albedo table tab, bsdf.cuh)
-__device__ void bsdf_eval(const sty_pf_material &m, V3 ns, V3 ng, V3 wo, V3 wi, float f[3], float *pdf,
+// the fields of a material the diffuse / GGX evaluation and the style lookup read (the principled
+// path reads its precomputed closure instead)
+struct MatCore {
+    int32_t kind;
+    float albedo[3];
+    float alpha;
+    int32_t style[4];
+};
+__device__ __forceinline__ MatCore mat_core(const sty_pf_material &m) {
+    MatCore c;
+    c.kind = m.kind;
+    c.albedo[0] = m.albedo[0];
+    c.albedo[1] = m.albedo[1];
+    c.albedo[2] = m.albedo[2];
+    c.alpha = m.alpha;
+    for (int i = 0; i < 4; i++) c.style[i] = m.style[i];
+    return c;
+}
+template <bool PRINC>
+__device__ __forceinline__ void bsdf_eval(const MatCore &m, V3 ns, V3 ng, V3 wo, V3 wi, float f[3], float *pdf,
                           const bsdf::PClosure *pc, const float *tab) {
-    if (m.kind == STY_MAT_PRINCIPLED) {
-        *pdf = princ_eval(pc, tab, ns, ng, wo, wi, f);
-        return;
+    if constexpr (PRINC) {
+        if (m.kind == STY_MAT_PRINCIPLED) {
+            *pdf = princ_eval(pc, tab, ns, ng, wo, wi, f);
+            return;
+        }
     }
     f[0] = f[1] = f[2] = 0.0f;
     *pdf = 0.0f;
@@ -322,12 +343,15 @@ __device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, uint32_t
 }
 // the pdf of bsdf_eval for a precomputed frame (same arithmetic; the lane-dependent validity tests
 // become selects, only the frame's lobe -- the same on every lane -- branches)
+template <bool PRINC>
 __device__ __forceinline__ float frame_pdf(const NbFrame &f, V3 wi, const bsdf::PClosure *cls, const float *tab) {
     auto sgn = [](float x) { return x > 0.0f ? 1.0f : -1.0f; };
     const V3 ns = {f.ns[0], f.ns[1], f.ns[2]}, ng = {f.ng[0], f.ng[1], f.ng[2]};
-    if (f.bits & 4u) {  // principled: the closure's pdf (no precomputed terms)
-        float fv[3];
-        return princ_eval(cls + f.mat, tab, ns, ng, V3{f.wo[0], f.wo[1], f.wo[2]}, wi, fv);
+    if constexpr (PRINC) {
+        if (f.bits & 4u) {  // principled: the closure's pdf (no precomputed terms)
+            float fv[3];
+            return princ_eval(cls + f.mat, tab, ns, ng, V3{f.wo[0], f.wo[1], f.wo[2]}, wi, fv);
+        }
     }
     const float ci = dot3(wi, ns), co = f.co;
     const bool ok = (f.bits & 1u) && sgn(f.fl * ci) * sgn(dot3(wi, ng)) > 0.0f && co * ci >= 0.0f;
@@ -363,6 +387,9 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
     const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)x, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(x >> 32), src);
     return ((uint64_t)hi << 32) | lo;
 }
+// PRINC: some material is STY_MAT_PRINCIPLED (the variant without it keeps the diffuse / GGX path's
+// registers and stack as they were)
+template <bool PRINC>
 __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uint32_t *num, uint32_t *next,
                                                     const uint2 *ranges,
                                                     const uint32_t *sorted, const float4 *spos, const uint32_t *scid,
@@ -478,7 +505,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
 
     // ---- evaluate
     const uint32_t mvi = min(v.material[vi], n_mats - 1);
-    const sty_pf_material mv = mats[mvi];
+    const MatCore mv = mat_core(mats[mvi]);
     const bsdf::PClosure *pcv = cls + mvi;
     const V3 wo = ld3(v.wo, vi), ns = ld3(v.ns, vi), ng = ld3(v.ng, vi);
     float direct[3] = {0.f, 0.f, 0.f}, indirect[3] = {0.f, 0.f, 0.f};
@@ -495,7 +522,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             const float dpdf = v.dir_pdf[u];
             if (dpdf > 0.0f) {  // :839-863
                 float f[3], pdf;
-                bsdf_eval(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf, pcv, tab);
+                bsdf_eval<PRINC>(mv, ns, ng, wo, ld3(v.dir_wi, u), f, &pdf, pcv, tab);
                 const float w = dpdf / (dpdf + pdf);
 #pragma unroll
                 for (int c = 0; c < 3; c++) direct[c] += f[c] * v.dir_l[c][u] * w / dpdf * invk;
@@ -504,7 +531,7 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             if (dot3(wi, wi) != 0.0f) {
                 ind = true;
                 float f[3];
-                bsdf_eval(mv, ns, ng, wo, wi, f, &pdf_v, pcv, tab);
+                bsdf_eval<PRINC>(mv, ns, ng, wo, wi, f, &pdf_v, pcv, tab);
                 const float mis = v.ind_mis[u];
 #pragma unroll
                 for (int c = 0; c < 3; c++) reused[c] = f[c] * (in_next ? in_next[c * n + u] : 0.0f) * mis;
@@ -514,14 +541,16 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
             float sum_pdf = 0.0f;
             uint32_t a = 0;
             for (; a + 4 <= k; a += 4) {
-                const float p0 = frame_pdf(frames[a], wi, cls, tab), p1 = frame_pdf(frames[a + 1], wi, cls, tab);
-                const float p2 = frame_pdf(frames[a + 2], wi, cls, tab), p3 = frame_pdf(frames[a + 3], wi, cls, tab);
+                const float p0 = frame_pdf<PRINC>(frames[a], wi, cls, tab);
+                const float p1 = frame_pdf<PRINC>(frames[a + 1], wi, cls, tab);
+                const float p2 = frame_pdf<PRINC>(frames[a + 2], wi, cls, tab);
+                const float p3 = frame_pdf<PRINC>(frames[a + 3], wi, cls, tab);
                 sum_pdf += p0;  // in list order, as the sequential sum
                 sum_pdf += p1;
                 sum_pdf += p2;
                 sum_pdf += p3;
             }
-            for (; a < k; a++) sum_pdf += frame_pdf(frames[a], wi, cls, tab);
+            for (; a < k; a++) sum_pdf += frame_pdf<PRINC>(frames[a], wi, cls, tab);
             if (ind && sum_pdf > 0.0f)
 #pragma unroll
                 for (int c = 0; c < 3; c++) indirect[c] += reused[c] / sum_pdf;
@@ -799,12 +828,15 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     uint32_t wpb = (uint32_t)std::min<size_t>(8, (96u * 1024u) / wsb);
     if (wpb < 1) wpb = 1;
     const size_t smem = wpb * wsb;
+    bool any_princ = false;
+    for (uint32_t i = 0; i < n_materials; i++) any_princ = any_princ || materials[i].kind == STY_MAT_PRINCIPLED;
+    auto kern = any_princ ? k_ref_filter<true> : k_ref_filter<false>;
     if (smem > 48u * 1024u)
-        STY_TRY(check_cuda(cudaFuncSetAttribute(k_ref_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+        STY_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                            "attr k_ref_filter"));
     // persistent warps: as many blocks as stay resident, each warp looping over vertices
     int per_sm = 0, dev = 0, sms = 0;
-    STY_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ref_filter, 32 * wpb, smem),
+    STY_TRY(check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * wpb, smem),
                        "occupancy k_ref_filter"));
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -813,7 +845,7 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     k_sorted_view<<<nb, bs, 0, st>>>(va, ctx->num, ctx->vals_s, ctx->cid, prm->cluster, ctx->spos, ctx->scid);
     STY_TRY(check_launch("k_sorted_view"));
     STY_TRY(check_cuda(cudaMemsetAsync(ctx->counter, 0, 4, st), "reset work counter"));
-    k_ref_filter<<<nbf, 32 * wpb, smem, st>>>(va, g, ctx->num, ctx->counter, ctx->ranges, ctx->vals_s, ctx->spos,
+    kern<<<nbf, 32 * wpb, smem, st>>>(va, g, ctx->num, ctx->counter, ctx->ranges, ctx->vals_s, ctx->spos,
                                               ctx->scid, ctx->cid,
                                               in_next, *prm, ctx->mats, n_materials, ctx->cls, ggx_tab, ctx->progs,
                                               n_programs, rng, out, neighbours);
