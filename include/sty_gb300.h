@@ -96,6 +96,18 @@ STY_API sty_status sty_device_status(uint32_t *status_out, int32_t clear);
  *                         n steps (1..8), p[0] = sharpness s, p[1..8] = thresholds t_k,
  *                         p[9+3k .. 11+3k] = colour c_k;
  *                         out = sum_k sigmoid(s * (lum - t_k)) * (c_k - c_{k-1}), c_{-1} = 0
+ *   STY_STYLE_HALF_TONE   reference sty_half_tone (mod.rs:1091-1233), a world-space dot screen:
+ *                         p[0] = indirect_scale, p[1] = radius_scale, p[2] = radius,
+ *                         p[3] = grid_distance d, p[4] = max_depth, p[5] = blend,
+ *                         p[6..8] = dark_tone, p[9..11] = light_tone, p[12..23] = the node's TRS as
+ *                         a 3 x 4 row-major affine map. At depth <= max_depth with
+ *                         lum = (r + g + b) / 3 != 0: r' = 1 - clamp(lum / radius_scale (depth 0) or
+ *                         round(lum / indirect_scale) / radius_scale, 0, 1), dot radius
+ *                         r' d radius / 2; the nearest of the 8 corners q of
+ *                         floor(affine(p) / d) d (distance |q - p|, p untransformed, as the
+ *                         reference computes it) picks dark_tone (inside) or light_tone; out =
+ *                         lerp(li, tone * li, blend). Needs the shaded point p: calls without one
+ *                         (sty_style_apply, the screen-space filter) use p = 0.
  * -------------------------------------------------------------------------------------- */
 #define STY_STYLE_NONE 0
 #define STY_STYLE_TOON 1
@@ -105,6 +117,7 @@ STY_API sty_status sty_device_status(uint32_t *status_out, int32_t clear);
 #define STY_STYLE_EIGHT_BIT 5
 #define STY_STYLE_TOON_STEPS 7
 #define STY_STYLE_RAMP_SMOOTH 8
+#define STY_STYLE_HALF_TONE 9
 
 #define STY_STYLE_MAX_NODES 4
 #define STY_STYLE_MAX_PARAMS 60
@@ -128,6 +141,10 @@ typedef struct sty_style_program {
  * (crates/akari_render/src/svm/surface/mod.rs:262-285). */
 STY_API sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
                            float *rgb_out, uint64_t n, void *stream);
+/* sty_style_apply with the shaded point of each colour (device, 3 floats per item), which
+ * STY_STYLE_HALF_TONE reads; a null `pos` is the point 0 for every item (sty_style_apply). */
+STY_API sty_status sty_style_apply_at(const sty_style_program *program, uint32_t depth, const float *rgb_in,
+                                      const float *pos, float *rgb_out, uint64_t n, void *stream);
 
 /* ----------------------------------------------------------------------------------------
  * Screen-space NL-PF filter

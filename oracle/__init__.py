@@ -28,6 +28,7 @@ def lib() -> C.CDLL:
         L.orc_num_threads.restype = C.c_int32
         L.orc_set_num_threads.argtypes = [C.c_int32]
         L.orc_style_apply_f64.argtypes = [vp, C.c_uint32, vp, vp, C.c_uint64]
+        L.orc_style_apply_at_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, C.c_uint64]
         L.orc_pf_screen_filter_depth_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp]
         L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
         L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
@@ -60,6 +61,15 @@ def style_apply(program, depth: int, rgb: np.ndarray) -> np.ndarray:
     out = np.empty_like(rgb)
     lib().orc_style_apply_f64(C.addressof(program) if program is not None else None, depth, _p(rgb), _p(out),
                               rgb.shape[0])
+    return out
+
+
+def style_apply_at(program, depth: int, rgb: np.ndarray, pos: np.ndarray) -> np.ndarray:
+    """style_apply with the shaded point of each colour (read by the half-tone node)."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float64).reshape(-1, 3)
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    out = np.empty_like(rgb)
+    lib().orc_style_apply_at_f64(C.addressof(program), depth, _p(rgb), _p(pos), _p(out), rgb.shape[0])
     return out
 
 

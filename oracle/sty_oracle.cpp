@@ -87,8 +87,33 @@ inline T round_half_away(T v) {
 
 // ---- style nodes: crates/akari_render/src/svm/surface/mod.rs ---------------------------------
 template <class T>
-V3<T> style_node(const sty_style_node &nd, uint32_t depth, V3<T> li) {
+V3<T> style_node(const sty_style_node &nd, uint32_t depth, V3<T> li, V3<T> pos) {
     switch (nd.kind) {
+        case STY_STYLE_HALF_TONE: {  // HalfToneSurface::apply_stylization, mod.rs:1180-1232
+            if ((double)depth > (double)nd.p[4]) return li;
+            const T lum = (li.x + li.y + li.z) / T(3);
+            if (lum == T(0)) return li;
+            T r = depth == 0 ? lum / T(nd.p[1]) : round_half_away(lum / T(nd.p[0])) / T(nd.p[1]);
+            r = T(1) - clampv(r, T(0), T(1));
+            const T d = T(nd.p[3]);
+            r = r * d * T(0.5) * T(nd.p[2]);
+            const float *A = nd.p + 12;
+            const T tp[3] = {T(A[0]) * pos.x + T(A[1]) * pos.y + T(A[2]) * pos.z + T(A[3]),
+                             T(A[4]) * pos.x + T(A[5]) * pos.y + T(A[6]) * pos.z + T(A[7]),
+                             T(A[8]) * pos.x + T(A[9]) * pos.y + T(A[10]) * pos.z + T(A[11])};
+            const T ip[3] = {std::floor(tp[0] / d) * d, std::floor(tp[1] / d) * d, std::floor(tp[2] / d) * d};
+            T mind = T(1e16);
+            for (int i = 0; i < 2; i++)
+                for (int j = 0; j < 2; j++)
+                    for (int k = 0; k < 2; k++) {
+                        const T qx = ip[0] + T(i) * d - pos.x, qy = ip[1] + T(j) * d - pos.y, qz = ip[2] + T(k) * d - pos.z;
+                        mind = std::min(mind, (T)std::sqrt(qx * qx + qy * qy + qz * qz));
+                    }
+            const float *tone = mind < r ? nd.p + 6 : nd.p + 9;
+            const T b = T(nd.p[5]);
+            return {li.x + (T(tone[0]) * li.x - li.x) * b, li.y + (T(tone[1]) * li.y - li.y) * b,
+                    li.z + (T(tone[2]) * li.z - li.z) * b};
+        }
         case STY_STYLE_TOON: {  // ToonSurface::apply_stylization, mod.rs:573-610
             T w = T(nd.p[0]);
             V3<T> c = {clampv(li.x, T(0), T(1e5)), clampv(li.y, T(0), T(1e5)),
@@ -213,16 +238,21 @@ V3<T> style_node(const sty_style_node &nd, uint32_t depth, V3<T> li) {
     }
 }
 
+// pos: the shaded point (read by STY_STYLE_HALF_TONE only)
 template <class T>
-V3<T> style_apply(const sty_style_program *prog, uint32_t depth, V3<T> li) {
+V3<T> style_apply(const sty_style_program *prog, uint32_t depth, V3<T> li, V3<T> pos) {
     if (!prog) return li;
     uint32_t bit = depth > 31 ? 31 : depth;
     for (int i = 0; i < prog->n_nodes && i < STY_STYLE_MAX_NODES; i++) {
         const sty_style_node &nd = prog->nodes[i];
         if (!((nd.depth_mask >> bit) & 1u)) continue;
-        li = style_node<T>(nd, depth, li);
+        li = style_node<T>(nd, depth, li, pos);
     }
     return li;
+}
+template <class T>
+V3<T> style_apply(const sty_style_program *prog, uint32_t depth, V3<T> li) {
+    return style_apply<T>(prog, depth, li, V3<T>{T(0), T(0), T(0)});
 }
 
 inline size_t rec_index(const sty_pf_records *r, int d, int y, int x, int s) {
@@ -252,6 +282,16 @@ void orc_style_apply_f64(const sty_style_program *prog, uint32_t depth, const do
                          double *out, uint64_t n) {
     for (uint64_t i = 0; i < n; i++) {
         V3<double> c = style_apply<double>(prog, depth, v3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+        out[3 * i] = c.x;
+        out[3 * i + 1] = c.y;
+        out[3 * i + 2] = c.z;
+    }
+}
+void orc_style_apply_at_f64(const sty_style_program *prog, uint32_t depth, const double *in, const double *pos,
+                            double *out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) {
+        V3<double> c = style_apply<double>(prog, depth, v3(in[3 * i], in[3 * i + 1], in[3 * i + 2]),
+                                           v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
         out[3 * i] = c.x;
         out[3 * i + 1] = c.y;
         out[3 * i + 2] = c.z;
@@ -1047,7 +1087,8 @@ D3 br_radiance(const BrScene &s, uint32_t depth, const double *p, uint32_t prim,
                     if (std::isfinite(lpdf) && lpdf > 0) {
                         if (!(nf & 1u)) {
                             const int32_t pi = lm.style[style_idx(nf)];
-                            if (pi >= 0 && (uint32_t)pi < s.n_progs) lli = style_apply<double>(&s.progs[pi], depth + 1, lli);
+                            if (pi >= 0 && (uint32_t)pi < s.n_progs)
+                                lli = style_apply<double>(&s.progs[pi], depth + 1, lli, v3(q[0], q[1], q[2]));
                         }
                         double tt, c1, c2;
                         const uint32_t blk = hit_bf(s.pt, p, wi, dist * (1 - 1e-3), prim, lt, &tt, &c1, &c2);
@@ -1098,7 +1139,7 @@ D3 br_radiance(const BrScene &s, uint32_t depth, const double *p, uint32_t prim,
     if (!(flags & 1u)) {
         const int32_t pi = m.style[style_idx(flags)];
         if (pi >= 0 && (uint32_t)pi < s.n_progs) {
-            const V3<double> o = style_apply<double>(&s.progs[pi], depth, v3(li[0], li[1], li[2]));
+            const V3<double> o = style_apply<double>(&s.progs[pi], depth, v3(li[0], li[1], li[2]), v3(p[0], p[1], p[2]));
             li = {o.x, o.y, o.z};
         }
     }

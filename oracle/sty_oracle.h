@@ -27,6 +27,8 @@ int32_t orc_num_threads(void);
 void orc_set_num_threads(int32_t n);
 
 /* Style program on n interleaved rgb triples (double). */
+void orc_style_apply_at_f64(const sty_style_program *prog, uint32_t depth, const double *rgb_in, const double *pos,
+                            double *rgb_out, uint64_t n);
 void orc_style_apply_f64(const sty_style_program *prog, uint32_t depth, const double *rgb_in,
                          double *rgb_out, uint64_t n);
 

@@ -307,7 +307,10 @@ int32_t orc_pf_ref_filter(const sty_pf_vertices *v, const float *in_next,
         const bool stylize = (prm->depth > 0 || !prm->no_first_hit_stylization) && !(v->flags[vi] & 1u);
         if (stylize) {
             const int32_t pi = mv.style[style_index(v->flags[vi])];
-            if (pi >= 0 && (uint32_t)pi < n_progs) orc_style_apply_f64(&progs[pi], prm->depth, rad, rad, 1);
+            if (pi >= 0 && (uint32_t)pi < n_progs) {
+                const double pp[3] = {(double)v->p[0][vi], (double)v->p[1][vi], (double)v->p[2][vi]};
+                orc_style_apply_at_f64(&progs[pi], prm->depth, rad, pp, rad, 1);
+            }
         }
         for (int c = 0; c < 3; c++) out[c * n + vi] = rad[c];
     }

@@ -29,6 +29,7 @@ STY_STYLE_SAT_REX = 4
 STY_STYLE_EIGHT_BIT = 5
 STY_STYLE_TOON_STEPS = 7
 STY_STYLE_RAMP_SMOOTH = 8
+STY_STYLE_HALF_TONE = 9
 STY_STYLE_MAX_NODES = 4
 STY_STYLE_MAX_PARAMS = 60
 
@@ -92,6 +93,7 @@ SIGNATURES = {
     "sty_launch_count": (C.c_uint64, []),
     "sty_device_status": (C.c_int32, [C.POINTER(C.c_uint32), C.c_int32]),
     "sty_style_apply": (C.c_int32, [C.POINTER(StyleProgram), C.c_uint32, _VP, _VP, C.c_uint64, _VP]),
+    "sty_style_apply_at": (C.c_int32, [C.POINTER(StyleProgram), C.c_uint32, _VP, _VP, _VP, C.c_uint64, _VP]),
     "sty_pf_screen_filter_depth": (C.c_int32, [C.POINTER(PfRecords), C.c_uint32, C.POINTER(PfScreenParams),
                                                C.POINTER(StyleProgram), _VP, _VP, _VP, _VP]),
     "sty_pf_screen_filter": (C.c_int32, [C.POINTER(PfRecords), C.POINTER(PfScreenParams),
@@ -228,3 +230,25 @@ def ramp_smooth(sharpness: float, thresholds, colors, depth_mask: int = 0xFFFFFF
     for k, c in enumerate(colors):
         p[9 + 3 * k:12 + 3 * k] = c
     return style_node(STY_STYLE_RAMP_SMOOTH, p, n, depth_mask)
+
+
+def half_tone(radius_scale: float, radius: float, grid_distance: float, dark_tone, light_tone,
+              indirect_scale: float = 1.0, blend: float = 1.0, max_depth: int = 0, affine=None) -> StyleNode:
+    """sty_half_tone (svm/surface/mod.rs:1091-1233): a world-space dot screen of spacing
+    `grid_distance`. `affine` is the node's TRS matrix (4 x 4 or 3 x 4, row-major); like
+    AffineTransform::from_matrix (geometry.rs:216-222) a matrix within 1e-4 of the identity is
+    applied as the identity. The node applies at depths <= max_depth."""
+    if grid_distance <= 0:
+        raise ValueError("half_tone wants grid_distance > 0")
+    m = [[1.0, 0.0, 0.0, 0.0], [0.0, 1.0, 0.0, 0.0], [0.0, 0.0, 1.0, 0.0]]
+    if affine is not None:
+        rows = [list(map(float, r)) for r in affine]
+        if len(rows) == 4 and any(abs(a - b) > 1e-12 for a, b in zip(rows[3], (0.0, 0.0, 0.0, 1.0))):
+            raise ValueError("half_tone wants an affine map (last row 0 0 0 1)")
+        eye = [[float(i == j) for j in range(4)] for i in range(4)]
+        if any(abs(rows[i][j] - eye[i][j]) > 1e-4 for i in range(len(rows)) for j in range(4)):
+            m = rows[:3]
+    p = [indirect_scale, radius_scale, radius, grid_distance, float(max_depth), blend,
+         *map(float, dark_tone), *map(float, light_tone)] + [x for r in m for x in r]
+    mask = 0xFFFFFFFF if max_depth >= 31 else (1 << (max_depth + 1)) - 1
+    return style_node(STY_STYLE_HALF_TONE, p, 0, mask)

@@ -1,6 +1,7 @@
 // api.cu -- status/error plumbing and the small element-wise entry points of the C ABI:
 // style application, Pcg32 streams, hash-grid cells and the FP64 film accumulation.
 #include <cstdarg>
+#include <cmath>
 #include <cstring>
 
 #include "common.cuh"
@@ -50,6 +51,9 @@ bool style_program_valid(const sty_style_program *p) {
             case STY_STYLE_RAMP_SMOOTH:
                 if (n.n < 1 || n.n > 8) return false;
                 break;
+            case STY_STYLE_HALF_TONE:  // the dot spacing divides the mapped point
+                if (!(n.p[3] > 0.0f) || !std::isfinite(n.p[3])) return false;
+                break;
             default:
                 return false;
         }
@@ -73,12 +77,13 @@ uint32_t *device_status_ptr() {
 }
 
 // ---- kernels ------------------------------------------------------------------------------
-__global__ void k_style_apply(sty_style_program prog, uint32_t depth, const float *in, float *out,
+__global__ void k_style_apply(sty_style_program prog, uint32_t depth, const float *in, const float *pos, float *out,
                               uint64_t n) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     f3 c = {in[3 * i], in[3 * i + 1], in[3 * i + 2]};
-    c = style_apply(prog, depth, c);
+    const f3 p = pos ? f3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]} : f3{0.0f, 0.0f, 0.0f};
+    c = style_apply(prog, depth, c, p);
     out[3 * i] = c.x;
     out[3 * i + 1] = c.y;
     out[3 * i + 2] = c.z;
@@ -191,8 +196,21 @@ sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, con
     STY_ARG_CHECK(style_program_valid(program), "sty_style_apply: invalid style program");
     if (n == 0) return STY_OK;
     const int bs = 256;
-    k_style_apply<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(*program, depth, rgb_in, rgb_out, n);
+    k_style_apply<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(*program, depth, rgb_in, nullptr,
+                                                                             rgb_out, n);
     return check_launch("sty_style_apply");
+}
+
+sty_status sty_style_apply_at(const sty_style_program *program, uint32_t depth, const float *rgb_in, const float *pos,
+                              float *rgb_out, uint64_t n, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(program && rgb_in && rgb_out, "sty_style_apply_at: null argument");
+    STY_ARG_CHECK(style_program_valid(program), "sty_style_apply_at: invalid style program");
+    if (n == 0) return STY_OK;
+    const int bs = 256;
+    k_style_apply<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(*program, depth, rgb_in, pos, rgb_out,
+                                                                             n);
+    return check_launch("sty_style_apply_at");
 }
 
 sty_status sty_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n, uint32_t draws,

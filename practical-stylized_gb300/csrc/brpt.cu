@@ -234,7 +234,10 @@ __global__ void k_br_propagate(SceneView sc, uint32_t n, uint32_t base, uint32_t
         const uint32_t fl = s.flags[g];
         if (!(fl & 1u)) {
             const int32_t pi = sc.materials[sc.tri_material[prim]].style[style_index(fl)];
-            if (pi >= 0 && (uint32_t)pi < n_progs) out = style_apply(progs[pi], depth, out);
+            if (pi >= 0 && (uint32_t)pi < n_progs) {
+                const F3 p = get3(s.p, g);
+                out = style_apply(progs[pi], depth, out, f3{p.x, p.y, p.z});
+            }
         }
         put3(s.rad, g, f3m(out.x, out.y, out.z));
     } else if (depth == 0) {

@@ -572,7 +572,10 @@ __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uin
         const uint32_t fl = v.flags[vi];
         if ((prm.depth > 0 || !prm.no_first_hit_stylization) && !(fl & 1u)) {
             const int32_t pi = mv.style[style_index(fl)];
-            if (pi >= 0 && (uint32_t)pi < n_progs) rad = style_apply(progs[pi], prm.depth, rad);
+            if (pi >= 0 && (uint32_t)pi < n_progs) {
+                const V3 pp = ld3(v.p, vi);
+                rad = style_apply(progs[pi], prm.depth, rad, f3{pp.x, pp.y, pp.z});
+            }
         }
         out[vi] = rad.x;
         out[n + vi] = rad.y;

@@ -58,8 +58,35 @@ __device__ inline f3 hsv2rgb(f3 hsv) {
     return {f(5), f(3), f(1)};
 }
 
-__device__ inline f3 style_node(const sty_style_node &nd, uint32_t depth, f3 li) {
+__device__ inline f3 style_node(const sty_style_node &nd, uint32_t depth, f3 li, f3 pos) {
     switch (nd.kind) {
+        case STY_STYLE_HALF_TONE: {  // mod.rs:1180-1232
+            if ((float)depth > nd.p[4]) return li;
+            const float lum = (li.x + li.y + li.z) / 3.0f;
+            if (lum == 0.0f) return li;
+            float r = depth == 0 ? lum / nd.p[1] : roundf(lum / nd.p[0]) / nd.p[1];
+            r = 1.0f - clampf(r, 0.0f, 1.0f);
+            const float d = nd.p[3];
+            r = r * d * 0.5f * nd.p[2];
+            const float *A = nd.p + 12;
+            const float tp[3] = {A[0] * pos.x + A[1] * pos.y + A[2] * pos.z + A[3],
+                                 A[4] * pos.x + A[5] * pos.y + A[6] * pos.z + A[7],
+                                 A[8] * pos.x + A[9] * pos.y + A[10] * pos.z + A[11]};
+            const float ip[3] = {floorf(tp[0] / d) * d, floorf(tp[1] / d) * d, floorf(tp[2] / d) * d};
+            float mind = 1e16f;
+            for (int i = 0; i < 2; i++)
+                for (int j = 0; j < 2; j++)
+                    for (int k = 0; k < 2; k++) {
+                        const float qx = ip[0] + (float)i * d - pos.x, qy = ip[1] + (float)j * d - pos.y,
+                                    qz = ip[2] + (float)k * d - pos.z;
+                        const float dist = sqrtf(qx * qx + qy * qy + qz * qz);
+                        if (dist < mind) mind = dist;
+                    }
+            const float *tone = mind < r ? nd.p + 6 : nd.p + 9;
+            const float b = nd.p[5];
+            return {li.x + (tone[0] * li.x - li.x) * b, li.y + (tone[1] * li.y - li.y) * b,
+                    li.z + (tone[2] * li.z - li.z) * b};
+        }
         case STY_STYLE_TOON: {  // mod.rs:573-610
             const float w = nd.p[0];
             f3 c = clamp3(li, 0.0f, 1e5f);
@@ -174,13 +201,17 @@ __device__ inline f3 style_node(const sty_style_node &nd, uint32_t depth, f3 li)
     }
 }
 
-__device__ inline f3 style_apply(const sty_style_program &prog, uint32_t depth, f3 li) {
+// pos: the shaded point (read by STY_STYLE_HALF_TONE only)
+__device__ inline f3 style_apply(const sty_style_program &prog, uint32_t depth, f3 li, f3 pos) {
     const uint32_t bit = depth > 31u ? 31u : depth;
     for (int i = 0; i < prog.n_nodes && i < STY_STYLE_MAX_NODES; i++) {
         const sty_style_node &nd = prog.nodes[i];
-        if ((nd.depth_mask >> bit) & 1u) li = style_node(nd, depth, li);
+        if ((nd.depth_mask >> bit) & 1u) li = style_node(nd, depth, li, pos);
     }
     return li;
+}
+__device__ inline f3 style_apply(const sty_style_program &prog, uint32_t depth, f3 li) {
+    return style_apply(prog, depth, li, f3{0.0f, 0.0f, 0.0f});
 }
 
 // Host-side validation of a style program's sizes.

@@ -183,7 +183,7 @@ __global__ void k_splat(uint32_t npx, uint32_t branch, const float *out0, VertOu
         if (!no_first_hit) {
             // the path's flags before its first hit are all clear: style index 0
             const int32_t pi = mats[v0.material[i]].style[0];
-            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c);
+            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c, f3{v0.p[0][i], v0.p[1][i], v0.p[2][i]});
         }
         acc[0] += c.x;
         acc[1] += c.y;
@@ -325,7 +325,7 @@ __global__ void k_nrc_style_pred(SceneView sc, uint32_t n, VertOut v, const floa
         const uint32_t fl = v.flags[i];
         if (stylize && !(fl & 1u)) {
             const int32_t pi = sc.materials[v.material[i]].style[style_index(fl)];
-            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], depth, c);
+            if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], depth, c, f3{v.p[0][i], v.p[1][i], v.p[2][i]});
         }
     }
     out[i] = c.x;
@@ -344,7 +344,7 @@ __global__ void k_nrc_splat_pred(uint32_t npx, VertOut v0, const float *pred, co
     const uint32_t fl = v0.flags[px];
     if (!no_first_hit && !(fl & 1u)) {
         const int32_t pi = mats[v0.material[px]].style[style_index(fl)];
-        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c);
+        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], 0, c, f3{v0.p[0][px], v0.p[1][px], v0.p[2][px]});
     }
     film[3 * (size_t)px] += weight * c.x;
     film[3 * (size_t)px + 1] += weight * c.y;
@@ -465,6 +465,7 @@ __global__ void k_fg_accumulate(SceneView sc, uint32_t n, const uint32_t *split,
     const uint32_t fl = gflags[i];
     if (stylize && !(fl & 1u)) {
         const int32_t pi = sc.materials[gmat[i]].style[style_index(fl)];
+        // the gather hit's position is not kept: a half-tone node reads p = 0 here
         if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], split[i] + 1, c);
     }
     const float w = gmis[i];
@@ -520,7 +521,7 @@ __global__ void k_fg_sweep(SceneView sc, uint32_t n, uint32_t d, VertOut v, cons
         const uint32_t fl = v.flags[i];
         if (stylize && !(fl & 1u)) {
             const int32_t pi = m.style[style_index(fl)];
-            if (pi >= 0 && (uint32_t)pi < n_progs) r = style_apply(progs[pi], d, r);
+            if (pi >= 0 && (uint32_t)pi < n_progs) r = style_apply(progs[pi], d, r, f3{v.p[0][i], v.p[1][i], v.p[2][i]});
         }
     }
     out[i] = r.x;

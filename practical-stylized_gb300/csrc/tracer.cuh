@@ -232,7 +232,7 @@ __device__ bool nee_sample(const SceneView &sc, F3 p, F3 ng, uint32_t prim, uint
     if (!(isfinite(lpdf) && lpdf > 0.0f)) return false;
     if (!(new_flags & 1u)) {  // the light's style node at the next depth (sample_light :1286-1305)
         const int32_t pi = lm.style[style_index(new_flags)];
-        if (pi >= 0 && (uint32_t)pi < n_progs) li = style_apply(progs[pi], depth + 1, li);
+        if (pi >= 0 && (uint32_t)pi < n_progs) li = style_apply(progs[pi], depth + 1, li, f3{q.x, q.y, q.z});
     }
     const F3 so = offset_ray_origin(p, face_forward(ng, wi));
     const float s3[3] = {so.x, so.y, so.z}, w3[3] = {wi.x, wi.y, wi.z};

@@ -111,6 +111,14 @@ def style_ops(nodes, node_id, s: int):
                                        const_float(nodes, n.get("indirect_scale"), 1.0))]
     if t == "sty_saturation_adjust_rex":
         return inner + [abi.sat_rex(const_float(nodes, n["blend"]))]
+    if t == "sty_half_tone":
+        m = trs_matrix(n["trs"])
+        return inner + [abi.half_tone(const_float(nodes, n["radius_scale"]), const_float(nodes, n["radius"]),
+                                      const_float(nodes, n["grid_distance"]), const_rgb(nodes, n["dark_tone"]),
+                                      const_rgb(nodes, n["light_tone"]),
+                                      indirect_scale=const_float(nodes, n["indirect_scale"]),
+                                      blend=const_float(nodes, n["blend"]), max_depth=int(n["max_depth"]),
+                                      affine=m.tolist())]
     raise UnsupportedNode(f"style node {t} has no GPU counterpart")
 
 
