@@ -228,6 +228,11 @@ STY_API sty_status sty_film_accumulate(const float *out0, int32_t width, int32_t
                              (Gulbrandsen) and a clear coat; albedo = base colour, the
                              roughness / metallic / ior / transmission / specular / coat fields
                              below. Flat shading (normal maps are not supported). */
+#define STY_MAT_GLASS 3      /* the reference's glass node (svm/surface/glass.rs:13-44, compiled from
+                             the scene's "glass" node at svm/compiler.rs:249-263): rough dielectric
+                             reflection + transmission, both tinted by albedo, added with the
+                             Fresnel term of cos(wo) as the lobe-choice weight; reads `ior` and
+                             `roughness` (alpha = max(roughness^2, 1e-4)). */
 
 typedef struct sty_pf_material {
     int32_t kind;        /* STY_MAT_* */
@@ -431,7 +436,7 @@ STY_API sty_status sty_nrc_gradient(sty_nrc *nrc, uint32_t batch, const float *i
  * triangle id. Flat shading (shading normal = geometric normal).
  * -------------------------------------------------------------------------------------- */
 typedef struct sty_scene_material {
-    int32_t kind;        /* STY_MAT_DIFFUSE or STY_MAT_GGX */
+    int32_t kind;        /* STY_MAT_* */
     float albedo[3];
     float alpha;         /* GGX alpha */
     float emission[3];   /* radiance leaving the front (geometric-normal) side; 0 = not a light */

@@ -1373,6 +1373,7 @@ double p_albedo(double rough, double mu, double eta) {
 struct PCl {
     double base[3], tcol[3], alpha, rough, rough_d, metallic, trans, ior, seta, sf0, stint[3], stl, cn[3], ck[3];
     double cw, calpha, crough, crough_d, cior, ctint[3];
+    bool glass;  // STY_MAT_GLASS: glass.rs alone (p_glass_eval / p_glass_sample)
 };
 PCl p_closure(const sty_scene_material &m) {
     PCl c;
@@ -1409,6 +1410,7 @@ PCl p_closure(const sty_scene_material &m) {
     c.calpha = std::max(c.crough * c.crough, 1e-4);
     c.crough_d = std::sqrt(c.calpha);
     c.cior = m.coat_ior;
+    c.glass = m.kind == STY_MAT_GLASS;
     return c;
 }
 double p_refl(P3 wo, P3 wi, double a, int fk, double eta, const double *n, const double *k, const double *col, double f[3]) {
@@ -1438,7 +1440,18 @@ double p_trans(P3 wo, P3 wi, double a, double eta, const double *col, double f[3
     }
     return q * q == 0 ? 0 : p_vpdf(wo, wh, a) * std::fabs(pdot(wi, wh)) / (q * q);
 }
+// glass.rs:13-44: BsdfMixture{a: MicrofacetTransmission(kt), b: MicrofacetReflection(kr), frac =
+// fr_dielectric(cos wo, eta), additive}: f = f_t + f_r, pdf = lerp(pdf_t, pdf_r, frac); kr = kt =
+// the node's colour
+double p_glass_eval(const PCl &c, P3 wo, P3 wi, double f[3]) {
+    double ft[3], fr[3];
+    const double pt = p_trans(wo, wi, c.alpha, c.ior, c.base, ft);
+    const double pr = p_refl(wo, wi, c.alpha, 0, c.ior, nullptr, nullptr, c.base, fr);
+    for (int i = 0; i < 3; i++) f[i] = ft[i] + fr[i];
+    return plerp(pt, pr, p_fr_diel(wo[2], c.ior));
+}
 double p_eval(const PCl &c, P3 wo, P3 wi, double f[3]) {
+    if (c.glass) return p_glass_eval(c, wo, wi, f);
     const double mu = std::fabs(wo[2]), E = 1e-4;
     double f1[3], p1;
     {
@@ -1497,6 +1510,15 @@ inline bool p_choose_b(double frac, double &u) {
     return false;
 }
 bool p_sample(const PCl &c, P3 wo, double u, double u0, double u1, P3 *wi) {
+    if (c.glass) {  // the mixture picks reflection with probability frac, else transmission
+        const P3 wh = p_sample_wh(wo, c.alpha, u0, u1);
+        if (p_choose_b(p_fr_diel(wo[2], c.ior), u)) {
+            *wi = p_reflect(wo, wh);
+            return psame(wo, *wi);
+        }
+        if (!p_refract(wo, wh, c.ior, wi)) return false;
+        return !psame(wo, *wi);
+    }
     const double mu = std::fabs(wo[2]);
     if (p_choose_b(c.cw * p_albedo(c.crough, mu, c.cior), u)) {
         *wi = p_reflect(wo, p_sample_wh(wo, c.calpha, u0, u1));

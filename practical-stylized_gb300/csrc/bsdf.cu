@@ -116,7 +116,7 @@ sty_status sty_bsdf_eval(const sty_scene_material *material, uint64_t n, const f
                          float *pdf, void *stream) {
     clear_error();
     STY_ARG_CHECK(material && (n == 0 || (wo && wi && f && pdf)), "sty_bsdf_eval: null argument");
-    STY_ARG_CHECK(material->kind == STY_MAT_PRINCIPLED, "sty_bsdf_eval: only STY_MAT_PRINCIPLED is exposed");
+    STY_ARG_CHECK(bsdf::closure_kind(material->kind), "sty_bsdf_eval: only STY_MAT_PRINCIPLED and STY_MAT_GLASS are exposed");
     if (n == 0) return STY_OK;
     const float *t = principled_table();
     if (!t) {
@@ -131,7 +131,7 @@ sty_status sty_bsdf_sample(const sty_scene_material *material, uint64_t n, const
                            float *f, float *pdf, void *stream) {
     clear_error();
     STY_ARG_CHECK(material && (n == 0 || (wo && u && wi && f && pdf)), "sty_bsdf_sample: null argument");
-    STY_ARG_CHECK(material->kind == STY_MAT_PRINCIPLED, "sty_bsdf_sample: only STY_MAT_PRINCIPLED is exposed");
+    STY_ARG_CHECK(bsdf::closure_kind(material->kind), "sty_bsdf_sample: only STY_MAT_PRINCIPLED and STY_MAT_GLASS are exposed");
     if (n == 0) return STY_OK;
     const float *t = principled_table();
     if (!t) {

@@ -26,6 +26,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "sty_gb300.h"
+
 namespace sty {
 namespace bsdf {
 
@@ -194,6 +196,13 @@ struct PClosure {
     float cn[3], ck[3];                    // conductor n, k
     float coat_w, coat_alpha, coat_rough, coat_rough_d, coat_ior, coat_tint[3];
 };
+// kinds evaluated through PClosure
+__host__ __device__ __forceinline__ bool closure_kind(int32_t kind) {
+    return kind == STY_MAT_PRINCIPLED || kind == STY_MAT_GLASS;
+}
+// STY_MAT_PRINCIPLED: the principled layers. STY_MAT_GLASS (glass.rs:13-44) is the dielectric layer
+// alone -- transmission 1, no specular, metal or coat layer -- with the transmitted lobe tinted by
+// the colour itself rather than its square root.
 template <class M>
 __host__ __device__ __forceinline__ PClosure make_closure(const M &m) {
     PClosure c;
@@ -233,6 +242,16 @@ __host__ __device__ __forceinline__ PClosure make_closure(const M &m) {
     c.coat_alpha = fmaxf(m.coat_roughness * m.coat_roughness, 1e-4f);
     c.coat_rough_d = sqrtf(c.coat_alpha);
     c.coat_ior = m.coat_ior;
+    if (m.kind == STY_MAT_GLASS) {
+        for (int i = 0; i < 3; i++) {
+            c.tcol[i] = m.albedo[i];
+            c.spec_tint[i] = 0.0f;
+        }
+        c.spec_tint_lum = 0.0f;
+        c.transmission = 1.0f;
+        c.metallic = 0.0f;
+        c.coat_w = 0.0f;
+    }
     return c;
 }
 

@@ -151,7 +151,7 @@ template <bool PRINC>
 __device__ __forceinline__ void bsdf_eval(const MatCore &m, V3 ns, V3 ng, V3 wo, V3 wi, float f[3], float *pdf,
                           const bsdf::PClosure *pc, const float *tab) {
     if constexpr (PRINC) {
-        if (m.kind == STY_MAT_PRINCIPLED) {
+        if (bsdf::closure_kind(m.kind)) {
             *pdf = princ_eval(pc, tab, ns, ng, wo, wi, f);
             return;
         }
@@ -336,7 +336,7 @@ __device__ __forceinline__ NbFrame make_frame(const sty_pf_material &m, uint32_t
     const bool ggx = m.kind != STY_MAT_DIFFUSE;
     f.alpha = fmaxf(m.alpha, 1e-4f);
     f.g1 = ggx ? 1.0f / (1.0f + tr_lambda(f.co, f.alpha)) : 0.0f;
-    f.bits = (ok ? 1u : 0u) | (ggx ? 2u : 0u) | (m.kind == STY_MAT_PRINCIPLED ? 4u : 0u);
+    f.bits = (ok ? 1u : 0u) | (ggx ? 2u : 0u) | (bsdf::closure_kind(m.kind) ? 4u : 0u);
     f.mat = mi;
     f.pad = 0;
     return f;
@@ -387,7 +387,7 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t x, int src) {
     const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)x, src), hi = __shfl_sync(0xffffffffu, (uint32_t)(x >> 32), src);
     return ((uint64_t)hi << 32) | lo;
 }
-// PRINC: some material is STY_MAT_PRINCIPLED (the variant without it keeps the diffuse / GGX path's
+// PRINC: some material is STY_MAT_PRINCIPLED or STY_MAT_GLASS (the variant without it keeps the diffuse / GGX path's
 // registers and stack as they were)
 template <bool PRINC>
 __global__ void __launch_bounds__(256, 4) k_ref_filter(VArgs v, Geo g, const uint32_t *num, uint32_t *next,
@@ -832,7 +832,7 @@ sty_status sty_pf_ref_filter(sty_pf_ref_ctx *ctx, const sty_pf_vertices *v, cons
     if (wpb < 1) wpb = 1;
     const size_t smem = wpb * wsb;
     bool any_princ = false;
-    for (uint32_t i = 0; i < n_materials; i++) any_princ = any_princ || materials[i].kind == STY_MAT_PRINCIPLED;
+    for (uint32_t i = 0; i < n_materials; i++) any_princ = any_princ || bsdf::closure_kind(materials[i].kind);
     auto kern = any_princ ? k_ref_filter<true> : k_ref_filter<false>;
     if (smem > 48u * 1024u)
         STY_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),

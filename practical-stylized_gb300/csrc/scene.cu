@@ -208,13 +208,13 @@ sty_status sty_scene_create(const float *pos, const uint32_t *tmat, uint32_t n, 
     for (uint32_t i = 0; i < n; i++) STY_ARG_CHECK(tmat[i] < nm, "triangle %u has material %u >= %u", i, tmat[i], nm);
     for (uint32_t i = 0; i < nm; i++)
         STY_ARG_CHECK(mats[i].kind == STY_MAT_DIFFUSE || mats[i].kind == STY_MAT_GGX ||
-                          mats[i].kind == STY_MAT_PRINCIPLED,
+                          bsdf::closure_kind(mats[i].kind),
                       "material %u: unknown kind", i);
     for (uint32_t i = 0; i < nm; i++)
-        STY_ARG_CHECK(mats[i].kind != STY_MAT_PRINCIPLED ||
+        STY_ARG_CHECK(!bsdf::closure_kind(mats[i].kind) ||
                           (mats[i].ior > 0.0f && mats[i].coat_ior > 0.0f && mats[i].roughness >= 0.0f &&
                            mats[i].coat_roughness >= 0.0f),
-                      "material %u: principled ior / coat_ior must be > 0 and roughness >= 0", i);
+                      "material %u: principled / glass ior / coat_ior must be > 0 and roughness >= 0", i);
     sty_scene *s = new sty_scene();
     s->n_tris = n;
     s->n_materials = nm;

@@ -113,7 +113,8 @@ __device__ __forceinline__ float tr_lambda(float cw, float a) {
     return isfinite(at) ? l : 0.0f;
 }
 __device__ __forceinline__ bsdf::B3 tob(F3 v) { return bsdf::b3(v.x, v.y, v.z); }
-// STY_MAT_PRINCIPLED through the shared closure (bsdf.cuh); tab = the scene's albedo table
+// STY_MAT_PRINCIPLED / STY_MAT_GLASS through the shared closure (bsdf.cuh); tab = the scene's
+// albedo table
 __device__ __forceinline__ float princ_eval(const sty_scene_material &m, const float *tab, F3 ns, F3 ng, F3 wo, F3 wi,
                                             F3 *f) {
     float fv[3];
@@ -122,7 +123,7 @@ __device__ __forceinline__ float princ_eval(const sty_scene_material &m, const f
     return p;
 }
 __device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, const float *tab) {
-    if (m.kind == STY_MAT_PRINCIPLED) {
+    if (bsdf::closure_kind(m.kind)) {
         F3 f;
         return princ_eval(m, tab, ns, ng, wo, wi, &f);
     }
@@ -142,7 +143,7 @@ __device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 w
 // Surface::sample: wi (world) and its pdf (0 = invalid)
 __device__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, float u_sel, float u0, float u1,
                           float *pdf, const float *tab) {
-    if (m.kind == STY_MAT_PRINCIPLED) {
+    if (bsdf::closure_kind(m.kind)) {
         bsdf::B3 w = bsdf::b3(0.0f, 0.0f, 0.0f);
         float fv[3];
         bsdf::sample_world(bsdf::make_closure(m), tab, tob(ns), tob(ng), tob(wo), u_sel, u0, u1, &w, fv, pdf);
@@ -245,7 +246,7 @@ __device__ bool nee_sample(const SceneView &sc, F3 p, F3 ng, uint32_t prim, uint
 // Surface::avg_roughness: diffuse 1, the GGX lobe its alpha (as the NL-PF paths have used it), the
 // principled closure the frac-weighted mean of its lobes' (which depends on wo)
 __device__ __forceinline__ float lobe_roughness(const sty_scene_material &m, const float *tab, F3 ns, F3 wo) {
-    if (m.kind == STY_MAT_PRINCIPLED) return bsdf::avg_roughness_world(bsdf::make_closure(m), tab, tob(ns), tob(wo));
+    if (bsdf::closure_kind(m.kind)) return bsdf::avg_roughness_world(bsdf::make_closure(m), tab, tob(ns), tob(wo));
     return m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
 }
 
@@ -272,7 +273,7 @@ __global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
 // f * |cos| (rgb) and pdf of a scene material (Surface::evaluate; diffuse.rs:17-48,
 // svm/surface/mod.rs:1877-1910 with unit Fresnel)
 __device__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f, const float *tab) {
-    if (m.kind == STY_MAT_PRINCIPLED) return princ_eval(m, tab, ns, ng, wo, wi, f);
+    if (bsdf::closure_kind(m.kind)) return princ_eval(m, tab, ns, ng, wo, wi, f);
     *f = f3m(0.0f, 0.0f, 0.0f);
     if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
     const float co = dot(wo, ns), ci = dot(wi, ns);

@@ -17,6 +17,8 @@ from .synth import REF_FIELDS, REF_SCALARS
 
 STY_MAT_DIFFUSE = 0
 STY_MAT_GGX = 1
+STY_MAT_PRINCIPLED = 2
+STY_MAT_GLASS = 3
 
 
 class PfMaterial(C.Structure):

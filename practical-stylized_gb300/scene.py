@@ -17,6 +17,7 @@ from .abi import check, lib
 MAT_DIFFUSE = 0
 MAT_GGX = 1
 MAT_PRINCIPLED = 2
+MAT_GLASS = 3
 NRC_SAMPLES_TRAIN = 0
 NRC_SAMPLES_QUERY = 1
 NRC_ROWS_REF = 0
@@ -116,6 +117,16 @@ def principled(base_color=(0.8, 0.8, 0.8), roughness=0.5, metallic=0.0, ior=1.5,
     m.specular_tint[:] = list(specular_tint)
     m.coat_weight, m.coat_roughness, m.coat_ior = coat_weight, coat_roughness, coat_ior
     m.coat_tint[:] = list(coat_tint)
+    return m
+
+
+def glass(color=(1.0, 1.0, 1.0), ior=1.5, roughness=0.0, emission=(0, 0, 0), style=(-1, -1, -1, -1),
+          set_style=-1) -> SceneMaterial:
+    """The reference's glass node (svm/surface/glass.rs): rough dielectric reflection and
+    transmission, both tinted by `color`."""
+    m = material(MAT_GLASS, color, alpha=max(roughness * roughness, 1e-4), emission=emission, style=style,
+                 set_style=set_style)
+    m.roughness, m.ior = roughness, ior
     return m
 
 

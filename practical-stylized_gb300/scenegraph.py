@@ -10,7 +10,8 @@ What the GPU path needs from a scene is extracted here on the host:
     camera/mod.rs:129-151) as a look-at sty_camera;
   * materials: the surface under the style wrappers (principled -> STY_MAT_PRINCIPLED, the
     reference's principled closure with the node's roughness, metallic, ior, transmission,
-    specular and coat inputs, principled.rs:118-330; diffuse -> Lambert; emission -> emitter, the
+    specular and coat inputs, principled.rs:118-330; glass -> STY_MAT_GLASS, glass.rs:13-44;
+    diffuse -> Lambert; emission -> emitter, the
     mesh lights of load.rs:95-128); constant inputs only -- textured inputs (and normal maps) fall
     back to constants and are listed in `warnings`;
   * the style graphs: for each style index s = 0..3 the ordered list of style nodes the graph
@@ -30,7 +31,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import abi
-from .scene import MAT_DIFFUSE, MAT_PRINCIPLED, camera, material, principled
+from .scene import MAT_DIFFUSE, MAT_GLASS, MAT_PRINCIPLED, camera, glass, material, principled
 
 
 class UnsupportedNode(ValueError):
@@ -215,6 +216,12 @@ def convert_material(name, mat) -> LoadedMaterial:
         if strength and strength > 0:
             e = rgb(base.get("emission_color"), (0.0, 0.0, 0.0))
             emission = tuple(c * strength for c in e)
+    elif t == "glass":  # svm/compiler.rs:249-263 -> glass.rs
+        kind = MAT_GLASS
+        albedo = rgb(base.get("color"), (1.0, 1.0, 1.0))
+        r = flt(base.get("roughness"), 0.0)
+        alpha = max(r * r, 1e-4)
+        params = dict(roughness=r, ior=flt(base.get("ior"), 1.5))
     elif t == "diffuse":
         albedo = rgb(base.get("color"), (0.5, 0.5, 0.5))
     elif t == "emission":
@@ -353,9 +360,13 @@ def load(path, bin_paths=None, width=None, height=None):
     names = list(graph["materials"].keys())
     loaded = [convert_material(k, graph["materials"][k]) for k in names]
     table, slots = build_style_table(loaded)
-    mats = [principled(m.albedo, emission=m.emission, style=slots[i], set_style=m.set_style, **m.params)
-            if m.kind == MAT_PRINCIPLED else material(m.kind, m.albedo, m.alpha, m.emission, slots[i], m.set_style)
-            for i, m in enumerate(loaded)]
+    def build(i, m):
+        if m.kind == MAT_PRINCIPLED:
+            return principled(m.albedo, emission=m.emission, style=slots[i], set_style=m.set_style, **m.params)
+        if m.kind == MAT_GLASS:
+            return glass(m.albedo, emission=m.emission, style=slots[i], set_style=m.set_style, **m.params)
+        return material(m.kind, m.albedo, m.alpha, m.emission, slots[i], m.set_style)
+    mats = [build(i, m) for i, m in enumerate(loaded)]
     mindex = {k: i for i, k in enumerate(names)}
     tris, mids = [], []
     for iname, inst in graph["instances"].items():

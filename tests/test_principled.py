@@ -21,6 +21,14 @@ MATS = {  # name: principled(...) keyword arguments
     "mixed": dict(base_color=(0.5, 0.5, 0.4), roughness=0.35, metallic=0.24, transmission=0.3,
                   specular_tint=(0.9, 0.8, 0.7), coat_weight=0.2, coat_roughness=0.2, coat_tint=(0.9, 1.0, 0.9)),
 }
+GLASS = {  # name: glass(...) keyword arguments (STY_MAT_GLASS, glass.rs)
+    "glass_node": dict(color=(0.9, 0.8, 0.95), roughness=0.25, ior=1.5),
+    "glass_node_rough": dict(color=(1.0, 0.7, 0.5), roughness=0.6, ior=1.33),
+}
+
+
+def _mat(sty, name):
+    return sty.scene.glass(**GLASS[name]) if name in GLASS else sty.scene.principled(**MATS[name])
 
 
 def _dirs(rng, n, both=True):
@@ -41,6 +49,46 @@ def test_oracle_principled_diffuse_limit(sty):
     k = np.abs(wi[:, 2]) / np.pi
     np.testing.assert_allclose(pdf, np.where(same, k, 0.0), rtol=1e-12, atol=0)
     np.testing.assert_allclose(f, np.where(same, k, 0.0)[:, None] * np.array([0.3, 0.5, 0.7]), rtol=1e-6, atol=1e-15)
+
+
+def test_oracle_glass_is_the_dielectric_layer(sty):
+    """glass.rs is the principled closure's dielectric layer on its own: with a white colour (where the
+    principled transmission tint sqrt(base) equals the glass tint) and the specular, metal and coat
+    layers off, the two oracle closures agree; at normal incidence the reflection is chosen with the
+    Fresnel probability ((ior - 1) / (ior + 1))^2."""
+    rng = np.random.default_rng(5)
+    wo, wi = _dirs(rng, 4000), _dirs(rng, 4000)
+    g = sty.scene.glass((1.0, 1.0, 1.0), ior=1.5, roughness=0.3)
+    p = sty.scene.principled((1.0, 1.0, 1.0), roughness=0.3, ior=1.5, transmission=1.0, specular_tint=(0, 0, 0))
+    fg, pg = oracle.principled_eval(g, wo, wi)
+    fp, pp = oracle.principled_eval(p, wo, wi)
+    np.testing.assert_allclose(fg, fp, rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(pg, pp, rtol=1e-12, atol=1e-300)
+    # a tinted glass scales both lobes by its colour (the principled closure would use sqrt for the
+    # transmitted one)
+    gt = sty.scene.glass((0.5, 0.25, 1.0), ior=1.5, roughness=0.3)
+    ft, pt = oracle.principled_eval(gt, wo, wi)
+    np.testing.assert_allclose(ft, fg * np.array([0.5, 0.25, 1.0]), rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(pt, pg, rtol=1e-12)
+    n = 20000
+    wo0 = np.tile([0.0, 0.0, 1.0], (n, 1))
+    u = rng.random((n, 3))
+    wis, _, ps = oracle.principled_sample(sty.scene.glass((1, 1, 1), ior=1.5, roughness=0.1), wo0, u)
+    refl = wis[:, 2] > 0
+    assert (refl == (u[:, 0] < 0.04)).mean() > 0.999
+    assert (ps > 0).mean() > 0.99
+
+
+def test_glass_scene_graph(sty):
+    sg = sty.scenegraph
+    nodes = {"c": {"type": "rgb", "value": [0.9, 0.95, 1.0], "colorspace": "srgb"},
+             "i": {"type": "float", "value": 1.45}, "r": {"type": "float", "value": 0.1},
+             "g": {"type": "glass", "color": {"id": "c"}, "ior": {"id": "i"}, "roughness": {"id": "r"}},
+             "o": {"type": "output", "node": {"id": "g"}}}
+    lm = sg.convert_material("Glass", {"shader": {"nodes": nodes, "output": "o"}})
+    assert lm.kind == sty.scene.MAT_GLASS and not lm.warnings
+    assert lm.params == pytest.approx(dict(roughness=0.1, ior=1.45))
+    assert lm.alpha == pytest.approx(0.01)
 
 
 def test_oracle_principled_table_limits():
@@ -101,9 +149,9 @@ def _close(a, b, scale):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", sorted(MATS))
+@pytest.mark.parametrize("name", sorted(MATS) + sorted(GLASS))
 def test_principled_eval_matches_oracle(sty, cuda, name):
-    m = sty.scene.principled(**MATS[name])
+    m = _mat(sty, name)
     rng = np.random.default_rng(1)
     wo, wi = _dirs(rng, 20000), _dirs(rng, 20000)
     wo32, wi32 = wo.astype(np.float32).astype(np.float64), wi.astype(np.float32).astype(np.float64)
@@ -118,9 +166,9 @@ def test_principled_eval_matches_oracle(sty, cuda, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", sorted(MATS))
+@pytest.mark.parametrize("name", sorted(MATS) + sorted(GLASS))
 def test_principled_sample_matches_oracle(sty, cuda, name):
-    m = sty.scene.principled(**MATS[name])
+    m = _mat(sty, name)
     rng = np.random.default_rng(2)
     wo = _dirs(rng, 20000).astype(np.float32).astype(np.float64)
     u = rng.random((20000, 3)).astype(np.float32).astype(np.float64)
@@ -135,7 +183,7 @@ def test_principled_sample_matches_oracle(sty, cuda, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", sorted(MATS) + ["mirror_metal", "clear_glass"])
+@pytest.mark.parametrize("name", sorted(MATS) + sorted(GLASS) + ["mirror_metal", "clear_glass"])
 def test_principled_energy_and_sampling_consistency(sty, cuda, name):
     """E[f/pdf] over the closure's own samples equals the sphere integral of f estimated with uniform
     directions (sampling and pdf agree: within 4 standard errors), and no energy is gained for wo
@@ -147,7 +195,9 @@ def test_principled_energy_and_sampling_consistency(sty, cuda, name):
         kw = dict(base_color=(0.9, 0.9, 0.9), roughness=0.02, metallic=1.0)
     if name == "clear_glass":
         kw = dict(base_color=(1, 1, 1), roughness=0.05, transmission=1.0, ior=1.5)
-    m = sty.scene.principled(**kw)
+    m = sty.scene.glass(**GLASS[name]) if name in GLASS else sty.scene.principled(**kw)
+    if name in GLASS:
+        kw = dict(transmission=1.0)
     rng = np.random.default_rng(3)
     n = 1 << 20
     for mu in (0.9, 0.4, -0.7):
@@ -189,17 +239,19 @@ def test_principled_diffuse_limit_renders_like_lambert(sty, cuda):
 
 
 @pytest.mark.gpu
-def test_principled_scene_two_integrators_agree(sty, cuda):
-    """A Cornell box with a metal, a glass and a coated principled box: the plain path tracer (BrPT
-    with branching 1) and the NL-PF self-only render are both unbiased here and converge to the same
-    image."""
+@pytest.mark.parametrize("glass_kind", ["principled", "glass_node"])
+def test_principled_scene_two_integrators_agree(sty, cuda, glass_kind):
+    """A Cornell box with a metal, a glass (a principled one or the glass node) and a coated principled
+    box: the plain path tracer (BrPT with branching 1) and the NL-PF self-only render are both
+    unbiased here and converge to the same image."""
     W = H = 24
     D = 6
     pos, mids, mats, cam = sty.scene.cornell_box(W, H)
     mats = list(mats)
     mats[0] = sty.scene.principled((0.75, 0.75, 0.75), roughness=0.5, coat_weight=0.3)
     mats[1] = sty.scene.principled((0.95, 0.64, 0.54), roughness=0.25, metallic=1.0)
-    mats[2] = sty.scene.principled((0.9, 0.95, 1.0), roughness=0.15, transmission=1.0, ior=1.45)
+    mats[2] = (sty.scene.principled((0.9, 0.95, 1.0), roughness=0.15, transmission=1.0, ior=1.45)
+               if glass_kind == "principled" else sty.scene.glass((0.8, 0.9, 1.0), ior=1.45, roughness=0.15))
     sc = sty.scene.Scene(pos, mids, mats, cam)
     a, _ = sc.brpt_render(sty.scene.brpt_config(max_depth=D, inner_samples=(1,), repeats=2048, seed=1))
     rc = sty.scene.render_config(max_depth=D, branch=64, repeats=32, radius_scale=(1e-4,), reuse=(8,), seed=2)
