@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import pathlib
 import statistics
@@ -104,6 +105,30 @@ class ClockSampler:
         loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
         return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def expanded_fraction(planes, valid, W, H, S, D, sigma_pos, tw=32, th=16, lim=16.0):
+    """Fraction of the filter's (tile, depth) launches units that take the expanded exponent form:
+    every valid query of a 32 x 16 tile within |p * pscale - c|^2 <= 16 of the tile's mean c
+    (the kernel's own test, done here in FP64 on the host)."""
+    pscale = math.sqrt(1.4426950408889634 / (2.0 * sigma_pos * sigma_pos))
+    hp, wp = -(-H // th) * th, -(-W // tw) * tw
+    exp_tiles = tiles = 0
+    for d in range(D):
+        sl = slice(d * W * H * S, (d + 1) * W * H * S)
+        v = np.zeros((hp, wp, S), bool)
+        v[:H, :W] = valid[sl].reshape(H, W, S) != 0
+        p = np.zeros((3, hp, wp, S))
+        p[:, :H, :W] = planes[0:3, sl].reshape(3, H, W, S) * pscale
+        v = v.reshape(hp // th, th, wp // tw, tw, S).transpose(0, 2, 1, 3, 4).reshape(hp // th, wp // tw, -1)
+        p = p.reshape(3, hp // th, th, wp // tw, tw, S).transpose(0, 1, 3, 2, 4, 5).reshape(3, hp // th, wp // tw, -1)
+        cnt = v.sum(-1)
+        c = (p * v).sum(-1) / np.maximum(cnt, 1)
+        q = (((p - c[..., None]) ** 2).sum(0) * v).max(-1)
+        live = cnt > 0
+        tiles += int(live.sum())
+        exp_tiles += int((live & (q <= lim)).sum())
+    return exp_tiles / max(tiles, 1)
 
 
 def cpu_baseline(sty, orc, planes, valid, depths: int = D_, budget_s: float = 12.0):
@@ -622,16 +647,9 @@ def run(args):
         barrier()
         e2e_ms = e0.elapsed_time(e1)
 
-    # ---- max over ranks
-    def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
-
-    ms_total = max_over_ranks(ms_total)
-    e2e_ms = max_over_ranks(e2e_ms)
+    # ---- max over ranks (replicas: the job's time is its slowest rank's)
+    ms_total = sty.replicas.max_over_ranks(ms_total, device=dev)
+    e2e_ms = sty.replicas.max_over_ranks(e2e_ms, device=dev)
     ms_step = ms_total / args.steps
     value = nvalid * world * args.steps / (ms_total / 1e3) / 1e6
     e2e_value = nvalid * world * args.steps / (e2e_ms / 1e3) / 1e6
@@ -645,7 +663,10 @@ def run(args):
     pairs_launch = n * (2 * prm.radius + 1) ** 2 * S_
     sm_clock = (clk or {}).get("sm_mhz") or 1900.0
     fp32_peak = 152 * 128 * 2 * sm_clock * 1e6 / 1e12  # TFLOP/s, FFMA = 2 FLOP, at the sampled clock
-    flops_pair = 2 * 13  # 13 FP32 FMA/ADD-class instructions per pair (exponent 9, accumulate 4)
+    # FP32-pipe instructions per pair: expanded exponent 6 FFMA + 4 FFMA accumulate; direct form
+    # 3 FADD + 6 FFMA + 4 FFMA. The tile's form depends on its positions (see expanded_fraction).
+    f_exp = expanded_fraction(planes, valid, W_, H_, S_, D_, prm.sigma_pos)
+    flops_pair = 2 * (10 * f_exp + 13 * (1 - f_exp))
     alu_achieved = pairs_launch * flops_pair / mean_launch_s / 1e12
 
     if rank != 0:
@@ -670,8 +691,10 @@ def run(args):
                      "algorithmic_bytes_per_launch": bytes_launch, "mean_launch_ms": mean_launch_s * 1e3},
         "alu_roofline": {"bound": "fp32", "achieved": alu_achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                          "frac": alu_achieved / fp32_peak, "pairs_per_launch": pairs_launch,
-                         "flops_per_pair": flops_pair,
-                         "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 at the sampled SM clock"},
+                         "flops_per_pair": flops_pair, "expanded_tile_fraction": f_exp,
+                         "mufu_ex2_per_s": pairs_launch / mean_launch_s,
+                         "peak_source": "nominal 152 SM x 128 FP32 lanes x 2 at the sampled SM clock",
+                         "note": "the binding roof of this kernel (pair arithmetic); HBM traffic is ~0.6 % of it"},
         "clocks": clk,
     }
     if world == 1 and not args.no_c1:

@@ -66,6 +66,9 @@ STY_API const char *sty_last_error(void);
 /* Number of kernels this library launched since load (all threads, all devices). Used by
  * benchmarks to count launches inside a timed region. */
 STY_API uint64_t sty_launch_count(void);
+/* sizeof of the struct this header names `name` (e.g. "sty_brpt_config") as the library was
+ * compiled, 0 for an unknown name: lets a binding check its struct layouts against the library. */
+STY_API uint64_t sty_struct_size(const char *name);
 
 /* Device status word of the current device: kernels that hit a bounded wait (instead of
  * hanging) OR a STY_DEV_* bit into it and return. Reading synchronises the device;
@@ -600,6 +603,11 @@ typedef struct sty_brpt_config {
     uint32_t repeats;                            /* Config::repeats */
     uint32_t vram_mb;                            /* Config::vram: vertex-tree budget per pass, MB */
     uint64_t seed;
+    uint32_t first_repeat; /* this call renders repeats first_repeat .. first_repeat + repeats - 1 of the
+                              seed's sample sequence (0 for a whole render): replicas that split the
+                              repeats of one render produce films whose repeat-weighted sum is that
+                              render's film */
+    uint32_t reserved;     /* 0 */
 } sty_brpt_config;
 typedef struct sty_brpt_stats {
     uint64_t vertices;        /* surface hits (tree vertices) over all passes and repeats */

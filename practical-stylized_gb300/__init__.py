@@ -26,5 +26,6 @@ from . import pf_ref  # noqa: F401
 from . import nrc  # noqa: F401
 from . import scene  # noqa: F401
 from . import scenegraph  # noqa: F401
+from . import replicas  # noqa: F401
 
 PKG_DIR = pathlib.Path(__file__).resolve().parent

@@ -178,6 +178,28 @@ const char *sty_last_error(void) { return g_last_error; }
 
 uint64_t sty_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
+uint64_t sty_struct_size(const char *name) {
+    if (!name) return 0;
+    if (!strcmp(name, "sty_pcg32")) return sizeof(sty_pcg32);
+    if (!strcmp(name, "sty_style_node")) return sizeof(sty_style_node);
+    if (!strcmp(name, "sty_style_program")) return sizeof(sty_style_program);
+    if (!strcmp(name, "sty_pf_records")) return sizeof(sty_pf_records);
+    if (!strcmp(name, "sty_pf_screen_params")) return sizeof(sty_pf_screen_params);
+    if (!strcmp(name, "sty_pf_material")) return sizeof(sty_pf_material);
+    if (!strcmp(name, "sty_pf_vertices")) return sizeof(sty_pf_vertices);
+    if (!strcmp(name, "sty_pf_ref_params")) return sizeof(sty_pf_ref_params);
+    if (!strcmp(name, "sty_nrc_config")) return sizeof(sty_nrc_config);
+    if (!strcmp(name, "sty_nrc_grid_config")) return sizeof(sty_nrc_grid_config);
+    if (!strcmp(name, "sty_scene_material")) return sizeof(sty_scene_material);
+    if (!strcmp(name, "sty_camera")) return sizeof(sty_camera);
+    if (!strcmp(name, "sty_pf_render_config")) return sizeof(sty_pf_render_config);
+    if (!strcmp(name, "sty_nrc_render_config")) return sizeof(sty_nrc_render_config);
+    if (!strcmp(name, "sty_nrc_render_stats")) return sizeof(sty_nrc_render_stats);
+    if (!strcmp(name, "sty_brpt_config")) return sizeof(sty_brpt_config);
+    if (!strcmp(name, "sty_brpt_stats")) return sizeof(sty_brpt_stats);
+    return 0;
+}
+
 sty_status sty_device_status(uint32_t *status_out, int32_t clear) {
     clear_error();
     STY_ARG_CHECK(status_out, "sty_device_status: null status_out");

@@ -89,12 +89,12 @@ __host__ __device__ __forceinline__ uint64_t repeat_key(uint64_t seed, uint64_t 
 // depth 0: the camera slots of samples q0 .. q0 + n, sample q = repeat * npx + pixel (kernel_init
 // :501-541)
 __global__ void k_br_camera(SceneView sc, CamArgs cam, uint32_t n, uint64_t q0, uint32_t npx, uint64_t seed,
-                            BrSlots s, unsigned long long *hits) {
+                            uint64_t first_repeat, BrSlots s, unsigned long long *hits) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t q = q0 + i;
     const uint32_t px = (uint32_t)(q % npx);
-    const uint64_t key = splitmix64(repeat_key(seed, q / npx) + px);
+    const uint64_t key = splitmix64(repeat_key(seed, first_repeat + q / npx) + px);
     sty_pcg32 st = key_stream(key);
     F3 ro, rd;
     camera_ray(cam, px, st, &ro, &rd);
@@ -275,6 +275,7 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
         STY_ARG_CHECK(cfg->inner_samples[k] >= 1 && cfg->inner_samples[k] <= 65536, "inner_samples[%u] must be in [1, 65536]",
                       k);
     STY_ARG_CHECK(cfg->repeats >= 1 && cfg->vram_mb >= 1, "repeats and vram_mb must be >= 1");
+    STY_ARG_CHECK((uint64_t)cfg->first_repeat + cfg->repeats <= 0xFFFFFFFFull, "first_repeat + repeats overflows");
     STY_ARG_CHECK(n_programs <= 64 && (n_programs == 0 || programs), "bad style programs");
     for (uint32_t k = 0; k < n_programs; k++)
         STY_ARG_CHECK(style_program_valid(&programs[k]), "style program %u is invalid", k);
@@ -360,7 +361,8 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
                 const uint32_t P = (uint32_t)std::min<uint64_t>(ppp, total - q0);
                 cnt.assign(1, P);
                 off.assign(1, 0);
-                k_br_camera<<<(P + 255) / 256, 256, 0, st>>>(sv, ca, P, q0, npx, cfg->seed, sl, dhits);
+                k_br_camera<<<(P + 255) / 256, 256, 0, st>>>(sv, ca, P, q0, npx, cfg->seed, cfg->first_repeat, sl,
+                                                             dhits);
                 STY_TRY(check_launch("k_br_camera"));
                 for (uint32_t d = 0; d <= cfg->max_depth; d++) {
                     const uint32_t n = cnt[d], base = off[d];

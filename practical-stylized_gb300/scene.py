@@ -59,7 +59,8 @@ class NrcRenderStats(C.Structure):
 
 class BrptConfig(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("n_levels", C.c_uint32), ("inner_samples", C.c_uint32 * 8),
-                ("repeats", C.c_uint32), ("vram_mb", C.c_uint32), ("seed", C.c_uint64)]
+                ("repeats", C.c_uint32), ("vram_mb", C.c_uint32), ("seed", C.c_uint64),
+                ("first_repeat", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class BrptStats(C.Structure):
@@ -67,11 +68,13 @@ class BrptStats(C.Structure):
                 ("pixels_per_pass", C.c_uint64), ("max_pass_slots", C.c_uint64)]
 
 
-def brpt_config(max_depth=7, inner_samples=(256, 32, 8, 1), repeats=1, vram_mb=8192, seed=0) -> BrptConfig:
+def brpt_config(max_depth=7, inner_samples=(256, 32, 8, 1), repeats=1, vram_mb=8192, seed=0,
+                first_repeat=0) -> BrptConfig:
     """The branching path tracer's configuration (branching_pt.rs Config :77-100; the defaults are
-    the reference's)."""
+    the reference's). first_repeat: this call's share of a render split over replicas."""
     c = BrptConfig()
     c.max_depth, c.repeats, c.vram_mb, c.seed = max_depth, repeats, vram_mb, seed
+    c.first_repeat = first_repeat
     c.n_levels = len(inner_samples)
     for i, v in enumerate(inner_samples):
         c.inner_samples[i] = v

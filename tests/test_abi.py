@@ -35,6 +35,28 @@ def test_struct_layouts(sty):
     assert C.sizeof(a.Pcg32) == 16
 
 
+def test_struct_sizes_match_the_library(sty):
+    """Every struct the header declares has a ctypes mirror of the size the library was built with."""
+    from importlib import import_module
+    pkg = sty.__name__
+    mirrors = {"sty_pcg32": "abi.Pcg32", "sty_style_node": "abi.StyleNode", "sty_style_program": "abi.StyleProgram",
+               "sty_pf_records": "abi.PfRecords", "sty_pf_screen_params": "abi.PfScreenParams",
+               "sty_pf_material": "pf_ref.PfMaterial", "sty_pf_vertices": "pf_ref.PfVertices",
+               "sty_pf_ref_params": "pf_ref.PfRefParams", "sty_nrc_config": "nrc.NrcConfig",
+               "sty_nrc_grid_config": "nrc.NrcGridConfig", "sty_scene_material": "scene.SceneMaterial",
+               "sty_camera": "scene.Camera", "sty_pf_render_config": "scene.RenderConfig",
+               "sty_nrc_render_config": "scene.NrcRenderConfig", "sty_nrc_render_stats": "scene.NrcRenderStats",
+               "sty_brpt_config": "scene.BrptConfig", "sty_brpt_stats": "scene.BrptStats"}
+    declared = set(re.findall(r"\}\s*(sty_\w+)\s*;", (ROOT / "include" / "sty_gb300.h").read_text()))
+    assert declared == set(mirrors), declared ^ set(mirrors)
+    lib = sty.abi.lib()
+    for name, path in mirrors.items():
+        mod, cls = path.split(".")
+        size = C.sizeof(getattr(import_module(f"{pkg}.{mod}"), cls))
+        assert lib.sty_struct_size(name.encode()) == size, (name, lib.sty_struct_size(name.encode()), size)
+    assert lib.sty_struct_size(b"no_such_struct") == 0
+
+
 def test_version_and_status_strings(sty):
     lib = sty.abi.lib()
     assert lib.sty_version() >= 100
