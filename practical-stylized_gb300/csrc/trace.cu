@@ -381,7 +381,7 @@ __global__ void k_split_collect(uint32_t n, uint32_t d, VertOut v, const uint32_
 // the sample's throughput f |cos| / pdf and the hit's emission MIS weight.
 __global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t *split, SplitPlanes sp, sty_pcg32 *rng,
                           const sty_style_program *progs, uint32_t n_progs, float *rows, float *thr, float *gmis,
-                          uint32_t *gmat, uint32_t *gflags, float *acc_direct) {
+                          uint32_t *gmat, uint32_t *gflags, float *gpos, float *acc_direct) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float *row = rows + (size_t)i * fa.dims;
@@ -449,12 +449,15 @@ __global__ void k_fg_step(SceneView sc, FeatArgs fa, uint32_t n, const uint32_t 
     gmis[i] = mis;
     gmat[i] = qm;
     gflags[i] = qf;
+    gpos[i] = q.x;
+    gpos[n + i] = q.y;
+    gpos[2 * (size_t)n + i] = q.z;
     write_features(sc, fa, q, -wi, qn, qm, qf, s + 1, row);
 }
 // acc_indirect += style_{s+1}(cache prediction at the gather hit) * throughput * mis; every
 // iteration counts (a miss contributes 0)
 __global__ void k_fg_accumulate(SceneView sc, uint32_t n, const uint32_t *split, const float *pred, const float *thr,
-                                const float *gmis, const uint32_t *gmat, const uint32_t *gflags,
+                                const float *gmis, const uint32_t *gmat, const uint32_t *gflags, const float *gpos,
                                 const sty_style_program *progs, uint32_t n_progs, int stylize, float *acc_ind,
                                 float *ngath) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -465,8 +468,8 @@ __global__ void k_fg_accumulate(SceneView sc, uint32_t n, const uint32_t *split,
     const uint32_t fl = gflags[i];
     if (stylize && !(fl & 1u)) {
         const int32_t pi = sc.materials[gmat[i]].style[style_index(fl)];
-        // the gather hit's position is not kept: a half-tone node reads p = 0 here
-        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], split[i] + 1, c);
+        const f3 q = {gpos[i], gpos[n + i], gpos[2 * (size_t)n + i]};
+        if (pi >= 0 && (uint32_t)pi < n_progs) c = style_apply(progs[pi], split[i] + 1, c, q);
     }
     const float w = gmis[i];
     if (!(isfinite(c.x) && isfinite(c.y) && isfinite(c.z))) return;
@@ -979,12 +982,13 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
             continue;
         }
         // final gathering: per-path planes of the split vertex, accumulators, gather scratch
-        constexpr size_t kFgPlanes = 28;  // split vertex 15, accumulators 7, gather scratch 6
+        constexpr size_t kFgPlanes = 31;  // split vertex 15, accumulators 7, gather scratch 9
         float *fgb = (float *)job.alloc(kFinalGather, kFgPlanes * npx * 4, "alloc final gather");
         STY_TRY(job.s);
         SplitPlanes sp;
         float *acc_direct, *acc_ind, *ngath, *thr, *gmis;
         uint32_t *gmat, *gflags;
+        float *gpos;
         {
             int k = 0;
             auto pl = [&]() { return fgb + (size_t)(k++) * npx; };
@@ -1008,6 +1012,9 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
             gmis = pl();
             gmat = (uint32_t *)pl();
             gflags = (uint32_t *)pl();
+            gpos = pl();
+            pl();
+            pl();
             if ((size_t)k != kFgPlanes) {
                 set_error("final gather planes: %d carved, %zu allocated", k, kFgPlanes);
                 return STY_ERR_ARG;
@@ -1020,12 +1027,12 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         }
         for (uint32_t it = 0; it < fg; it++) {
             k_fg_step<<<nb, 256, 0, st>>>(job.sv, fa, npx, job.ps.split, sp, job.rng, job.dprog, n_programs, qin, thr, gmis,
-                                          gmat, gflags, acc_direct);
+                                          gmat, gflags, gpos, acc_direct);
             STY_TRY(check_launch("k_fg_step"));
             STY_TRY(sty_nrc_inference(nrc, npx, qin, qpred, stream));
             acc.inference_queries += npx;
-            k_fg_accumulate<<<nb, 256, 0, st>>>(job.sv, npx, job.ps.split, qpred, thr, gmis, gmat, gflags, job.dprog,
-                                                n_programs, stylize_pred, acc_ind, ngath);
+            k_fg_accumulate<<<nb, 256, 0, st>>>(job.sv, npx, job.ps.split, qpred, thr, gmis, gmat, gflags, gpos,
+                                                job.dprog, n_programs, stylize_pred, acc_ind, ngath);
             STY_TRY(check_launch("k_fg_accumulate"));
         }
         for (int d = (int)D; d >= 0; d--) {
