@@ -1,15 +1,17 @@
 // pf_screen4.cu -- warp-specialised screen-space NL-PF filter for 4 spp.
 //
-// CTA = 32 x 16 pixel tile, 8 consumer + NPW producer warps:
-//   * 8 consumer warps: thread (lx, ly) owns pixels A = (x0+lx, y0+2ly) and B = (x0+lx, y0+2ly+1),
-//     i.e. 8 query records (2 pixels x 4 spp). A warp is one pixel-row pair, so every branch on
-//     the candidate row is warp-uniform.
-//   * producer warps: stream the (32+2R) x (16+2R) candidate halo, CH rows at a time, into a
+// CTA = 32 x 12 pixel tile, 12 consumer + NPW producer warps:
+//   * consumer warp w owns pixel row y0 + w; lane l owns pixel x0 + l and its 4 query records
+//     (the 4 spp), so every branch on the candidate row is warp-uniform. Three consumer warps per
+//     scheduler hide the latency of the dependent exponent chains and the MUFU round trips.
+//   * producer warps: stream the (32+2R) x (12+2R) candidate halo, CH rows at a time, into a
 //     double-buffered shared-memory ring guarded by mbarriers (full / empty per buffer). While
 //     staging they transform each candidate once (recentred scaled position, normal, incoming
 //     radiance in_d = rad + thr * out_{d+1} with the propagate fused in, weight factors).
-// Kahan totals of the 8 queries live in shared memory (touched once per candidate row), which
-// keeps the consumer under the 168 registers a 10-warp CTA can have per thread.
+// Packed FP32: a candidate pixel's 4 samples arrive as one 16-byte shared load per field; the
+// consumer pairs samples (0, 1) and (2, 3) in the two lanes of `fma.rn.f32x2` against its query
+// duplicated in both lanes, so the candidate pair needs no register moves. Kahan totals of the 4
+// queries live in shared memory (touched once per candidate row).
 // All mbarrier waits are bounded (~2 s of %globaltimer); on expiry the thread records
 // STY_DEV_WAIT_TIMEOUT in the device status word and leaves its loop, so a protocol fault ends
 // the kernel with a status instead of hanging the GPU.
@@ -37,22 +39,23 @@ namespace {
 
 constexpr int S = 4;
 constexpr int TW = 32;
-constexpr int TH = 16;
-constexpr int NCW = 8;  // consumer warps
+constexpr int NCW = 12;  // consumer warps = pixel rows of the tile
+constexpr int TH = NCW;
 #ifndef STY_PF4_NPW
 #define STY_PF4_NPW 4
 #endif
-#ifndef STY_PF4_NB
-#define STY_PF4_NB 3
+#ifndef STY_PF4_PU
+#define STY_PF4_PU 4
 #endif
-constexpr int NPW = STY_PF4_NPW;  // producer warps (10 or 12 warps both allow 168 registers)
+constexpr int NPW = STY_PF4_NPW;  // producer warps (16 warps: 128 registers a thread)
 constexpr int NC = NCW * 32;
 constexpr int NP = NPW * 32;
 constexpr int NTH = NC + NP;
 constexpr int CH = 4;   // candidate rows per buffer
-constexpr int NB = STY_PF4_NB;  // ring depth
-constexpr int PU = 4;   // records staged per producer thread per batch (loads in flight)
+constexpr int kMaxNB = 4;  // ring depth: 4 buffers when they fit in shared memory (R <= 19), else 3
+constexpr int PU = STY_PF4_PU;  // records staged per producer thread per batch (loads in flight)
 constexpr int NF = 10;  // staged fields: p'(3) n(3) m, v(3)   [direct form: m = 1/0, v = in]
+constexpr int NQ = S;   // query records per consumer thread
 constexpr float kLimQ = 16.0f;
 constexpr float kLimC = 120.0f;
 constexpr float kFar = 1e18f;
@@ -94,65 +97,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32
 }
 
 struct Smem {
-    uint64_t full[NB];
-    uint64_t empty[NB];
+    uint64_t full[kMaxNB];
+    uint64_t empty[kMaxNB];
     float red[NCW][4];
     float cx, cy, cz;
     int mode;  // 0 = expanded, 1 = direct, 2 = no valid query
 };
-
-template <bool EXP, bool DA, bool DB>
-__device__ __forceinline__ void row_pass(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
-                                         const float (&qa)[8][3], const float (&qn)[8][3], float rbA, float rbB,
-                                         float (&part)[8][4]) {
-#pragma unroll 1
-    for (int dx = -R; dx <= R; dx++) {
-        const float cx = -pix2 * (float)(dx * dx);
-        const float *cp = rowp + (lx + R + dx) * S;
-        float c[NF][S];
-#pragma unroll
-        for (int f = 0; f < NF; f++) {
-            const float4 v = *reinterpret_cast<const float4 *>(cp + f * plane);
-            c[f][0] = v.x;
-            c[f][1] = v.y;
-            c[f][2] = v.z;
-            c[f][3] = v.w;
-        }
-        const float bA = rbA + cx, bB = rbB + cx;
-#pragma unroll
-        for (int q = 0; q < 8; q++) {
-            if ((q < 4 && !DA) || (q >= 4 && !DB)) continue;
-            const float base = q < 4 ? bA : bB;
-#pragma unroll
-            for (int t = 0; t < S; t++) {
-                float arg;
-                if (EXP) {
-                    arg = fmaf(qa[q][0], c[0][t], base);
-                    arg = fmaf(qa[q][1], c[1][t], arg);
-                    arg = fmaf(qa[q][2], c[2][t], arg);
-                    arg = fmaf(qn[q][0], c[3][t], arg);
-                    arg = fmaf(qn[q][1], c[4][t], arg);
-                    arg = fmaf(qn[q][2], c[5][t], arg);
-                } else {
-                    arg = fmaf(qn[q][0], c[3][t], base);
-                    arg = fmaf(qn[q][1], c[4][t], arg);
-                    arg = fmaf(qn[q][2], c[5][t], arg);
-                    const float ex = qa[q][0] - c[0][t];
-                    const float ey = qa[q][1] - c[1][t];
-                    const float ez = qa[q][2] - c[2][t];
-                    arg = fmaf(-ex, ex, arg);
-                    arg = fmaf(-ey, ey, arg);
-                    arg = fmaf(-ez, ez, arg);
-                }
-                const float e = ex2_approx(arg);
-                part[q][0] = fmaf(e, c[6][t], part[q][0]);
-                part[q][1] = fmaf(e, c[7][t], part[q][1]);
-                part[q][2] = fmaf(e, c[8][t], part[q][2]);
-                part[q][3] = fmaf(e, c[9][t], part[q][3]);
-            }
-        }
-    }
-}
 
 // Packed FP32: d = a * b + c on both lanes (fma.rn.f32x2; each lane rounds exactly like fmaf),
 // one issue slot for two FMAs.
@@ -164,16 +114,50 @@ __device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
         : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
     return d;
 }
-// The expanded-form row pass on pairs of queries (spp samples 2p, 2p+1 of one pixel) with packed
-// FMAs: each lane performs exactly the operation sequence of row_pass<true, ..>, so the sums are
-// bit-identical; the candidate's fields are duplicated once per candidate for the four pairs.
-template <bool DA, bool DB>
-__device__ __forceinline__ void row_pass2(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
-                                          const float2 (&qa2)[4][3], const float2 (&qn2)[4][3], float rbA, float rbB,
-                                          float2 (&part2)[4][4]) {
+
+// One candidate row, expanded form: for every dx the candidate pixel's 4 samples, taken as the
+// pairs (0, 1) and (2, 3); part2[q][k].x / .y collect samples 0, 2 / 1, 3 of query q (w, w*in).
+__device__ __forceinline__ void row_pass_exp(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
+                                             const float2 (&qa2)[NQ][3], const float2 (&qn2)[NQ][3], float rb,
+                                             float2 (&part2)[NQ][4]) {
 #pragma unroll 1
     for (int dx = -R; dx <= R; dx++) {
-        const float cx = -pix2 * (float)(dx * dx);
+        const float base = rb - pix2 * (float)(dx * dx);
+        const float2 base2 = make_float2(base, base);
+        const float *cp = rowp + (lx + R + dx) * S;
+        float4 v[NF];
+#pragma unroll
+        for (int f = 0; f < NF; f++) v[f] = *reinterpret_cast<const float4 *>(cp + f * plane);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float2 c[NF];
+#pragma unroll
+            for (int f = 0; f < NF; f++) c[f] = h == 0 ? make_float2(v[f].x, v[f].y) : make_float2(v[f].z, v[f].w);
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+                float2 arg = ffma2(qa2[q][0], c[0], base2);
+                arg = ffma2(qa2[q][1], c[1], arg);
+                arg = ffma2(qa2[q][2], c[2], arg);
+                arg = ffma2(qn2[q][0], c[3], arg);
+                arg = ffma2(qn2[q][1], c[4], arg);
+                arg = ffma2(qn2[q][2], c[5], arg);
+                const float2 e = make_float2(ex2_approx(arg.x), ex2_approx(arg.y));
+                part2[q][0] = ffma2(e, c[6], part2[q][0]);
+                part2[q][1] = ffma2(e, c[7], part2[q][1]);
+                part2[q][2] = ffma2(e, c[8], part2[q][2]);
+                part2[q][3] = ffma2(e, c[9], part2[q][3]);
+            }
+        }
+    }
+}
+
+// One candidate row, direct form (fallback tiles), scalar: part[q][k] over the 4 samples in order.
+__device__ __forceinline__ void row_pass_dir(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
+                                             const float2 (&qa2)[NQ][3], const float2 (&qn2)[NQ][3], float rb,
+                                             float (&part)[NQ][4]) {
+#pragma unroll 1
+    for (int dx = -R; dx <= R; dx++) {
+        const float base = rb - pix2 * (float)(dx * dx);
         const float *cp = rowp + (lx + R + dx) * S;
         float c[NF][S];
 #pragma unroll
@@ -184,27 +168,24 @@ __device__ __forceinline__ void row_pass2(const float *__restrict__ rowp, int pl
             c[f][2] = v.z;
             c[f][3] = v.w;
         }
-        const float bA = rbA + cx, bB = rbB + cx;
 #pragma unroll
-        for (int t = 0; t < S; t++) {
-            float2 cd[NF];
+        for (int q = 0; q < NQ; q++) {
 #pragma unroll
-            for (int f = 0; f < NF; f++) cd[f] = make_float2(c[f][t], c[f][t]);
-#pragma unroll
-            for (int qp = 0; qp < 4; qp++) {
-                if ((qp < 2 && !DA) || (qp >= 2 && !DB)) continue;
-                const float base = qp < 2 ? bA : bB;
-                float2 arg = ffma2(qa2[qp][0], cd[0], make_float2(base, base));
-                arg = ffma2(qa2[qp][1], cd[1], arg);
-                arg = ffma2(qa2[qp][2], cd[2], arg);
-                arg = ffma2(qn2[qp][0], cd[3], arg);
-                arg = ffma2(qn2[qp][1], cd[4], arg);
-                arg = ffma2(qn2[qp][2], cd[5], arg);
-                const float2 e = make_float2(ex2_approx(arg.x), ex2_approx(arg.y));
-                part2[qp][0] = ffma2(e, cd[6], part2[qp][0]);
-                part2[qp][1] = ffma2(e, cd[7], part2[qp][1]);
-                part2[qp][2] = ffma2(e, cd[8], part2[qp][2]);
-                part2[qp][3] = ffma2(e, cd[9], part2[qp][3]);
+            for (int t = 0; t < S; t++) {
+                float arg = fmaf(qn2[q][0].x, c[3][t], base);
+                arg = fmaf(qn2[q][1].x, c[4][t], arg);
+                arg = fmaf(qn2[q][2].x, c[5][t], arg);
+                const float ex = qa2[q][0].x - c[0][t];
+                const float ey = qa2[q][1].x - c[1][t];
+                const float ez = qa2[q][2].x - c[2][t];
+                arg = fmaf(-ex, ex, arg);
+                arg = fmaf(-ey, ey, arg);
+                arg = fmaf(-ez, ez, arg);
+                const float e = ex2_approx(arg);
+                part[q][0] = fmaf(e, c[6][t], part[q][0]);
+                part[q][1] = fmaf(e, c[7][t], part[q][1]);
+                part[q][2] = fmaf(e, c[8][t], part[q][2]);
+                part[q][3] = fmaf(e, c[9][t], part[q][3]);
             }
         }
     }
@@ -212,60 +193,37 @@ __device__ __forceinline__ void row_pass2(const float *__restrict__ rowp, int pl
 
 // Kahan totals: kst[(q * NC + ctid) * 2 + 0] = sums (w, r, g, b), [.. + 1] = compensations.
 template <bool EXP>
-__device__ __forceinline__ void consume_chunk(const float *__restrict__ buf, int plane, int cy0, int row_hi, int yA,
-                                              int lx, int R, float pix2, float nscale, const float (&qa)[8][3],
-                                              const float (&qn)[8][3], float4 *__restrict__ kst, int ctid) {
+__device__ __forceinline__ void consume_chunk(const float *__restrict__ buf, int plane, int cy0, int row_hi, int y,
+                                              int lx, int R, float pix2, float nscale, const float2 (&qa2)[NQ][3],
+                                              const float2 (&qn2)[NQ][3], float4 *__restrict__ kst, int ctid) {
     for (int r = 0; r < CH; r++) {
         const int yy = cy0 + r;
         if (yy > row_hi) break;
-        const int dyA = yy - yA, dyB = dyA - 1;
-        const bool ia = dyA >= -R && dyA <= R;
-        const bool ib = dyB >= -R && dyB <= R;
-        if (!ia && !ib) continue;
-        const float rbA = -pix2 * (float)(dyA * dyA) - nscale;
-        const float rbB = -pix2 * (float)(dyB * dyB) - nscale;
-        float part[8][4];
+        const int dy = yy - y;
+        if (dy < -R || dy > R) continue;
+        const float rb = -pix2 * (float)(dy * dy) - nscale;
         const float *rowp = buf + r * (plane / CH);
+        float part[NQ][4];
         if (EXP) {
-            float2 part2[4][4], qa2[4][3], qn2[4][3];
+            float2 part2[NQ][4];
 #pragma unroll
-            for (int qp = 0; qp < 4; qp++) {
+            for (int q = 0; q < NQ; q++)
 #pragma unroll
-                for (int k = 0; k < 4; k++) part2[qp][k] = make_float2(0.0f, 0.0f);
+                for (int k = 0; k < 4; k++) part2[q][k] = make_float2(0.0f, 0.0f);
+            row_pass_exp(rowp, plane, lx, R, pix2, qa2, qn2, rb, part2);
 #pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    qa2[qp][k] = make_float2(qa[2 * qp][k], qa[2 * qp + 1][k]);
-                    qn2[qp][k] = make_float2(qn[2 * qp][k], qn[2 * qp + 1][k]);
-                }
-            }
-            if (ia && ib)
-                row_pass2<true, true>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
-            else if (ia)
-                row_pass2<true, false>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
-            else
-                row_pass2<false, true>(rowp, plane, lx, R, pix2, qa2, qn2, rbA, rbB, part2);
+            for (int q = 0; q < NQ; q++)
 #pragma unroll
-            for (int qp = 0; qp < 4; qp++)
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    part[2 * qp][k] = part2[qp][k].x;
-                    part[2 * qp + 1][k] = part2[qp][k].y;
-                }
+                for (int k = 0; k < 4; k++) part[q][k] = part2[q][k].x + part2[q][k].y;
         } else {
 #pragma unroll
-            for (int q = 0; q < 8; q++)
+            for (int q = 0; q < NQ; q++)
 #pragma unroll
                 for (int k = 0; k < 4; k++) part[q][k] = 0.0f;
-            if (ia && ib)
-                row_pass<false, true, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
-            else if (ia)
-                row_pass<false, true, false>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
-            else
-                row_pass<false, false, true>(rowp, plane, lx, R, pix2, qa, qn, rbA, rbB, part);
+            row_pass_dir(rowp, plane, lx, R, pix2, qa2, qn2, rb, part);
         }
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            if ((q < 4 && !ia) || (q >= 4 && !ib)) continue;
+        for (int q = 0; q < NQ; q++) {
             float4 *slot = kst + ((size_t)q * NC + ctid) * 2;
             float4 sm4 = slot[0], cm4 = slot[1];
             KahanF k0 = {sm4.x, cm4.x}, k1 = {sm4.y, cm4.y}, k2 = {sm4.z, cm4.z}, k3 = {sm4.w, cm4.w};
@@ -279,6 +237,7 @@ __device__ __forceinline__ void consume_chunk(const float *__restrict__ buf, int
     }
 }
 
+template <int NB>
 __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const sty_style_program style) {
     extern __shared__ __align__(16) float stage[];
     __shared__ Smem sh;
@@ -302,18 +261,17 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
     }
 
     // ---- queries (consumers) and the tile centre
-    const int lx = lane, ly = warp;
-    const int x = tx0 + lx, yA = ty0 + 2 * ly;
-    float qp[8][3], qn[8][3];
-    bool qv[8];
+    const int lx = lane;
+    const int x = tx0 + lx, y = ty0 + warp;
+    float qp[NQ][3], qn[NQ][3];
+    bool qv[NQ];
     float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
     if (consumer) {
+        const bool in = x < a.W && y < a.H;
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int y = yA + (q >> 2);
-            const bool in = x < a.W && y < a.H;
+        for (int q = 0; q < NQ; q++) {
             size_t g = 0;
-            if (in) g = dbase + ((size_t)y * a.W + x) * S + (q & 3);
+            if (in) g = dbase + ((size_t)y * a.W + x) * S + q;
             qv[q] = in && a.valid[g] != 0;
 #pragma unroll
             for (int k = 0; k < 3; k++) {
@@ -357,7 +315,7 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
     float qmax = 0.0f;
     if (consumer) {
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
+        for (int q = 0; q < NQ; q++) {
             qp[q][0] = qp[q][0] * a.pscale - ccx;
             qp[q][1] = qp[q][1] * a.pscale - ccy;
             qp[q][2] = qp[q][2] * a.pscale - ccz;
@@ -374,12 +332,10 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
     const int mode = sh.mode;
 
     if (mode == 2) {  // no valid record in the tile: outputs are zero
-        if (consumer) {
+        if (consumer && x < a.W && y < a.H) {
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                const int y = yA + (q >> 2);
-                if (x >= a.W || y >= a.H) continue;
-                const size_t j = ((size_t)y * a.W + x) * S + (q & 3);
+            for (int q = 0; q < NQ; q++) {
+                const size_t j = ((size_t)y * a.W + x) * S + q;
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     a.out[c * N + j] = 0.0f;
@@ -481,12 +437,15 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
 
     // ================= consumer warps =================
     float4 *kst = reinterpret_cast<float4 *>(stage + (size_t)NB * NF * plane);
-    float qa[8][3];
+    float2 qa2[NQ][3], qn2[NQ][3];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
+    for (int q = 0; q < NQ; q++) {
         const float f = expf_mode ? 2.0f : 1.0f;
 #pragma unroll
-        for (int k = 0; k < 3; k++) qa[q][k] = f * qp[q][k];
+        for (int k = 0; k < 3; k++) {
+            qa2[q][k] = make_float2(f * qp[q][k], f * qp[q][k]);
+            qn2[q][k] = make_float2(qn[q][k], qn[q][k]);
+        }
         kst[((size_t)q * NC + tid) * 2 + 0] = make_float4(0.f, 0.f, 0.f, 0.f);
         kst[((size_t)q * NC + tid) * 2 + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -501,19 +460,18 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
         const float *buf = stage + (size_t)b * NF * plane;
         const int cy0 = row_lo + k * CH;
         if (expf_mode)
-            consume_chunk<true>(buf, plane, cy0, row_hi, yA, lx, R, a.pix2, a.nscale, qa, qn, kst, tid);
+            consume_chunk<true>(buf, plane, cy0, row_hi, y, lx, R, a.pix2, a.nscale, qa2, qn2, kst, tid);
         else
-            consume_chunk<false>(buf, plane, cy0, row_hi, yA, lx, R, a.pix2, a.nscale, qa, qn, kst, tid);
+            consume_chunk<false>(buf, plane, cy0, row_hi, y, lx, R, a.pix2, a.nscale, qa2, qn2, kst, tid);
         __syncwarp();
         if (lane == 0) mbar_arrive(&sh.empty[b]);
     }
 
     // ---- epilogue
+    if (x >= a.W || y >= a.H) return;
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int y = yA + (q >> 2);
-        if (x >= a.W || y >= a.H) continue;
-        const size_t j = ((size_t)y * a.W + x) * S + (q & 3);
+    for (int q = 0; q < NQ; q++) {
+        const size_t j = ((size_t)y * a.W + x) * S + q;
         f3 f = {0.0f, 0.0f, 0.0f}, o = {0.0f, 0.0f, 0.0f};
         if (qv[q]) {
             if (failed) {
@@ -540,11 +498,25 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
 
 sty_status launch_screen_s4(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st) {
     const int CW = TW + 2 * a.R;
-    const size_t smem = (size_t)NB * NF * CH * CW * S * sizeof(float) + (size_t)8 * NC * 2 * sizeof(float4);
-    STY_TRY(check_cuda(cudaFuncSetAttribute(k_pf_screen4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+    auto smem_for = [&](int nb) {
+        return (size_t)nb * NF * CH * CW * S * sizeof(float) + (size_t)NQ * NC * 2 * sizeof(float4);
+    };
+    int dev = 0, optin = 0;
+    STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    STY_TRY(check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                       "cudaDeviceGetAttribute(max shared memory)"));
+    const size_t room = (size_t)optin - sizeof(Smem);
+    const bool deep = smem_for(4) <= room;
+    const size_t smem = smem_for(deep ? 4 : 3);
+    if (smem > room) {
+        set_error("k_pf_screen4: radius %d needs %zu bytes of shared memory (%zu available)", a.R, smem, room);
+        return STY_ERR_ARG;
+    }
+    auto kern = deep ? k_pf_screen4<4> : k_pf_screen4<3>;
+    STY_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "cudaFuncSetAttribute(k_pf_screen4)"));
     dim3 grid((a.W + TW - 1) / TW, (a.H + TH - 1) / TH);
-    k_pf_screen4<<<grid, NTH, smem, st>>>(a, style);
+    kern<<<grid, NTH, smem, st>>>(a, style);
     return check_launch("k_pf_screen4");
 }
 
