@@ -5,7 +5,8 @@
 //     (the 4 spp), so every branch on the candidate row is warp-uniform. Three consumer warps per
 //     scheduler hide the latency of the dependent exponent chains and the MUFU round trips.
 //   * producer warps: stream the (32+2R) x (12+2R) candidate halo, CH rows at a time, into a
-//     double-buffered shared-memory ring guarded by mbarriers (full / empty per buffer). While
+//     shared-memory ring of 3 to 6 buffers (the deepest that fits) guarded by mbarriers (full /
+//     empty per buffer). While
 //     staging they transform each candidate once (recentred scaled position, normal, incoming
 //     radiance in_d = rad + thr * out_{d+1} with the propagate fused in, weight factors).
 // Packed FP32: a candidate pixel's 4 samples arrive as one 16-byte shared load per field; the
@@ -38,9 +39,20 @@ namespace sty {
 namespace {
 
 constexpr int S = 4;
-constexpr int TW = 32;
-constexpr int NCW = 12;  // consumer warps = pixel rows of the tile
-constexpr int TH = NCW;
+#ifndef STY_PF4_TW
+#define STY_PF4_TW 32
+#endif
+#ifndef STY_PF4_CH
+#define STY_PF4_CH 2
+#endif
+constexpr int NCW = 12;  // consumer warps
+constexpr int TW = STY_PF4_TW;  // tile width: TW / 32 consumer warps share a pixel row
+constexpr int WPR = TW / 32;
+constexpr int TH = NCW / WPR;   // tile height
+// Positions are recentred on the tile's mean before the exponent; wider tiles put the queries
+// further from it and lose FP32 digits of |p'_q - p'_c| on spread-out tiles (measured: 128-pixel
+// tiles miss 1e-5 on such data, 32 and 64 keep it).
+static_assert(TW % 32 == 0 && TW <= 64 && NCW % WPR == 0, "tile shape");
 #ifndef STY_PF4_NPW
 #define STY_PF4_NPW 4
 #endif
@@ -51,8 +63,8 @@ constexpr int NPW = STY_PF4_NPW;  // producer warps (16 warps: 128 registers a t
 constexpr int NC = NCW * 32;
 constexpr int NP = NPW * 32;
 constexpr int NTH = NC + NP;
-constexpr int CH = 4;   // candidate rows per buffer
-constexpr int kMaxNB = 4;  // ring depth: 4 buffers when they fit in shared memory (R <= 19), else 3
+constexpr int CH = STY_PF4_CH;  // candidate rows per buffer
+constexpr int kMaxNB = 6;  // ring depth: the deepest of 6 .. 3 buffers that fits in shared memory
 constexpr int PU = STY_PF4_PU;  // records staged per producer thread per batch (loads in flight)
 constexpr int NF = 10;  // staged fields: p'(3) n(3) m, v(3)   [direct form: m = 1/0, v = in]
 constexpr int NQ = S;   // query records per consumer thread
@@ -261,8 +273,8 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
     }
 
     // ---- queries (consumers) and the tile centre
-    const int lx = lane;
-    const int x = tx0 + lx, y = ty0 + warp;
+    const int lx = lane + 32 * (warp % WPR);
+    const int x = tx0 + lx, y = ty0 + warp / WPR;
     float qp[NQ][3], qn[NQ][3];
     bool qv[NQ];
     float sx = 0.f, sy = 0.f, sz = 0.f, cnt = 0.f;
@@ -506,13 +518,14 @@ sty_status launch_screen_s4(const ScreenArgs &a, const sty_style_program &style,
     STY_TRY(check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
                        "cudaDeviceGetAttribute(max shared memory)"));
     const size_t room = (size_t)optin - sizeof(Smem);
-    const bool deep = smem_for(4) <= room;
-    const size_t smem = smem_for(deep ? 4 : 3);
+    int nb = kMaxNB;
+    while (nb > 3 && smem_for(nb) > room) nb--;
+    const size_t smem = smem_for(nb);
     if (smem > room) {
         set_error("k_pf_screen4: radius %d needs %zu bytes of shared memory (%zu available)", a.R, smem, room);
         return STY_ERR_ARG;
     }
-    auto kern = deep ? k_pf_screen4<4> : k_pf_screen4<3>;
+    auto kern = nb == 6 ? k_pf_screen4<6> : nb == 5 ? k_pf_screen4<5> : nb == 4 ? k_pf_screen4<4> : k_pf_screen4<3>;
     STY_TRY(check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "cudaFuncSetAttribute(k_pf_screen4)"));
     dim3 grid((a.W + TW - 1) / TW, (a.H + TH - 1) / TH);
