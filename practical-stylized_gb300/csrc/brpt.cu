@@ -123,6 +123,7 @@ __global__ void k_br_camera(SceneView sc, CamArgs cam, uint32_t n, uint64_t q0, 
 }
 
 // branch count of each slot of one depth (kernel_advance :598-620)
+template <bool PRINC>
 __global__ void k_br_count(SceneView sc, uint32_t n, uint32_t base, uint32_t depth, uint32_t max_depth, BrInner inner,
                            BrSlots s) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,14 +135,17 @@ __global__ void k_br_count(SceneView sc, uint32_t n, uint32_t base, uint32_t dep
         const sty_scene_material m = sc.materials[sc.tri_material[prim]];
         const uint32_t ab = s.ab[g];
         const F3 ng = get3(s.ng, g), wo = get3(s.wo, g);
-        c = lobe_roughness(m, sc.ggx_tab, ng, wo) > 0.01f ? (ab < inner.n ? inner.v[ab] : 1u) : 1u;
+        c = lobe_roughness<PRINC>(m, sc.ggx_tab, ng, wo) > 0.01f ? (ab < inner.n ? inner.v[ab] : 1u) : 1u;
     }
     s.nchild[g] = c;
 }
 
 // one thread per branch of the parents of one depth: NEE + BSDF sample + continuation ray -> the
 // child slot (kernel_advance :622-712)
-__global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint32_t n_par, uint32_t cbase0,
+// 3 blocks of 256 per SM (80 registers): the BVH walk is latency-bound, and the compiler would
+// otherwise take 95 registers for the closure-free variant and drop to 2 blocks
+template <bool PRINC>
+__global__ void __launch_bounds__(256, 3) k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint32_t n_par, uint32_t cbase0,
                             uint32_t depth, const sty_style_program *progs, uint32_t n_progs, BrSlots s,
                             unsigned long long *hits) {
     const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,7 +161,7 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
     const F3 p = get3(s.p, pg), ng = get3(s.ng, pg), wo = get3(s.wo, pg);
     const sty_scene_material m = sc.materials[sc.tri_material[prim]];
     const uint32_t new_flags = update_flags(m, s.flags[pg]);
-    const uint32_t ab = s.ab[pg] + (lobe_roughness(m, sc.ggx_tab, ng, wo) > 0.01f ? 1u : 0u);
+    const uint32_t ab = s.ab[pg] + (lobe_roughness<PRINC>(m, sc.ggx_tab, ng, wo) > 0.01f ? 1u : 0u);
     const uint64_t key = child_key(s.key[pg], sidx);
     sty_pcg32 st = key_stream(key);
     // NEE (sample_light :727-783, shaded with balance MIS in sample_surface_and_shade_direct :170-197)
@@ -168,7 +172,7 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
         float lpdf;
         if (nee_sample(sc, p, ng, prim, new_flags, depth, progs, n_progs, st, &lwi, &li, &lpdf)) {
             F3 f;
-            const float bp = bsdf_eval(m, ng, ng, wo, lwi, &f, sc.ggx_tab);
+            const float bp = bsdf_eval<PRINC>(m, ng, ng, wo, lwi, &f, sc.ggx_tab);
             const float w = lpdf / (lpdf + bp) / lpdf;
             direct = f3m(li.x * f.x, li.y * f.y, li.z * f.z) * w;
         }
@@ -183,10 +187,10 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
     put3(s.thr, cg, f3m(0.0f, 0.0f, 0.0f));
     const float usel = next_1d(st), u0 = next_1d(st), u1 = next_1d(st);
     float pdf = 0.0f;
-    const F3 wi = bsdf_sample(m, ng, ng, wo, usel, u0, u1, &pdf, sc.ggx_tab);
+    const F3 wi = bsdf_sample<PRINC>(m, ng, ng, wo, usel, u0, u1, &pdf, sc.ggx_tab);
     if (!(pdf > 0.0f)) return;
     F3 f;
-    bsdf_eval(m, ng, ng, wo, wi, &f, sc.ggx_tab);
+    bsdf_eval<PRINC>(m, ng, ng, wo, wi, &f, sc.ggx_tab);
     const F3 ro = offset_ray_origin(p, face_forward(ng, wi));
     const float o3[3] = {ro.x, ro.y, ro.z}, d3[3] = {wi.x, wi.y, wi.z};
     const Hit h = trace_closest(sc, o3, d3, 0.0f, 1e20f, prim);
@@ -207,7 +211,7 @@ __global__ void k_br_branch(SceneView sc, uint32_t n_child, uint32_t pbase, uint
 }
 
 // bottom-up radiance of one depth (kernel_propagate); depth 0 leaves the pixel samples in `rad`
-__global__ void k_br_propagate(SceneView sc, uint32_t n, uint32_t base, uint32_t cbase0, uint32_t depth,
+__global__ void __launch_bounds__(256, 5) k_br_propagate(SceneView sc, uint32_t n, uint32_t base, uint32_t cbase0, uint32_t depth,
                                const sty_style_program *progs, uint32_t n_progs, BrSlots s) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -366,7 +370,8 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
                 STY_TRY(check_launch("k_br_camera"));
                 for (uint32_t d = 0; d <= cfg->max_depth; d++) {
                     const uint32_t n = cnt[d], base = off[d];
-                    k_br_count<<<(n + 255) / 256, 256, 0, st>>>(sv, n, base, d, cfg->max_depth, inner, sl);
+                    (sv.any_closure ? k_br_count<true> : k_br_count<false>)<<<(n + 255) / 256, 256, 0, st>>>(
+                        sv, n, base, d, cfg->max_depth, inner, sl);
                     STY_TRY(check_launch("k_br_count"));
                     size_t tb = scan_bytes;
                     STY_TRY(check_cuda(cub::DeviceScan::ExclusiveSum(dscan, tb, sl.nchild + base, sl.cbase + base,
@@ -390,7 +395,7 @@ sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *cfg, const s
                     }
                     off.push_back(base + n);
                     cnt.push_back((uint32_t)next);
-                    k_br_branch<<<(unsigned)((next + 255) / 256), 256, 0, st>>>(sv, (uint32_t)next, base, n, base + n,
+                    (sv.any_closure ? k_br_branch<true> : k_br_branch<false>)<<<(unsigned)((next + 255) / 256), 256, 0, st>>>(sv, (uint32_t)next, base, n, base + n,
                                                                                 d, dprog, n_programs, sl, dhits);
                     STY_TRY(check_launch("k_br_branch"));
                 }

@@ -41,6 +41,8 @@ SceneView scene_view(const sty_scene *s) {
     v.n_lights = s->n_lights;
     v.tri_pos = s->tri_pos;
     v.ggx_tab = principled_table();
+    v.any_closure = 0;
+    for (const sty_scene_material &m : s->materials_h) v.any_closure |= bsdf::closure_kind(m.kind) ? 1u : 0u;
     return v;
 }
 }  // namespace sty

@@ -32,6 +32,7 @@ struct SceneView {
     uint32_t n_lights;
     const float *tri_pos;           // by original id, 9 per triangle
     const float *ggx_tab;           // the principled BSDF's albedo table (bsdf.cuh)
+    uint32_t any_closure;           // some material is STY_MAT_PRINCIPLED / STY_MAT_GLASS
 };
 
 struct Hit {

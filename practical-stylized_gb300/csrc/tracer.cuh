@@ -122,10 +122,15 @@ __device__ __forceinline__ float princ_eval(const sty_scene_material &m, const f
     *f = f3m(fv[0], fv[1], fv[2]);
     return p;
 }
-__device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, const float *tab) {
-    if (bsdf::closure_kind(m.kind)) {
-        F3 f;
-        return princ_eval(m, tab, ns, ng, wo, wi, &f);
+// PRINC = false: a kernel variant for scenes without closure materials (SceneView::any_closure),
+// which then carries none of the closure's code, registers or stack.
+template <bool PRINC = true>
+__device__ __forceinline__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, const float *tab) {
+    if constexpr (PRINC) {
+        if (bsdf::closure_kind(m.kind)) {
+            F3 f;
+            return princ_eval(m, tab, ns, ng, wo, wi, &f);
+        }
     }
     if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
     const float co = dot(wo, ns), ci = dot(wi, ns);
@@ -141,13 +146,16 @@ __device__ float bsdf_pdf(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 w
     return d * g1 * owh / fabsf(co) / (4.0f * owh);
 }
 // Surface::sample: wi (world) and its pdf (0 = invalid)
-__device__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, float u_sel, float u0, float u1,
+template <bool PRINC = true>
+__device__ __forceinline__ F3 bsdf_sample(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, float u_sel, float u0, float u1,
                           float *pdf, const float *tab) {
-    if (bsdf::closure_kind(m.kind)) {
-        bsdf::B3 w = bsdf::b3(0.0f, 0.0f, 0.0f);
-        float fv[3];
-        bsdf::sample_world(bsdf::make_closure(m), tab, tob(ns), tob(ng), tob(wo), u_sel, u0, u1, &w, fv, pdf);
-        return f3m(w.x, w.y, w.z);
+    if constexpr (PRINC) {
+        if (bsdf::closure_kind(m.kind)) {
+            bsdf::B3 w = bsdf::b3(0.0f, 0.0f, 0.0f);
+            float fv[3];
+            bsdf::sample_world(bsdf::make_closure(m), tab, tob(ns), tob(ng), tob(wo), u_sel, u0, u1, &w, fv, pdf);
+            return f3m(w.x, w.y, w.z);
+        }
     }
     const Frame fr = frame_from_n(ns);
     const F3 wol = to_local(fr, wo);
@@ -245,8 +253,12 @@ __device__ bool nee_sample(const SceneView &sc, F3 p, F3 ng, uint32_t prim, uint
 }
 // Surface::avg_roughness: diffuse 1, the GGX lobe its alpha (as the NL-PF paths have used it), the
 // principled closure the frac-weighted mean of its lobes' (which depends on wo)
+template <bool PRINC = true>
 __device__ __forceinline__ float lobe_roughness(const sty_scene_material &m, const float *tab, F3 ns, F3 wo) {
-    if (bsdf::closure_kind(m.kind)) return bsdf::avg_roughness_world(bsdf::make_closure(m), tab, tob(ns), tob(wo));
+    if constexpr (PRINC) {
+        if (bsdf::closure_kind(m.kind))
+            return bsdf::avg_roughness_world(bsdf::make_closure(m), tab, tob(ns), tob(wo));
+    }
     return m.kind == STY_MAT_DIFFUSE ? 1.0f : m.alpha;
 }
 
@@ -272,8 +284,11 @@ __global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
 
 // f * |cos| (rgb) and pdf of a scene material (Surface::evaluate; diffuse.rs:17-48,
 // svm/surface/mod.rs:1877-1910 with unit Fresnel)
-__device__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f, const float *tab) {
-    if (bsdf::closure_kind(m.kind)) return princ_eval(m, tab, ns, ng, wo, wi, f);
+template <bool PRINC = true>
+__device__ __forceinline__ float bsdf_eval(const sty_scene_material &m, F3 ns, F3 ng, F3 wo, F3 wi, F3 *f, const float *tab) {
+    if constexpr (PRINC) {
+        if (bsdf::closure_kind(m.kind)) return princ_eval(m, tab, ns, ng, wo, wi, f);
+    }
     *f = f3m(0.0f, 0.0f, 0.0f);
     if (!wo_wi_valid(ns, ng, wo, wi)) return 0.0f;
     const float co = dot(wo, ns), ci = dot(wi, ns);
