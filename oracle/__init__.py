@@ -29,6 +29,7 @@ def lib() -> C.CDLL:
         L.orc_set_num_threads.argtypes = [C.c_int32]
         L.orc_style_apply_f64.argtypes = [vp, C.c_uint32, vp, vp, C.c_uint64]
         L.orc_style_apply_at_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, C.c_uint64]
+        L.orc_pf_screen_filter_records_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, C.c_uint64, vp, vp]
         L.orc_pf_screen_filter_depth_f64.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp]
         L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
         L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
@@ -83,6 +84,18 @@ def pf_screen_filter_depth(rec, depth, params, style, out_next=None, want_filter
     lib().orc_pf_screen_filter_depth_f64(C.addressof(rec), depth, C.addressof(params),
                                          C.addressof(style) if style is not None else None,
                                          _p(nxt), _p(out), _p(filt))
+    return out, filt
+
+
+def pf_screen_filter_records(rec, depth, params, style, idx, out_next=None):
+    """The FP64 filter at the given record indices of one depth only; returns (out, filtered) [3, len(idx)]."""
+    idx = np.ascontiguousarray(idx, dtype=np.uint64)
+    out = np.zeros((3, idx.size), dtype=np.float64)
+    filt = np.zeros((3, idx.size), dtype=np.float64)
+    nxt = None if out_next is None else np.ascontiguousarray(out_next, dtype=np.float64)
+    lib().orc_pf_screen_filter_records_f64(C.addressof(rec), depth, C.addressof(params),
+                                           C.addressof(style) if style is not None else None,
+                                           _p(nxt), _p(idx), idx.size, _p(out), _p(filt))
     return out, filt
 
 

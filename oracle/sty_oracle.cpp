@@ -371,6 +371,61 @@ void orc_pf_screen_filter_depth_f64(const sty_pf_records *r, uint32_t depth,
     }
 }
 
+// The FP64 filter above at the listed records only (idx: record indices within the depth), for
+// checks at full image sizes: out / filtered are [3][n_idx].
+void orc_pf_screen_filter_records_f64(const sty_pf_records *r, uint32_t depth, const sty_pf_screen_params *prm,
+                                      const sty_style_program *style, const double *out_next, const uint64_t *idx,
+                                      uint64_t n_idx, double *out, double *filtered) {
+    const int W = r->width, H = r->height, S = r->spp, R = prm->radius;
+    const size_t N = (size_t)W * H * S;
+    const size_t dbase = (size_t)depth * N;
+    const double inv2s2 = prm->sigma_pixel > 0 ? 1.0 / (2.0 * (double)prm->sigma_pixel * prm->sigma_pixel) : 0.0;
+    const double inv2p2 = 1.0 / (2.0 * (double)prm->sigma_pos * prm->sigma_pos);
+    const double invn2 = 1.0 / ((double)prm->sigma_nrm * prm->sigma_nrm);
+    auto in_of = [&](size_t j, int c) {
+        double v = r->rad[c][dbase + j];
+        if (out_next) v += (double)r->thr[c][dbase + j] * out_next[c * N + j];
+        return v;
+    };
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t k = 0; k < (int64_t)n_idx; k++) {
+        const size_t qi = idx[k];
+        const size_t gq = dbase + qi;
+        const int x = (int)((qi / S) % W), y = (int)(qi / S / W);
+        double o3[3] = {0, 0, 0}, f3v[3] = {0, 0, 0};
+        if (qi < N && r->valid[gq]) {
+            const double px = r->pos[0][gq], py = r->pos[1][gq], pz = r->pos[2][gq];
+            const double nx = r->nrm[0][gq], ny = r->nrm[1][gq], nz = r->nrm[2][gq];
+            double sw = 0, sr = 0, sg = 0, sb = 0;
+            for (int yy = std::max(0, y - R); yy <= std::min(H - 1, y + R); yy++)
+                for (int xx = std::max(0, x - R); xx <= std::min(W - 1, x + R); xx++) {
+                    const double dd2 = (double)(xx - x) * (xx - x) + (double)(yy - y) * (yy - y);
+                    for (int t = 0; t < S; t++) {
+                        const size_t j = ((size_t)yy * W + xx) * S + t;
+                        const size_t gj = dbase + j;
+                        if (!r->valid[gj]) continue;
+                        const double dx = px - r->pos[0][gj], dy = py - r->pos[1][gj], dz = pz - r->pos[2][gj];
+                        const double nd = nx * r->nrm[0][gj] + ny * r->nrm[1][gj] + nz * r->nrm[2][gj];
+                        const double w = std::exp(-dd2 * inv2s2 - (dx * dx + dy * dy + dz * dz) * inv2p2 -
+                                                  (1.0 - nd) * invn2);
+                        sw += w;
+                        sr += w * in_of(j, 0);
+                        sg += w * in_of(j, 1);
+                        sb += w * in_of(j, 2);
+                    }
+                }
+            const V3<double> f = {sr / sw, sg / sw, sb / sw};
+            const V3<double> o = style_apply<double>(style, depth, f);
+            f3v[0] = f.x, f3v[1] = f.y, f3v[2] = f.z;
+            o3[0] = o.x, o3[1] = o.y, o3[2] = o.z;
+        }
+        for (int c = 0; c < 3; c++) {
+            out[c * n_idx + k] = o3[c];
+            if (filtered) filtered[c * n_idx + k] = f3v[c];
+        }
+    }
+}
+
 // FP32 restatement (CPU baseline). Per candidate pixel row the partial sums are plain FP32 and
 // are folded into Kahan-compensated totals (CompensatedSum, crates/akari_render/src/util/mod.rs:
 // 337-356).

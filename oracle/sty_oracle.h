@@ -40,6 +40,9 @@ void orc_pf_screen_filter_depth_f64(const sty_pf_records *rec, uint32_t depth,
                                     double *out, double *filtered);
 /* Same on float planes, FP32 arithmetic with compensated sums (CPU baseline). Processes only
  * query rows [y0, y1) so a bounded sample can be timed. */
+void orc_pf_screen_filter_records_f64(const sty_pf_records *rec, uint32_t depth, const sty_pf_screen_params *params,
+                                      const sty_style_program *style, const double *out_next, const uint64_t *idx,
+                                      uint64_t n_idx, double *out, double *filtered);
 void orc_pf_screen_filter_depth_f32(const sty_pf_records *rec, uint32_t depth,
                                     const sty_pf_screen_params *params,
                                     const sty_style_program *style, const float *out_next,

@@ -158,3 +158,63 @@ def test_film_accumulate_fp64(sty, cuda):
     torch.cuda.synchronize()
     ref = 1.5 * out0.astype(np.float64).reshape(3, W * H, S).mean(2).T.reshape(-1)
     assert np.allclose(film.cpu().numpy(), ref, rtol=1e-15, atol=1e-15)
+
+
+def test_c2_full_size_sampled_parity(sty, orc, cuda):
+    """The benchmark workload at its full size (1920x1080 x 4 spp x 5 depths, radius 16, toon at
+    depth 1), all depths in one call: 1500 sampled records per depth against the FP64 oracle run on
+    the GPU's own deeper-depth output."""
+    import torch
+    W, H, S, D = 1920, 1080, 4, 5
+    planes, valid = sty.synth.records(W, H, S, D, seed=0)
+    rs = sty.RecordSet.from_numpy(planes, valid, W, H, S, D)
+    hrec = sty.pf.host_records(planes, valid, W, H, S, D)
+    prm, style = sty.c2_params(), sty.c2_style()
+    out_all = sty.pf_screen_filter(rs, prm, style)
+    torch.cuda.synchronize()
+    n = rs.n_per_depth
+    rng = np.random.default_rng(7)
+    thresholds = np.array([0.1, 0.3, 0.6], dtype=np.float32).astype(np.float64)
+    for d in range(D - 1, -1, -1):
+        idx = np.sort(rng.choice(n, size=1500, replace=False))
+        nxt = out_all[d + 1].cpu().numpy().astype(np.float64) if d + 1 < D else None
+        ref_o, ref_f = orc.pf_screen_filter_records(hrec, d, prm.c(), style, idx, out_next=nxt)
+        got = out_all[d][:, torch.from_numpy(idx.astype(np.int64)).cuda()].cpu().numpy()
+        m = valid[d * n + idx].astype(bool)
+        assert (got[:, ~m] == 0).all()
+        near = np.zeros(idx.size, dtype=bool)
+        if d == 1:
+            lum = ref_f[0] * 0.2126 + ref_f[1] * 0.7152 + ref_f[2] * 0.0722
+            for t in thresholds:
+                near |= np.abs(lum - t) <= 1e-5 * t
+        keep = m & ~near
+        assert keep.sum() > 1200
+        err = rel_err(got[:, keep], ref_o[:, keep], 1e-6).max()
+        assert err < TOL, f"depth {d}: rel err {err:.3e}"
+
+
+def test_full_size_constant_and_linear(sty, cuda):
+    """Size-independent properties over every record of a full 1920x1080 x 4 spp depth: constant
+    incoming radiance comes back unchanged, and the unstyled filter is linear in the radiance."""
+    import torch
+    W, H, S, D = 1920, 1080, 4, 1
+    planes, valid = sty.synth.records(W, H, S, D, seed=4)
+    prm = sty.c2_params()
+    m = torch.from_numpy(valid.astype(bool)).cuda()
+
+    def run(rad):
+        p = planes.copy()
+        p[6:9] = rad
+        rs = sty.RecordSet.from_numpy(p, valid, W, H, S, D)
+        o = sty.pf_screen_filter(rs, prm, None)[0]
+        torch.cuda.synchronize()
+        return o
+
+    c = run(np.float32(0.37))
+    assert (torch.abs(c[:, m] - 0.37) <= 2e-6 * 0.37).all()
+    assert (c[:, ~m] == 0).all()
+    a, b = planes[6:9].copy(), np.random.default_rng(5).random(planes[6:9].shape).astype(np.float32)
+    fa, fb, fab = run(a), run(b), run(a + 2.0 * b)
+    lin = fa + 2.0 * fb
+    err = (torch.abs(fab - lin) / torch.clamp(torch.abs(lin), min=1e-6))[:, m].max().item()
+    assert err < 1e-5, err

@@ -173,3 +173,22 @@ def test_synthetic_records_distribution(sty):
     p2, v2 = sty.synth.records(64, 48, 4, 2, seed=0)
     assert (p2 == planes).all() and (v2 == valid).all()
     assert n == 64 * 48 * 4 * 2
+
+
+def test_screen_filter_records_matches_full_depth(orc, sty):
+    """The sampled-record restatement (for checks at full image sizes) gives exactly the full-depth
+    filter's values at the requested records, styled and with a child depth."""
+    W, H, S, D = 21, 13, 4, 2
+    planes, valid, rec = _tiny(sty, W, H, S, D, seed=17)
+    prm = sty.ScreenParams(radius=5, sigma_pixel=3.0, sigma_pos=0.5, sigma_nrm=0.2)
+    style = sty.c2_style()
+    out1, f1 = orc.pf_screen_filter_depth(rec, 1, prm.c(), style, want_filtered=True)
+    out0, f0 = orc.pf_screen_filter_depth(rec, 0, prm.c(), style, out_next=out1, want_filtered=True)
+    rng = np.random.default_rng(3)
+    idx = rng.choice(W * H * S, size=150, replace=False)
+    o1, g1 = orc.pf_screen_filter_records(rec, 1, prm.c(), style, idx)
+    o0, g0 = orc.pf_screen_filter_records(rec, 0, prm.c(), style, idx, out_next=out1)
+    np.testing.assert_array_equal(o1, out1[:, idx])
+    np.testing.assert_array_equal(g1, f1[:, idx])
+    np.testing.assert_array_equal(o0, out0[:, idx])
+    np.testing.assert_array_equal(g0, f0[:, idx])
