@@ -49,6 +49,8 @@ def lib() -> C.CDLL:
         L.orc_principled_sample.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp]
         L.orc_pf_ref_filter.restype = C.c_int32
         L.orc_pf_ref_filter.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp]
+        L.orc_pf_ref_filter_select.restype = C.c_int32
+        L.orc_pf_ref_filter_select.argtypes = [vp, vp, vp, vp, C.c_uint32, vp, C.c_uint32, vp, vp, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -128,9 +130,11 @@ def hash_cells(points: np.ndarray, pmin, pmax, res, table_size: int):
     return cells, idx
 
 
-def pf_ref_filter(arrays: dict, params_c, mats, progs, n_progs: int, rng_states: np.ndarray, in_next=None):
+def pf_ref_filter(arrays: dict, params_c, mats, progs, n_progs: int, rng_states: np.ndarray, in_next=None,
+                  select=None):
     """Reference-mode filter of one depth on host arrays (dict from synth.ref_vertices).
-    Returns (status, out [3, n] float64, neighbours [n], cluster_id [n], rng_states_after)."""
+    Returns (status, out [3, n] float64, neighbours [n], cluster_id [n], rng_states_after).
+    select (bool [n], optional): filter only those vertices (the rest stay 0 / untouched)."""
     import importlib
     pfr = importlib.import_module(__package_name__() + ".pf_ref")
     n = int(arrays["active"].shape[0])
@@ -140,9 +144,10 @@ def pf_ref_filter(arrays: dict, params_c, mats, progs, n_progs: int, rng_states:
     cid = np.zeros(n, dtype=np.uint32)
     st = np.ascontiguousarray(rng_states.copy())
     nxt = None if in_next is None else np.ascontiguousarray(in_next, dtype=np.float32)
-    status = lib().orc_pf_ref_filter(C.addressof(v), _p(nxt), C.addressof(params_c), C.addressof(mats), len(mats),
-                                     C.addressof(progs) if progs is not None else None, n_progs, _p(st), _p(out),
-                                     _p(nb), _p(cid))
+    sel = None if select is None else np.ascontiguousarray(select, dtype=np.uint8)
+    status = lib().orc_pf_ref_filter_select(C.addressof(v), _p(nxt), C.addressof(params_c), C.addressof(mats),
+                                            len(mats), C.addressof(progs) if progs is not None else None, n_progs,
+                                            _p(st), _p(out), _p(nb), _p(cid), _p(sel))
     return status, out, nb, cid, st
 
 

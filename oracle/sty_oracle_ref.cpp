@@ -155,10 +155,13 @@ inline uint32_t style_index(uint32_t flags) {  // StylizationFlagsExpr::get_styl
 
 extern "C" {
 
-int32_t orc_pf_ref_filter(const sty_pf_vertices *v, const float *in_next,
-                          const sty_pf_ref_params *prm, const sty_pf_material *mats, uint32_t n_mats,
-                          const sty_style_program *progs, uint32_t n_progs, sty_pcg32 *rng, double *out,
-                          uint32_t *neighbours, uint32_t *cluster_id) {
+// select (nullable): filter only the active vertices with select[i] != 0 (the grid and clusters are
+// still built from every active vertex); the others keep out = 0 and their RNG state. For checks at
+// full vertex counts.
+int32_t orc_pf_ref_filter_select(const sty_pf_vertices *v, const float *in_next,
+                                 const sty_pf_ref_params *prm, const sty_pf_material *mats, uint32_t n_mats,
+                                 const sty_style_program *progs, uint32_t n_progs, sty_pcg32 *rng, double *out,
+                                 uint32_t *neighbours, uint32_t *cluster_id, const uint8_t *select) {
     const uint64_t n = v->n;
     View V{v};
     Grid g;
@@ -247,6 +250,7 @@ int32_t orc_pf_ref_filter(const sty_pf_vertices *v, const float *in_next,
         if (cluster_id) cluster_id[i] = prm->cluster ? cid[i] : NONE;
     }
     for (uint32_t vi : act) {
+        if (select && !select[vi]) continue;
         float q[3];
         V.pf(prm->cluster ? cid[vi] : vi, q);
         const uint32_t my_cluster = cid[vi];
@@ -315,6 +319,14 @@ int32_t orc_pf_ref_filter(const sty_pf_vertices *v, const float *in_next,
         for (int c = 0; c < 3; c++) out[c * n + vi] = rad[c];
     }
     return STY_OK;
+}
+
+int32_t orc_pf_ref_filter(const sty_pf_vertices *v, const float *in_next,
+                          const sty_pf_ref_params *prm, const sty_pf_material *mats, uint32_t n_mats,
+                          const sty_style_program *progs, uint32_t n_progs, sty_pcg32 *rng, double *out,
+                          uint32_t *neighbours, uint32_t *cluster_id) {
+    return orc_pf_ref_filter_select(v, in_next, prm, mats, n_mats, progs, n_progs, rng, out, neighbours, cluster_id,
+                                    nullptr);
 }
 
 }  // extern "C"

@@ -168,3 +168,41 @@ def test_ref_filter_iteration_cap(sty, cuda):
     with pytest.raises(sty.StyError) as ei:
         _gpu(sty, arr, mats, progs, rng, prm)
     assert ei.value.status == sty.STY_ERR_ITER_LIMIT
+
+
+def test_oracle_select_matches_full(orc, sty):
+    """Filtering a selection of vertices gives exactly the full run's values there (each vertex draws
+    from its own PCG32 stream, the grid is built from every vertex)."""
+    arr, mats, progs, rng = _setup(sty, n=2500, seed=31)
+    prm = sty.pf_ref.RefParams(depth=1, radius=0.1, reuse=16, smis=True)
+    st, out, nb, _, r = orc.pf_ref_filter(arr, prm.c(), mats, progs, 2, rng, in_next=arr["in_next"])
+    sel = np.zeros(2500, bool)
+    sel[np.random.default_rng(1).choice(2500, 300, replace=False)] = True
+    st2, out2, nb2, _, r2 = orc.pf_ref_filter(arr, prm.c(), mats, progs, 2, rng, in_next=arr["in_next"], select=sel)
+    assert st == st2 == 0
+    np.testing.assert_array_equal(out2[:, sel], out[:, sel])
+    np.testing.assert_array_equal(nb2[sel], nb[sel])
+    np.testing.assert_array_equal(r2[sel], r[sel])
+    assert (out2[:, ~sel] == 0).all() and (r2[~sel] == rng[~sel]).all()
+
+
+@pytest.mark.gpu
+def test_ref_filter_full_vertex_count(sty, orc, cuda):
+    """A depth of the end-to-end render's size (256x256 pixels x 16 paths = 1 048 576 vertex slots,
+    radius 0.05, reuse 64, SMIS): 2000 sampled vertices against the oracle -- neighbour counts and
+    reservoir RNG states bit-exact, radiance within 1e-5."""
+    n = 1 << 20
+    arr, mats, progs, rng = _setup(sty, n=n, seed=41)
+    prm = sty.pf_ref.RefParams(depth=1, radius=0.05, reuse=64, smis=True, table_size=(1 << 22) + 15)
+    out, nb, _, r = _gpu(sty, arr, mats, progs, rng, prm)
+    sel = np.zeros(n, bool)
+    sel[np.random.default_rng(2).choice(n, 2000, replace=False)] = True
+    sel &= arr["active"].astype(bool)
+    st, ref_out, ref_nb, _, ref_rng = orc.pf_ref_filter(arr, prm.c(), mats, progs, 2, rng, in_next=arr["in_next"],
+                                                        select=sel)
+    assert st == 0 and sel.sum() > 1500
+    assert (nb[sel] == ref_nb[sel]).all()
+    assert np.median(nb[sel]) > 100  # a dense neighbourhood, as in the render
+    assert (r[sel] == ref_rng[sel]).all()
+    err = rel_err(out[:, sel], ref_out[:, sel], 1e-4)
+    assert err.max() < TOL, f"max rel err {err.max():.3e}"
