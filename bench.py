@@ -401,6 +401,29 @@ def c3_bench(sty, reps: int = 20):
             "grad_finite": bool(torch.isfinite(grad).all().item())}
 
 
+def brpt_bench(sty, W: int = 160, H: int = 90):
+    """One branching path tracer render of the interior workload at the teaser's branching
+    (32, 14, 8, 6), after an untimed warm-up render (the `brpt` entry of c5_bench without the
+    reference image)."""
+    import torch
+    a = sty.abi
+    pos, mids, mats, cam = sty.scene.room_with_door(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    progs = [a.style_program([a.toon(0.2, depth_mask=0b11),
+                              a.ramp_smooth(30.0, [0.02, 0.15, 0.6],
+                                            [(0.08, 0.1, 0.2), (0.55, 0.45, 0.35), (1.3, 1.2, 1.0)],
+                                            depth_mask=0b11)])]
+    sc.brpt_render(sty.scene.brpt_config(max_depth=8, inner_samples=(4, 2), repeats=1, seed=2), progs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, st = sc.brpt_render(sty.scene.brpt_config(max_depth=8, inner_samples=(32, 14, 8, 6), repeats=1, seed=5), progs)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    sc.close()
+    return {"seconds": t, "vertices": int(st.vertices), "mvertices_per_s": st.vertices / t / 1e6,
+            "passes": int(st.passes)}
+
+
 def c5_bench(sty, W: int = 160, H: int = 90):
     """Full stylized render of the interior workload (6 x 3 x 4 m room of ~377 k triangles, door
     open 20 degrees, the only emitter behind it; GGX + diffuse; toon (band 0.2) and a 3-colour
@@ -550,6 +573,12 @@ def run(args):
         return
     if args.c5_only:  # the full stylized render alone
         print(json.dumps({"c5_render": c5_bench(sty)}), flush=True)
+        return
+    if args.c3_only:  # profiling case: the adjoint alone
+        print(json.dumps({"c3_adjoint": c3_bench(sty, reps=max(1, args.steps))}), flush=True)
+        return
+    if args.brpt_only:  # profiling case: one branching path tracer render of the interior workload
+        print(json.dumps({"brpt": brpt_bench(sty)}), flush=True)
         return
 
     D_ = args.depths
@@ -750,6 +779,9 @@ def main():
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
     ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
+    ap.add_argument("--c3-only", action="store_true", help="profiling case: only the adjoint")
+    ap.add_argument("--brpt-only", action="store_true",
+                    help="profiling case: one branching path tracer render of the interior workload")
     ap.add_argument("--grid-only", action="store_true", help="only the reference's NL-NRC network frames")
     ap.add_argument("--grid-frames", type=int, default=32, help="frames of the reference's NL-NRC network")
     args = ap.parse_args()
