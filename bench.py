@@ -21,6 +21,7 @@ import argparse
 import json
 import math
 import os
+import tempfile
 import pathlib
 import statistics
 import subprocess
@@ -64,7 +65,9 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.proc = None
         self.gpu = gpu_index
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{gpu_index}.csv"
+        # the raw samples (the JSON line carries their summary); STY_CLOCKS_DIR keeps them
+        out_dir = os.environ.get("STY_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = pathlib.Path(out_dir) / f"clocks_rank{gpu_index}.csv"
 
     def start(self):
         try:

@@ -49,7 +49,7 @@ typedef int32_t sty_status;
 #define STY_ERR_CUDA 3        /* a CUDA runtime call failed (message in sty_last_error())    */
 #define STY_ERR_ITER_LIMIT 4  /* a bounded device loop hit its iteration cap                 */
 #define STY_ERR_NAN 5         /* a non-finite value was detected where it is not allowed     */
-#define STY_ERR_UNSUPPORTED 6 /* the request is valid but not supported by this build/device */
+#define STY_ERR_UNSUPPORTED 6 /* the request is valid but the library as compiled or the device cannot serve it */
 
 /* Pcg32 generator state (crates/akari_render/src/sampler/mod.rs:82-88). */
 typedef struct sty_pcg32 {
