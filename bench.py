@@ -643,8 +643,10 @@ def run(args):
     # a copy stream; the filter of a depth waits only for its own records, and a depth's slice is
     # overwritten by the next step's upload as soon as this step's filter of that depth is done, so
     # uploads overlap the filters of the other depths (also across steps). The result (depth 0) goes
-    # down on the copy stream; the next step's depth-0 filter waits for that copy.
+    # down on its own stream (on the upload stream it would hold the next step's uploads behind the
+    # end of this step); the next step's depth-0 filter waits for that copy.
     copy_stream = torch.cuda.Stream(dev)
+    down_stream = torch.cuda.Stream(dev)
     ev_filtered = [torch.cuda.Event() for _ in range(D_)]
     ev_copied = [torch.cuda.Event() for _ in range(D_)]
     ev_out_read = torch.cuda.Event()
@@ -667,10 +669,10 @@ def run(args):
             nxt = out[d + 1] if d + 1 < D_ else None
             sty.pf_screen_filter_depth(rs, d, prm, style, out_next=nxt, out=out[d], stream=stream)
             ev_filtered[d].record(stream)
-        with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(ev_filtered[0])
+        with torch.cuda.stream(down_stream):
+            down_stream.wait_event(ev_filtered[0])
             h_out.copy_(out[0], non_blocking=True)
-            ev_out_read.record(copy_stream)
+            ev_out_read.record(down_stream)
         first[0] = False
 
     e2e_ms = float("nan")
