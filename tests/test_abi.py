@@ -102,3 +102,24 @@ def test_style_builders_validate(sty):
         a.palette([(0, 0, 0)] * 20)
     p = a.style_program([a.toon(0.2), a.sat_rex(0.3)])
     assert p.n_nodes == 2 and abs(p.nodes[0].p[0] - 0.2) < 1e-7
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    """Without the CUDA library the package raises on first use: there is no CPU fallback."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, pathlib; sys.path.insert(0, %r)\n"
+        "import __graft_entry__ as g\n"
+        "sty = g.package()\n"
+        "sty.abi.LIB_PATH = pathlib.Path(%r) / 'libsty_gb300.so'\n"
+        "sty.abi._lib = None\n"
+        "try:\n"
+        "    sty.abi.lib()\n"
+        "except RuntimeError as e:\n"
+        "    print('raised:', e)\n"
+        "    sys.exit(0)\n"
+        "sys.exit(3)\n" % (str(ROOT), str(tmp_path)))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "not built" in r.stdout
