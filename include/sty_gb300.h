@@ -145,7 +145,7 @@ typedef struct sty_style_program {
 STY_API sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
                            float *rgb_out, uint64_t n, void *stream);
 /* sty_style_apply with the shaded point of each colour (device, 3 floats per item), which
- * STY_STYLE_HALF_TONE reads; a null `pos` is the point 0 for every item (sty_style_apply). */
+ * STY_STYLE_HALF_TONE reads (si.p in HalfToneSurface::apply_stylization, svm/surface/mod.rs:1180-1232); a null `pos` is the point 0 for every item (sty_style_apply). */
 STY_API sty_status sty_style_apply_at(const sty_style_program *program, uint32_t depth, const float *rgb_in,
                                       const float *pos, float *rgb_out, uint64_t n, void *stream);
 
@@ -476,13 +476,17 @@ typedef struct sty_scene sty_scene;
 
 /* Build a scene from HOST triangle soup: positions (9 floats per triangle: v0, v1, v2), one
  * material index per triangle, the material table and the camera. Builds the BVH on the host and
- * uploads everything. */
+ * uploads everything. Replaces the reference's scene upload and acceleration-structure build
+ * (crates/akari_render/src/load.rs:481-700, LuisaCompute's Accel): the mesh lights are the
+ * triangles of emissive materials (load.rs:95-128). */
 STY_API sty_status sty_scene_create(const float *tri_positions, const uint32_t *tri_material, uint32_t n_tris,
                                     const sty_scene_material *materials, uint32_t n_materials,
                                     const sty_camera *camera, sty_scene **out);
 STY_API sty_status sty_scene_destroy(sty_scene *scene);
 /* Closest hit of n rays (device, 8 floats per ray: origin, direction, tmin, tmax). Outputs
- * (device): prim (UINT32_MAX on a miss), t, bary (2 per ray: weights of v1 and v2). */
+ * (device): prim (UINT32_MAX on a miss), t, bary (2 per ray: weights of v1 and v2). The ray query
+ * the reference's integrators issue through LuisaCompute (`accel.intersect`), exposed for
+ * checking the traversal against a brute-force closest hit. */
 STY_API sty_status sty_scene_closest_hit(sty_scene *scene, const float *rays, uint64_t n, uint32_t *prim, float *t,
                                          float *bary, void *stream);
 
