@@ -49,6 +49,17 @@ __device__ __forceinline__ float ex2_approx(float x) {
     return y;
 }
 
+// Packed FP32: d = a * b + c on both lanes (fma.rn.f32x2; each lane rounds exactly like fmaf),
+// one issue slot for two FMAs.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+
 struct KahanF {
     float s, c;
     __device__ __forceinline__ void add(float v) {

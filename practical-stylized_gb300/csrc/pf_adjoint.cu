@@ -39,6 +39,98 @@ struct AdjArgs {
 
 __device__ __forceinline__ float sigm(float x) { return 1.0f / (1.0f + expf(-x)); }
 
+// One candidate row for 4 spp on packed FP32: the candidate pixel's 4 samples come in as one
+// 16-byte load per field, and queries (0, 1) and (2, 3) share the lanes of `fma.rn.f32x2`.
+// Sweep 0 accumulates (w, w in) into part, sweep 1 the three bandwidth sums into pe (as the scalar
+// loop below, with the log2(e) factor folded into the exponent's scales).
+__device__ __forceinline__ void pair_row4(const float *__restrict__ rowp, const float *__restrict__ rowi, int plane,
+                                          int lx, int R, int dy, float isx2, float isp2, float isn2,
+                                          const float (&qp)[4][3], const float (&qn)[4][3], const float (&h)[4][3],
+                                          const float (&hf)[4], int sweep, float (&part)[4][4], float (&pe)[4][3]) {
+    const float2 zero2 = make_float2(0.0f, 0.0f), one2 = make_float2(1.0f, 1.0f), m1 = make_float2(-1.0f, -1.0f);
+    const float2 nisp2 = make_float2(-isp2 * kL2E, -isp2 * kL2E), nisn2 = make_float2(-isn2 * kL2E, -isn2 * kL2E);
+    float2 qa[2][3], qb[2][3], hh[2][3], nhf[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            qa[p][k] = make_float2(qp[2 * p][k], qp[2 * p + 1][k]);
+            qb[p][k] = make_float2(qn[2 * p][k], qn[2 * p + 1][k]);
+            hh[p][k] = make_float2(h[2 * p][k], h[2 * p + 1][k]);
+        }
+        nhf[p] = make_float2(-hf[2 * p], -hf[2 * p + 1]);
+    }
+    float2 acc[2][4];
+#pragma unroll
+    for (int p = 0; p < 2; p++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[p][k] = zero2;
+#pragma unroll 1
+    for (int dx = -R; dx <= R; dx++) {
+        const float rho = (float)(dx * dx + dy * dy);
+        const float2 arho = make_float2(-rho * isx2 * kL2E, -rho * isx2 * kL2E), rho2 = make_float2(rho, rho);
+        const int cb = (lx + R + dx) * 4;
+        const float4 v[10] = {*reinterpret_cast<const float4 *>(rowp + cb),
+                              *reinterpret_cast<const float4 *>(rowp + plane + cb),
+                              *reinterpret_cast<const float4 *>(rowp + 2 * plane + cb),
+                              *reinterpret_cast<const float4 *>(rowp + 3 * plane + cb),
+                              *reinterpret_cast<const float4 *>(rowp + 4 * plane + cb),
+                              *reinterpret_cast<const float4 *>(rowp + 5 * plane + cb),
+                              *reinterpret_cast<const float4 *>(rowp + 6 * plane + cb),
+                              *reinterpret_cast<const float4 *>(rowi + cb),
+                              *reinterpret_cast<const float4 *>(rowi + plane + cb),
+                              *reinterpret_cast<const float4 *>(rowi + 2 * plane + cb)};
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            float c[10];
+#pragma unroll
+            for (int f = 0; f < 10; f++) c[f] = t == 0 ? v[f].x : t == 1 ? v[f].y : t == 2 ? v[f].z : v[f].w;
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+                const float2 ex = ffma2(make_float2(c[0], c[0]), m1, qa[p][0]);
+                const float2 ey = ffma2(make_float2(c[1], c[1]), m1, qa[p][1]);
+                const float2 ez = ffma2(make_float2(c[2], c[2]), m1, qa[p][2]);
+                float2 d2 = ffma2(ex, ex, zero2);
+                d2 = ffma2(ey, ey, d2);
+                d2 = ffma2(ez, ez, d2);
+                float2 dn = ffma2(qb[p][0], make_float2(c[3], c[3]), zero2);
+                dn = ffma2(qb[p][1], make_float2(c[4], c[4]), dn);
+                dn = ffma2(qb[p][2], make_float2(c[5], c[5]), dn);
+                const float2 om = ffma2(dn, m1, one2);
+                float2 a = ffma2(d2, nisp2, arho);
+                a = ffma2(om, nisn2, a);
+                const float2 w = ffma2(make_float2(ex2_approx(a.x), ex2_approx(a.y)), make_float2(c[6], c[6]), zero2);
+                if (sweep == 0) {
+                    acc[p][0] = ffma2(w, one2, acc[p][0]);
+                    acc[p][1] = ffma2(w, make_float2(c[7], c[7]), acc[p][1]);
+                    acc[p][2] = ffma2(w, make_float2(c[8], c[8]), acc[p][2]);
+                    acc[p][3] = ffma2(w, make_float2(c[9], c[9]), acc[p][3]);
+                } else {
+                    float2 u = ffma2(hh[p][0], make_float2(c[7], c[7]), nhf[p]);
+                    u = ffma2(hh[p][1], make_float2(c[8], c[8]), u);
+                    u = ffma2(hh[p][2], make_float2(c[9], c[9]), u);
+                    const float2 tt = ffma2(w, u, zero2);
+                    acc[p][0] = ffma2(tt, rho2, acc[p][0]);
+                    acc[p][1] = ffma2(tt, d2, acc[p][1]);
+                    acc[p][2] = ffma2(tt, om, acc[p][2]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < 2; p++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            if (sweep == 0) {
+                part[2 * p][k] = acc[p][k].x;
+                part[2 * p + 1][k] = acc[p][k].y;
+            } else if (k < 3) {
+                pe[2 * p][k] = acc[p][k].x;
+                pe[2 * p + 1][k] = acc[p][k].y;
+            }
+        }
+}
+
 template <int S>
 __global__ void __launch_bounds__(NT) k_pf_adjoint(const AdjArgs a) {
     extern __shared__ __align__(16) float sm[];
@@ -123,6 +215,9 @@ __global__ void __launch_bounds__(NT) k_pf_adjoint(const AdjArgs a) {
                     }
                 const float *rowp = sm + r * CW * S;
                 const float *rowi = sin_ + r * CW * S;
+                if constexpr (S == 4) {
+                    pair_row4(rowp, rowi, plane, lx, R, dy, isx2, isp2, isn2, qp, qn, h, hf, sweep, part, pe);
+                } else {
                 for (int dx = -R; dx <= R; dx++) {
                     const float rho = (float)(dx * dx + dy * dy);
                     const int cb = (lx + R + dx) * S;
@@ -153,6 +248,7 @@ __global__ void __launch_bounds__(NT) k_pf_adjoint(const AdjArgs a) {
                             }
                         }
                     }
+                }
                 }
 #pragma unroll
                 for (int q = 0; q < S; q++) {

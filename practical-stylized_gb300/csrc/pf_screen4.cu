@@ -116,17 +116,6 @@ struct Smem {
     int mode;  // 0 = expanded, 1 = direct, 2 = no valid query
 };
 
-// Packed FP32: d = a * b + c on both lanes (fma.rn.f32x2; each lane rounds exactly like fmaf),
-// one issue slot for two FMAs.
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-    float2 d;
-    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
-        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(d.x), "=f"(d.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return d;
-}
-
 // One candidate row, expanded form: for every dx the candidate pixel's 4 samples, taken as the
 // pairs (0, 1) and (2, 3); part2[q][k].x / .y collect samples 0, 2 / 1, 3 of query q (w, w*in).
 __device__ __forceinline__ void row_pass_exp(const float *__restrict__ rowp, int plane, int lx, int R, float pix2,
