@@ -6,11 +6,13 @@ One step = one full NL-PF pass: the 5 depths filtered deepest-first through the 
           second; 41.47 M records, ~90 % valid, per step). Inputs (2.2 GB) exceed the 129 MB L2,
           so no explicit flush is needed between steps.
   e2e   : the same metric through the public API with HOST buffers: every step copies the
-          records from pinned host memory (per depth, deepest first, on a copy stream so that a
-          depth's upload overlaps the filter of the depth below it), runs the pass and reads back
-          the depth-0 result.
-  roofline: the dominant kernel (k_pf_screen) against measured HBM bandwidth, from CUDA events
-          around each launch on the launching stream; `alu_roofline` gives the binding FP32 roof.
+          records from pinned host memory (per depth, deepest first, on a copy stream; a depth's
+          upload waits only for the previous step's filter of that depth, so uploads overlap the
+          filters), runs the pass and reads the depth-0 result back on a third stream; the result
+          is checked equal to the resident pass's.
+  roofline: the dominant kernel (k_pf_screen4) against measured HBM bandwidth, from CUDA events
+          around each launch on the launching stream; `alu_roofline` gives the binding FP32 roof
+          (FMAs per pair by the exponent form the tiles take).
   cpu_baseline: the FP32 CPU restatement (oracle, all host cores) on a bounded band of rows.
 `--impl reference` times the reference's CPU path (the restatement; the reference's own Rust /
 LuisaCompute CPU backend cannot be built on these machines) and prints the same metric.
