@@ -75,6 +75,11 @@ STY_API uint64_t sty_struct_size(const char *name);
  * clear != 0 resets the word to 0 after reading. */
 #define STY_DEV_WAIT_TIMEOUT 1u
 STY_API sty_status sty_device_status(uint32_t *status_out, int32_t clear);
+/* Exercises the bounded-wait failure path without a fault: one block waits on an mbarrier that
+ * nothing completes; after `limit_us` microseconds (1 .. 2 000 000) of %globaltimer the wait gives
+ * up, ORs STY_DEV_WAIT_TIMEOUT into the device status word and the kernel returns, leaving the
+ * context usable. No counterpart in the reference (its kernels have no bounded waits). */
+STY_API sty_status sty_wait_timeout_probe(uint32_t limit_us, void *stream);
 
 /* ----------------------------------------------------------------------------------------
  * Style programs: the nonlinear "svm/surface" style nodes

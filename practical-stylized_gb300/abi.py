@@ -92,6 +92,7 @@ SIGNATURES = {
     "sty_last_error": (C.c_char_p, []),
     "sty_launch_count": (C.c_uint64, []),
     "sty_struct_size": (C.c_uint64, [C.c_char_p]),
+    "sty_wait_timeout_probe": (C.c_int32, [C.c_uint32, _VP]),
     "sty_device_status": (C.c_int32, [C.POINTER(C.c_uint32), C.c_int32]),
     "sty_style_apply": (C.c_int32, [C.POINTER(StyleProgram), C.c_uint32, _VP, _VP, C.c_uint64, _VP]),
     "sty_style_apply_at": (C.c_int32, [C.POINTER(StyleProgram), C.c_uint32, _VP, _VP, _VP, C.c_uint64, _VP]),

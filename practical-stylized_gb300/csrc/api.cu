@@ -77,6 +77,32 @@ uint32_t *device_status_ptr() {
 }
 
 // ---- kernels ------------------------------------------------------------------------------
+// A wait on an mbarrier whose phase nothing completes, bounded by %globaltimer (and by an
+// iteration cap, so the loop ends even if the timer stalled): the timeout path of every bounded
+// wait in the library, in isolation.
+__global__ void k_wait_timeout_probe(unsigned long long limit_ns, uint32_t *status) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(&bar));
+    if (threadIdx.x == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(a) : "memory");
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (uint32_t it = 0; it < (1u << 26); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a)
+            : "memory");
+        if (done) return;
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > limit_ns) break;
+    }
+    atomicOr(status, (uint32_t)STY_DEV_WAIT_TIMEOUT);
+}
+
 __global__ void k_style_apply(sty_style_program prog, uint32_t depth, const float *in, const float *pos, float *out,
                               uint64_t n) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -209,6 +235,18 @@ sty_status sty_device_status(uint32_t *status_out, int32_t clear) {
         STY_TRY(check_cuda(cudaMemcpyToSymbol(g_device_status, &zero, sizeof(uint32_t)), "clear device status"));
     }
     return STY_OK;
+}
+
+sty_status sty_wait_timeout_probe(uint32_t limit_us, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(limit_us >= 1 && limit_us <= 2000000u, "sty_wait_timeout_probe: limit_us must be in [1, 2e6]");
+    uint32_t *st = device_status_ptr();
+    if (!st) {
+        set_error("sty_wait_timeout_probe: device status word unavailable");
+        return STY_ERR_CUDA;
+    }
+    k_wait_timeout_probe<<<1, 32, 0, as_stream(stream)>>>((unsigned long long)limit_us * 1000ull, st);
+    return check_launch("k_wait_timeout_probe");
 }
 
 sty_status sty_style_apply(const sty_style_program *program, uint32_t depth, const float *rgb_in,
