@@ -218,3 +218,20 @@ def test_full_size_constant_and_linear(sty, cuda):
     lin = fa + 2.0 * fb
     err = (torch.abs(fab - lin) / torch.clamp(torch.abs(lin), min=1e-6))[:, m].max().item()
     assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("R", [3, 16, 24])
+def test_expanded_form_matches_oracle(sty, orc, cuda, R):
+    """Small images with the workload's per-tile spread (a gentle offset, as the 1920-px image
+    has): every tile takes the expanded exponent, the form the benchmark runs."""
+    import importlib.util
+    from conftest import ROOT
+    spec = importlib.util.spec_from_file_location("bench_host", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    W, H, S, D = 100, 40, 4, 1
+    planes, valid, rs, hrec = _setup(sty, W, H, S, D, seed=50 + R, offset_scale=0.2)
+    assert bench.expanded_fraction(planes, valid, W, H, S, D, 0.5) == 1.0
+    prm = sty.ScreenParams(radius=R, sigma_pixel=max(R / 2, 1.0), sigma_pos=0.5, sigma_nrm=0.2)
+    _, got_o, ref_o, _, m, ef = _depth_parity(sty, orc, rs, hrec, valid, 0, prm, sty.c2_style())
+    assert ef < TOL, f"filtered rel err {ef:.3e}"
