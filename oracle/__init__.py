@@ -43,7 +43,7 @@ def lib() -> C.CDLL:
         L.orc_closest_hit.argtypes = [vp, C.c_uint32, vp, C.c_uint64, vp, vp, vp]
         L.orc_path_trace.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, C.c_uint64, vp]
         L.orc_brpt.argtypes = [vp, vp, C.c_uint32, vp, vp, vp, C.c_uint32, C.c_uint32, vp, C.c_uint32, C.c_uint32,
-                               C.c_uint64, vp]
+                               C.c_uint32, C.c_uint64, vp]
         L.orc_principled_table.argtypes = [vp]
         L.orc_principled_eval.argtypes = [vp, C.c_uint64, vp, vp, vp, vp]
         L.orc_principled_sample.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, vp]
@@ -208,7 +208,7 @@ def path_trace(tri_pos, mat_ids, albedo, emission, cam, spp: int, max_depth: int
 
 
 def brpt(tri_pos, mat_ids, materials, cam, programs, max_depth: int, inner_samples, repeats: int = 1,
-         seed: int = 0):
+         seed: int = 0, first_repeat: int = 0):
     """Recursive FP64 branching path tracer on the same sampling keys as sty_brpt_render (diffuse
     surfaces) -> image [H, W, 3]. `materials` is a ctypes array of sty_scene_material, `programs` a
     sequence of sty_style_program, cam = (eye3, target3, up3, fov_y, W, H, filter_radius)."""
@@ -223,7 +223,7 @@ def brpt(tri_pos, mat_ids, materials, cam, programs, max_depth: int, inner_sampl
     W, H = int(c[10]), int(c[11])
     img = np.zeros((H, W, 3), dtype=np.float64)
     lib().orc_brpt(_p(pos), _p(m), m.size, C.addressof(materials), _p(c), None if parr is None else C.addressof(parr),
-                   len(progs), max_depth, _p(inner), inner.size, repeats, seed, _p(img))
+                   len(progs), max_depth, _p(inner), inner.size, repeats, first_repeat, seed, _p(img))
     return img
 
 

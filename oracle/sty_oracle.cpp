@@ -1205,7 +1205,7 @@ D3 br_radiance(const BrScene &s, uint32_t depth, const double *p, uint32_t prim,
 extern "C" void orc_brpt(const float *pos, const uint32_t *mat, uint32_t n_tris, const sty_scene_material *mats,
                          const float *cam /* eye3 target3 up3 fov W H radius */, const sty_style_program *progs,
                          uint32_t n_progs, uint32_t max_depth, const uint32_t *inner, uint32_t n_levels,
-                         uint32_t repeats, uint64_t seed, double *img) {
+                         uint32_t repeats, uint32_t first_repeat, uint64_t seed, double *img) {
     BrScene s;
     s.pt.pos = pos;
     s.pt.mat = mat;
@@ -1261,7 +1261,7 @@ extern "C" void orc_brpt(const float *pos, const uint32_t *mat, uint32_t n_tris,
     const double th = std::tan(cam[9] * 0.5 * M_PI / 180.0), asp = (double)W / H, rad = cam[12];
     std::fill(img, img + 3 * (size_t)W * H, 0.0);
     for (uint32_t rep = 0; rep < repeats; rep++) {
-        const uint64_t rkey = smix64(smix64(seed ^ 0x4252505400000000ull) + rep);
+        const uint64_t rkey = smix64(smix64(seed ^ 0x4252505400000000ull) + (uint64_t)first_repeat + rep);
 #pragma omp parallel for schedule(dynamic, 1)
         for (int py = 0; py < (int)H; py++)
             for (uint32_t px = 0; px < W; px++) {

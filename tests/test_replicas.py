@@ -95,3 +95,19 @@ def test_brpt_replicas_merge_to_the_single_render(sty, cuda):
     # a replica is not a re-run of the first repeats
     assert not np.allclose(parts[1][0].cpu().numpy(), sc.brpt_render(cfg(0, 2), progs)[0].cpu().numpy())
     sc.close()
+
+
+def test_oracle_brpt_replicas_merge(sty):
+    """The oracle's branching path tracer keys on the same (seed, repeat) as the GPU: two replica
+    runs of repeats 0-1 and 2 merge (repeat-weighted) to the single run of repeats 0-2."""
+    import oracle
+    pos, mids, mats, cam = sty.scene.cornell_box(8, 6, style=(0, -1, -1, -1))
+    progs = [sty.abi.style_program([sty.abi.toon(0.2)])]
+    marr = (sty.scene.SceneMaterial * len(mats))(*mats)
+    camv = list(cam.eye) + list(cam.target) + list(cam.up) + [cam.fov_y, cam.width, cam.height, cam.filter_radius]
+    run = lambda first, n: oracle.brpt(pos, mids, marr, camv, progs, 3, (2,), repeats=n, seed=4,  # noqa: E731
+                                       first_repeat=first)
+    full = run(0, 3)
+    merged = (run(0, 2) * 2 + run(2, 1)) / 3
+    np.testing.assert_allclose(merged, full, rtol=1e-12, atol=1e-15)
+    assert not np.allclose(run(2, 1), run(0, 1))
