@@ -359,6 +359,97 @@ def c1_bench(sty, repeats: int = 3):
             "image_mean": float(film.mean())}
 
 
+def c1_screen_setup(sty, W: int = 256, H: int = 256):
+    """The plain NL-PF workload with the screen-space bilateral filter on traced vertices: the Cornell
+    box at W x H, 16 paths per pixel, vertex depths 0..5, radius 8 px, sigma_pos 0.05, sigma_nrm 0.2
+    (no pixel-distance term), 4-level toon (0.1 / 0.3 / 0.6) of the first-bounce radiance."""
+    a = sty.abi
+    pos, mids, mats, cam = sty.scene.cornell_box(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    progs = [a.style_program([a.toon_steps([0.1, 0.3, 0.6], [0.05, 0.2, 0.45, 1.0], depth_mask=1 << 1)])]
+    cfg = sty.scene.screen_render_config(max_depth=5, branch=16, radius=8, sigma_pixel=0.0, sigma_pos=0.05,
+                                         sigma_nrm=0.2, screen_style=0, seed=0)
+    return sc, progs, cfg
+
+
+def c1_bilateral_bench(sty, repeats: int = 5):
+    """End-to-end NL-PF render of the Cornell box workload with the screen-space bilateral filter
+    (STY_PF_MODE_SCREEN, c1_screen_setup): trace (the tracer writes the screen records) + filter
+    from depth 5 down to 0 + splat into the FP64 film. Mpath-vertices/s = traced and filtered
+    vertices / time of sty_pf_render (CUDA events on its stream, after an untimed warm-up render);
+    the breakdown times the trace (sty_pf_trace_records) and the filter pass apart."""
+    import torch
+    sc, progs, cfg = c1_screen_setup(sty)
+    stream = torch.cuda.current_stream()
+    sc.render(cfg, progs)  # warm-up (module load, render buffers)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times, nv, film = [], 0, None
+    for r in range(repeats):
+        cfg.seed = r + 1
+        e0.record(stream)
+        film, nv = sc.render(cfg, progs)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = statistics.median(times)
+    rs, _, nvr = sc.trace_records(cfg, progs)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sc.trace_records(cfg, progs)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_trace = e0.elapsed_time(e1) / 1e3
+    prm = sty.ScreenParams(radius=8, sigma_pixel=0.0, sigma_pos=0.05, sigma_nrm=0.2)
+    out = sty.pf_screen_filter(rs, prm, progs[0])
+    torch.cuda.synchronize()
+    e0.record(stream)
+    sty.pf_screen_filter(rs, prm, progs[0], out=out)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_filter = e0.elapsed_time(e1) / 1e3
+    n_q = rs.width * rs.height * rs.spp * rs.depths
+    pairs = n_q * (2 * prm.radius + 1) ** 2 * rs.spp
+    res = {"workload": "Cornell box 256x256, 16 paths/px, depth 5, traced vertices -> screen-space bilateral "
+                       "filter (radius 8 px, sigma_pos 0.05, sigma_nrm 0.2), toon 0.1/0.3/0.6 at depth 1",
+           "mpath_vertices_per_s": nv / t / 1e6, "vertices": nv, "seconds_per_render": t,
+           "trace_ms": t_trace * 1e3, "filter_ms": t_filter * 1e3,
+           "filter_pair_evaluations": pairs, "filter_gpairs_per_s": pairs / t_filter / 1e9,
+           "image_mean": float(film.mean())}
+    sc.close()
+    return res, rs
+
+
+def c1_bilateral_cpu_baseline(sty, orc, rs, budget_s: float = 8.0):
+    """The FP32 restatement of the filter (oracle, all host threads) on a band of depth-1 query rows
+    of the traced Cornell records (depth-2 input zero): the filter stage of the render on the CPU,
+    tracing not included (a lower bound of the CPU time per vertex)."""
+    import torch
+    torch.cuda.synchronize()
+    planes = rs.planes.cpu().numpy()
+    valid = rs.valid.cpu().numpy()
+    W, H, S, D = rs.width, rs.height, rs.spp, rs.depths
+    n = W * H * S
+    rec = sty.pf.host_records(planes, valid, W, H, S, D)
+    prm = sty.ScreenParams(radius=8, sigma_pixel=0.0, sigma_pos=0.05, sigma_nrm=0.2).c()
+    a = sty.abi
+    style = a.style_program([a.toon_steps([0.1, 0.3, 0.6], [0.05, 0.2, 0.45, 1.0], depth_mask=1 << 1)])
+    nxt = np.zeros((3, n), dtype=np.float32)
+    rows, y0 = 2, H // 2 - 16
+    while True:
+        t0 = time.perf_counter()
+        orc.pf_screen_filter_depth_f32(rec, 1, prm, style, out_next=nxt, y0=y0, y1=y0 + rows)
+        elapsed = time.perf_counter() - t0
+        if elapsed >= budget_s / 4 or rows >= 64:
+            break
+        rows = min(64, max(rows * 2, int(rows * (budget_s / 4) / max(elapsed, 1e-3))))
+    nvalid = int(valid[n + y0 * W * S: n + (y0 + rows) * W * S].sum())
+    return {"value": nvalid / elapsed / 1e6, "unit": "Mpath-vertices/s", "cores": orc.num_threads(), "kind": "port",
+            "sample": f"depth-1 query rows {y0}..{y0 + rows - 1} of {H} of the traced records (x {W} px x {S} "
+                      f"paths, radius 8), {nvalid} valid vertices in {elapsed:.2f} s, FP32 restatement of the "
+                      f"filter; tracing not timed"}
+
+
 def c3_bench(sty, reps: int = 20):
     """Adjoint of the screen-space filter + smoothed ramp (36 parameters: sharpness 50, 8
     thresholds, 8 RGB ramp colours, sigma_pixel / sigma_pos / sigma_nrm) on 512 x 512 x 4 spp
@@ -572,6 +663,9 @@ def run(args):
     if args.c1_only:  # profiling case: the end-to-end render alone
         print(json.dumps({"c1_render": c1_bench(sty, repeats=max(1, args.steps))}), flush=True)
         return
+    if args.c1b_only:  # profiling case: the traced Cornell render with the screen-space filter alone
+        print(json.dumps({"c1_bilateral": c1_bilateral_bench(sty, repeats=max(1, args.steps))[0]}), flush=True)
+        return
     if args.grid_only:  # the reference's NL-NRC network alone
         print(json.dumps({"nrc_ref_network": grid_nrc_bench(sty, args.grid_frames, max(3, args.warmup), dev, 1943.8)}),
               flush=True)
@@ -753,6 +847,11 @@ def run(args):
     }
     if world == 1 and not args.no_c1:
         line["c1_render"] = c1_bench(sty)
+        line["c1_bilateral"], c1_rs = c1_bilateral_bench(sty)
+        if not args.no_cpu_baseline:
+            import oracle as orc
+            line["c1_bilateral"]["cpu_baseline"] = c1_bilateral_cpu_baseline(sty, orc, c1_rs)
+        del c1_rs
         line["c3_adjoint"] = c3_bench(sty)
         line["c5_render"] = c5_bench(sty)
     if world == 1 and not args.no_nrc:
@@ -785,6 +884,8 @@ def main():
     ap.add_argument("--no-c1", action="store_true", help="skip the end-to-end Cornell box render")
     ap.add_argument("--nrc-only", action="store_true", help="profiling case: only the NL-NRC frames")
     ap.add_argument("--c1-only", action="store_true", help="profiling case: only the end-to-end Cornell box render")
+    ap.add_argument("--c1b-only", action="store_true",
+                    help="profiling case: only the traced Cornell render with the screen-space filter")
     ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
     ap.add_argument("--c3-only", action="store_true", help="profiling case: only the adjoint")
     ap.add_argument("--brpt-only", action="store_true",

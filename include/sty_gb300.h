@@ -185,6 +185,8 @@ typedef struct sty_pf_screen_params {
     float sigma_nrm;   /* > 0 */
 } sty_pf_screen_params;
 
+/* spp must be 1, 2, 4, 8 or 16; radius up to 32 (up to 24 at 4 spp for the fastest kernel). */
+
 /* Filter one depth. `out_next` (device, 3 planes of width*height*spp floats: r plane, g plane,
  * b plane) holds out_{d+1} or is NULL at the deepest depth. `out` receives out_d with the same
  * layout. `filtered` (optional, same layout) receives f_d before the style node. */
@@ -470,11 +472,21 @@ STY_API sty_status sty_bsdf_sample(const sty_scene_material *material, uint64_t 
                                    float *wi, float *f, float *pdf, void *stream);
 STY_API sty_status sty_principled_table(float *host_table);
 
+/* Pixel filters (PixelFilter, crates/akari_render/src/film.rs:20-48): the film-plane offset of a
+ * camera ray from the sampler draw (u0, u1).
+ *   STY_FILTER_BOX       (u - 0.5) * radius per axis
+ *   STY_FILTER_GAUSSIAN  Box-Muller: sqrt(-2 ln u0) * (cos 2 pi u1, sin 2 pi u1) * radius / 3, each
+ *                        axis clamped to [-radius, radius] (the reference's default, radius 1.5,
+ *                        and the filter of every teaser config). */
+#define STY_FILTER_BOX 0
+#define STY_FILTER_GAUSSIAN 1
+
 typedef struct sty_camera {
     float eye[3], target[3], up[3];
     float fov_y;         /* degrees */
     uint32_t width, height;
-    float filter_radius; /* box pixel filter radius in pixels (PixelFilter::Box, film.rs:31-33) */
+    float filter_radius; /* pixel filter radius in pixels */
+    int32_t filter;      /* STY_FILTER_BOX or STY_FILTER_GAUSSIAN */
 } sty_camera;
 
 typedef struct sty_scene sty_scene;
@@ -495,6 +507,9 @@ STY_API sty_status sty_scene_destroy(sty_scene *scene);
 STY_API sty_status sty_scene_closest_hit(sty_scene *scene, const float *rays, uint64_t n, uint32_t *prim, float *t,
                                          float *bary, void *stream);
 
+#define STY_PF_MODE_REF 0    /* the reference's world-space hash-grid filter (sty_pf_ref_filter) */
+#define STY_PF_MODE_SCREEN 1 /* the screen-space bilateral filter (sty_pf_screen_filter) */
+
 typedef struct sty_pf_render_config {
     uint32_t max_depth;             /* vertex depths 0..max_depth */
     uint32_t branch;                /* paths per pixel */
@@ -506,17 +521,59 @@ typedef struct sty_pf_render_config {
     int32_t smis, cluster, disable_flag_check, no_first_hit_stylization;
     int32_t has_scene_bounds;
     float scene_bounds[6];          /* min xyz, max xyz (else the scene AABB) */
-    uint64_t seed;                  /* per-path Pcg32 streams: seq = path index, seed = mix(seed, path) */
+    uint64_t seed;                  /* path slot i of pixel px and branch b (i = b * width * height + px)
+                                       starts from Pcg32::new_seq_offset(i, seed_i), seed_i the i-th
+                                       gen::<u64>() of StdRng::seed_from_u64(seed) (ChaCha12; the
+                                       reference renders with seed 0, sampler/mod.rs:157-173) */
+    int32_t mode;                   /* STY_PF_MODE_REF (0) or STY_PF_MODE_SCREEN */
+    int32_t screen_style;           /* SCREEN: index into `programs` of the filter's style program
+                                       (applied per depth by its nodes' depth masks), -1 = none */
+    sty_pf_screen_params screen;    /* SCREEN: the bilateral filter's window and bandwidths */
 } sty_pf_render_config;
 
 /* Full NL-PF render (lm_path_filtering.rs:1629-1793): per repeat, trace every depth, filter the
- * depths backwards with the reference-mode filter, splat the depth-0 result with the first-hit
- * style and add (1/repeats) of the pixel values into `film` (device, width*height*3 doubles,
- * interleaved rgb; the caller zeroes it). `programs` is a HOST array. Optional `vertex_count`
- * (host) receives the number of path vertices traced. */
+ * depths backwards, splat the depth-0 result and add (1/repeats) of the pixel values into `film`
+ * (device, width*height*3 doubles, interleaved rgb; the caller zeroes it). `programs` is a HOST
+ * array. Optional `vertex_count` (host) receives the number of path vertices traced.
+ *   STY_PF_MODE_REF: the reference-mode filter (sty_pf_ref_filter) at every depth; the splat
+ *     applies each hit material's style program at the first hit (kernel_splat :480-506).
+ *   STY_PF_MODE_SCREEN: the tracer writes every depth's vertices as screen-space records
+ *     (sty_pf_records, spp = branch: pos = hit point, nrm = shading normal, rad = emitted radiance
+ *     with its MIS weight + the light sample with balance MIS, thr = f |cos| / pdf of the sampled
+ *     continuation times the MIS weight of the emission found there, valid = hit), and
+ *     sty_pf_screen_filter filters them from max_depth down to 0 with `screen` and the program
+ *     `screen_style`; the film receives the mean over the branch samples of the depth-0 output
+ *     (sty_film_accumulate). branch must be 1, 2, 4, 8 or 16. */
 STY_API sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *config,
                                  const sty_style_program *programs, uint32_t n_programs, double *film,
                                  uint64_t *vertex_count, void *stream);
+
+/* Writable record planes: each of the 13 planes holds (max_depth + 1) * height * width * branch
+ * elements in the sty_pf_records order; `prim` (optional) receives the hit triangle id of each
+ * record (UINT32_MAX where the record is invalid). */
+typedef struct sty_pf_records_out {
+    float *pos[3];
+    float *nrm[3];
+    float *rad[3];
+    float *thr[3];
+    int32_t *valid;
+    uint32_t *prim;
+} sty_pf_records_out;
+
+/* The screen-space records of the first repeat of a STY_PF_MODE_SCREEN render of `config`
+ * (device planes owned by the caller): sty_pf_render with repeats = 1 equals
+ * sty_pf_screen_filter on these records followed by sty_film_accumulate, bit for bit. Lets a
+ * caller dump the traced buffers the filter sees. */
+STY_API sty_status sty_pf_trace_records(sty_scene *scene, const sty_pf_render_config *config,
+                                        const sty_style_program *programs, uint32_t n_programs,
+                                        const sty_pf_records_out *records, uint64_t *vertex_count, void *stream);
+
+/* The depth-0 camera rays of every path slot of a render with `branch` paths per pixel and seed
+ * `seed` (device output, 8 floats per slot: origin, direction, tmin = 0, tmax = 1e20; slot
+ * i = b * width * height + px): PerspectiveCamera::generate_ray (camera/mod.rs:73-126) with the
+ * scene camera's pixel filter, fed by the slot's Pcg32 stream exactly as sty_pf_render and
+ * sty_nrc_render feed it. */
+STY_API sty_status sty_scene_camera_rays(sty_scene *scene, uint32_t branch, uint64_t seed, float *rays, void *stream);
 
 /* NL-NRC samples generated by the tracer (nrc_pt.rs:231-434 tracing, write_nrc_inputs :583-663,
  * training targets :723-776).
@@ -637,6 +694,11 @@ STY_API sty_status sty_brpt_render(sty_scene *scene, const sty_brpt_config *conf
  * n * draws, stream-major) and the final states to states (device, n). */
 STY_API sty_status sty_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n,
                              uint32_t draws, uint32_t *out, sty_pcg32 *states, void *stream);
+
+/* The gen::<u64>() outputs first .. first + n - 1 of rand's StdRng::seed_from_u64(seed) (rand 0.8.5:
+ * ChaCha12Rng of rand_chacha 0.3.1 keyed by rand_core 0.6.4's PCG32 expansion of the seed), the
+ * per-path seeds of init_pcg32_buffer_with_seed (sampler/mod.rs:157-173); device output. */
+STY_API sty_status sty_std_rng_u64(uint64_t seed, uint64_t first, uint64_t n, uint64_t *out, void *stream);
 
 /* Hash-grid cell index of each point (lm_path_filtering.rs:20-59): cell = clamp((p - pmin) /
  * (pmax - pmin), 0, 1) * res truncated and clamped to res-1; index = (x*73856093 ^ y*19349663

@@ -34,6 +34,10 @@ def lib() -> C.CDLL:
         L.orc_pf_screen_filter_depth_f32.argtypes = [vp, C.c_uint32, vp, vp, vp, vp, vp, C.c_int32, C.c_int32]
         L.orc_pcg32_streams.argtypes = [vp, C.c_uint64, C.c_uint64, C.c_uint32, vp, vp]
         L.orc_hash_cells.argtypes = [vp, C.c_uint64, vp, vp, vp, C.c_uint32, vp, vp]
+        L.orc_chacha_block.argtypes = [vp, vp, C.c_int32]
+        L.orc_std_rng_key.argtypes = [C.c_uint64, vp]
+        L.orc_std_rng_u64.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64, vp]
+        L.orc_camera_rays.argtypes = [vp, C.c_uint32, C.c_uint64, vp]
         L.orc_pf_adjoint_loss_f64.restype = C.c_double
         L.orc_pf_adjoint_loss_f64.argtypes = [vp, C.c_uint32, C.c_int32, vp, C.c_uint32, vp, vp]
         L.orc_pf_adjoint_f64.restype = C.c_double
@@ -117,6 +121,34 @@ def pcg32_streams(seeds: np.ndarray, first_seq: int, draws: int):
     states = np.zeros((seeds.size, 2), dtype=np.uint64)
     lib().orc_pcg32_streams(_p(seeds), first_seq, seeds.size, draws, _p(out), _p(states))
     return out, states
+
+
+def chacha_block(words, rounds: int = 20) -> np.ndarray:
+    """ChaCha block function of a 16-word input state (rounds of it, plus the input)."""
+    w = np.ascontiguousarray(words, dtype=np.uint32).reshape(16)
+    out = np.zeros(16, dtype=np.uint32)
+    lib().orc_chacha_block(_p(w), _p(out), rounds)
+    return out
+
+
+def std_rng_key(seed: int) -> np.ndarray:
+    key = np.zeros(8, dtype=np.uint32)
+    lib().orc_std_rng_key(seed, _p(key))
+    return key
+
+
+def std_rng_u64(seed: int, first: int, n: int) -> np.ndarray:
+    """gen::<u64>() outputs first .. first+n-1 of rand's StdRng::seed_from_u64(seed)."""
+    out = np.zeros(n, dtype=np.uint64)
+    lib().orc_std_rng_u64(seed, first, n, _p(out))
+    return out
+
+
+def camera_rays(cam, branch: int, seed: int) -> np.ndarray:
+    """Depth-0 rays [W*H*branch, 8] of every path slot (slot = b * W * H + pixel)."""
+    out = np.zeros((cam.width * cam.height * branch, 8), dtype=np.float32)
+    lib().orc_camera_rays(C.addressof(cam), branch, seed, _p(out))
+    return out
 
 
 def hash_cells(points: np.ndarray, pmin, pmax, res, table_size: int):

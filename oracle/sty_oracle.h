@@ -52,6 +52,15 @@ void orc_pf_screen_filter_depth_f32(const sty_pf_records *rec, uint32_t depth,
 void orc_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t n, uint32_t draws,
                        uint32_t *out, sty_pcg32 *states);
 
+/* ChaCha block function (out = rounds of `in` + in; 16 words each). */
+void orc_chacha_block(const uint32_t *in, uint32_t *out, int32_t rounds);
+/* rand_core 0.6.4 seed_from_u64 key of a ChaCha12Rng (8 words). */
+void orc_std_rng_key(uint64_t seed, uint32_t *key);
+/* gen::<u64>() outputs first .. first+n-1 of StdRng::seed_from_u64(seed) (sampler/mod.rs:157-173). */
+void orc_std_rng_u64(uint64_t seed, uint64_t first, uint64_t n, uint64_t *out);
+/* Depth-0 camera rays of every path slot (as sty_scene_camera_rays). */
+void orc_camera_rays(const sty_camera *cam, uint32_t branch, uint64_t seed, float *rays);
+
 /* Hash-grid cell (lm_path_filtering.rs:20-59), float arithmetic as in the reference. */
 void orc_hash_cells(const float *points, uint64_t n, const float pmin[3], const float pmax[3],
                     const uint32_t res[3], uint32_t table_size, uint32_t *cell_xyz,

@@ -24,6 +24,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+    # host code: no FMA contraction (the camera frame and other host-side set-up round the same way on
+    # x86-64 and Arm hosts)
+    "-Xcompiler", "-ffp-contract=off",
     "-I", str(ROOT / "include"), "-I", str(CSRC),
 ]
 

@@ -5,6 +5,7 @@
 #include <cstring>
 
 #include "common.cuh"
+#include "rng.cuh"
 #include "style.cuh"
 
 namespace sty {
@@ -141,6 +142,16 @@ __global__ void k_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint6
     if (states) states[i] = g;
 }
 
+struct RngKey {
+    uint32_t k[8];
+};
+// gen::<u64>() outputs first .. first + n - 1 of StdRng::seed_from_u64 (rng.cuh)
+__global__ void k_std_rng_u64(RngKey key, uint64_t first, uint64_t n, uint64_t *out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = std_rng_u64(key.k, first + i);
+}
+
 struct GridDesc {
     float pmin[3], pmax[3];
     uint32_t res[3];
@@ -223,6 +234,7 @@ uint64_t sty_struct_size(const char *name) {
     if (!strcmp(name, "sty_nrc_render_stats")) return sizeof(sty_nrc_render_stats);
     if (!strcmp(name, "sty_brpt_config")) return sizeof(sty_brpt_config);
     if (!strcmp(name, "sty_brpt_stats")) return sizeof(sty_brpt_stats);
+    if (!strcmp(name, "sty_pf_records_out")) return sizeof(sty_pf_records_out);
     return 0;
 }
 
@@ -282,6 +294,18 @@ sty_status sty_pcg32_streams(const uint64_t *seeds, uint64_t first_seq, uint64_t
     const int bs = 256;
     k_pcg32_streams<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(seeds, first_seq, n, draws, out, states);
     return check_launch("sty_pcg32_streams");
+}
+
+sty_status sty_std_rng_u64(uint64_t seed, uint64_t first, uint64_t n, uint64_t *out, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(out, "sty_std_rng_u64: null out");
+    STY_ARG_CHECK(n < (1ull << 40), "sty_std_rng_u64: n too large");
+    if (n == 0) return STY_OK;
+    RngKey key;
+    std_rng_key(seed, key.k);
+    const int bs = 256;
+    k_std_rng_u64<<<(unsigned)((n + bs - 1) / bs), bs, 0, as_stream(stream)>>>(key, first, n, out);
+    return check_launch("sty_std_rng_u64");
 }
 
 sty_status sty_hash_cells(const float *points, uint64_t n, const float pmin[3], const float pmax[3],

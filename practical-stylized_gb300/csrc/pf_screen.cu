@@ -211,6 +211,174 @@ __global__ void __launch_bounds__(NT, S >= 8 ? 1 : 2) k_pf_screen(const ScreenAr
     }
 }
 
+// Many samples per pixel (S = 16): G = S / Q threads share a pixel, each owning Q of its S queries
+// (one warp = 32 pixels of one row and one query group, so the row skip stays warp-uniform);
+// candidate samples are read 4 at a time (16-byte loads), so registers stay within two CTAs per SM.
+template <int S, int Q>
+__global__ void __launch_bounds__(NT, 2) k_pf_screen_g(const ScreenArgs a, const sty_style_program style) {
+    constexpr int G = S / Q;
+    constexpr int GTH = NT / (TW * G);  // pixel rows per CTA
+    extern __shared__ __align__(16) float sm[];
+    const int R = a.R;
+    const int CW = TW + 2 * R;
+    const int plane = CH * CW * S;
+    const int tx0 = blockIdx.x * TW, ty0 = blockIdx.y * GTH;
+    const int lx = threadIdx.x % TW, grp = (threadIdx.x / TW) % G, ly = threadIdx.x / (TW * G);
+    const int x = tx0 + lx, y = ty0 + ly;
+    const bool inside = (x < a.W) && (y < a.H);
+    const size_t N = (size_t)a.W * a.H * S;
+    const size_t dbase = (size_t)a.depth * N;
+
+    float qpx[Q], qpy[Q], qpz[Q], qnx[Q], qny[Q], qnz[Q];
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        if (inside) {
+            const size_t g = dbase + ((size_t)y * a.W + x) * S + grp * Q + q;
+            qpx[q] = a.pos[0][g] * a.pscale;
+            qpy[q] = a.pos[1][g] * a.pscale;
+            qpz[q] = a.pos[2][g] * a.pscale;
+            qnx[q] = a.nrm[0][g] * a.nscale;
+            qny[q] = a.nrm[1][g] * a.nscale;
+            qnz[q] = a.nrm[2][g] * a.nscale;
+        } else {
+            qpx[q] = qpy[q] = qpz[q] = 0.0f;
+            qnx[q] = qny[q] = qnz[q] = 0.0f;
+        }
+    }
+    KahanF acc[Q][4];
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[q][c] = {0.0f, 0.0f};
+
+    const int row_lo = ty0 - R, row_hi = ty0 + GTH - 1 + R;
+    for (int cy = row_lo; cy <= row_hi; cy += CH) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < plane; idx += NT) {
+            const int r = idx / (CW * S);
+            const int rem = idx - r * (CW * S);
+            const int col = rem / S;
+            const int smp = rem - col * S;
+            const int gy = cy + r, gx = tx0 - R + col;
+            float v[NF];
+            bool ok = (gy >= 0) && (gy < a.H) && (gx >= 0) && (gx < a.W) && (gy <= row_hi);
+            size_t j = 0;
+            if (ok) {
+                j = ((size_t)gy * a.W + gx) * S + smp;
+                ok = a.valid[dbase + j] != 0;
+            }
+            if (ok) {
+                const size_t g = dbase + j;
+                v[0] = a.pos[0][g] * a.pscale;
+                v[1] = a.pos[1][g] * a.pscale;
+                v[2] = a.pos[2][g] * a.pscale;
+                v[3] = a.nrm[0][g];
+                v[4] = a.nrm[1][g];
+                v[5] = a.nrm[2][g];
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    float in = a.rad[c][g];
+                    if (a.out_next) in = fmaf(a.thr[c][g], a.out_next[c * N + j], in);
+                    v[6 + c] = in;
+                }
+            } else {
+                v[0] = v[1] = v[2] = kFar;
+                v[3] = v[4] = v[5] = 0.0f;
+                v[6] = v[7] = v[8] = 0.0f;
+            }
+#pragma unroll
+            for (int f = 0; f < NF; f++) sm[f * plane + idx] = v[f];
+        }
+        __syncthreads();
+        for (int r = 0; r < CH; r++) {
+            const int dy = cy + r - y;
+            if (dy < -R || dy > R) continue;  // uniform across a warp
+            float part[Q][4];
+#pragma unroll
+            for (int q = 0; q < Q; q++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) part[q][c] = 0.0f;
+            const float cy_term = -(a.pix2 * (float)(dy * dy)) - a.nscale;
+            const float *rowp = sm + (size_t)r * CW * S;
+            for (int dx = -R; dx <= R; dx++) {
+                const float cst = fmaf(-a.pix2, (float)(dx * dx), cy_term);
+                const float *cp0 = rowp + (lx + R + dx) * S;
+#pragma unroll
+                for (int tc = 0; tc < S; tc += 4) {
+                    const float *cp = cp0 + tc;
+                    float cpx[4], cpy[4], cpz[4], cnx[4], cny[4], cnz[4], cr[4], cg[4], cb[4];
+                    Vec<4>::ld(cp + 0 * plane, cpx);
+                    Vec<4>::ld(cp + 1 * plane, cpy);
+                    Vec<4>::ld(cp + 2 * plane, cpz);
+                    Vec<4>::ld(cp + 3 * plane, cnx);
+                    Vec<4>::ld(cp + 4 * plane, cny);
+                    Vec<4>::ld(cp + 5 * plane, cnz);
+                    Vec<4>::ld(cp + 6 * plane, cr);
+                    Vec<4>::ld(cp + 7 * plane, cg);
+                    Vec<4>::ld(cp + 8 * plane, cb);
+#pragma unroll
+                    for (int t = 0; t < 4; t++) {
+#pragma unroll
+                        for (int q = 0; q < Q; q++) {
+                            float arg = fmaf(qnx[q], cnx[t], cst);
+                            arg = fmaf(qny[q], cny[t], arg);
+                            arg = fmaf(qnz[q], cnz[t], arg);
+                            const float ex = qpx[q] - cpx[t];
+                            const float ey = qpy[q] - cpy[t];
+                            const float ez = qpz[q] - cpz[t];
+                            arg = fmaf(-ex, ex, arg);
+                            arg = fmaf(-ey, ey, arg);
+                            arg = fmaf(-ez, ez, arg);
+                            const float w = ex2_approx(arg);
+                            part[q][0] += w;
+                            part[q][1] = fmaf(w, cr[t], part[q][1]);
+                            part[q][2] = fmaf(w, cg[t], part[q][2]);
+                            part[q][3] = fmaf(w, cb[t], part[q][3]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < Q; q++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[q][c].add(part[q][c]);
+        }
+    }
+    if (!inside) return;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const size_t j = ((size_t)y * a.W + x) * S + grp * Q + q;
+        f3 f = {0.0f, 0.0f, 0.0f}, o = {0.0f, 0.0f, 0.0f};
+        if (a.valid[dbase + j]) {
+            const float sw = acc[q][0].s;
+            f = {acc[q][1].s / sw, acc[q][2].s / sw, acc[q][3].s / sw};
+            o = style_apply(style, a.depth, f);
+        }
+        a.out[j] = o.x;
+        a.out[N + j] = o.y;
+        a.out[2 * N + j] = o.z;
+        if (a.filtered) {
+            a.filtered[j] = f.x;
+            a.filtered[N + j] = f.y;
+            a.filtered[2 * N + j] = f.z;
+        }
+    }
+}
+
+template <int S, int Q>
+sty_status launch_screen_g(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st) {
+    constexpr int GTH = NT / (TW * (S / Q));
+    const int CW = TW + 2 * a.R;
+    const size_t smem = (size_t)NF * CH * CW * S * sizeof(float);
+    STY_ARG_CHECK(smem <= 227 * 1024, "radius %d too large for %d samples per pixel", a.R, S);
+    STY_TRY(check_cuda(cudaFuncSetAttribute(k_pf_screen_g<S, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)smem),
+                       "cudaFuncSetAttribute(k_pf_screen_g)"));
+    dim3 grid((a.W + TW - 1) / TW, (a.H + GTH - 1) / GTH);
+    k_pf_screen_g<S, Q><<<grid, NT, smem, st>>>(a, style);
+    return check_launch("k_pf_screen_g");
+}
+
 template <int S>
 sty_status launch_screen(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st) {
     const int CW = TW + 2 * a.R;
@@ -226,8 +394,8 @@ sty_status validate(const sty_pf_records *rec, const sty_pf_screen_params *p) {
     STY_ARG_CHECK(rec && p, "null records or params");
     STY_ARG_CHECK(rec->width > 0 && rec->height > 0 && rec->depths > 0, "bad record dimensions %dx%d, depths %d",
                   rec->width, rec->height, rec->depths);
-    STY_ARG_CHECK(rec->spp == 1 || rec->spp == 2 || rec->spp == 4 || rec->spp == 8,
-                  "spp must be 1, 2, 4 or 8 (got %d)", rec->spp);
+    STY_ARG_CHECK(rec->spp == 1 || rec->spp == 2 || rec->spp == 4 || rec->spp == 8 || rec->spp == 16,
+                  "spp must be 1, 2, 4, 8 or 16 (got %d)", rec->spp);
     for (int c = 0; c < 3; c++)
         STY_ARG_CHECK(rec->pos[c] && rec->nrm[c] && rec->rad[c] && rec->thr[c], "null record field");
     STY_ARG_CHECK(rec->valid, "null valid field");
@@ -283,7 +451,8 @@ sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth,
         case 2: return launch_screen<2>(a, prog, st);
         case 4:  // the warp-specialised kernel's shared-memory ring fits up to radius 24
             return a.R <= 24 ? launch_screen_s4(a, prog, st) : launch_screen<4>(a, prog, st);
-        default: return launch_screen<8>(a, prog, st);
+        case 8: return launch_screen<8>(a, prog, st);
+        default: return launch_screen_g<16, 4>(a, prog, st);
     }
 }
 

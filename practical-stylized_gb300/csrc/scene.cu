@@ -207,6 +207,9 @@ sty_status sty_scene_create(const float *pos, const uint32_t *tmat, uint32_t n, 
     STY_ARG_CHECK(pos && tmat && mats && cam && out, "sty_scene_create: null argument");
     STY_ARG_CHECK(n > 0 && nm > 0, "empty scene");
     STY_ARG_CHECK(cam->width > 0 && cam->height > 0 && cam->fov_y > 0.0f && cam->fov_y < 180.0f, "bad camera");
+    STY_ARG_CHECK(cam->filter == STY_FILTER_BOX || cam->filter == STY_FILTER_GAUSSIAN, "unknown pixel filter %d",
+                  cam->filter);
+    STY_ARG_CHECK(cam->filter_radius >= 0.0f && cam->filter_radius < 1e6f, "bad pixel filter radius");
     for (uint32_t i = 0; i < n; i++) STY_ARG_CHECK(tmat[i] < nm, "triangle %u has material %u >= %u", i, tmat[i], nm);
     for (uint32_t i = 0; i < nm; i++)
         STY_ARG_CHECK(mats[i].kind == STY_MAT_DIFFUSE || mats[i].kind == STY_MAT_GGX ||

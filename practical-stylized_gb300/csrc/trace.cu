@@ -35,9 +35,17 @@ namespace sty {
 namespace {
 
 
+// Screen-space record planes of one depth that the tracer writes in STY_PF_MODE_SCREEN (the
+// position, normal and valid planes are the vertex planes themselves); rad[0] == nullptr: none.
+struct RecOut {
+    float *rad[3], *thr[3];
+    uint32_t *prim;
+};
+
 __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t depth, uint32_t max_depth,
                         PathState ps, VertOut v, VertOut parent, sty_pcg32 *rng, const sty_style_program *progs,
-                        uint32_t n_progs, unsigned long long *vcount, float split_rough) {
+                        uint32_t n_progs, unsigned long long *vcount, float split_rough, RecOut rec,
+                        RecOut rec_parent) {
     const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
     if (tid >= n_paths) return;
     sty_pcg32 st = rng[tid];
@@ -45,9 +53,10 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
     uint32_t flags, exclude;
     float prev_pdf;
     F3 prev_p;
+    const bool recs = rec.rad[0] != nullptr;
     if (depth == 0) {
         const uint32_t npx = cam.W * cam.H;
-        const uint32_t px = cam.random_px ? pcg_next(st) % npx : tid % npx;
+        const uint32_t px = cam.random_px ? pcg_next(st) % npx : cam.pixel_major ? tid / cam.pixel_major : tid % npx;
         camera_ray(cam, px, st, &ro, &rd);
         flags = 0;
         exclude = NONE;
@@ -110,6 +119,14 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
         parent.ind_wi[1][tid] = rd.y;
         parent.ind_wi[2][tid] = rd.z;
         parent.ind_mis[tid] = mis;
+        if (recs && mis != 1.0f)  // the parent's throughput carries this vertex's emission MIS weight
+            for (int c = 0; c < 3; c++) rec_parent.thr[c][tid] *= mis;
+    }
+    F3 rad = le;  // screen record: emission (with its MIS weight) + light sample (balance MIS)
+    if (recs) {
+        if (rec.prim) rec.prim[tid] = prim;
+        rec.rad[0][tid] = le.x; rec.rad[1][tid] = le.y; rec.rad[2][tid] = le.z;
+        rec.thr[0][tid] = 0.0f; rec.thr[1][tid] = 0.0f; rec.thr[2][tid] = 0.0f;
     }
     if (depth >= max_depth) {
         ps.terminated[tid] = 1;
@@ -129,6 +146,13 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
             v.dir_l[1][tid] = li.y;
             v.dir_l[2][tid] = li.z;
             v.dir_pdf[tid] = lpdf;
+            if (recs) {  // the direct term of the reference's filter with the vertex as its own neighbour
+                F3 f;
+                const float bp = bsdf_eval(m, ns, ng, wo, lwi, &f, sc.ggx_tab);
+                const float w = lpdf / (lpdf + bp) / lpdf;
+                rad = rad + f3m(f.x * li.x, f.y * li.y, f.z * li.z) * w;
+                rec.rad[0][tid] = rad.x; rec.rad[1][tid] = rad.y; rec.rad[2][tid] = rad.z;
+            }
         }
     }
     // final-gathering renders stop at the first rough vertex (splitting, nrc_pt.rs:372-375)
@@ -143,6 +167,14 @@ __global__ void k_trace(SceneView sc, CamArgs cam, uint32_t n_paths, uint32_t de
     const float usel = next_1d(st), us0 = next_1d(st), us1 = next_1d(st);
     float pdf = 0.0f;
     const F3 wi = bsdf_sample(m, ns, ng, wo, usel, us0, us1, &pdf, sc.ggx_tab);
+    if (recs && pdf > 0.0f) {  // throughput to the child: f |cos| / pdf (times the child's MIS weight, above)
+        F3 f;
+        const float bp = bsdf_eval(m, ns, ng, wo, wi, &f, sc.ggx_tab);
+        if (bp > 0.0f) {
+            const float k = 1.0f / bp;
+            rec.thr[0][tid] = f.x * k; rec.thr[1][tid] = f.y * k; rec.thr[2][tid] = f.z * k;
+        }
+    }
     if (pdf > 0.0f) {
         const F3 no = offset_ray_origin(p, face_forward(ng, wi));
         ps.o[0][tid] = no.x; ps.o[1][tid] = no.y; ps.o[2][tid] = no.z;
@@ -549,7 +581,7 @@ namespace {
 // of one scene reuse them, so calls on one scene are serialised by the caller.
 enum CacheSlot {
     kVerts, kOuts, kPathState, kRng, kPrograms, kVertexCount, kRowCount, kRowIndex, kScanTmp,
-    kQueryIn, kQueryPred, kQueryScratch, kTargets, kRowsIn, kRowsTgt, kFinalGather, kSlots
+    kQueryIn, kQueryPred, kQueryScratch, kTargets, kRowsIn, kRowsTgt, kFinalGather, kRecords, kSlots
 };
 struct RenderCache {
     void *p[kSlots] = {};
@@ -585,6 +617,11 @@ struct TraceJob {
     PathState ps;
     float bmin[3], bmax[3];
     float split_rough = 0.0f;  // > 0: stop paths at the first vertex rougher than this
+    // STY_PF_MODE_SCREEN: slots in pixel-major order, and the screen-space record planes the tracer
+    // writes (each plane D * n, sty_pf_records order); the vertex planes p, ns and active alias them
+    uint32_t pixel_major = 0;
+    sty_pf_records_out rp{};
+    std::vector<RecOut> ro;
     sty_status s = STY_OK;
 
     void *alloc(CacheSlot k, size_t bytes, const char *what) {
@@ -600,7 +637,7 @@ struct TraceJob {
         return cache->p[k];
     }
     sty_status init(sty_scene *scene, uint32_t branch, uint32_t maxd, const sty_style_program *programs,
-                    uint32_t nprog, uint64_t seed, cudaStream_t st, uint32_t paths = 0) {
+                    uint32_t nprog, uint64_t seed, cudaStream_t st, uint32_t paths = 0, uint32_t pmajor = 0) {
         const sty_camera &cam = scene_camera(scene);
         npx = cam.width * cam.height;
         const uint64_t np64 = paths ? (uint64_t)paths : (uint64_t)npx * branch;
@@ -614,6 +651,7 @@ struct TraceJob {
         n_programs = nprog;
         cache = &render_cache(scene);
         ca = make_camera(cam);
+        ca.pixel_major = pixel_major = pmajor;
         sv = scene_view(scene);
         scene_bounds(scene, bmin, bmax);
         verts = (float *)alloc(kVerts, (size_t)D * kPlanes * n * 4, "alloc vertices");
@@ -677,15 +715,78 @@ struct TraceJob {
         ps.exclude = (uint32_t *)pl();
         ps.terminated = (uint32_t *)pl();
         ps.split = (uint32_t *)pl();
-        k_rng_init<<<(n + 255) / 256, 256, 0, st>>>(n, seed, rng);
+        ro.assign(D, RecOut{});
+        k_rng_init<<<(n + 255) / 256, 256, 0, st>>>(n, std_rng_key_of(seed), pixel_major, npx, rng);
         return check_launch("k_rng_init");
+    }
+    // SCREEN mode: the tracer writes screen records, into `ext` (caller planes) or into the scene's
+    // cache; the vertex planes p, ns and active of every depth become views of the record planes
+    sty_status init_records(const sty_pf_records_out *ext) {
+        if (ext) {
+            rp = *ext;
+        } else {
+            float *b = (float *)alloc(kRecords, (size_t)13 * D * n * 4, "alloc records");
+            if (s != STY_OK) return s;
+            for (int a = 0; a < 3; a++) {
+                rp.pos[a] = b + (size_t)a * D * n;
+                rp.nrm[a] = b + (size_t)(3 + a) * D * n;
+                rp.rad[a] = b + (size_t)(6 + a) * D * n;
+                rp.thr[a] = b + (size_t)(9 + a) * D * n;
+            }
+            rp.valid = (int32_t *)(b + (size_t)12 * D * n);
+            rp.prim = nullptr;
+        }
+        for (uint32_t d = 0; d < D; d++) {
+            const size_t o = (size_t)d * n;
+            VertOut &w = vo[d];
+            sty_pf_vertices &r = vin[d];
+            w.active = rp.valid + o;
+            r.active = w.active;
+            for (int a = 0; a < 3; a++) {
+                w.p[a] = rp.pos[a] + o;
+                w.ns[a] = rp.nrm[a] + o;
+                r.p[a] = w.p[a];
+                r.ns[a] = w.ns[a];
+                ro[d].rad[a] = rp.rad[a] + o;
+                ro[d].thr[a] = rp.thr[a] + o;
+            }
+            ro[d].prim = rp.prim ? rp.prim + o : nullptr;
+        }
+        return STY_OK;
+    }
+    sty_pf_records records(uint32_t spp) const {
+        sty_pf_records r;
+        for (int a = 0; a < 3; a++) {
+            r.pos[a] = rp.pos[a];
+            r.nrm[a] = rp.nrm[a];
+            r.rad[a] = rp.rad[a];
+            r.thr[a] = rp.thr[a];
+        }
+        r.valid = rp.valid;
+        r.width = (int32_t)ca.W;
+        r.height = (int32_t)ca.H;
+        r.spp = (int32_t)spp;
+        r.depths = (int32_t)D;
+        return r;
     }
     // all depths of one wavefront (kernel_trace dispatch loop, lm_path_filtering.rs:1646-1654)
     sty_status trace(cudaStream_t st) {
         STY_TRY(check_cuda(cudaMemsetAsync(verts, 0, (size_t)D * kPlanes * n * 4, st), "reset vertices"));
+        if (rp.valid) {  // records of slots without a hit read as invalid zeros
+            const size_t pl = (size_t)D * n * 4;
+            for (int a = 0; a < 3; a++) {
+                STY_TRY(check_cuda(cudaMemsetAsync(rp.pos[a], 0, pl, st), "reset records"));
+                STY_TRY(check_cuda(cudaMemsetAsync(rp.nrm[a], 0, pl, st), "reset records"));
+                STY_TRY(check_cuda(cudaMemsetAsync(rp.rad[a], 0, pl, st), "reset records"));
+                STY_TRY(check_cuda(cudaMemsetAsync(rp.thr[a], 0, pl, st), "reset records"));
+            }
+            STY_TRY(check_cuda(cudaMemsetAsync(rp.valid, 0, pl, st), "reset records"));
+            if (rp.prim) STY_TRY(check_cuda(cudaMemsetAsync(rp.prim, 0xff, pl, st), "reset records"));
+        }
         for (uint32_t d = 0; d < D; d++) {
             k_trace<<<(n + 255) / 256, 256, 0, st>>>(sv, ca, n, d, max_depth, ps, vo[d], vo[d > 0 ? d - 1 : 0], rng,
-                                                     dprog, n_programs, vc, split_rough);
+                                                     dprog, n_programs, vc, split_rough, ro[d],
+                                                     ro[d > 0 ? d - 1 : 0]);
             STY_TRY(check_launch("k_trace"));
         }
         return STY_OK;
@@ -699,84 +800,122 @@ namespace sty {
 void render_cache_free(void *cache) { delete static_cast<RenderCache *>(cache); }
 }  // namespace sty
 
+namespace {
+sty_status check_render_config(const sty_pf_render_config *cfg, const sty_style_program *programs,
+                               uint32_t n_programs) {
+    STY_ARG_CHECK(cfg->branch >= 1 && cfg->repeats >= 1 && cfg->max_depth <= 30, "bad branch / repeats / max_depth");
+    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
+    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
+    STY_ARG_CHECK(cfg->mode == STY_PF_MODE_REF || cfg->mode == STY_PF_MODE_SCREEN, "unknown render mode %d",
+                  cfg->mode);
+    if (cfg->mode == STY_PF_MODE_REF) {
+        STY_ARG_CHECK(cfg->n_radius_scale >= 1 && cfg->n_radius_scale <= 16 && cfg->n_reuse >= 1 && cfg->n_reuse <= 16,
+                      "radius_scale and reuse need 1..16 entries");
+    } else {
+        const uint32_t b = cfg->branch;
+        STY_ARG_CHECK(b == 1 || b == 2 || b == 4 || b == 8 || b == 16, "SCREEN mode: branch must be 1, 2, 4, 8 or 16");
+        STY_ARG_CHECK(cfg->screen_style < (int32_t)n_programs, "SCREEN mode: screen_style %d >= %u programs",
+                      cfg->screen_style, n_programs);
+    }
+    return STY_OK;
+}
+// the SCREEN-mode filter pass over the job's records (deepest depth first) into the job's outputs
+sty_status screen_filter_job(TraceJob &job, const sty_pf_render_config *cfg, const sty_style_program *programs,
+                             cudaStream_t st) {
+    const sty_pf_records r = job.records(cfg->branch);
+    const sty_style_program *prog = cfg->screen_style >= 0 ? &programs[cfg->screen_style] : nullptr;
+    return sty_pf_screen_filter(&r, &cfg->screen, prog, job.outs, st);
+}
+}  // namespace
+
 extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config *cfg,
                                     const sty_style_program *programs, uint32_t n_programs, double *film,
                                     uint64_t *vertex_count, void *stream) {
     clear_error();
     STY_ARG_CHECK(scene && cfg && film, "sty_pf_render: null argument");
-    STY_ARG_CHECK(cfg->branch >= 1 && cfg->repeats >= 1 && cfg->max_depth <= 30, "bad branch / repeats / max_depth");
-    STY_ARG_CHECK(cfg->n_radius_scale >= 1 && cfg->n_radius_scale <= 16 && cfg->n_reuse >= 1 && cfg->n_reuse <= 16,
-                  "radius_scale and reuse need 1..16 entries");
-    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
-    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
+    STY_TRY(check_render_config(cfg, programs, n_programs));
     cudaStream_t st = as_stream(stream);
     TraceJob job;
-    STY_TRY(job.init(scene, cfg->branch, cfg->max_depth, programs, n_programs, cfg->seed, st));
+    const bool screen = cfg->mode == STY_PF_MODE_SCREEN;
+    STY_TRY(job.init(scene, cfg->branch, cfg->max_depth, programs, n_programs, cfg->seed, st, 0,
+                     screen ? cfg->branch : 0u));
     const uint32_t n = job.n, D = job.D, npx = job.npx;
-    RenderCache &rc = *job.cache;
-    if (!rc.ctx || rc.ctx_cap < n) {
-        if (rc.ctx) sty_pf_ref_destroy(rc.ctx);
-        rc.ctx = nullptr;
-        rc.ctx_cap = 0;
-        STY_TRY(sty_pf_ref_create(n, 1u << 26, &rc.ctx));
-        rc.ctx_cap = n;
-    }
-    sty_pf_ref_ctx *ctx = rc.ctx;
-    const auto &mh = scene_materials(scene);
-    std::vector<sty_pf_material> pm(mh.size());
-    for (size_t i = 0; i < mh.size(); i++) {
-        pm[i].kind = mh[i].kind;
-        for (int c = 0; c < 3; c++) pm[i].albedo[c] = mh[i].albedo[c];
-        pm[i].alpha = mh[i].alpha;
-        for (int c = 0; c < 4; c++) pm[i].style[c] = mh[i].style[c];
-        pm[i].roughness = mh[i].roughness;
-        pm[i].metallic = mh[i].metallic;
-        pm[i].ior = mh[i].ior;
-        pm[i].transmission = mh[i].transmission;
-        pm[i].specular_ior_level = mh[i].specular_ior_level;
-        pm[i].coat_weight = mh[i].coat_weight;
-        pm[i].coat_roughness = mh[i].coat_roughness;
-        pm[i].coat_ior = mh[i].coat_ior;
-        for (int c = 0; c < 3; c++) {
-            pm[i].specular_tint[c] = mh[i].specular_tint[c];
-            pm[i].coat_tint[c] = mh[i].coat_tint[c];
-        }
-    }
-    float bmin[3], bmax[3];
-    for (int a = 0; a < 3; a++) {
-        bmin[a] = cfg->has_scene_bounds ? cfg->scene_bounds[a] : job.bmin[a];
-        bmax[a] = cfg->has_scene_bounds ? cfg->scene_bounds[3 + a] : job.bmax[a];
-    }
-    const float avg = ((bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) + (bmax[2] - bmin[2])) / 3.0f;
     sty_status s = STY_OK;
-    for (uint32_t rep = 0; rep < cfg->repeats && s == STY_OK; rep++) {
-        s = job.trace(st);
-        for (int d = (int)D - 1; d >= 0 && s == STY_OK; d--) {
-            sty_pf_ref_params prm;
-            memset(&prm, 0, sizeof(prm));
-            prm.depth = (uint32_t)d;
-            const float rs = cfg->radius_scale[std::min<uint32_t>((uint32_t)d, cfg->n_radius_scale - 1)];
-            prm.radius = avg * 0.01f * rs;  // lm_path_filtering.rs:1579-1586
-            prm.reuse = cfg->reuse[std::min<uint32_t>((uint32_t)d, cfg->n_reuse - 1)];
-            prm.smis = cfg->smis;
-            prm.cluster = cfg->cluster;
-            prm.disable_flag_check = cfg->disable_flag_check;
-            prm.no_first_hit_stylization = cfg->no_first_hit_stylization;
-            prm.table_size = 1u << 26;
-            for (int a = 0; a < 3; a++) {
-                prm.pmin[a] = bmin[a];
-                prm.pmax[a] = bmax[a];
-            }
-            prm.max_cluster_rounds = 64;
-            const float *next = (uint32_t)d + 1 < D ? job.out((uint32_t)d + 1) : nullptr;
-            s = sty_pf_ref_filter(ctx, &job.vin[d], next, &prm, pm.data(), (uint32_t)pm.size(), programs, n_programs,
-                                  job.rng, job.out((uint32_t)d), nullptr, nullptr, stream);
+    if (screen) {
+        STY_TRY(job.init_records(nullptr));
+        const sty_camera &cam = scene_camera(scene);
+        for (uint32_t rep = 0; rep < cfg->repeats && s == STY_OK; rep++) {
+            s = job.trace(st);
+            if (s == STY_OK) s = screen_filter_job(job, cfg, programs, st);
+            if (s == STY_OK)
+                s = sty_film_accumulate(job.out(0), (int32_t)cam.width, (int32_t)cam.height, (int32_t)cfg->branch,
+                                        1.0 / cfg->repeats, film, st);
         }
-        if (s == STY_OK) {
-            k_splat<<<(npx + 255) / 256, 256, 0, st>>>(npx, cfg->branch, job.out(0), job.vo[0], job.sv.materials,
-                                                       job.dprog, n_programs, cfg->no_first_hit_stylization,
-                                                       1.0 / cfg->repeats, film);
-            s = check_launch("k_splat");
+    } else {
+        RenderCache &rc = *job.cache;
+        if (!rc.ctx || rc.ctx_cap < n) {
+            if (rc.ctx) sty_pf_ref_destroy(rc.ctx);
+            rc.ctx = nullptr;
+            rc.ctx_cap = 0;
+            STY_TRY(sty_pf_ref_create(n, 1u << 26, &rc.ctx));
+            rc.ctx_cap = n;
+        }
+        sty_pf_ref_ctx *ctx = rc.ctx;
+        const auto &mh = scene_materials(scene);
+        std::vector<sty_pf_material> pm(mh.size());
+        for (size_t i = 0; i < mh.size(); i++) {
+            pm[i].kind = mh[i].kind;
+            for (int c = 0; c < 3; c++) pm[i].albedo[c] = mh[i].albedo[c];
+            pm[i].alpha = mh[i].alpha;
+            for (int c = 0; c < 4; c++) pm[i].style[c] = mh[i].style[c];
+            pm[i].roughness = mh[i].roughness;
+            pm[i].metallic = mh[i].metallic;
+            pm[i].ior = mh[i].ior;
+            pm[i].transmission = mh[i].transmission;
+            pm[i].specular_ior_level = mh[i].specular_ior_level;
+            pm[i].coat_weight = mh[i].coat_weight;
+            pm[i].coat_roughness = mh[i].coat_roughness;
+            pm[i].coat_ior = mh[i].coat_ior;
+            for (int c = 0; c < 3; c++) {
+                pm[i].specular_tint[c] = mh[i].specular_tint[c];
+                pm[i].coat_tint[c] = mh[i].coat_tint[c];
+            }
+        }
+        float bmin[3], bmax[3];
+        for (int a = 0; a < 3; a++) {
+            bmin[a] = cfg->has_scene_bounds ? cfg->scene_bounds[a] : job.bmin[a];
+            bmax[a] = cfg->has_scene_bounds ? cfg->scene_bounds[3 + a] : job.bmax[a];
+        }
+        const float avg = ((bmax[0] - bmin[0]) + (bmax[1] - bmin[1]) + (bmax[2] - bmin[2])) / 3.0f;
+        for (uint32_t rep = 0; rep < cfg->repeats && s == STY_OK; rep++) {
+            s = job.trace(st);
+            for (int d = (int)D - 1; d >= 0 && s == STY_OK; d--) {
+                sty_pf_ref_params prm;
+                memset(&prm, 0, sizeof(prm));
+                prm.depth = (uint32_t)d;
+                const float rs = cfg->radius_scale[std::min<uint32_t>((uint32_t)d, cfg->n_radius_scale - 1)];
+                prm.radius = avg * 0.01f * rs;  // lm_path_filtering.rs:1579-1586
+                prm.reuse = cfg->reuse[std::min<uint32_t>((uint32_t)d, cfg->n_reuse - 1)];
+                prm.smis = cfg->smis;
+                prm.cluster = cfg->cluster;
+                prm.disable_flag_check = cfg->disable_flag_check;
+                prm.no_first_hit_stylization = cfg->no_first_hit_stylization;
+                prm.table_size = 1u << 26;
+                for (int a = 0; a < 3; a++) {
+                    prm.pmin[a] = bmin[a];
+                    prm.pmax[a] = bmax[a];
+                }
+                prm.max_cluster_rounds = 64;
+                const float *next = (uint32_t)d + 1 < D ? job.out((uint32_t)d + 1) : nullptr;
+                s = sty_pf_ref_filter(ctx, &job.vin[d], next, &prm, pm.data(), (uint32_t)pm.size(), programs,
+                                      n_programs, job.rng, job.out((uint32_t)d), nullptr, nullptr, stream);
+            }
+            if (s == STY_OK) {
+                k_splat<<<(npx + 255) / 256, 256, 0, st>>>(npx, cfg->branch, job.out(0), job.vo[0], job.sv.materials,
+                                                           job.dprog, n_programs, cfg->no_first_hit_stylization,
+                                                           1.0 / cfg->repeats, film);
+                s = check_launch("k_splat");
+            }
         }
     }
     if (s == STY_OK && vertex_count) {
@@ -787,6 +926,64 @@ extern "C" sty_status sty_pf_render(sty_scene *scene, const sty_pf_render_config
     }
     if (s == STY_OK) s = check_cuda(cudaStreamSynchronize(st), "sync render");
     return s;
+}
+
+extern "C" sty_status sty_pf_trace_records(sty_scene *scene, const sty_pf_render_config *cfg,
+                                           const sty_style_program *programs, uint32_t n_programs,
+                                           const sty_pf_records_out *records, uint64_t *vertex_count, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && cfg && records, "sty_pf_trace_records: null argument");
+    STY_TRY(check_render_config(cfg, programs, n_programs));
+    STY_ARG_CHECK(cfg->mode == STY_PF_MODE_SCREEN, "sty_pf_trace_records: the config is not a SCREEN-mode render");
+    for (int a = 0; a < 3; a++)
+        STY_ARG_CHECK(records->pos[a] && records->nrm[a] && records->rad[a] && records->thr[a],
+                      "sty_pf_trace_records: null record plane");
+    STY_ARG_CHECK(records->valid, "sty_pf_trace_records: null valid plane");
+    cudaStream_t st = as_stream(stream);
+    TraceJob job;
+    STY_TRY(job.init(scene, cfg->branch, cfg->max_depth, programs, n_programs, cfg->seed, st, 0, cfg->branch));
+    STY_TRY(job.init_records(records));
+    STY_TRY(job.trace(st));
+    if (vertex_count) {
+        unsigned long long h = 0;
+        STY_TRY(check_cuda(cudaMemcpyAsync(&h, job.vc, 8, cudaMemcpyDeviceToHost, st), "read vertex count"));
+        STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync trace"));
+        *vertex_count = h;
+    }
+    return STY_OK;
+}
+
+namespace sty {
+namespace {
+__global__ void k_camera_rays(CamArgs cam, uint32_t n, StdRngKey key, float *rays) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    sty_pcg32 g;  // Pcg32::new_seq_offset(i, seed_i), as k_rng_init
+    g.state = 0;
+    g.inc = ((uint64_t)i << 1) | 1ull;
+    pcg_next(g);
+    g.state += std_rng_u64(key.k, i);
+    pcg_next(g);
+    F3 o, d;
+    camera_ray(cam, i % (cam.W * cam.H), g, &o, &d);
+    float *r = rays + 8 * (size_t)i;
+    r[0] = o.x; r[1] = o.y; r[2] = o.z;
+    r[3] = d.x; r[4] = d.y; r[5] = d.z;
+    r[6] = 0.0f; r[7] = 1e20f;
+}
+}  // namespace
+}  // namespace sty
+
+extern "C" sty_status sty_scene_camera_rays(sty_scene *scene, uint32_t branch, uint64_t seed, float *rays,
+                                            void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && rays, "sty_scene_camera_rays: null argument");
+    const sty_camera &cam = scene_camera(scene);
+    const uint64_t n = (uint64_t)cam.width * cam.height * branch;
+    STY_ARG_CHECK(branch >= 1 && n < (1ull << 31), "sty_scene_camera_rays: bad branch %u", branch);
+    k_camera_rays<<<(unsigned)((n + 255) / 256), 256, 0, as_stream(stream)>>>(make_camera(cam), (uint32_t)n,
+                                                                            std_rng_key_of(seed), rays);
+    return check_launch("k_camera_rays");
 }
 
 extern "C" sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t layout, uint32_t spp, uint32_t max_depth,

@@ -8,6 +8,7 @@
 
 #include "bsdf.cuh"
 #include "common.cuh"
+#include "rng.cuh"
 #include "scene.cuh"
 #include "style.cuh"
 
@@ -205,6 +206,8 @@ struct CamArgs {
     float tan_half, aspect, radius;
     uint32_t W, H;
     uint32_t random_px;  // 1: path tid starts at pixel pcg32() % (W*H) (training paths, nrc_pt.rs:1394)
+    uint32_t filter;     // STY_FILTER_BOX / STY_FILTER_GAUSSIAN (PixelFilter, film.rs:20-48)
+    uint32_t pixel_major;  // k > 0: path slot tid is sample tid % k of pixel tid / k (screen-record order)
 };
 
 // One light sample for a vertex at p (sample_light, lm_path_filtering.rs:1261-1316): emitter chosen
@@ -268,16 +271,29 @@ __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
     return x ^ (x >> 31);
 }
-// Pcg32::new_seq_offset(i, seed_i) with seed_i = splitmix64(seed + i) (the reference draws seed_i
-// from rand's StdRng, sampler/mod.rs:157-173)
-__global__ void k_rng_init(uint32_t n, uint64_t seed, sty_pcg32 *rng) {
+// init_pcg32_buffer_with_seed (sampler/mod.rs:157-173): path slot i gets
+// Pcg32::new_seq_offset(i, seed_i), seed_i the i-th gen::<u64>() of StdRng::seed_from_u64(seed);
+// `key` is that generator's ChaCha12 key (std_rng_key)
+struct StdRngKey {
+    uint32_t k[8];
+};
+inline StdRngKey std_rng_key_of(uint64_t seed) {
+    StdRngKey r;
+    std_rng_key(seed, r.k);
+    return r;
+}
+// With pixel_major = k > 0 the slots are stored pixel-major (slot = px * k + b) but each keeps the
+// stream of the reference's slot b * npx + px, so a pixel sample draws the same numbers in either
+// order.
+__global__ void k_rng_init(uint32_t n, StdRngKey key, uint32_t pixel_major, uint32_t npx, sty_pcg32 *rng) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const uint32_t seq = pixel_major ? (i % pixel_major) * npx + i / pixel_major : i;
     sty_pcg32 g;
     g.state = 0;
-    g.inc = ((uint64_t)i << 1) | 1ull;
+    g.inc = ((uint64_t)seq << 1) | 1ull;
     pcg_next(g);
-    g.state += splitmix64(seed + i);
+    g.state += std_rng_u64(key.k, seq);
     pcg_next(g);
     rng[i] = g;
 }
@@ -312,17 +328,36 @@ __device__ __forceinline__ float bsdf_eval(const sty_scene_material &m, F3 ns, F
     return d * g1 * owh / fabsf(co) / (4.0f * owh);
 }
 
-// Camera ray of pixel px (camera/mod.rs:73-126, box pixel filter film.rs:31-33): 2 sampler draws
+// PixelFilter::sample (film.rs:30-48) of the sampler draw (u0, u1): box (u - 0.5) r; Gaussian
+// Box-Muller offset sigma (r cos 2 pi u1, r sin 2 pi u1), r = sqrt(-2 ln u0), sigma = radius / 3,
+// clamped to [-radius, radius] (u0 = 0 gives an infinite r; min(max(., -radius), radius) maps the
+// resulting infinities and NaNs to -radius or radius)
+__device__ __forceinline__ float2 pixel_filter_offset(const CamArgs &cam, float u0, float u1) {
+    if (cam.filter != STY_FILTER_GAUSSIAN)
+        return make_float2(__fmul_rn(__fsub_rn(u0, 0.5f), cam.radius), __fmul_rn(__fsub_rn(u1, 0.5f), cam.radius));
+    const float sigma = __fdiv_rn(cam.radius, 3.0f);
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, ex_ln(u0)));
+    float sn, cs;
+    ex_sincos_turns(u1, &sn, &cs);
+    const float ox = __fmul_rn(__fmul_rn(r, cs), sigma), oy = __fmul_rn(__fmul_rn(r, sn), sigma);
+    return make_float2(fminf(fmaxf(ox, -cam.radius), cam.radius), fminf(fmaxf(oy, -cam.radius), cam.radius));
+}
+// Camera ray of pixel px (PerspectiveCamera::generate_ray, camera/mod.rs:73-126): 2 sampler draws
+// for the pixel filter; film point (px + 0.5 + offset) mapped to the pinhole's direction; every
+// operation explicitly rounded (a CPU restatement reproduces it bit for bit)
 __device__ __forceinline__ void camera_ray(const CamArgs &cam, uint32_t px, sty_pcg32 &st, F3 *ro, F3 *rd) {
     const float fx = (float)(px % cam.W) + 0.5f, fy = (float)(px / cam.W) + 0.5f;
     const float u0 = next_1d(st), u1 = next_1d(st);
-    const float ox = (u0 - 0.5f) * cam.radius, oy = (u1 - 0.5f) * cam.radius;
-    const float sx = (2.0f * (fx + ox) / (float)cam.W - 1.0f) * cam.tan_half * cam.aspect;
-    const float sy = (1.0f - 2.0f * (fy + oy) / (float)cam.H) * cam.tan_half;
-    const F3 fwd = f3m(cam.fwd[0], cam.fwd[1], cam.fwd[2]), rt = f3m(cam.right[0], cam.right[1], cam.right[2]),
-             up = f3m(cam.up[0], cam.up[1], cam.up[2]);
+    const float2 o = pixel_filter_offset(cam, u0, u1);
+    const float ndx = __fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn(fx, o.x)), (float)cam.W), 1.0f);
+    const float ndy = __fsub_rn(1.0f, __fdiv_rn(__fmul_rn(2.0f, __fadd_rn(fy, o.y)), (float)cam.H));
+    const float sx = __fmul_rn(__fmul_rn(ndx, cam.tan_half), cam.aspect), sy = __fmul_rn(ndy, cam.tan_half);
+    const float dx = __fmaf_rn(cam.up[0], sy, __fmaf_rn(cam.right[0], sx, cam.fwd[0]));
+    const float dy = __fmaf_rn(cam.up[1], sy, __fmaf_rn(cam.right[1], sx, cam.fwd[1]));
+    const float dz = __fmaf_rn(cam.up[2], sy, __fmaf_rn(cam.right[2], sx, cam.fwd[2]));
+    const float inv = __fdiv_rn(1.0f, __fsqrt_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)))));
     *ro = f3m(cam.eye[0], cam.eye[1], cam.eye[2]);
-    *rd = normalize(fwd + rt * sx + up * sy);
+    *rd = f3m(__fmul_rn(dx, inv), __fmul_rn(dy, inv), __fmul_rn(dz, inv));
 }
 // Emitter radiance at a hit and its balance-heuristic weight against the light pdf seen from the
 // previous vertex (handle_surface_light, lm_path_filtering.rs:388-426 / branching_pt.rs:199-238;
@@ -360,11 +395,13 @@ __device__ __forceinline__ uint32_t update_flags(const sty_scene_material &m, ui
     return f;
 }
 
+// The camera frame in double, rounded once to float (no host FMA contraction or libm difference
+// between machines can change a bit of it).
 inline CamArgs make_camera(const sty_camera &cam) {
     CamArgs ca;
-    float f[3], r[3], u[3];
-    for (int a = 0; a < 3; a++) f[a] = cam.target[a] - cam.eye[a];
-    float l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    double f[3], r[3], u[3];
+    for (int a = 0; a < 3; a++) f[a] = (double)cam.target[a] - (double)cam.eye[a];
+    double l = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
     for (int a = 0; a < 3; a++) f[a] /= l;
     r[0] = f[1] * cam.up[2] - f[2] * cam.up[1];
     r[1] = f[2] * cam.up[0] - f[0] * cam.up[2];
@@ -376,16 +413,18 @@ inline CamArgs make_camera(const sty_camera &cam) {
     u[2] = r[0] * f[1] - r[1] * f[0];
     for (int a = 0; a < 3; a++) {
         ca.eye[a] = cam.eye[a];
-        ca.fwd[a] = f[a];
-        ca.right[a] = r[a];
-        ca.up[a] = u[a];
+        ca.fwd[a] = (float)f[a];
+        ca.right[a] = (float)r[a];
+        ca.up[a] = (float)u[a];
     }
-    ca.tan_half = std::tan(cam.fov_y * 0.5f * 3.14159265358979f / 180.0f);
-    ca.aspect = (float)cam.width / (float)cam.height;
+    ca.tan_half = (float)std::tan((double)cam.fov_y * 0.5 * 3.14159265358979323846 / 180.0);
+    ca.aspect = (float)((double)cam.width / (double)cam.height);
     ca.radius = cam.filter_radius;
     ca.W = cam.width;
     ca.H = cam.height;
     ca.random_px = 0;
+    ca.filter = (uint32_t)cam.filter;
+    ca.pixel_major = 0;
     return ca;
 }
 

@@ -32,9 +32,15 @@ class SceneMaterial(C.Structure):
                 ("coat_roughness", C.c_float), ("coat_ior", C.c_float), ("coat_tint", C.c_float * 3)]
 
 
+FILTER_BOX = 0
+FILTER_GAUSSIAN = 1
+PF_MODE_REF = 0
+PF_MODE_SCREEN = 1
+
+
 class Camera(C.Structure):
     _fields_ = [("eye", C.c_float * 3), ("target", C.c_float * 3), ("up", C.c_float * 3), ("fov_y", C.c_float),
-                ("width", C.c_uint32), ("height", C.c_uint32), ("filter_radius", C.c_float)]
+                ("width", C.c_uint32), ("height", C.c_uint32), ("filter_radius", C.c_float), ("filter", C.c_int32)]
 
 
 class RenderConfig(C.Structure):
@@ -42,7 +48,13 @@ class RenderConfig(C.Structure):
                 ("radius_scale", C.c_float * 16), ("n_radius_scale", C.c_uint32), ("reuse", C.c_uint32 * 16),
                 ("n_reuse", C.c_uint32), ("smis", C.c_int32), ("cluster", C.c_int32),
                 ("disable_flag_check", C.c_int32), ("no_first_hit_stylization", C.c_int32),
-                ("has_scene_bounds", C.c_int32), ("scene_bounds", C.c_float * 6), ("seed", C.c_uint64)]
+                ("has_scene_bounds", C.c_int32), ("scene_bounds", C.c_float * 6), ("seed", C.c_uint64),
+                ("mode", C.c_int32), ("screen_style", C.c_int32), ("screen", abi.PfScreenParams)]
+
+
+class RecordsOut(C.Structure):
+    _fields_ = [("pos", C.c_void_p * 3), ("nrm", C.c_void_p * 3), ("rad", C.c_void_p * 3), ("thr", C.c_void_p * 3),
+                ("valid", C.c_void_p), ("prim", C.c_void_p)]
 
 
 class NrcRenderConfig(C.Structure):
@@ -133,12 +145,29 @@ def glass(color=(1.0, 1.0, 1.0), ior=1.5, roughness=0.0, emission=(0, 0, 0), sty
     return m
 
 
-def camera(eye, target, up=(0, 1, 0), fov_y=40.0, width=256, height=256, filter_radius=1.0) -> Camera:
+def camera(eye, target, up=(0, 1, 0), fov_y=40.0, width=256, height=256, filter_radius=1.0,
+           filter=FILTER_BOX) -> Camera:
+    """Pinhole camera; `filter` is the pixel filter (FILTER_BOX or FILTER_GAUSSIAN, film.rs:20-48)
+    of radius `filter_radius` pixels."""
     c = Camera()
     c.eye[:] = list(eye)
     c.target[:] = list(target)
     c.up[:] = list(up)
     c.fov_y, c.width, c.height, c.filter_radius = fov_y, width, height, filter_radius
+    c.filter = filter
+    return c
+
+
+def screen_render_config(max_depth=5, branch=16, repeats=1, radius=8, sigma_pixel=4.0, sigma_pos=0.05,
+                         sigma_nrm=0.2, screen_style=0, seed=0) -> RenderConfig:
+    """An NL-PF render with the screen-space bilateral filter (STY_PF_MODE_SCREEN): the tracer's
+    vertex records of `branch` samples per pixel filtered over a (2 radius + 1)^2 pixel window with
+    the program programs[screen_style] (-1: none)."""
+    c = render_config(max_depth=max_depth, branch=branch, repeats=repeats, seed=seed)
+    c.mode = PF_MODE_SCREEN
+    c.screen_style = screen_style
+    c.screen.radius, c.screen.sigma_pixel, c.screen.sigma_pos, c.screen.sigma_nrm = (radius, sigma_pixel, sigma_pos,
+                                                                                     sigma_nrm)
     return c
 
 
@@ -404,6 +433,40 @@ class Scene:
         check(lib().sty_pf_render(self.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(vc),
                                   _stream_ptr(stream)))
         return film, vc.value
+
+    def trace_records(self, cfg: RenderConfig, programs=(), with_prim=False, stream=None):
+        """The screen-space records a SCREEN-mode render filters (sty_pf_trace_records): returns
+        (RecordSet over device planes, prim ids [depths, H, W, branch] or None, vertex count)."""
+        import torch
+        from .pf import RecordSet, _stream_ptr
+        W, H, S, D = self.camera.width, self.camera.height, cfg.branch, cfg.max_depth + 1
+        n = D * H * W * S
+        planes = torch.empty((12, n), dtype=torch.float32, device="cuda")
+        valid = torch.empty(n, dtype=torch.int32, device="cuda")
+        prim = torch.empty((D, H, W, S), dtype=torch.int32, device="cuda") if with_prim else None
+        ro = RecordsOut()
+        for a in range(3):
+            ro.pos[a] = planes[a].data_ptr()
+            ro.nrm[a] = planes[3 + a].data_ptr()
+            ro.rad[a] = planes[6 + a].data_ptr()
+            ro.thr[a] = planes[9 + a].data_ptr()
+        ro.valid = valid.data_ptr()
+        ro.prim = prim.data_ptr() if prim is not None else None
+        progs = list(programs)
+        arr = (abi.StyleProgram * max(1, len(progs)))(*progs) if progs else None
+        vc = C.c_uint64()
+        check(lib().sty_pf_trace_records(self.h, C.byref(cfg), arr, len(progs), C.byref(ro), C.byref(vc),
+                                         _stream_ptr(stream)))
+        return RecordSet(planes, valid, W, H, S, D), prim, vc.value
+
+    def camera_rays(self, branch: int, seed: int = 0, stream=None):
+        """Depth-0 rays [W*H*branch, 8] (device) of every path slot (sty_scene_camera_rays)."""
+        import torch
+        from .pf import _stream_ptr
+        n = self.camera.width * self.camera.height * branch
+        rays = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+        check(lib().sty_scene_camera_rays(self.h, branch, seed, rays.data_ptr(), _stream_ptr(stream)))
+        return rays
 
     def nrc_samples(self, mode: int, spp: int, max_depth: int, layout: int = NRC_ROWS_SPHERICAL, seed: int = 0,
                     capacity: int | None = None, stream=None):

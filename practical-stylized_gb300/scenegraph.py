@@ -307,6 +307,20 @@ def transform_matrix(tr, is_camera=False):
     raise ValueError(f"unknown transform {tr['type']}")
 
 
+def apply_film_filter(cam, method_config):
+    """The pixel filter of a method config's `film.filter` (PixelFilter, film.rs:20-48: {"type": "box"
+    | "gaussian", "radius": r}) set on a loaded camera; no `film.filter` keeps the reference's default,
+    the Gaussian of radius 1.5 (film.rs:50-54). Returns the camera."""
+    from .scene import FILTER_BOX, FILTER_GAUSSIAN
+    filt = ((method_config or {}).get("film") or {}).get("filter") or {"type": "gaussian", "radius": 1.5}
+    kinds = {"box": FILTER_BOX, "gaussian": FILTER_GAUSSIAN}
+    if filt.get("type") not in kinds:
+        raise UnsupportedNode(f"pixel filter {filt.get('type')}")
+    cam.filter = kinds[filt["type"]]
+    cam.filter_radius = float(filt.get("radius", 1.5))
+    return cam
+
+
 def load_camera(cam, width=None, height=None):
     if cam["type"] != "perspective":
         raise UnsupportedNode(f"camera {cam['type']}")

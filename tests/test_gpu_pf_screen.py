@@ -48,6 +48,18 @@ def test_filter_depth_matches_oracle(sty, orc, cuda, S, R):
     assert rel_err(got_o[:, m], ref_o[:, m], 1e-6).max() < TOL
 
 
+@pytest.mark.parametrize("R", [0, 3, 8, 16])
+def test_filter_depth_16spp_matches_oracle(sty, orc, cuda, R):
+    """16 samples per pixel (the traced Cornell-box render's 16 paths per pixel): four threads
+    share a pixel's queries."""
+    W, H, S, D = 45, 21, 16, 1
+    planes, valid, rs, hrec = _setup(sty, W, H, S, D, seed=1600 + R)
+    prm = sty.ScreenParams(radius=R, sigma_pixel=max(R / 2, 1.0), sigma_pos=0.5, sigma_nrm=0.2)
+    _, got_o, ref_o, _, m, ef = _depth_parity(sty, orc, rs, hrec, valid, 0, prm, None)
+    assert ef < TOL, f"filtered rel err {ef:.3e}"
+    assert rel_err(got_o[:, m], ref_o[:, m], 1e-6).max() < TOL
+
+
 def test_full_chain_c2_style(sty, orc, cuda):
     """All depths with the C2 toon node at depth 1, each depth checked against the oracle run
     on the GPU's own deeper-depth output (identical dumped buffers)."""

@@ -102,8 +102,12 @@ def test_query_rows_both_layouts(sty, cornell):
         th, ph = t * np.pi, p * 2 * np.pi - np.pi
         return np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], 1)
 
-    np.testing.assert_allclose(unsph(xs[hit, 3], xs[hit, 4]), xr[hit, 3:6] * 2 - 1, atol=2e-5)
-    np.testing.assert_allclose(unsph(xs[hit, 5], xs[hit, 6]), xr[hit, 6:9] * 2 - 1, atol=2e-5)
+    # theta = acos(z) loses digits near the poles (d theta = dz / sin theta): the allowance grows there
+    for a, b in ((3, 3), (5, 6)):
+        ref = xr[hit, b:b + 3] * 2 - 1
+        sin_t = np.sqrt(np.maximum(1.0 - ref[:, 2] ** 2, 1e-12))
+        err = np.abs(unsph(xs[hit, a], xs[hit, a + 1]) - ref).max(1)
+        assert (err <= 2e-5 + 2e-7 / sin_t).all(), err.max()
     np.testing.assert_array_equal(xs[hit, 7:11], xr[hit, 9:13])
     assert (xr[hit, 19] == 1).all() and (xr[hit, 20:] == 0).all()  # depth one-hot 0
 
@@ -123,6 +127,14 @@ def test_bad_arguments_rejected(sty, cornell):
     # training rows beyond the capacity are dropped, not written
     assert lib.sty_nrc_samples(sc.h, 0, 1, 1, D, 0, x.data_ptr(), y.data_ptr(), 16, C.byref(cnt), None) == 0
     assert cnt.value == 16
+
+
+def _sees_light(sty, sc, spp=64):
+    """Pixels whose footprint covers some of the emitter: any of `spp` first hits is on the light.
+    Their radiance (17 where covered) dwarfs the rest of the image, so an edge pixel a few samples
+    miss would otherwise dominate an MSE meant for the indirectly lit pixels."""
+    _, le = sc.nrc_samples(sty.scene.NRC_SAMPLES_QUERY, spp, D, seed=99)
+    return (le.reshape(spp, H, W, 3).amax((0, 3)) > 0).cpu().numpy()
 
 
 def _train_cache(sty, sc, precision, frames, iters, spp=4, lr=1e-2, seed=0):
@@ -152,8 +164,8 @@ def test_trained_cache_beats_cache_free_render(sty, cornell):
     sc, _ = cornell
     gt, _ = sc.render(_self_only(sty, 4242, 256, repeats=8))
     gt = gt.cpu().numpy()
-    xq, le = sc.nrc_samples(sty.scene.NRC_SAMPLES_QUERY, 4, D, seed=5)
-    lit = (le.reshape(4, H, W, 3).amax((0, 3)) > 0).cpu().numpy()
+    xq, _ = sc.nrc_samples(sty.scene.NRC_SAMPLES_QUERY, 4, D, seed=5)
+    lit = _sees_light(sty, sc)
 
     def mse(im, mask=None):
         e = ((im - gt) ** 2).mean(2)
@@ -223,7 +235,9 @@ def test_nrc_render_final_gather(sty, cornell):
     sc, _ = cornell
     gt, _ = sc.render(_self_only(sty, 4242, 256, repeats=8))
     gt = gt.cpu().numpy()
-    mse_pt = np.mean([np.mean((sc.render(_self_only(sty, 10 + s, 1))[0].cpu().numpy() - gt) ** 2) for s in range(8)])
+    dk = ~_sees_light(sty, sc)
+    mse_pt = np.mean([np.mean(((sc.render(_self_only(sty, 10 + s, 1))[0].cpu().numpy() - gt) ** 2)[dk])
+                      for s in range(8)])
     out = {}
     for fg in (0, 16, 16):
         net = sty.nrc.NRC(sty.nrc.config(precision=sty.nrc.STY_NRC_BF16, batch_size=1 << 12, learning_rate=1e-2,
@@ -236,8 +250,11 @@ def test_nrc_render_final_gather(sty, cornell):
         out.setdefault(fg, []).append(img)
         net.close()
     assert (out[16][0] == out[16][1]).all()
-    m0 = float(np.mean((out[0][0] - gt) ** 2))
-    m16 = float(np.mean((out[16][0] - gt) ** 2))
-    print(f"final gather mse {m16:.5f}, first-hit cache {m0:.5f}, 1spp {mse_pt:.5f}")
+    # on the pixels that do not see the emitter (final gathering improves the indirect light; at the
+    # emitter's edge both renders carry the same coverage noise of the 4 camera samples)
+    dark = ~_sees_light(sty, sc)
+    m0 = float(np.mean(((out[0][0] - gt) ** 2)[dark]))
+    m16 = float(np.mean(((out[16][0] - gt) ** 2)[dark]))
+    print(f"final gather mse {m16:.5f}, first-hit cache {m0:.5f}, 1spp {mse_pt:.5f} (pixels off the emitter)")
     assert m16 < m0 and m16 < 0.5 * mse_pt
     assert sty.abi.device_status() == 0

@@ -1,0 +1,189 @@
+"""NL-PF on traced path vertices with the screen-space bilateral filter (STY_PF_MODE_SCREEN): the
+wavefront tracer writes every depth's vertices as screen records, the filter runs from max_depth
+down to 0, the depth-0 result is splatted into the FP64 film (lm_path_filtering.rs:1629-1793 with
+the bilateral filter in place of the hash-grid one).
+
+- records dumped from the tracer (sty_pf_trace_records) are filtered on the GPU within 1e-5 of the
+  FP64 oracle on those exact buffers, at every depth (the oracle fed the GPU's own deeper output);
+- the dumped first hits are the oracle's: the oracle regenerates every camera ray from the seeded
+  streams (ChaCha12 seeds -> Pcg32 -> pixel filter -> pinhole) and its brute-force closest hit
+  gives the same triangle id for every depth-0 record, bit for bit;
+- sty_pf_render in SCREEN mode equals the dump filtered and splatted, bit for bit;
+- with a window that lets every vertex see only itself the render is the NEE + MIS path tracer
+  and converges to the independent FP64 CPU path tracer;
+- at the Cornell workload's full size (256 x 256 x 16 spp, depth 5, radius 8) sampled records of
+  every depth match the FP64 oracle evaluated at just those records."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+THRESH = (0.1, 0.3, 0.6)
+
+
+def _style(a):
+    """4-level toon of the first-bounce radiance (depth 1), thresholds 0.1 / 0.3 / 0.6."""
+    return a.style_program([a.toon_steps(list(THRESH), [0.05, 0.2, 0.45, 1.0], depth_mask=1 << 1)])
+
+
+def _cornell(sty, W, H, **kw):
+    pos, mids, mats, cam = sty.scene.cornell_box(W, H)
+    for k, v in kw.items():
+        setattr(cam, k, v)
+    return pos, mids, mats, cam, sty.scene.Scene(pos, mids, mats, cam)
+
+
+def _host_planes(rs):
+    import torch
+    torch.cuda.synchronize()
+    planes = rs.planes.cpu().numpy()
+    valid = rs.valid.cpu().numpy()
+    return planes, valid
+
+
+def _prm(cfg, sty):
+    s = cfg.screen
+    return sty.ScreenParams(radius=s.radius, sigma_pixel=s.sigma_pixel, sigma_pos=s.sigma_pos, sigma_nrm=s.sigma_nrm)
+
+
+@pytest.mark.parametrize("filt", [0, 1])
+def test_traced_records_filter_matches_oracle(sty, orc, cuda, filt):
+    import torch
+    W, H, B, D = 48, 32, 16, 5
+    pos, mids, mats, cam, sc = _cornell(sty, W, H, filter=filt, filter_radius=1.5 if filt else 1.0)
+    cfg = sty.scene.screen_render_config(max_depth=D, branch=B, radius=8, sigma_pixel=0.0, sigma_pos=0.05,
+                                         sigma_nrm=0.2, screen_style=0, seed=0)
+    progs = [_style(sty.abi)]
+    rs, prim, nv = sc.trace_records(cfg, progs, with_prim=True)
+    planes, valid = _host_planes(rs)
+    n = W * H * B
+    assert nv == int(valid.sum()) and nv > n  # depth-0 hits plus deeper vertices
+    # first hits: the oracle's camera rays and brute-force closest hit, bit for bit
+    rays = orc.camera_rays(cam, B, 0)
+    rp, _, _ = orc.closest_hit(pos, rays)
+    ref_prim = rp.reshape(B, H * W).T.reshape(-1)  # slot b * npx + px -> record px * B + b
+    got_prim = prim.cpu().numpy().reshape(D + 1, -1)[0].view(np.uint32)
+    assert (got_prim == ref_prim).all(), f"{(got_prim != ref_prim).sum()} first-hit ids differ"
+    assert (valid[:n].astype(bool) == (ref_prim != 0xFFFFFFFF)).all()
+    # the filter on the dumped buffers, every depth, against the FP64 oracle
+    hrec = sty.pf.host_records(planes, valid, W, H, B, D + 1)
+    prm = _prm(cfg, sty)
+    out_all = sty.pf_screen_filter(rs, prm, progs[0])
+    torch.cuda.synchronize()
+    for d in range(D, -1, -1):
+        filt_dev = torch.empty((3, n), dtype=torch.float32, device="cuda")
+        nxt = out_all[d + 1] if d < D else None
+        o = sty.pf_screen_filter_depth(rs, d, prm, progs[0], out_next=nxt, filtered=filt_dev)
+        torch.cuda.synchronize()
+        ref_o, ref_f = orc.pf_screen_filter_depth(hrec, d, prm.c(), progs[0],
+                                                  out_next=None if nxt is None else nxt.cpu().numpy().astype(np.float64),
+                                                  want_filtered=True)
+        m = valid[d * n:(d + 1) * n].astype(bool)
+        got_f, got_o = filt_dev.cpu().numpy(), o.cpu().numpy()
+        assert (got_o == out_all[d].cpu().numpy()).all()
+        if not m.any():
+            continue
+        scale = np.abs(ref_f[:, m]).max()
+        ef = (np.abs(got_f[:, m] - ref_f[:, m]) / np.maximum(np.abs(ref_f[:, m]), 1e-6 * scale)).max()
+        assert ef < TOL, f"depth {d}: filtered rel err {ef:.3e}"
+        lum = ref_f[0] * 0.2126 + ref_f[1] * 0.7152 + ref_f[2] * 0.0722
+        near = np.zeros(n, dtype=bool)
+        if d == 1:
+            for t in THRESH:
+                near |= np.abs(lum - t) <= 1e-5 * t
+        keep = m & ~near
+        eo = (np.abs(got_o[:, keep] - ref_o[:, keep]) / np.maximum(np.abs(ref_o[:, keep]), 1e-6 * scale)).max()
+        assert eo < TOL, f"depth {d}: output rel err {eo:.3e}"
+    sc.close()
+
+
+def test_screen_render_equals_filtered_dump(sty, cuda):
+    import torch
+    W, H, B, D = 40, 24, 4, 3
+    *_, sc = _cornell(sty, W, H, filter=1, filter_radius=1.5)
+    cfg = sty.scene.screen_render_config(max_depth=D, branch=B, radius=6, sigma_pixel=3.0, sigma_pos=0.05,
+                                         sigma_nrm=0.2, screen_style=0, seed=9)
+    progs = [_style(sty.abi)]
+    film, nv = sc.render(cfg, progs)
+    rs, _, nv2 = sc.trace_records(cfg, progs)
+    out = sty.pf_screen_filter(rs, _prm(cfg, sty), progs[0])
+    ref = torch.zeros_like(film)
+    sty.pf.film_accumulate(out[0], W, H, B, 1.0, ref)
+    torch.cuda.synchronize()
+    assert nv == nv2 > 0
+    assert torch.equal(film, ref)
+    f2, _ = sc.render(cfg, progs)  # deterministic
+    assert torch.equal(film, f2)
+    assert sty.abi.device_status() == 0
+    sc.close()
+
+
+def test_self_only_screen_render_matches_cpu_path_tracer(sty, cuda):
+    """A window of one pixel and a position bandwidth far below the spacing of distinct hits: each
+    vertex keeps only itself, the estimator is the NEE + MIS path tracer and the render converges to
+    the independent FP64 CPU path tracer."""
+    W = H = 32
+    D = 4
+    pos, mids, mats, cam, sc = _cornell(sty, W, H)
+    cfg = sty.scene.screen_render_config(max_depth=D, branch=16, repeats=16, radius=0, sigma_pixel=0.0,
+                                         sigma_pos=1e-7, sigma_nrm=0.2, screen_style=-1, seed=5)
+    film, nv = sc.render(cfg)
+    img = film.cpu().numpy()
+    alb = np.array([m.albedo[:] for m in mats], np.float32)
+    em = np.array([m.emission[:] for m in mats], np.float32)
+    camv = list(cam.eye) + list(cam.target) + list(cam.up) + [cam.fov_y, W, H, cam.filter_radius]
+    ref = oracle.path_trace(pos, mids, alb, em, camv, 256, D, seed=11)
+    assert np.isfinite(img).all()
+    m_img, m_ref = img.mean(), ref.mean()
+    assert abs(m_img - m_ref) < 0.02 * m_ref, (m_img, m_ref)
+    bi = img.reshape(4, 8, 4, 8, 3).mean((1, 3))
+    br = ref.reshape(4, 8, 4, 8, 3).mean((1, 3))
+    rel = np.abs(bi - br) / np.maximum(br, 0.05 * m_ref)
+    assert rel.max() < 0.15, rel.max()
+    sc.close()
+
+
+def test_cornell_workload_full_size_sampled(sty, orc, cuda):
+    """The plain NL-PF workload at full size: 256 x 256, 16 paths per pixel, depth 5, radius 8 px,
+    sigma_pos 0.05, sigma_nrm 0.2, toon 0.1 / 0.3 / 0.6 at the first bounce: 1500 sampled valid
+    records per depth against the FP64 oracle evaluated at just those records (fed the GPU's deeper
+    output); the filtered planes are finite and the film is lit."""
+    import torch
+    W = H = 256
+    B, D = 16, 5
+    *_, sc = _cornell(sty, W, H)
+    cfg = sty.scene.screen_render_config(max_depth=D, branch=B, radius=8, sigma_pixel=0.0, sigma_pos=0.05,
+                                         sigma_nrm=0.2, screen_style=0, seed=0)
+    progs = [_style(sty.abi)]
+    rs, _, nv = sc.trace_records(cfg, progs)
+    prm = _prm(cfg, sty)
+    out = sty.pf_screen_filter(rs, prm, progs[0])
+    torch.cuda.synchronize()
+    planes, valid = _host_planes(rs)
+    hrec = sty.pf.host_records(planes, valid, W, H, B, D + 1)
+    n = W * H * B
+    rng = np.random.default_rng(3)
+    outs = out.cpu().numpy()
+    assert np.isfinite(outs).all()
+    for d in range(D, -1, -1):
+        vi = np.flatnonzero(valid[d * n:(d + 1) * n])
+        if vi.size == 0:
+            continue
+        idx = np.sort(rng.choice(vi, size=min(1500, vi.size), replace=False)).astype(np.uint64)
+        nxt = outs[d + 1].astype(np.float64) if d < D else None
+        ref_o, ref_f = orc.pf_screen_filter_records(hrec, d, prm.c(), progs[0], idx, out_next=nxt)
+        filt = torch.empty((3, n), dtype=torch.float32, device="cuda")
+        sty.pf_screen_filter_depth(rs, d, prm, progs[0], out_next=out[d + 1] if d < D else None, filtered=filt)
+        torch.cuda.synchronize()
+        got_f = filt.cpu().numpy()[:, idx.astype(np.int64)]
+        scale = np.abs(ref_f).max()
+        ef = (np.abs(got_f - ref_f) / np.maximum(np.abs(ref_f), 1e-6 * scale)).max()
+        assert ef < TOL, f"depth {d}: filtered rel err {ef:.3e}"
+    film, nv2 = sc.render(cfg, progs)
+    img = film.cpu().numpy()
+    assert nv2 == nv and np.isfinite(img).all() and img.mean() > 0.01
+    sc.close()

@@ -163,3 +163,20 @@ def test_synthetic_scene_renders(sty, cuda, tmp_path):
     film, nv = scene.render(cfg, sc["programs"])
     img = film.cpu().numpy()
     assert nv > 0 and np.isfinite(img).all() and img.mean() > 0
+
+
+def test_film_filter_from_method_config(sty):
+    """film.filter of a method config (the teaser configs select {"type": "gaussian", "radius": 1.5})
+    sets the camera's pixel filter; no entry keeps the reference's default Gaussian of radius 1.5."""
+    sg, sc = sty.scenegraph, sty.scene
+    cam = sc.camera((0, 0, 1), (0, 0, 0))
+    assert cam.filter == sc.FILTER_BOX
+    sg.apply_film_filter(cam, {"film": {"filter": {"type": "gaussian", "radius": 1.5}}})
+    assert cam.filter == sc.FILTER_GAUSSIAN and abs(cam.filter_radius - 1.5) < 1e-7
+    sg.apply_film_filter(cam, {"film": {"filter": {"type": "box", "radius": 0.5}}})
+    assert cam.filter == sc.FILTER_BOX and abs(cam.filter_radius - 0.5) < 1e-7
+    sg.apply_film_filter(cam, {})
+    assert cam.filter == sc.FILTER_GAUSSIAN and abs(cam.filter_radius - 1.5) < 1e-7
+    import pytest
+    with pytest.raises(sg.UnsupportedNode):
+        sg.apply_film_filter(cam, {"film": {"filter": {"type": "mitchell"}}})
