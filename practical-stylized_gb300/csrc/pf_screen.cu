@@ -452,7 +452,14 @@ sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth,
         case 4:  // the warp-specialised kernel's shared-memory ring fits up to radius 24
             return a.R <= 24 ? launch_screen_s4(a, prog, st) : launch_screen<4>(a, prog, st);
         case 8: return launch_screen<8>(a, prog, st);
-        default: return launch_screen_g<16, 4>(a, prog, st);
+        default: {  // the warp-specialised kernel where its shared-memory ring fits
+            int dev = 0, optin = 0;
+            STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+            STY_TRY(check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev),
+                               "cudaDeviceGetAttribute(max shared memory)"));
+            return a.R <= screen_ws_max_radius(16, (size_t)optin) ? launch_screen_s16(a, prog, st)
+                                                                  : launch_screen_g<16, 4>(a, prog, st);
+        }
     }
 }
 

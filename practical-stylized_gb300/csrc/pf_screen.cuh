@@ -22,7 +22,10 @@ struct ScreenArgs {
     uint32_t *status;  // device status word (STY_DEV_* bits)
 };
 
-// Warp-specialised spp=4 kernel (pf_screen4.cu).
+// Warp-specialised kernels for 4 and 16 spp (pf_screen4.cu), and the largest radius they serve
+// with `optin` bytes of shared memory per block.
 sty_status launch_screen_s4(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st);
+sty_status launch_screen_s16(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st);
+int screen_ws_max_radius(int spp, size_t optin);
 
 }  // namespace sty
