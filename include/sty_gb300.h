@@ -332,8 +332,11 @@ STY_API sty_status sty_pf_adjoint(const sty_pf_records *rec, uint32_t depth, int
  * on it until the process exits. Same arguments and results as sty_pf_adjoint; limits: at most
  * 2^18 records per depth (width * height * spp), 2^16 pixels and 4096 32x8 tiles, larger inputs
  * are rejected with STY_ERR_ARG. It calls no cudaMalloc / cudaFree. Its first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that first call before any
- * stream capture. All calls share the one array: calls whose work overlaps on the GPU (other
+ * looks up the array's device address (cudaGetSymbolAddress) with that device current, and looks
+ * it up again if the device's context was replaced (cudaDeviceReset); make that first call before
+ * any stream capture. A non-null loss_out is read back with a stream synchronisation, as in
+ * sty_pf_adjoint. All calls share the one array, which keeps the last call's contents (every
+ * region is fully written before it is read): calls whose work overlaps on the GPU (other
  * streams, other host threads) race and must be serialised by the caller. */
 STY_API sty_status sty_pf_adjoint_noalloc(const sty_pf_records *rec, uint32_t depth, int32_t radius,
                                           const float params[36], uint32_t n_steps, const float *in_next,

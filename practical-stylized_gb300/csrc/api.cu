@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "common.cuh"
 #include "rng.cuh"
@@ -62,19 +63,56 @@ bool style_program_valid(const sty_style_program *p) {
     return true;
 }
 
+// Unique id of the calling thread's current CUDA context (0 if there is none or the driver does not
+// say). A device address looked up for a module symbol is valid only while the context that loaded
+// the module lives: cudaDeviceReset destroys the primary context and the next use reloads the
+// module, possibly at another address, so such caches are keyed on this id.
+uint64_t current_context_id() {
+    using GetCurrent = int (*)(void **);                  // CUresult cuCtxGetCurrent(CUcontext *)
+    using GetId = int (*)(void *, unsigned long long *);  // CUresult cuCtxGetId(CUcontext, unsigned long long *)
+    static GetCurrent get_cur = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<GetCurrent>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<GetId>(f);
+    });
+    if (!get_cur || !get_id) return 0;
+    void *ctx = nullptr;
+    if (get_cur(&ctx) != 0 || !ctx) return 0;
+    unsigned long long id = 0;
+    if (get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
 // Device status word: one per device (a __device__ variable exists once per device context).
 static __device__ uint32_t g_device_status = 0;
 
 uint32_t *device_status_ptr() {
-    static uint32_t *cache[64] = {nullptr};
+    struct Entry {
+        uint32_t *ptr = nullptr;
+        uint64_t ctx = 0;
+    };
+    static Entry cache[64];
+    static std::mutex mu;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    if (!cache[dev]) {
+    std::lock_guard<std::mutex> lock(mu);
+    const uint64_t ctx = current_context_id();
+    if (!cache[dev].ptr || ctx == 0 || cache[dev].ctx != ctx) {
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_device_status) != cudaSuccess) return nullptr;
-        cache[dev] = static_cast<uint32_t *>(p);
+        cache[dev].ptr = static_cast<uint32_t *>(p);
+        cache[dev].ctx = current_context_id();
     }
-    return cache[dev];
+    return cache[dev].ptr;
 }
 
 // ---- kernels ------------------------------------------------------------------------------

@@ -21,6 +21,9 @@ void count_launch(uint64_t n = 1);
 
 // Device status word of the current device (bits STY_DEV_*); kernels OR failure bits into it.
 uint32_t *device_status_ptr();
+// Unique id of the calling thread's current CUDA context, 0 if unknown: keys caches of device
+// addresses of module symbols (a device reset reloads the module).
+uint64_t current_context_id();
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 

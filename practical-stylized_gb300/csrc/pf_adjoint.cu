@@ -13,6 +13,8 @@
 // sweep 1 rebuilds D_i, N_i (hence f_i and h_i), sweep 2 accumulates the three bandwidth sums.
 // Per-thread results are reduced per block into a partial vector; a final single-block kernel sums
 // the partials in a fixed order (deterministic).
+#include <mutex>
+
 #include "common.cuh"
 #include "pf_screen.cuh"
 #include "style.cuh"
@@ -498,23 +500,31 @@ constexpr size_t kNaFloats = kNaLoss + 64;                  // 1,130,816 floats 
 // stand-in for the symbol; the device address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) float g_adjoint_scratch[kNaFloats];
 
-// Device address of g_adjoint_scratch on the current device, looked up once per device.
+// Device address of g_adjoint_scratch on the current device, looked up with that device current on
+// the first call there (and again if the device's context was replaced: a device reset reloads the
+// module, possibly at another address).
 sty_status noalloc_scratch(float **out) {
-    static std::atomic<float *> cache[64];
+    struct Entry {
+        float *ptr = nullptr;
+        uint64_t ctx = 0;
+    };
+    static Entry cache[64];
+    static std::mutex mu;
     int dev = -1;
     STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
     if (dev < 0 || dev >= 64) {
         set_error("device ordinal %d out of range", dev);
         return STY_ERR_UNSUPPORTED;
     }
-    float *p = cache[dev].load();
-    if (!p) {
+    std::lock_guard<std::mutex> lock(mu);
+    const uint64_t ctx = current_context_id();
+    if (!cache[dev].ptr || ctx == 0 || cache[dev].ctx != ctx) {
         void *addr = nullptr;
         STY_TRY(check_cuda(cudaGetSymbolAddress(&addr, g_adjoint_scratch), "cudaGetSymbolAddress(adjoint scratch)"));
-        p = static_cast<float *>(addr);
-        cache[dev].store(p);
+        cache[dev].ptr = static_cast<float *>(addr);
+        cache[dev].ctx = current_context_id();
     }
-    *out = p;
+    *out = cache[dev].ptr;
     return STY_OK;
 }
 }  // namespace

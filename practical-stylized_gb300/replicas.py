@@ -38,13 +38,15 @@ def replica_seed(seed: int, rank: int) -> int:
 
 def merge_film(film: torch.Tensor, count: int, group=None) -> torch.Tensor:
     """The repeat-weighted mean of every rank's film (each the mean over its own `count` repeats),
-    returned on every rank. FP64; one all-reduce of film * count and one of the counts. Without an
-    initialised process group the film is returned as it is."""
+    returned on every rank. FP64; one all-reduce of film * count and one of the counts. A rank with
+    no repeats (count 0, more ranks than repeats) renders nothing: its film is not read (it adds
+    zeros, so an unset film holding NaN cannot poison the merge). Without an initialised process
+    group the film is returned as it is."""
     if film.dtype != torch.float64:
         raise TypeError("merge_film wants the FP64 film")
     if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
         return film.clone()
-    acc = film * float(count)
+    acc = film * float(count) if count > 0 else torch.zeros_like(film)
     n = torch.tensor([float(count)], dtype=torch.float64, device=film.device)
     torch.distributed.all_reduce(acc, group=group)
     torch.distributed.all_reduce(n, group=group)

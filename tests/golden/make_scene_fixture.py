@@ -1,12 +1,21 @@
 """Writes tests/golden/scene_sty_materials.json from the reference's stylized teaser scene
 (scenes/veach-ajar-sty-v2/scene-sty.json): its camera and every material's shader graph, pruned to
-the nodes reachable from the material's output node. Run in a checkout that has the reference at
-$STY_REFERENCE (the geometry buffer Scene.bin is not needed and not read)."""
+the nodes reachable from the material's output node. Usage: python make_scene_fixture.py
+<reference checkout> (or set STY_REFERENCE); the geometry buffer Scene.bin is not needed and not
+read."""
 import json
 import os
 import pathlib
+import sys
 
-SRC = pathlib.Path(os.environ.get("STY_REFERENCE", "/root/reference")) / "scenes/veach-ajar-sty-v2/scene-sty.json"
+
+def _source() -> pathlib.Path:
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STY_REFERENCE")
+    if not root:
+        sys.exit("usage: make_scene_fixture.py <reference checkout>  (or set STY_REFERENCE)")
+    return pathlib.Path(root) / "scenes/veach-ajar-sty-v2/scene-sty.json"
+
+
 OUT = pathlib.Path(__file__).with_name("scene_sty_materials.json")
 
 
@@ -32,7 +41,7 @@ def reachable(nodes, root):
 
 
 def main():
-    g = json.loads(SRC.read_text())
+    g = json.loads(_source().read_text())
     mats = {}
     for name, m in g["materials"].items():
         nodes = m["shader"]["nodes"]

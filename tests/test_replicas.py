@@ -17,7 +17,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank_main(rank, world, port, out):
+def _rank_main(rank, world, port, out, total=7):
     import sys
     sys.path.insert(0, os.getcwd())
     import __graft_entry__ as g
@@ -25,11 +25,14 @@ def _rank_main(rank, world, port, out):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     torch.distributed.init_process_group("gloo", rank=rank, world_size=world)
     try:
-        total = 7
         first, count = rp.shard_repeats(total, world, rank)
-        # each rank's film: the mean over its repeats of a per-repeat image f(r) = r + pixel index
+        # each rank's film: the mean over its repeats of a per-repeat image f(r) = r + pixel index;
+        # a rank without repeats never renders, so its film is left unset (NaN)
         px = torch.arange(6, dtype=torch.float64)
-        film = torch.stack([r + px for r in range(first, first + count)]).mean(0)
+        if count:
+            film = torch.stack([r + px for r in range(first, first + count)]).mean(0)
+        else:
+            film = torch.full((6,), float("nan"), dtype=torch.float64)
         merged = rp.merge_film(film, count)
         t = rp.max_over_ranks(10.0 * (rank + 1))
         out.put((rank, first, count, merged.numpy(), t, rp.replica_seed(5, rank)))
@@ -56,6 +59,26 @@ def test_replicas_merge_over_gloo_ranks(sty):
     np.testing.assert_array_equal(m0, m1)
     assert t0 == t1 == 20.0
     assert s0 != s1
+
+
+def test_merge_ignores_ranks_without_repeats(sty):
+    """One repeat over two ranks: the second rank renders nothing and its unset (NaN) film must not
+    reach the merged film."""
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, world, port, q, 1)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (_, f0, c0, m0, _, _), (_, f1, c1, m1, _, _) = res
+    assert (f0, c0, c1) == (0, 1, 0)
+    np.testing.assert_array_equal(m0, np.arange(6, dtype=np.float64))
+    np.testing.assert_array_equal(m0, m1)
 
 
 def test_shard_repeats_covers_every_repeat(sty):

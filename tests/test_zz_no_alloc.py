@@ -60,6 +60,30 @@ def test_noalloc_adjoint_matches_allocating_entry_point(sty, cuda):
     assert not np.allclose(results[0][0], results[1][0])  # the second call computed its own answer
 
 
+def test_noalloc_adjoint_allocates_no_device_memory(sty, cuda):
+    """The property the entry point exists for: after a first call on the device (which looks up the
+    scratch array's address and loads the kernels), further calls leave the device's free memory
+    exactly unchanged."""
+    import torch
+    lib = sty.lib()
+    W, H, S, R = 80, 48, 4, 6
+    planes, valid = sty.synth.records(W, H, S, 1, seed=8)
+    rs = sty.RecordSet.from_numpy(planes, valid, W, H, S, 1)
+    target = torch.rand((W * H * 3,), generator=torch.Generator(device="cuda").manual_seed(8), device="cuda")
+    p = _params(8)
+    _run(sty, lib.sty_pf_adjoint_noalloc, rs, R, p, target)  # first call on the device: set-up
+    grad = torch.zeros(36, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        sty.check(lib.sty_pf_adjoint_noalloc(C.byref(rs.c()), 0, R, (C.c_float * 36)(*p), 8, None,
+                                             target.data_ptr(), grad.data_ptr(), None, None))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
+    assert torch.isfinite(grad).all()
+
+
 def test_noalloc_adjoint_rejects_oversize_input(sty, cuda):
     import torch
     lib = sty.lib()
