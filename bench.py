@@ -452,29 +452,46 @@ def c1_bilateral_cpu_baseline(sty, orc, rs, budget_s: float = 8.0):
 
 def c3_bench(sty, reps: int = 20):
     """Adjoint of the screen-space filter + smoothed ramp (36 parameters: sharpness 50, 8
-    thresholds, 8 RGB ramp colours, sigma_pixel / sigma_pos / sigma_nrm) on 512 x 512 x 4 spp
-    synthetic records (the filter workload's distributions), radius 16, one depth with a child
-    input: one gradient = forward + loss + backward (weights recomputed, two sweeps), timed with
-    CUDA events over `reps` gradients. The loss target is a seeded image (the time does not
-    depend on it); gradient correctness is checked against FP64 central differences in the tests."""
+    thresholds, 8 RGB ramp colours, sigma_pixel / sigma_pos / sigma_nrm) on the plain NL-PF
+    workload's traced buffers at 512 x 512 x 4 paths per pixel (the Cornell box, depth 5): the
+    depth-0 records with the filtered depth-1 result (radius 8, sigma_pos 0.05, sigma_nrm 0.2, toon
+    0.1 / 0.3 / 0.6) as child input, radius 8, bandwidths (4, 0.05, 0.2). The loss target is the
+    image the forward renders from the parameters perturbed by N(0, 0.05^2) (relative, seed 1). One
+    gradient = forward + loss + backward (weights recomputed, two sweeps), timed with CUDA events
+    over `reps` gradients; correctness against FP64 central differences is in the tests."""
     import ctypes as C
-    import numpy as np
     import torch
-    W, H, S, R = 512, 512, 4, 16
-    planes, valid = sty.synth.records(W, H, S, 1, seed=3)
-    rs = sty.RecordSet.from_numpy(planes, valid, W, H, S, 1)
+    a = sty.abi
+    W, H, S, R = 512, 512, 4, 8
+    pos, mids, mats, cam = sty.scene.cornell_box(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    cfg = sty.scene.screen_render_config(max_depth=5, branch=S, radius=R, sigma_pixel=0.0, sigma_pos=0.05,
+                                         sigma_nrm=0.2, screen_style=0, seed=0)
+    toon = a.style_program([a.toon_steps([0.1, 0.3, 0.6], [0.05, 0.2, 0.45, 1.0], depth_mask=1 << 1)])
+    rs_all, _, _ = sc.trace_records(cfg, [toon])
+    out = sty.pf_screen_filter(rs_all, sty.ScreenParams(R, 0.0, 0.05, 0.2), toon)
+    n = W * H * S
+    rs = sty.RecordSet(rs_all.planes[:, :n].contiguous(), rs_all.valid[:n].contiguous(), W, H, S, 1)
+    child = out[1].contiguous()
+    del rs_all, out
     rng = np.random.default_rng(4)
-    p = np.zeros(36, np.float32)
+    p = np.zeros(36, np.float64)
     p[0] = 50.0
-    p[1:9] = np.sort(rng.uniform(0.05, 1.2, 8))
+    p[1:9] = np.sort(rng.uniform(0.02, 0.8, 8))
     p[9:33] = np.sort(rng.uniform(0.0, 1.0, 24))
-    p[33:36] = [8.0, 0.5, 0.2]
-    prm = (C.c_float * 36)(*p)
-    child = torch.rand((3, W * H * S), device="cuda")
-    target = torch.rand((H, W, 3), device="cuda")
+    p[33:36] = [4.0, 0.05, 0.2]
+    pt = p + np.random.default_rng(1).normal(0.0, 0.05, 36) * np.abs(p)
+    pt[33:36] = np.abs(pt[33:36])
+    # the target image: the forward (filter + ramp at depth 0, pixel mean over the paths) at pt
+    ramp = a.style_program([a.ramp_smooth(float(pt[0]), pt[1:9].tolist(), pt[9:33].reshape(8, 3).tolist(),
+                                          depth_mask=1)])
+    tout = sty.pf_screen_filter_depth(rs, 0, sty.ScreenParams(R, float(pt[33]), float(pt[34]), float(pt[35])), ramp,
+                                      out_next=child)
+    target = tout.reshape(3, H, W, S).mean(-1).permute(1, 2, 0).contiguous()
     grad = torch.zeros(36, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
+    prm = (C.c_float * 36)(*p.astype(np.float32))
 
     def one():
         sty.check(sty.lib().sty_pf_adjoint(C.byref(rs.c()), 0, R, prm, 8, C.c_void_p(child.data_ptr()),
@@ -491,9 +508,16 @@ def c3_bench(sty, reps: int = 20):
     e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    nrec = W * H * S
-    return {"workload": "adjoint 512x512 x 4 spp, radius 16, 36 parameters (filter + smoothed ramp)",
-            "ms_per_gradient": ms, "gradients_per_s": 1e3 / ms, "mrecords_per_s": nrec / ms / 1e3,
+    loss = C.c_float()
+    sty.check(sty.lib().sty_pf_adjoint(C.byref(rs.c()), 0, R, prm, 8, C.c_void_p(child.data_ptr()),
+                                       C.c_void_p(target.data_ptr()), C.c_void_p(grad.data_ptr()), C.byref(loss),
+                                       C.c_void_p(sp)))
+    sc.close()
+    return {"workload": "adjoint on the traced Cornell records 512x512 x 4 paths (depth 0, child = filtered "
+                        "depth 1), radius 8, 36 parameters (filter bandwidths + smoothed ramp, sharpness 50), "
+                        "target rendered from parameters perturbed by N(0, 0.05^2), seed 1",
+            "ms_per_gradient": ms, "gradients_per_s": 1e3 / ms, "mrecords_per_s": n / ms / 1e3,
+            "valid_records": int(rs.valid.sum().item()), "loss": loss.value,
             "grad_finite": bool(torch.isfinite(grad).all().item())}
 
 
