@@ -273,8 +273,10 @@ def grid_nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
     per row in the reference's row layout) on the interior workload scene. Per frame: one training
     step on a 2^16 batch from that frame's tracer rows (1 path per pixel of a 192 x 108 view) and
     inference of the 1920 x 1080 first-hit queries (2 073 600 rows), as in the NL-NRC frames of the
-    spherical network. Inference runs the tensor-core path (k_grid_tiles + k_grid_mlp_tc); the
-    layer-by-layer cuBLAS path is timed beside it on the same rows."""
+    spherical network. Training runs layer by layer on the tcgen05 GEMMs of gemm_tc.cu (BF16
+    operands; FP16, tiny-cuda-nn's precision, timed beside it); inference runs the fused tensor-core
+    path (k_grid_tiles + k_grid_mlp_tc), the layer-by-layer GEMM path timed beside it on the same
+    rows."""
     import numpy as np
     import torch
     D, nt = 12, 1 << 16
@@ -290,9 +292,9 @@ def grid_nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
     nq = qx.shape[0]
     out = torch.empty((nq, 3), device=dev)
     res = {}
-    for name, layered in (("tensor_core", False), ("layered", True)):
+    for name, layered, fp16 in (("tensor_core", False, False), ("layered", True, False), ("fp16", False, True)):
         net = sty.nrc.NRC(sty.nrc.grid_config(max_depth=D, batch_size=nt, learning_rate=1e-2, seed=1,
-                                              layered=layered))
+                                              layered=layered, fp16=fp16))
         for f in range(warmup):
             net.train(rows[frames + f][0], rows[frames + f][1], 1, stream=stream, want_loss=False)
             net.inference(qx, out, stream=stream)
@@ -312,9 +314,17 @@ def grid_nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
         i1.record(stream)
         torch.cuda.synchronize()
         inf_ms = i0.elapsed_time(i1) / frames
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for f in range(frames):
+            net.train(rows[f][0], rows[f][1], 1, stream=stream, want_loss=False)
+        t1.record(stream)
+        torch.cuda.synchronize()
         res[name] = {"ms_per_frame": ms, "msamples_per_s": (nq + nt) / ms / 1e3, "inference_ms": inf_ms,
-                     "inference_mqueries_per_s": nq / inf_ms / 1e3, "train_ms": ms - inf_ms,
-                     "params": net.param_count(), "frames": frames}
+                     "inference_mqueries_per_s": nq / inf_ms / 1e3, "train_ms": t0.elapsed_time(t1) / frames,
+                     "params": net.param_count(), "frames": frames,
+                     "operands": "FP16 (loss scale 128)" if fp16 else "BF16",
+                     "inference_path": "layer by layer" if (layered or fp16) else "fused tensor-core"}
         net.close()
     mlp_flops = 2.0 * (144 * 128 + 4 * 128 * 128 + 16 * 128)  # MMA work per query incl. the padded output rows
     tc = res["tensor_core"]

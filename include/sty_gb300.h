@@ -387,18 +387,22 @@ STY_API sty_status sty_nrc_create(const sty_nrc_config *config, sty_nrc **out); 
  * `base_resolution`, `per_level_scale` growth; the reference uses 22 x 4, 2^19, 16, 2.0),
  * one-blob (`blob_bins` bins) on the next `blob_dims` inputs (7 / 4), identity on the rest -- and
  * a ReLU MLP of `hidden_units` (128) x `hidden_layers` (5) without biases, linear output. BF16
- * GEMM operands with FP32 accumulation, FP32 master parameters (MLP weights, then the tables),
- * relative L2, Adam + exponential decay, EMA for inference. The handle works with every other
+ * GEMM operands (FP16 with STY_NRC_GRID_FP16, tiny-cuda-nn's precision, its backward scaled by
+ * the loss scale 128) with FP32 accumulation on the tensor cores, FP32 master parameters (MLP
+ * weights, then the tables), relative L2, Adam + exponential decay, EMA for inference. The
+ * encoded width is at most 256. The handle works with every other
  * sty_nrc_* call; param_count covers the tables. Table gradients are accumulated with atomics,
  * so training on this network is not bit-deterministic. No counterpart of the encodings' exact
  * numerics exists here (tiny-cuda-nn is not vendored): they follow the published definitions.
  * The forward reads FP16 copies of the tables (as tiny-cuda-nn's half-precision forward does).
  * Inference runs on the tensor cores in two launches per chunk -- the encoding written as 128-row
  * MMA operand tiles, then one kernel running every layer on chip -- when hidden_units is 32, 64 or
- * 128, the encoded width is at most 160 and the weights fit in shared memory (the reference's
- * 144 -> 128 x 5 -> 3 network does); otherwise, or with STY_NRC_GRID_LAYERED in `flags`, it runs
- * the layer-by-layer path (one BF16 GEMM per layer). */
+ * 128, the encoded width is at most 160, the weights fit in shared memory (the reference's
+ * 144 -> 128 x 5 -> 3 network does) and the operands are BF16; otherwise, or with
+ * STY_NRC_GRID_LAYERED in `flags`, it runs the layer-by-layer path (one tensor-core GEMM per
+ * layer, as training does). */
 #define STY_NRC_GRID_LAYERED 1u
+#define STY_NRC_GRID_FP16 2u
 typedef struct sty_nrc_grid_config {
     uint32_t input_dims, output_dims, batch_size;
     uint32_t hidden_layers, hidden_units;

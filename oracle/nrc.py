@@ -20,6 +20,12 @@ import numpy as np
 W = 64
 
 
+def fp16_round(x: np.ndarray) -> np.ndarray:
+    """Round values to FP32 and then to the nearest IEEE half (ties to even), as float64: the GPU's
+    cvt.rn.f16.f32 of an FP32 value."""
+    return np.asarray(x, dtype=np.float32).astype(np.float16).astype(np.float64)
+
+
 def bf16_round(x: np.ndarray) -> np.ndarray:
     """Round float values to the nearest bfloat16 (ties to even), returned as float64."""
     f = np.asarray(x, dtype=np.float32).copy()

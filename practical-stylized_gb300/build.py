@@ -70,8 +70,7 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
         objs = list(ex.map(compile_one, sources))
     if force or not _newer(LIB, objs):
         # -z defs: an unresolved symbol fails the link here, not the first load of the library
-        cmd = [nvcc, *ARCH, "-shared", "-Xlinker", "-z", "-Xlinker", "defs", "-o", str(LIB), *map(str, objs),
-               "-lcublas"]
+        cmd = [nvcc, *ARCH, "-shared", "-Xlinker", "-z", "-Xlinker", "defs", "-o", str(LIB), *map(str, objs)]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -459,7 +459,7 @@ sty_status sty_nrc_create_grid(const sty_nrc_grid_config *gc, sty_nrc **out) {
     STY_ARG_CHECK(gc && out, "sty_nrc_create_grid: null argument");
     STY_ARG_CHECK(gc->batch_size >= 128 && gc->batch_size % 128 == 0, "batch_size must be a multiple of 128");
     STY_ARG_CHECK(gc->decay_interval > 0 && gc->learning_rate > 0.0f, "decay_interval and learning_rate must be > 0");
-    STY_ARG_CHECK((gc->flags & ~STY_NRC_GRID_LAYERED) == 0, "unknown flags 0x%x", gc->flags);
+    STY_ARG_CHECK((gc->flags & ~(STY_NRC_GRID_LAYERED | STY_NRC_GRID_FP16)) == 0, "unknown flags 0x%x", gc->flags);
     sty_nrc *nr = new sty_nrc();
     nr->layered = (gc->flags & STY_NRC_GRID_LAYERED) != 0;
     size_t np = 0, n_mlp = 0;

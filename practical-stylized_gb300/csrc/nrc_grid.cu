@@ -13,10 +13,13 @@
 //   one-blob: bin k of B gets the mass of N(x, (1/B)^2) over [k/B, (k+1)/B] (erf).
 // Inference (networks with H in {32, 64, 128}): k_grid_tiles writes the encoding as 128-row MMA
 // operand tiles, k_grid_mlp_tc runs every layer on the tensor cores with the weights in shared
-// memory. Training and other widths: the layer-by-layer path -- the encoding as row-major BF16
-// [rows][E] (k_grid_enc, k_blob_ident), each layer a BF16 GEMM with FP32 accumulation (cuBLAS),
-// ReLU / mask / loss-gradient kernels, BF16 activations kept for the backward; output padded to 8.
-#include <cublas_v2.h>
+// memory. Training and other widths: the layer-by-layer path -- the encoding as row-major 16-bit
+// [rows][E] (k_grid_enc, k_blob_ident), each layer product a tcgen05 GEMM with FP32 accumulation
+// and a fused epilogue (gemm_tc.cu: ReLU into the next layer's 16-bit input; in the backward the
+// ReLU mask of the layer below; the weight gradients reduced over the batch in a fixed order),
+// 16-bit activations kept for the backward; output padded to 16. The MLP operands are BF16, or
+// FP16 with STY_NRC_GRID_FP16 (tiny-cuda-nn's precision, with its loss scale of 128 on the
+// backward so the per-sample gradients of a 2^16 batch stay out of the FP16 subnormals).
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -25,6 +28,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "gemm_tc.cuh"
 #include "nrc.cuh"
 #include "tc.cuh"
 
@@ -33,7 +37,8 @@ namespace {
 using namespace tc;
 
 constexpr int kMaxLevels = 32;
-constexpr int kOpad = 8;
+constexpr int kOpad = 16;         // output columns of the layer-by-layer path (the MMA's N granule)
+constexpr float kFp16LossScale = 128.0f;
 
 struct GridGeo {
     int in_dims, levels, feats, blob_dims, bins, out_w;
@@ -174,7 +179,7 @@ __device__ __forceinline__ float extra_column(const GridGeo &g, int r, const flo
 // one thread per (sample, level): the level's F features into enc[s][l F ..]
 template <int F>
 __global__ void k_grid_enc(uint64_t n, const float *__restrict__ x, GridGeo g, const __half *__restrict__ tab,
-                           __nv_bfloat16 *__restrict__ enc) {
+                           uint16_t *__restrict__ enc, bool f16) {
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= n * (uint64_t)g.levels) return;
     const uint64_t s = t / g.levels;
@@ -182,19 +187,19 @@ __global__ void k_grid_enc(uint64_t n, const float *__restrict__ x, GridGeo g, c
     const float *xs = x + s * g.in_dims;
     float acc[F];
     gather_level<F>(g, l, xs[0], xs[1], xs[2], tab, acc);
-    __nv_bfloat16 *o = enc + s * g.out_w + (size_t)l * F;
+    uint16_t *o = enc + s * g.out_w + (size_t)l * F;
 #pragma unroll
-    for (int f = 0; f < F; f++) o[f] = __float2bfloat16_rn(acc[f]);
+    for (int f = 0; f < F; f++) o[f] = to16(acc[f], f16);
 }
 // one thread per (row, non-grid column): one-blob bins, identity dims, zero padding; consecutive
 // threads write consecutive columns of a row
-__global__ void k_blob_ident(uint64_t n, const float *__restrict__ x, GridGeo g, __nv_bfloat16 *__restrict__ enc) {
+__global__ void k_blob_ident(uint64_t n, const float *__restrict__ x, GridGeo g, uint16_t *__restrict__ enc, bool f16) {
     const int G = g.levels * g.feats, nx = g.out_w - G;
     const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (t >= n * (uint64_t)nx) return;
     const uint64_t s = t / (uint64_t)nx;
     const int r = (int)(t % (uint64_t)nx);
-    enc[s * g.out_w + G + r] = __float2bfloat16_rn(extra_column(g, r, x + s * g.in_dims));
+    enc[s * g.out_w + G + r] = to16(extra_column(g, r, x + s * g.in_dims), f16);
 }
 // the hash-grid part of the backward: gtab[entry][f] += w * denc[s][l F + f], one vector atomic per
 // corner for F >= 2 (the table gradient starts at a multiple of 16 floats: n_mlp = H (E + ...))
@@ -229,31 +234,10 @@ __global__ void k_grid_bwd(uint64_t n, const float *__restrict__ x, GridGeo g, c
         }
     }
 }
-// element-wise kernels, 8 elements per thread (n = rows x H, a multiple of 16)
-__global__ void k_relu_bf16(size_t n8, const float4 *__restrict__ z, uint4 *__restrict__ a) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n8) return;
-    const float4 p = z[2 * i], q = z[2 * i + 1];
-    a[i] = make_uint4(pack2_relu_bf16(p.x, p.y), pack2_relu_bf16(p.z, p.w), pack2_relu_bf16(q.x, q.y),
-                      pack2_relu_bf16(q.z, q.w));
-}
-__device__ __forceinline__ float bf16_pos_sel(uint32_t act_half, float v) {  // v where the BF16 act > 0
-    return (act_half & 0x8000u) == 0u && (act_half & 0x7fffu) != 0u ? v : 0.0f;
-}
-__global__ void k_mask_bf16(size_t n8, const float4 *__restrict__ dh, const uint4 *__restrict__ act,
-                            uint4 *__restrict__ dp) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n8) return;
-    const float4 p = dh[2 * i], q = dh[2 * i + 1];
-    const uint4 a = act[i];
-    dp[i] = make_uint4(pack2_bf16(bf16_pos_sel(a.x & 0xffffu, p.x), bf16_pos_sel(a.x >> 16, p.y)),
-                       pack2_bf16(bf16_pos_sel(a.y & 0xffffu, p.z), bf16_pos_sel(a.y >> 16, p.w)),
-                       pack2_bf16(bf16_pos_sel(a.z & 0xffffu, q.x), bf16_pos_sel(a.z >> 16, q.y)),
-                       pack2_bf16(bf16_pos_sel(a.w & 0xffffu, q.z), bf16_pos_sel(a.w >> 16, q.w)));
-}
-// relative L2 (prediction constant in the denominator): dP = 2 (p - t) / (p^2 + 0.01) / (B O)
+// relative L2 (prediction constant in the denominator): dP = 2 (p - t) / (p^2 + 0.01) / (B O), stored
+// 16-bit times `scale` (the FP16 loss scale; 1 for BF16)
 __global__ void k_rel_l2_grad(uint32_t B, int O, const float *__restrict__ pred, const float *__restrict__ tgt,
-                              __nv_bfloat16 *__restrict__ dp, float *__restrict__ loss) {
+                              uint16_t *__restrict__ dp, float *__restrict__ loss, bool f16, float scale) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.0f;
     if (i < B) {
@@ -266,31 +250,27 @@ __global__ void k_rel_l2_grad(uint32_t B, int O, const float *__restrict__ pred,
                 l += (p - t) * (p - t) / den;
                 g = 2.0f * (p - t) / den * norm;
             }
-            dp[(size_t)i * kOpad + c] = __float2bfloat16_rn(g);
+            dp[(size_t)i * kOpad + c] = to16(g * scale, f16);
         }
     }
     for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
     if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, l / ((float)B * (float)O));
 }
-// FP32 parameters -> BF16 GEMM operands; the output layer padded to kOpad rows of zeros
-__global__ void k_weights_bf16(size_t n_mlp, size_t out_off, int O, int H, const float *__restrict__ w,
-                               __nv_bfloat16 *__restrict__ wb) {
+// FP32 parameters -> 16-bit GEMM operands; the output layer padded to kOpad rows of zeros
+__global__ void k_weights16(size_t n_mlp, size_t out_off, int O, int H, const float *__restrict__ w,
+                            uint16_t *__restrict__ wb, bool f16) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     const size_t total = out_off + (size_t)kOpad * H;
     if (i >= total) return;
     float v = 0.0f;
     if (i < out_off) v = w[i];
     else if ((i - out_off) / H < (size_t)O) v = w[i];
-    wb[i] = __float2bfloat16_rn(v);
+    wb[i] = to16(v, f16);
     (void)n_mlp;
 }
 __global__ void k_out_rows(uint64_t n, int O, const float *__restrict__ pad, float *__restrict__ out) {
     const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i < n * (uint64_t)O) out[i] = pad[(i / O) * kOpad + i % O];
-}
-__global__ void k_copy_rows(size_t rows, size_t cols, size_t ld_src, const float *__restrict__ src, float *__restrict__ dst) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < rows * cols) dst[i] = src[(i / cols) * ld_src + i % cols];
 }
 __device__ __forceinline__ uint32_t mix32(uint64_t x) {
     x ^= x >> 33;
@@ -623,7 +603,9 @@ struct GridModel {
     int H, L, O, E;
     size_t n_mlp, n_tab, out_off;
     std::vector<size_t> loff;  // FP32 offsets of W_0 .. W_L (W_L = output layer)
-    __nv_bfloat16 *wb = nullptr, *wb_ema = nullptr;
+    bool f16 = false;          // MLP operands FP16 (else BF16)
+    float loss_scale = 1.0f;   // the backward's scale of the loss gradient (FP16: 128)
+    uint16_t *wb = nullptr, *wb_ema = nullptr;  // 16-bit weights: W_0 .. W_{L-1}, W_out padded to kOpad rows
     __half *tab16 = nullptr, *tab16_ema = nullptr;  // FP16 copies of the tables the forward reads
     bool tab16_valid = false;     // tab16 == fp16(current tables) (kept by k_adam_grid)
     bool tab16_ema_valid = false; // tab16_ema == fp16(EMA tables) (kept by k_adam_grid)
@@ -635,94 +617,66 @@ struct GridModel {
     uint16_t *img = nullptr, *img_ema = nullptr;
     uint8_t *tiles = nullptr;
     uint64_t tiles_cap = 0;
-    cublasHandle_t h = nullptr;
-    // batch scratch
+    // batch scratch: 16-bit encoding and activations, two layer-gradient buffers, FP32 output /
+    // encoding gradient, the weight gradients' per-chunk partial sums
     uint64_t cap = 0;
-    __nv_bfloat16 *enc = nullptr, *acts = nullptr, *dp = nullptr;
-    float *z = nullptr, *dh = nullptr;
+    uint16_t *enc = nullptr, *acts = nullptr, *dp = nullptr, *dp2 = nullptr;
+    float *z = nullptr, *dh = nullptr, *parts = nullptr;
     int *d_fan_in = nullptr, *d_fan_out = nullptr;
     size_t *d_loff = nullptr;
 };
 
 namespace {
 
-sty_status cublas_ok(cublasStatus_t s, const char *what) {
-    if (s == CUBLAS_STATUS_SUCCESS) return STY_OK;
-    set_error("%s: cuBLAS status %d", what, (int)s);
-    return STY_ERR_CUDA;
-}
-// row-major Y[B][N] (fp32) = X[B][K] (bf16) . W[N][K]^T (bf16)
-sty_status gemm_fwd(GridModel *g, int B, int N, int K, const __nv_bfloat16 *X, const __nv_bfloat16 *W, float *Y) {
-    const float one = 1.0f, zero = 0.0f;
-    return cublas_ok(cublasGemmEx(g->h, CUBLAS_OP_T, CUBLAS_OP_N, N, B, K, &one, W, CUDA_R_16BF, K, X, CUDA_R_16BF, K,
-                                  &zero, Y, CUDA_R_32F, N, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT),
-                     "gemm forward");
-}
-// row-major dX[B][K] (fp32) = dY[B][N] (bf16) . W[N][K] (bf16)
-sty_status gemm_dx(GridModel *g, int B, int N, int K, const __nv_bfloat16 *dY, const __nv_bfloat16 *W, float *dX) {
-    const float one = 1.0f, zero = 0.0f;
-    return cublas_ok(cublasGemmEx(g->h, CUBLAS_OP_N, CUBLAS_OP_N, K, B, N, &one, W, CUDA_R_16BF, K, dY, CUDA_R_16BF, N,
-                                  &zero, dX, CUDA_R_32F, K, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT),
-                     "gemm input gradient");
-}
-// row-major dW[N][K] (fp32) = dY[B][N]^T (bf16) . X[B][K] (bf16)
-sty_status gemm_dw(GridModel *g, int B, int N, int K, const __nv_bfloat16 *dY, const __nv_bfloat16 *X, float *dW) {
-    const float one = 1.0f, zero = 0.0f;
-    return cublas_ok(cublasGemmEx(g->h, CUBLAS_OP_N, CUBLAS_OP_T, K, N, B, &one, X, CUDA_R_16BF, K, dY, CUDA_R_16BF, N,
-                                  &zero, dW, CUDA_R_32F, K, CUBLAS_COMPUTE_32F, CUBLAS_GEMM_DEFAULT),
-                     "gemm weight gradient");
-}
-
 sty_status ensure_cap(GridModel *g, uint64_t B) {
     if (B <= g->cap) return STY_OK;
-    void *ptrs[] = {g->enc, g->acts, g->dp, g->z, g->dh};
+    void *ptrs[] = {g->enc, g->acts, g->dp, g->dp2, g->z, g->dh, g->parts};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    g->enc = g->acts = g->dp = nullptr;
-    g->z = g->dh = nullptr;
-    const size_t wide = (size_t)std::max(g->H, g->E);
+    g->enc = g->acts = g->dp = g->dp2 = nullptr;
+    g->z = g->dh = g->parts = nullptr;
+    g->cap = 0;
+    STY_ARG_CHECK(B < (1ull << 31), "batch of %llu rows too large", (unsigned long long)B);
+    const size_t wide = (size_t)std::max({g->H, g->E, kOpad});
+    const size_t parts = tc_dw_partials_floats((int)B, std::max({g->H, g->E, kOpad}));
     STY_TRY(check_cuda(cudaMalloc(&g->enc, B * g->E * 2), "alloc encoding"));
     STY_TRY(check_cuda(cudaMalloc(&g->acts, (size_t)g->L * B * g->H * 2), "alloc activations"));
     STY_TRY(check_cuda(cudaMalloc(&g->dp, B * wide * 2), "alloc layer gradient"));
-    STY_TRY(check_cuda(cudaMalloc(&g->z, B * wide * 4), "alloc pre-activations"));
-    STY_TRY(check_cuda(cudaMalloc(&g->dh, B * wide * 4), "alloc input gradient"));
+    STY_TRY(check_cuda(cudaMalloc(&g->dp2, B * wide * 2), "alloc layer gradient"));
+    STY_TRY(check_cuda(cudaMalloc(&g->z, B * wide * 4), "alloc output"));
+    STY_TRY(check_cuda(cudaMalloc(&g->dh, B * wide * 4), "alloc encoding gradient"));
+    STY_TRY(check_cuda(cudaMalloc(&g->parts, parts * 4), "alloc weight-gradient partials"));
     g->cap = B;
     return STY_OK;
 }
 
-// forward of B rows with the given BF16 weights and FP32 tables: leaves enc, acts (for the backward)
-// and the padded output (B x kOpad) in g->z
-sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const __half *tables, const __nv_bfloat16 *wb,
+// forward of B rows with the given 16-bit weights and FP16 tables: leaves enc, acts (for the
+// backward) and the padded output (B x kOpad, FP32) in g->z
+sty_status grid_forward(GridModel *g, uint64_t B, const float *x, const __half *tables, const uint16_t *wb,
                         cudaStream_t st) {
-    STY_TRY(cublas_ok(cublasSetStream(g->h, st), "cublasSetStream"));
     const uint64_t nl = B * (uint64_t)g->geo.levels;
     const unsigned blocks = (unsigned)((nl + 255) / 256);
     switch (g->geo.feats) {
-        case 1: k_grid_enc<1><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
-        case 2: k_grid_enc<2><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
-        case 4: k_grid_enc<4><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
-        default: k_grid_enc<8><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc); break;
+        case 1: k_grid_enc<1><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc, g->f16); break;
+        case 2: k_grid_enc<2><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc, g->f16); break;
+        case 4: k_grid_enc<4><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc, g->f16); break;
+        default: k_grid_enc<8><<<blocks, 256, 0, st>>>(B, x, g->geo, tables, g->enc, g->f16); break;
     }
     STY_TRY(check_launch("k_grid_enc"));
     const uint64_t nx = B * (uint64_t)(g->E - g->geo.levels * g->geo.feats);
-    k_blob_ident<<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->enc);
+    k_blob_ident<<<(unsigned)((nx + 255) / 256), 256, 0, st>>>(B, x, g->geo, g->enc, g->f16);
     STY_TRY(check_launch("k_blob_ident"));
-    const __nv_bfloat16 *a = g->enc;
+    const uint16_t *a = g->enc;
     int K = g->E;
-    for (int l = 0; l < g->L; l++) {
-        STY_TRY(gemm_fwd(g, (int)B, g->H, K, a, wb + g->loff[l], g->z));
-        count_launch();
-        __nv_bfloat16 *nx = g->acts + (size_t)l * B * g->H;
-        const size_t n8 = (size_t)B * g->H / 8;
-        k_relu_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->z),
-                                                                  reinterpret_cast<uint4 *>(nx));
-        STY_TRY(check_launch("k_relu_bf16"));
+    for (int l = 0; l < g->L; l++) {  // z = a W_l^T, ReLU into the next layer's 16-bit input
+        uint16_t *nx = g->acts + (size_t)l * B * g->H;
+        STY_TRY(tc_gemm_rows(a, K, wb + g->loff[l], (int)B, K, g->H, false, g->f16, kEpiRelu16, nullptr, nx, nullptr,
+                             1.0f, st));
         a = nx;
         K = g->H;
     }
-    STY_TRY(gemm_fwd(g, (int)B, kOpad, g->H, a, wb + g->out_off, g->z));
-    count_launch();
-    return STY_OK;
+    return tc_gemm_rows(a, g->H, wb + g->out_off, (int)B, g->H, kOpad, false, g->f16, kEpiF32, g->z, nullptr, nullptr,
+                        1.0f, st);
 }
 
 // the two tensor-core launches per chunk of kInferChunk rows (tile images in g->tiles)
@@ -792,6 +746,7 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
                   "hidden_units must be a multiple of 16 in [16, 256]");
     STY_ARG_CHECK(c->hidden_layers >= 1 && c->hidden_layers <= 8, "hidden_layers must be in [1, 8]");
     STY_ARG_CHECK(c->output_dims >= 1 && c->output_dims <= kOpad, "output_dims must be in [1, %d]", kOpad);
+    STY_ARG_CHECK((c->flags & ~(STY_NRC_GRID_LAYERED | STY_NRC_GRID_FP16)) == 0, "unknown flags 0x%x", c->flags);
     STY_ARG_CHECK(c->base_resolution >= 2 && c->per_level_scale >= 1.0f, "bad grid resolution");
     GridModel *g = new GridModel();
     g->cfg = *c;
@@ -821,6 +776,13 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     }
     const int enc = geo.levels * geo.feats + geo.blob_dims * geo.bins + (geo.in_dims - 3 - geo.blob_dims);
     geo.out_w = (enc + 15) / 16 * 16;
+    if (geo.out_w > 256) {
+        set_error("encoded width %d exceeds 256 (the GEMMs' operand width)", geo.out_w);
+        delete g;
+        return STY_ERR_ARG;
+    }
+    g->f16 = (c->flags & STY_NRC_GRID_FP16) != 0;
+    g->loss_scale = g->f16 ? kFp16LossScale : 1.0f;
     g->E = geo.out_w;
     g->H = (int)c->hidden_units;
     g->L = (int)c->hidden_layers;
@@ -843,10 +805,11 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     g->img_elems = img_layer(g->L, g->H, g->E) + (size_t)kOutN * g->H;
     g->tc_smem = ((g->img_elems * 2 + 1023) & ~(size_t)1023) + (size_t)kTM * std::max(g->E, g->H) * 2 + 1024;
-    g->tc = (g->H == 32 || g->H == 64 || g->H == 128) && g->E <= kMaxE && g->tc_smem + 64 <= (size_t)smem_optin;
-    sty_status s = cublas_ok(cublasCreate(&g->h), "cublasCreate");
-    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc bf16 weights");
-    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb_ema, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc bf16 ema");
+    // (BF16 only: FP16 networks infer layer by layer on the same tensor-core GEMMs as training)
+    g->tc = !g->f16 && (g->H == 32 || g->H == 64 || g->H == 128) && g->E <= kMaxE &&
+            g->tc_smem + 64 <= (size_t)smem_optin;
+    sty_status s = check_cuda(cudaMalloc(&g->wb, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc 16-bit weights");
+    if (s == STY_OK) s = check_cuda(cudaMalloc(&g->wb_ema, (g->out_off + (size_t)kOpad * g->H) * 2), "alloc 16-bit ema");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16, g->n_tab * 2), "alloc fp16 tables");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tab16_ema, g->n_tab * 2), "alloc fp16 ema tables");
     if (s == STY_OK) s = check_cuda(cudaMalloc(&g->tsteps, g->n_tab * 4), "alloc table step counts");
@@ -864,10 +827,9 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
 void grid_destroy(GridModel *g) {
     if (!g) return;
     void *ptrs[] = {g->wb, g->wb_ema, g->tab16, g->tab16_ema, g->tsteps, g->img, g->img_ema, g->tiles, g->enc,
-                    g->acts, g->dp, g->z, g->dh, g->d_fan_in, g->d_fan_out, g->d_loff};
+                    g->acts, g->dp, g->dp2, g->z, g->dh, g->parts, g->d_fan_in, g->d_fan_out, g->d_loff};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    if (g->h) cublasDestroy(g->h);
     delete g;
 }
 
@@ -899,8 +861,8 @@ sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t 
 sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_t st) {
     const size_t total = g->out_off + (size_t)kOpad * g->H;
     const unsigned tblocks = (unsigned)((g->n_tab + 255) / 256);
-    k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, w, g->wb);
-    STY_TRY(check_launch("k_weights_bf16"));
+    k_weights16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, w, g->wb, g->f16);
+    STY_TRY(check_launch("k_weights16"));
     if (!g->tab16_valid) {
         k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, w + g->n_mlp, g->tab16);
         STY_TRY(check_launch("k_tab_half"));
@@ -908,9 +870,9 @@ sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_
     }
     if (!ema) return STY_OK;
     // the inference set: EMA copies and the tensor-core weight images of both parameter sets
-    k_weights_bf16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema,
-                                                                     g->wb_ema);
-    STY_TRY(check_launch("k_weights_bf16"));
+    k_weights16<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(g->n_mlp, g->out_off, g->O, g->H, ema, g->wb_ema,
+                                                                  g->f16);
+    STY_TRY(check_launch("k_weights16"));
     if (!g->tab16_ema_valid) {
         k_tab_half<<<tblocks, 256, 0, st>>>(g->n_tab, ema + g->n_mlp, g->tab16_ema);
         STY_TRY(check_launch("k_tab_half"));
@@ -941,42 +903,48 @@ sty_status grid_infer(GridModel *g, bool ema, bool allow_tc, uint64_t count, con
     return STY_OK;
 }
 
+// dW[m][n] (pitch ldd; transposed: dW[n][m]) = scale * P^T Q for P = [B][mp] of any width: the
+// tensor-core reduction takes 128 columns of P at a time
+sty_status weight_grad(GridModel *g, const uint16_t *P, int mp, const uint16_t *Q, int nq, int B, int n_valid,
+                       bool transpose, float scale, float *dst, cudaStream_t st) {
+    for (int m0 = 0; m0 < mp; m0 += 128) {
+        const int w = std::min(128, mp - m0);
+        float *d = transpose ? dst + m0 : dst + (size_t)m0 * nq;
+        STY_TRY(tc_gemm_dw(P + m0, mp, w, Q, nq, B, nq, g->f16, g->parts, d, n_valid, transpose, transpose ? mp : nq,
+                           scale, st));
+    }
+    return STY_OK;
+}
+
 // loss gradient, backward and the full parameter gradient (MLP weights and tables) of B rows
 sty_status grid_gradient(GridModel *g, uint32_t B, const float *x, const float *target, float *grad, float *loss,
                          cudaStream_t st) {
     STY_TRY(ensure_cap(g, B));
     STY_TRY(grid_forward(g, B, x, g->tab16, g->wb, st));
-    // dP_out = dLoss/dpred (B x kOpad) in g->dp
-    k_rel_l2_grad<<<(B + 255) / 256, 256, 0, st>>>(B, g->O, g->z, target, g->dp, loss);
+    const float S = g->loss_scale, inv = 1.0f / S;
+    const int H = g->H, L = g->L, Bi = (int)B;
+    // dP_out = S dLoss/dpred (B x kOpad, 16-bit) in g->dp
+    k_rel_l2_grad<<<(B + 255) / 256, 256, 0, st>>>(B, g->O, g->z, target, g->dp, loss, g->f16, S);
     STY_TRY(check_launch("k_rel_l2_grad"));
-    const __nv_bfloat16 *aL = g->acts + (size_t)(g->L - 1) * B * g->H;
-    // dW_out (kOpad x H) into scratch, first O rows into the gradient
-    STY_TRY(gemm_dw(g, (int)B, kOpad, g->H, g->dp, aL, g->dh));
-    count_launch();
-    k_copy_rows<<<(unsigned)(((size_t)g->O * g->H + 255) / 256), 256, 0, st>>>(g->O, g->H, g->H, g->dh,
-                                                                                grad + g->out_off);
-    STY_TRY(check_launch("k_copy_rows"));
-    // dH_{L-1} = dP_out W_out, masked by act_{L-1} > 0
-    STY_TRY(gemm_dx(g, (int)B, kOpad, g->H, g->dp, g->wb + g->out_off, g->dh));
-    count_launch();
-    __nv_bfloat16 *dp = g->dp;
-    const size_t n8 = (size_t)B * g->H / 8;
-    k_mask_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->dh),
-                                                              reinterpret_cast<const uint4 *>(aL),
-                                                              reinterpret_cast<uint4 *>(dp));
-    STY_TRY(check_launch("k_mask_bf16"));
-    for (int l = g->L - 1; l >= 0; l--) {
-        const __nv_bfloat16 *al = l == 0 ? g->enc : g->acts + (size_t)(l - 1) * B * g->H;
-        const int K = l == 0 ? g->E : g->H;
-        STY_TRY(gemm_dw(g, (int)B, g->H, K, dp, al, grad + g->loff[l]));
-        count_launch();
-        STY_TRY(gemm_dx(g, (int)B, g->H, K, dp, g->wb + g->loff[l], g->dh));
-        count_launch();
-        if (l > 0) {
-            k_mask_bf16<<<(unsigned)((n8 + 255) / 256), 256, 0, st>>>(n8, reinterpret_cast<const float4 *>(g->dh),
-                                                                      reinterpret_cast<const uint4 *>(al),
-                                                                      reinterpret_cast<uint4 *>(dp));
-            STY_TRY(check_launch("k_mask_bf16"));
+    const uint16_t *aL = g->acts + (size_t)(L - 1) * B * H;
+    // dW_out [O][H] = (A_{L-1}^T dP_out)^T / S
+    STY_TRY(weight_grad(g, aL, H, g->dp, kOpad, Bi, g->O, true, inv, grad + g->out_off, st));
+    // dP_{L-1} = (dP_out W_out) where A_{L-1} > 0
+    STY_TRY(tc_gemm_rows(g->dp, kOpad, g->wb + g->out_off, Bi, kOpad, H, true, g->f16, kEpiMask16, nullptr, g->dp2, aL,
+                         1.0f, st));
+    uint16_t *dp = g->dp2, *other = g->dp;
+    for (int l = L - 1; l >= 0; l--) {
+        const uint16_t *al = l == 0 ? g->enc : g->acts + (size_t)(l - 1) * B * H;
+        const int K = l == 0 ? g->E : H;
+        // dW_l [H][K] = dP_l^T A_{l-1} / S
+        STY_TRY(weight_grad(g, dp, H, al, K, Bi, K, false, inv, grad + g->loff[l], st));
+        if (l > 0) {  // dP_{l-1} = (dP_l W_l) where A_{l-1} > 0
+            STY_TRY(tc_gemm_rows(dp, H, g->wb + g->loff[l], Bi, H, K, true, g->f16, kEpiMask16, nullptr, other, al,
+                                 1.0f, st));
+            std::swap(dp, other);
+        } else {  // dLoss/dencoding = dP_0 W_0 / S (FP32)
+            STY_TRY(tc_gemm_rows(dp, H, g->wb + g->loff[0], Bi, H, g->E, true, g->f16, kEpiF32, g->dh, nullptr, nullptr,
+                                 inv, st));
         }
     }
     // g->dh now holds dLoss/dencoding (B x E): the tables' gradient

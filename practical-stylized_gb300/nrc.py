@@ -12,6 +12,7 @@ from .abi import check, lib
 STY_NRC_FP32 = 0
 STY_NRC_BF16 = 1
 GRID_LAYERED = 1  # STY_NRC_GRID_LAYERED
+GRID_FP16 = 2     # STY_NRC_GRID_FP16
 
 # the spherical row layout's frequency table: pos 3, dir 2, normal 2, roughness 1, albedo 3
 # -> 3*8 + 4*6 + 4*4 = 64 encoded columns
@@ -55,10 +56,11 @@ class NrcGridConfig(C.Structure):
 def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5, hidden_units=128, grid_levels=22,
                 grid_features=4, log2_table=19, base_resolution=16, per_level_scale=2.0, blob_dims=7, blob_bins=4,
                 learning_rate=1e-3, beta1=0.9, beta2=0.99, epsilon=1e-8, ema_decay=0.95, decay_base=1.0,
-                decay_interval=100, seed=1337, layered=False) -> NrcGridConfig:
+                decay_interval=100, seed=1337, layered=False, fp16=False) -> NrcGridConfig:
     """The reference's NL-NRC network (nrc_pt.rs:1159-1352; defaults of configs/teaser/nl-nrc.json):
     rows of 20 + max_depth inputs in the reference layout. `layered` forces the layer-by-layer
-    inference path instead of the tensor-core path (tile encoder + on-chip MLP kernel)."""
+    inference path instead of the fused tensor-core path (tile encoder + on-chip MLP kernel);
+    `fp16` makes the MLP operands FP16 (tiny-cuda-nn's precision) instead of BF16."""
     c = NrcGridConfig()
     c.input_dims, c.output_dims, c.batch_size = 20 + max_depth, output_dims, batch_size
     c.hidden_layers, c.hidden_units = hidden_layers, hidden_units
@@ -67,7 +69,7 @@ def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5
     c.blob_dims, c.blob_bins = blob_dims, blob_bins
     c.learning_rate, c.beta1, c.beta2, c.epsilon = learning_rate, beta1, beta2, epsilon
     c.ema_decay, c.decay_base, c.decay_interval, c.seed = ema_decay, decay_base, decay_interval, seed
-    c.flags = GRID_LAYERED if layered else 0
+    c.flags = (GRID_LAYERED if layered else 0) | (GRID_FP16 if fp16 else 0)
     return c
 
 

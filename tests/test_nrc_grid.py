@@ -1,6 +1,6 @@
 """The reference's NL-NRC network (sty_nrc_create_grid): composite encoding (hash grid + one-blob +
-identity) and a ReLU MLP, against the FP64 oracle (oracle/nrc_grid.py + a BF16 emulation of the
-GEMM operands).
+identity) and a ReLU MLP, against the FP64 oracle (oracle/nrc_grid.py + an emulation of the 16-bit
+GEMM operands: BF16, or FP16 with tiny-cuda-nn's loss scale of 128 on the backward).
 
 The forward reads FP16 copies of the tables (the emulation rounds them the same way); grid features
 accumulate in FP32 and are rounded to BF16 like every GEMM operand, so outputs are compared to the
@@ -75,15 +75,16 @@ def _split(p, c):
 
 
 def _emulate(p, c, x):
+    r16 = onrc.fp16_round if c.get("fp16") else onrc.bf16_round
     mats, tables, Ep = _split(p.astype(np.float64), c)
     tables = tables.astype(np.float16).astype(np.float64)
     enc = og.encode(x, tables, c["grid_levels"], c["grid_features"], c["log2_table"], c["base_resolution"],
                     c["per_level_scale"], c["blob_dims"], c["blob_bins"], Ep)
-    mb = [onrc.bf16_round(m) for m in mats]
-    acts = [onrc.bf16_round(enc)]
+    mb = [r16(m) for m in mats]
+    acts = [r16(enc)]
     h = acts[0]
     for l in range(c["hidden_layers"]):
-        h = onrc.bf16_round(np.maximum(h @ mb[l].T, 0.0))
+        h = r16(np.maximum(h @ mb[l].T, 0.0))
         acts.append(h)
     return h @ mb[-1].T, acts, mb, enc
 
@@ -100,8 +101,9 @@ def _dev(a):
 
 
 @pytest.mark.gpu
-def test_grid_inference_matches_emulation(sty, cuda):
-    net, c = _net(sty)
+@pytest.mark.parametrize("fp16", [False, True], ids=["bf16", "fp16"])
+def test_grid_inference_matches_emulation(sty, cuda, fp16):
+    net, c = _net(sty, fp16=fp16)
     p = net.save_params().astype(np.float64)
     # spread the tables so the encoding matters
     mats, tables, _ = _split(p, c)
@@ -158,8 +160,14 @@ def test_grid_tc_matches_layered(sty, cuda, kw):
 
 
 @pytest.mark.gpu
-def test_grid_gradient_matches_emulation(sty, cuda):
-    net, c = _net(sty, seed=5)
+@pytest.mark.parametrize("kw", [dict(), dict(fp16=True), dict(hidden_units=128, grid_levels=12, grid_features=4),
+                                dict(hidden_units=128, grid_levels=12, grid_features=4, fp16=True)],
+                         ids=["bf16", "fp16", "bf16-h128", "fp16-h128"])
+def test_grid_gradient_matches_emulation(sty, cuda, kw):
+    """The full parameter gradient (tensor-core GEMMs forward, input and weight gradients reduced over
+    the batch in a fixed order; table gradient by atomics) against the emulation of the same 16-bit
+    operands; deterministic for the MLP part."""
+    net, c = _net(sty, seed=5, **kw)
     p = net.save_params().astype(np.float64)
     rng = np.random.default_rng(2)
     mats, tables, Ep = _split(p, c)
@@ -171,17 +179,21 @@ def test_grid_gradient_matches_emulation(sty, cuda):
     t = rng.random((B, 3)) + 0.1
     g, loss = net.gradient(_dev(x), _dev(t))
     g = g.cpu().numpy().astype(np.float64)
-    # emulated backward: BF16 loss gradient and layer gradients, FP32-like sums in FP64
+    # emulated backward: 16-bit loss gradient (times the loss scale S) and layer gradients, sums in
+    # FP64, the weight and encoding gradients divided by S
+    r16 = onrc.fp16_round if c.get("fp16") else onrc.bf16_round
+    S = 128.0 if c.get("fp16") else 1.0
     pred, acts, mb, enc = _emulate(p, c, x)
     den = pred * pred + 0.01
-    gp = onrc.bf16_round(2.0 * (pred - t) / den / (B * 3))
+    gp = r16(S * 2.0 * (pred - t) / den / (B * 3))
     grads = [None] * (c["hidden_layers"] + 1)
-    grads[-1] = gp.T @ acts[-1]
+    grads[-1] = gp.T @ acts[-1] / S
     dh = gp @ mb[-1]
     for l in range(c["hidden_layers"] - 1, -1, -1):
-        dp = onrc.bf16_round(dh * (acts[l + 1] > 0))
-        grads[l] = dp.T @ acts[l]
+        dp = r16(dh * (acts[l + 1] > 0))
+        grads[l] = dp.T @ acts[l] / S
         dh = dp @ mb[l]
+    dh = dh / S
     ng = c["grid_levels"] * c["grid_features"]
     _, _, total = _geo(c)
     gt = og.grid_backward(x[:, :3], dh[:, :ng], c["grid_levels"], c["grid_features"], c["log2_table"],
@@ -191,6 +203,9 @@ def test_grid_gradient_matches_emulation(sty, cuda):
     assert np.linalg.norm(g[:n_mlp] - ref_mlp) <= 1e-2 * np.linalg.norm(ref_mlp)
     assert np.linalg.norm(g[n_mlp:] - gt.reshape(-1)) <= 2e-2 * np.linalg.norm(gt)
     assert loss == pytest.approx(float(((pred - t) ** 2 / den).mean()), rel=1e-2)
+    g2, _ = net.gradient(_dev(x), _dev(t))
+    assert np.array_equal(g2.cpu().numpy()[:n_mlp], g[:n_mlp].astype(np.float32))  # fixed-order reductions
+    net.close()
 
 
 def test_oracle_adam_sparse_rule():
@@ -246,8 +261,9 @@ def test_grid_optimiser_matches_oracle(sty, cuda):
 
 
 @pytest.mark.gpu
-def test_grid_training_reduces_loss(sty, cuda):
-    net, c = _net(sty, seed=7, batch=4096, learning_rate=1e-2)
+@pytest.mark.parametrize("fp16", [False, True], ids=["bf16", "fp16"])
+def test_grid_training_reduces_loss(sty, cuda, fp16):
+    net, c = _net(sty, seed=7, batch=4096, learning_rate=1e-2, fp16=fp16)
     rng = np.random.default_rng(4)
     x = _rows(rng, 1 << 15, c)
     tgt = np.stack([0.5 + 0.4 * np.sin(4 * x[:, 0] + 3 * x[:, 1]), 0.3 + 0.3 * x[:, 2] * x[:, 4],
