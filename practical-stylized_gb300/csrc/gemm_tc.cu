@@ -22,7 +22,7 @@
 //   k_gemm_dw: the weight gradient P^T Q: both operands MN-major, the reduction runs over a chunk
 //     of batch rows in steps of 64 (two staging buffers: the next step's rows are staged while the
 //     current MMAs run), the 128 x nq accumulator stays in TMEM across the chunk; k_dw_reduce then
-//     adds the chunks' partial sums in chunk order.
+//     adds the chunks' partial sums in a fixed order.
 #include <algorithm>
 
 #include "gemm_tc.cuh"
@@ -46,20 +46,28 @@ __host__ __device__ constexpr uint32_t idesc16(uint32_t m, uint32_t n, uint32_t 
 __host__ __device__ constexpr uint32_t tmem_cols(int n) { return n <= 32 ? 32u : n <= 64 ? 64u : n <= 128 ? 128u : 256u; }
 
 // rows [r0, r0 + R) x C columns of a row-major 16-bit matrix (leading dimension ld) into a
-// core-matrix image; slot q holds core matrix q / 8, row q % 8, so consecutive threads store
-// consecutive 16-byte slots; rows at or past `rows` and columns at or past `cvalid` are zero
+// core-matrix image, as asynchronous 16-byte copies (cp.async: every copy of the thread in flight at
+// once; the caller commits and waits); slot q holds core matrix q / 8, row q % 8, so consecutive
+// threads fill consecutive 16-byte slots; rows at or past `rows` and columns at or past `cvalid`
+// are zero-filled (source size 0, the source address then unread)
 __device__ __forceinline__ void stage(uint8_t *img, const uint16_t *src, int ld, int r0, int R, int C, int rows,
                                       int tid, int cvalid = 1 << 30) {
     const int ncb = C >> 3, nq = R * ncb;
+    const uint32_t dst0 = smem_u32(img);
     for (int q = tid; q < nq; q += kThreads) {
         const int g = q >> 3, rr = q & 7;
         const int rb = g / ncb, cb = g - rb * ncb;
         const int r = r0 + rb * 8 + rr;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (r < rows && cb * 8 < cvalid) v = __ldg(reinterpret_cast<const uint4 *>(src + (size_t)r * ld + cb * 8));
-        *reinterpret_cast<uint4 *>(img + (size_t)q * 16) = v;
+        const bool ok = r < rows && cb * 8 < cvalid;
+        const uint16_t *p = ok ? src + (size_t)r * ld + cb * 8 : src;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst0 + (uint32_t)q * 16u), "l"(p),
+                     "r"(ok ? 16 : 0)
+                     : "memory");
     }
 }
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t cols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(cols)
@@ -98,35 +106,48 @@ __global__ void __launch_bounds__(kThreads) k_gemm_rows(const RowArgs a) {
     __shared__ uint32_t tmem_slot;
     const int tid = threadIdx.x, warp = tid >> 5;
     const uint32_t cols = tmem_cols(a.n);
-    const uint32_t wbytes = (uint32_t)a.n * a.ka * 2u;
+    const uint32_t wbytes = (uint32_t)a.n * a.ka * 2u, abytes = (uint32_t)TM * a.ka * 2u;
     uint8_t *wimg = smem;
-    uint8_t *aimg = smem + ((wbytes + 1023u) & ~1023u);
+    uint8_t *aimgs[2] = {smem + ((wbytes + 1023u) & ~1023u), smem + ((wbytes + 1023u) & ~1023u) + ((abytes + 1023u) & ~1023u)};
+    const int ntiles = (a.rows + TM - 1) / TM;
+    // the weights and the first tile in one copy group
     if (a.w_mn) stage(wimg, a.w, a.n, 0, a.ka, a.n, a.ka, tid);  // W [ka][n]
     else stage(wimg, a.w, a.ka, 0, a.n, a.ka, a.n, tid);         // W [n][ka]
+    if ((int)blockIdx.x < ntiles) stage(aimgs[0], a.a, a.lda, (int)blockIdx.x * TM, TM, a.ka, a.rows, tid);
+    cp_commit();
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(&tmem_slot, cols);
-    fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
     const uint32_t tmem = tmem_slot;
     const uint32_t lane_base = tmem + (((uint32_t)warp * 32u) << 16);
-    const uint32_t abase = smem_u32(aimg), wbase = smem_u32(wimg);
+    const uint32_t wbase = smem_u32(wimg);
     const uint32_t sbo_k = (uint32_t)(a.ka / 8) * 128u, nstride = (uint32_t)(a.n / 8) * 128u;
     const uint32_t idesc = idesc16(TM, (uint32_t)a.n, 0u, (uint32_t)a.w_mn, (uint32_t)a.f16);
     const bool f16 = a.f16 != 0;
     uint32_t phase = 0;
     bool failed = false;
-    const int ntiles = (a.rows + TM - 1) / TM;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    int k = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, k++) {
         const int r0 = tile * TM;
-        stage(aimg, a.a, a.lda, r0, TM, a.ka, a.rows, tid);
+        // prefetch the next tile into the other buffer (its last reader, the previous tile's MMA, has
+        // completed: its commit was waited for before that tile's epilogue)
+        const int next = tile + (int)gridDim.x;
+        if (next < ntiles) {
+            stage(aimgs[(k + 1) & 1], a.a, a.lda, next * TM, TM, a.ka, a.rows, tid);
+            cp_commit();
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
+        }
         fence_async_smem();
         fence_before();
         __syncthreads();
+        const uint32_t abase = smem_u32(aimgs[k & 1]);
         if (tid == 0) {
             fence_after();
             for (int ks = 0; ks < a.ka / 16; ks++) {
@@ -184,6 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_rows(const RowArgs a) {
         fence_before();
         __syncthreads();
     }
+    cp_wait<0>();  // no copy into shared memory outlives the loop
     if (failed) mbar_wait(&bar, phase, a.status);  // the MMAs may still run: one more bounded wait
     fence_before();
     __syncthreads();
@@ -222,19 +244,31 @@ __global__ void __launch_bounds__(kThreads) k_gemm_dw(const DwArgs a) {
     const uint32_t pstride = (TM / 8) * 128u, qstride = (uint32_t)(a.nq / 8) * 128u;
     const uint32_t idesc = idesc16(TM, (uint32_t)a.nq, 1u, 1u, (uint32_t)a.f16);
     bool failed = false;
+    auto issue = [&](int s) {  // step s's rows into buffer s & 1 (P's columns past mp are zero)
+        uint8_t *pimg = smem + (size_t)(s & 1) * bufbytes, *qimg = pimg + pbytes;
+        const int r0 = b0 + s * kDwStep;
+        stage(pimg, a.p, a.ldp, r0, kDwStep, TM, b1, tid, a.mp);
+        stage(qimg, a.q, a.ldq, r0, kDwStep, a.nq, b1, tid);
+        cp_commit();
+    };
+    if (steps > 0) issue(0);
     for (int s = 0; s < steps; s++) {
         const int buf = s & 1;
-        if (s >= 2) {
-            const bool got = mbar_wait(&bars[buf], (uint32_t)((s - 2) >> 1) & 1u, a.status);
-            if (!__syncthreads_and(got)) {
-                failed = true;
-                break;
+        if (s + 1 < steps) {
+            // buffer (s + 1) & 1 was last read by step s - 1's MMAs
+            if (s >= 1) {
+                const bool got = mbar_wait(&bars[(s + 1) & 1], (uint32_t)((s - 1) >> 1) & 1u, a.status);
+                if (!__syncthreads_and(got)) {
+                    failed = true;
+                    break;
+                }
             }
+            issue(s + 1);
+            cp_wait<1>();
+        } else {
+            cp_wait<0>();
         }
         uint8_t *pimg = smem + (size_t)buf * bufbytes, *qimg = pimg + pbytes;
-        const int r0 = b0 + s * kDwStep;
-        stage(pimg, a.p, a.ldp, r0, kDwStep, TM, b1, tid, a.mp);  // P's columns past mp are zero
-        stage(qimg, a.q, a.ldq, r0, kDwStep, a.nq, b1, tid);
         fence_async_smem();
         fence_before();
         __syncthreads();
@@ -247,6 +281,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_dw(const DwArgs a) {
             mma_commit(&bars[buf]);
         }
     }
+    cp_wait<0>();
     if (!failed) {
         bool got = true;
         for (int s = steps >= 2 ? steps - 2 : 0; s < steps; s++)
@@ -276,16 +311,30 @@ __global__ void __launch_bounds__(kThreads) k_gemm_dw(const DwArgs a) {
     if (warp == 0) tmem_free(tmem, cols);
 }
 
-__global__ void k_dw_reduce(const float *__restrict__ partials, int nchunks, int mp, int nq, int n_valid,
-                            int transpose, int ldd, float scale, float *__restrict__ dst) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= mp * nq) return;
+// 32 consecutive outputs per block, 8 thread groups: group j sums chunks j, j + 8, j + 16, ... in
+// order (for one chunk the block reads 32 consecutive floats), then thread j = 0 adds the 8 group
+// sums in order -- a fixed summation order for every output
+constexpr int kRedOut = 32, kRedGroups = 8;
+__global__ void __launch_bounds__(kRedOut * kRedGroups) k_dw_reduce(const float *__restrict__ partials, int nchunks,
+                                                                  int mp, int nq, int n_valid, int transpose, int ldd,
+                                                                  float scale, float *__restrict__ dst) {
+    __shared__ float part[kRedGroups][kRedOut];
+    const int o = threadIdx.x % kRedOut, j = threadIdx.x / kRedOut;
+    const int i = blockIdx.x * kRedOut + o;
+    const size_t stride = (size_t)TM * nq;
+    float s = 0.0f;
+    if (i < mp * nq)
+        for (int c = j; c < nchunks; c += kRedGroups) s += partials[(size_t)c * stride + i];
+    part[j][o] = s;
+    __syncthreads();
+    if (j != 0 || i >= mp * nq) return;
+    float t = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kRedGroups; k++) t += part[k][o];
     const int m = i / nq, n = i - m * nq;
     if (n >= n_valid) return;
-    float s = 0.0f;
-    for (int c = 0; c < nchunks; c++) s += partials[(size_t)c * TM * nq + i];
-    if (transpose) dst[(size_t)n * ldd + m] = s * scale;
-    else dst[(size_t)m * ldd + n] = s * scale;
+    if (transpose) dst[(size_t)n * ldd + m] = t * scale;
+    else dst[(size_t)m * ldd + n] = t * scale;
 }
 
 int sm_count() {
@@ -330,7 +379,7 @@ sty_status tc_gemm_rows(const uint16_t *a, int lda, const uint16_t *w, int rows,
     g.epi = epi;
     g.scale = scale;
     const size_t wb = ((size_t)n * ka * 2 + 1023) & ~(size_t)1023;
-    const size_t smem = std::max(kMinSmem, wb + (size_t)TM * ka * 2);
+    const size_t smem = std::max(kMinSmem, wb + 2 * (((size_t)TM * ka * 2 + 1023) & ~(size_t)1023));
     STY_TRY(check_cuda(cudaFuncSetAttribute(k_gemm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "cudaFuncSetAttribute(k_gemm_rows)"));
     const int ntiles = (rows + TM - 1) / TM;
@@ -366,8 +415,8 @@ sty_status tc_gemm_dw(const uint16_t *p, int ldp, int mp, const uint16_t *q, int
                        "cudaFuncSetAttribute(k_gemm_dw)"));
     k_gemm_dw<<<nchunks, kThreads, smem, st>>>(g);
     STY_TRY(check_launch("k_gemm_dw"));
-    k_dw_reduce<<<(mp * nq + 255) / 256, 256, 0, st>>>(partials, nchunks, mp, nq, n_valid, transpose ? 1 : 0, ldd,
-                                                        scale, dst);
+    k_dw_reduce<<<(mp * nq + kRedOut - 1) / kRedOut, kRedOut * kRedGroups, 0, st>>>(
+        partials, nchunks, mp, nq, n_valid, transpose ? 1 : 0, ldd, scale, dst);
     return check_launch("k_dw_reduce");
 }
 

@@ -308,38 +308,61 @@ __global__ void k_tab_half(size_t n, const float *__restrict__ t, __half *__rest
 //     count t_p and use it in the bias correction. Updated entries refresh their FP16 copy.
 //   EMA over every parameter: ema = (ema d (1 - d^(t-1)) + w (1 - d)) / (1 - d^t), with the FP16
 //     copy of the EMA tables written in place.
+// Four parameters per thread (the MLP block and the tables both start at multiples of 16 floats).
+// A table entry's bias correction 1 - b^t for its own step count t is 1 - 2^(t log2 b) with log2 b
+// computed once on the host (exp2f: a few instructions, where powf's exact-rounding path took most
+// of the kernel's time in the divergent lanes of stepped entries).
 __global__ void k_adam_grid(size_t n_mlp, size_t np, float *__restrict__ w, float *__restrict__ m,
                             float *__restrict__ v, const float *__restrict__ g, float *__restrict__ ema,
                             uint32_t *__restrict__ tsteps, __half *__restrict__ tab16, __half *__restrict__ tab16_ema,
-                            float lr, float b1, float b2, float eps, float bc1, float bc2, float ema_decay,
-                            float ema_old, float ema_new) {
-    const size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (p >= np) return;
-    const float gr = g[p];
-    float wn = w[p];
-    float c1 = bc1, c2 = bc2;
-    bool step = true;
-    if (p >= n_mlp) {
-        step = gr != 0.0f;
-        if (step) {
-            const uint32_t tp = tsteps[p - n_mlp] + 1u;
-            tsteps[p - n_mlp] = tp;
-            c1 = 1.0f - powf(b1, (float)tp);
-            c2 = 1.0f - powf(b2, (float)tp);
+                            float lr, float b1, float b2, float eps, float bc1, float bc2, float l2b1, float l2b2,
+                            float ema_decay, float ema_old, float ema_new) {
+    const size_t p0 = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * 4;
+    if (p0 >= np) return;
+    const float4 g4 = *reinterpret_cast<const float4 *>(g + p0);
+    float4 w4 = *reinterpret_cast<const float4 *>(w + p0);
+    float4 e4 = *reinterpret_cast<const float4 *>(ema + p0);
+    const float gr[4] = {g4.x, g4.y, g4.z, g4.w};
+    float wn[4] = {w4.x, w4.y, w4.z, w4.w}, en[4] = {e4.x, e4.y, e4.z, e4.w};
+    const bool table = p0 >= n_mlp;
+    const bool any = !table || gr[0] != 0.0f || gr[1] != 0.0f || gr[2] != 0.0f || gr[3] != 0.0f;
+    if (any) {
+        float4 m4 = *reinterpret_cast<const float4 *>(m + p0), v4 = *reinterpret_cast<const float4 *>(v + p0);
+        float mm[4] = {m4.x, m4.y, m4.z, m4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
+        uint4 t4 = make_uint4(0u, 0u, 0u, 0u);
+        if (table) t4 = *reinterpret_cast<const uint4 *>(tsteps + (p0 - n_mlp));
+        uint32_t tp[4] = {t4.x, t4.y, t4.z, t4.w};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            float c1 = bc1, c2 = bc2;
+            if (table) {
+                if (gr[k] == 0.0f) continue;  // untouched entry: weight, moments and step count stay
+                tp[k] += 1u;
+                c1 = 1.0f - exp2f((float)tp[k] * l2b1);
+                c2 = 1.0f - exp2f((float)tp[k] * l2b2);
+            }
+            mm[k] = b1 * mm[k] + (1.0f - b1) * gr[k];
+            vv[k] = b2 * vv[k] + (1.0f - b2) * gr[k] * gr[k];
+            wn[k] -= lr * (mm[k] / c1) / (sqrtf(vv[k] / c2) + eps);
+        }
+        *reinterpret_cast<float4 *>(m + p0) = make_float4(mm[0], mm[1], mm[2], mm[3]);
+        *reinterpret_cast<float4 *>(v + p0) = make_float4(vv[0], vv[1], vv[2], vv[3]);
+        *reinterpret_cast<float4 *>(w + p0) = make_float4(wn[0], wn[1], wn[2], wn[3]);
+        if (table) {
+            *reinterpret_cast<uint4 *>(tsteps + (p0 - n_mlp)) = make_uint4(tp[0], tp[1], tp[2], tp[3]);
+            __half2 *t16 = reinterpret_cast<__half2 *>(tab16 + (p0 - n_mlp));
+            t16[0] = __floats2half2_rn(wn[0], wn[1]);
+            t16[1] = __floats2half2_rn(wn[2], wn[3]);
         }
     }
-    if (step) {
-        const float mm = b1 * m[p] + (1.0f - b1) * gr;
-        const float vv = b2 * v[p] + (1.0f - b2) * gr * gr;
-        m[p] = mm;
-        v[p] = vv;
-        wn -= lr * (mm / c1) / (sqrtf(vv / c2) + eps);
-        w[p] = wn;
-        if (p >= n_mlp) tab16[p - n_mlp] = __float2half_rn(wn);
+#pragma unroll
+    for (int k = 0; k < 4; k++) en[k] = (en[k] * ema_decay * ema_old + wn[k] * (1.0f - ema_decay)) * ema_new;
+    *reinterpret_cast<float4 *>(ema + p0) = make_float4(en[0], en[1], en[2], en[3]);
+    if (table) {
+        __half2 *e16 = reinterpret_cast<__half2 *>(tab16_ema + (p0 - n_mlp));
+        e16[0] = __floats2half2_rn(en[0], en[1]);
+        e16[1] = __floats2half2_rn(en[2], en[3]);
     }
-    const float e = (ema[p] * ema_decay * ema_old + wn * (1.0f - ema_decay)) * ema_new;
-    ema[p] = e;
-    if (p >= n_mlp) tab16_ema[p - n_mlp] = __float2half_rn(e);
 }
 
 // ---- tensor-core inference --------------------------------------------------------------------------
@@ -794,7 +817,7 @@ sty_status grid_create(const sty_nrc_grid_config *c, GridModel **out, size_t *n_
     }
     g->out_off = o;
     g->loff.push_back(o);
-    g->n_mlp = o + (size_t)g->O * g->H;
+    g->n_mlp = o + (size_t)g->O * g->H;  // a multiple of 16 (H is), as the tables' size is of 8 entries
     g->n_tab = off * geo.feats;
     *n_params = g->n_mlp + g->n_tab;
     *n_mlp = g->n_mlp;
@@ -970,10 +993,12 @@ sty_status grid_reset_steps(GridModel *g) {
 sty_status grid_adam(GridModel *g, float *w, float *m, float *v, const float *grad, float *ema, float lr, float b1,
                      float b2, float eps, float bc1, float bc2, float ema_decay, float ema_old, float ema_new,
                      cudaStream_t st) {
-    const size_t np = g->n_mlp + g->n_tab;
-    k_adam_grid<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(g->n_mlp, np, w, m, v, grad, ema, g->tsteps, g->tab16,
-                                                              g->tab16_ema, lr, b1, b2, eps, bc1, bc2, ema_decay,
-                                                              ema_old, ema_new);
+    const size_t np = g->n_mlp + g->n_tab;  // a multiple of 4: n_mlp of 16, the tables of 8 entries
+    const size_t nt = (np + 3) / 4;
+    k_adam_grid<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g->n_mlp, np, w, m, v, grad, ema, g->tsteps, g->tab16,
+                                                              g->tab16_ema, lr, b1, b2, eps, bc1, bc2,
+                                                              (float)std::log2((double)b1), (float)std::log2((double)b2),
+                                                              ema_decay, ema_old, ema_new);
     return check_launch("k_adam_grid");
 }
 
