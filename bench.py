@@ -652,6 +652,81 @@ def c5_bench(sty, W: int = 160, H: int = 90):
     return res
 
 
+def c5_full_bench(sty, W: int = 1920, H: int = 1080, ref_spp: int = 1024):
+    """The full stylized render at its stated scale: the interior workload (6 x 3 x 4 m room of ~377 k
+    triangles, door open 20 degrees, the only emitter behind it; GGX + diffuse; toon (band 0.2) + a
+    3-colour luminance ramp at bounces 0-1) at 1920 x 1080, 64 spp (16 paths per pixel x 4
+    repeats), max depth 8, the screen-space NL-PF filter (radius 8 px, sigma_pos 0.05 m, sigma_nrm
+    0.2, program 0 by its depth mask). Each method is timed (CUDA-synchronised wall time, cache
+    training included) and scored by image MSE against a `ref_spp`-spp FP64-accumulated plain
+    NL-PF render of the same view (the same filter, max depth 8):
+      nl_pf_fp32             plain NL-PF: every path traced to depth 8 and filtered at every depth;
+      nl_pf_nrc_ref_network  NL-PF and NL-NRC together (sty_pf_nrc_render): paths traced to depth 3,
+                             the cache's prediction there standing in for the rest of each path,
+                             the filter on depths 2 .. 0; the cache is the reference's network (hash
+                             grid 22 x 4 on 2^19 tables + one-blob + identity, 5 x 128, BF16 tcgen05)
+                             trained online by the NL-NRC loop (128 iterations x 4 batches of 2^14);
+      nl_pf_nrc_bf16 / fp32  the same at cache depth 2 with the spherical-frequency cache (BF16
+                             tcgen05 / FP32 CUDA cores): the BF16-vs-FP32 comparison at equal MSE;
+      cut_at_depth_K         the paths simply ended at depth K (no cache): what the cache buys."""
+    import numpy as np
+    import torch
+    a = sty.abi
+    pos, mids, mats, cam = sty.scene.room_with_door(W, H)
+    sc = sty.scene.Scene(pos, mids, mats, cam)
+    progs = [a.style_program([a.toon(0.2, depth_mask=0b11),
+                              a.ramp_smooth(30.0, [0.02, 0.15, 0.6],
+                                            [(0.08, 0.1, 0.2), (0.55, 0.45, 0.35), (1.3, 1.2, 1.0)],
+                                            depth_mask=0b11)])]
+    scr = dict(radius=8, sigma_pixel=0.0, sigma_pos=0.05, sigma_nrm=0.2, screen_style=0)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        film, extra = fn()
+        torch.cuda.synchronize()
+        return film.cpu().numpy(), time.perf_counter() - t0, extra
+
+    def pf_cfg(depth, repeats, seed):
+        return sty.scene.screen_render_config(max_depth=depth, branch=16, repeats=repeats, seed=seed, **scr)
+
+    sc.render(pf_cfg(8, 1, 99), progs)  # warm-up
+    ref, t_ref, nv_ref = timed(lambda: sc.render(pf_cfg(8, ref_spp // 16, 4242), progs))
+    mse = lambda im: float(((im - ref) ** 2).mean())  # noqa: E731
+    res = {"workload": f"interior room {pos.shape[0]} tris, door 20 deg, {W}x{H}, 64 spp, max depth 8, toon + "
+                       "3-colour ramp at bounces 0-1, screen-space NL-PF radius 8 px",
+           "reference": {"spp": ref_spp, "seconds": t_ref, "vertices": nv_ref, "image_mean": float(ref.mean())}}
+    img, t, nv = timed(lambda: sc.render(pf_cfg(8, 4, 7), progs))
+    res["nl_pf_fp32"] = {"spp": 64, "seconds": t, "mpath_vertices_per_s": nv / t / 1e6, "image_mse": mse(img)}
+    for K in (2, 3):
+        img, t, _ = timed(lambda: sc.render(pf_cfg(K, 4, 7), progs))
+        res[f"cut_at_depth_{K}"] = {"spp": 64, "seconds": t, "image_mse": mse(img), "image_mean": float(img.mean())}
+    caches = (("nl_pf_nrc_ref_network", 3, lambda: sty.nrc.NRC(sty.nrc.grid_config(
+                  max_depth=8, batch_size=1 << 14, learning_rate=1e-2, seed=1))),
+              ("nl_pf_nrc_bf16", 2, lambda: sty.nrc.NRC(sty.nrc.config(
+                  sty.nrc.C4_FREQS, 3, 1 << 14, 5, sty.nrc.STY_NRC_BF16, learning_rate=1e-2, seed=1))),
+              ("nl_pf_nrc_fp32", 2, lambda: sty.nrc.NRC(sty.nrc.config(
+                  sty.nrc.C4_FREQS, 3, 1 << 14, 5, sty.nrc.STY_NRC_FP32, learning_rate=1e-2, seed=1))))
+    for name, K, make in caches:
+        w = make()  # untimed warm-up (the first use of a path loads its kernels)
+        sc.pf_nrc_render(w, sty.scene.screen_render_config(max_depth=8, branch=1, repeats=1, seed=1, **scr),
+                         sty.scene.nrc_render_config(max_depth=8, training_iters=2, batches_per_iter=1, seed=1), K,
+                         progs)
+        torch.cuda.synchronize()
+        w.close()
+        net = make()
+        nc = sty.scene.nrc_render_config(max_depth=8, training_iters=128, batches_per_iter=4, seed=3)
+        img, t, st = timed(lambda: sc.pf_nrc_render(net, pf_cfg(8, 4, 7), nc, K, progs))
+        res[name] = {"spp": 64, "cache_depth": K, "seconds": t, "training_rows": int(st.training_rows),
+                     "queries": int(st.inference_queries), "image_mse": mse(img), "image_mean": float(img.mean())}
+        net.close()
+    res["speedup_ref_network_over_plain"] = res["nl_pf_fp32"]["seconds"] / res["nl_pf_nrc_ref_network"]["seconds"]
+    res["speedup_bf16_over_fp32_cache"] = res["nl_pf_nrc_fp32"]["seconds"] / res["nl_pf_nrc_bf16"]["seconds"]
+    res["mse_ratio_bf16_over_fp32_cache"] = res["nl_pf_nrc_bf16"]["image_mse"] / res["nl_pf_nrc_fp32"]["image_mse"]
+    sc.close()
+    return res
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -706,6 +781,9 @@ def run(args):
         return
     if args.c5_only:  # the full stylized render alone
         print(json.dumps({"c5_render": c5_bench(sty)}), flush=True)
+        return
+    if args.c5_full:  # the full stylized render at 1920 x 1080 x 64 spp (minutes: not in the default run)
+        print(json.dumps({"c5_full": c5_full_bench(sty, ref_spp=args.c5_ref_spp)}), flush=True)
         return
     if args.c3_only:  # profiling case: the adjoint alone
         print(json.dumps({"c3_adjoint": c3_bench(sty, reps=max(1, args.steps))}), flush=True)
@@ -921,6 +999,9 @@ def main():
     ap.add_argument("--c1b-only", action="store_true",
                     help="profiling case: only the traced Cornell render with the screen-space filter")
     ap.add_argument("--c5-only", action="store_true", help="only the full stylized interior render")
+    ap.add_argument("--c5-full", action="store_true",
+                    help="the full stylized render at 1920x1080 x 64 spp against a high-spp NL-PF reference")
+    ap.add_argument("--c5-ref-spp", type=int, default=1024, help="spp of the --c5-full reference (multiple of 16)")
     ap.add_argument("--c3-only", action="store_true", help="profiling case: only the adjoint")
     ap.add_argument("--brpt-only", action="store_true",
                     help="profiling case: one branching path tracer render of the interior workload")

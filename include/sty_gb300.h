@@ -656,6 +656,28 @@ STY_API sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_
                                   const sty_style_program *programs, uint32_t n_programs, double *film,
                                   sty_nrc_render_stats *stats, void *stream);
 
+/* NL-PF and NL-NRC together: NL-PF's screen-space filter over the first `cache_depth` bounces, the
+ * neural radiance cache for the rest of the path. First the cache is trained by the NL-NRC
+ * training loop of `nrc` (sty_nrc_render's training iterations: nrc.training_iters,
+ * batches_per_iter, training_paths, per_level_training, learn_stylized_radiance, seed, max_depth;
+ * its rendering fields are not used). Then, `pf.repeats` times, the paths of a STY_PF_MODE_SCREEN
+ * render of `pf` (branch paths per pixel, pf.seed) are traced to depth K = cache_depth; at every
+ * depth-K vertex the cache's EMA prediction, styled at depth K (unless the cache learns styled
+ * radiance), is the radiance leaving the vertex (out_K, as the cache's prediction stands in for the
+ * traced continuation in nrc_pt.rs:723-776); sty_pf_screen_filter_depth filters depths K - 1 .. 0
+ * (each depth's input rad + thr * out of the depth below) and the film receives (1 / pf.repeats) of
+ * the pixel means of out_0. pf.max_depth is not used; the cache's rows are those of
+ * sty_nrc_render (11 inputs, or 20 + nrc.max_depth), and 1 <= cache_depth <= nrc.max_depth. */
+typedef struct sty_pf_nrc_config {
+    sty_pf_render_config pf;     /* mode STY_PF_MODE_SCREEN: branch, repeats, seed, screen, screen_style */
+    sty_nrc_render_config nrc;   /* the cache's training loop */
+    uint32_t cache_depth;
+    uint32_t reserved;
+} sty_pf_nrc_config;
+STY_API sty_status sty_pf_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_pf_nrc_config *config,
+                                     const sty_style_program *programs, uint32_t n_programs, double *film,
+                                     sty_nrc_render_stats *stats, void *stream);
+
 /* Branching path tracer (crates/akari_integrator/src/branching_pt.rs, Config :77-100): the paper's
  * BrPT baseline, and with inner_samples = {1} the plain stylized path tracer of
  * configs/teaser/pt.json. Per pixel a tree of vertices: the k-th rough vertex (average roughness

@@ -138,6 +138,7 @@ SIGNATURES = {
     "sty_std_rng_u64": (C.c_int32, [C.c_uint64, C.c_uint64, C.c_uint64, _VP, _VP]),
     "sty_pf_trace_records": (C.c_int32, [C.c_void_p, _VP, _VP, C.c_uint32, _VP, C.POINTER(C.c_uint64), _VP]),
     "sty_scene_camera_rays": (C.c_int32, [C.c_void_p, C.c_uint32, C.c_uint64, _VP, _VP]),
+    "sty_pf_nrc_render": (C.c_int32, [C.c_void_p, C.c_void_p, _VP, _VP, C.c_uint32, _VP, _VP, _VP]),
     "sty_hash_cells": (C.c_int32, [_VP, C.c_uint64, C.POINTER(C.c_float * 3), C.POINTER(C.c_float * 3),
                                    C.POINTER(C.c_uint32 * 3), C.c_uint32, _VP, _VP, _VP]),
 }

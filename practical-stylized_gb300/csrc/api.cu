@@ -273,6 +273,7 @@ uint64_t sty_struct_size(const char *name) {
     if (!strcmp(name, "sty_brpt_config")) return sizeof(sty_brpt_config);
     if (!strcmp(name, "sty_brpt_stats")) return sizeof(sty_brpt_stats);
     if (!strcmp(name, "sty_pf_records_out")) return sizeof(sty_pf_records_out);
+    if (!strcmp(name, "sty_pf_nrc_config")) return sizeof(sty_pf_nrc_config);
     return 0;
 }
 

@@ -1048,41 +1048,32 @@ extern "C" sty_status sty_nrc_samples(sty_scene *scene, uint32_t mode, uint32_t 
     return STY_OK;
 }
 
-extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_render_config *cfg,
-                                     const sty_style_program *programs, uint32_t n_programs, double *film,
-                                     sty_nrc_render_stats *stats, void *stream) {
-    clear_error();
-    STY_ARG_CHECK(scene && nrc && cfg && film, "sty_nrc_render: null argument");
-    STY_ARG_CHECK(cfg->max_depth >= 1 && cfg->max_depth <= 30 && cfg->repeats >= 1 && cfg->batches_per_iter >= 1,
-                  "bad max_depth / repeats / batches_per_iter");
-    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
-    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
-    const uint32_t in_dims = nrc_input_dims(nrc);
-    STY_ARG_CHECK(in_dims == 11 || in_dims == 20 + cfg->max_depth,
-                  "the cache must take 11-input rows (STY_NRC_ROWS_SPHERICAL) or 20 + max_depth (STY_NRC_ROWS_REF)");
-    cudaStream_t st = as_stream(stream);
-    const sty_camera &cam = scene_camera(scene);
-    const uint32_t npx = cam.width * cam.height, D = cfg->max_depth;
-    uint64_t tp = cfg->training_paths;
-    if (!tp) tp = (uint64_t)cfg->batches_per_iter * nrc_batch_size(nrc) / (D + 1);
-    tp = std::min<uint64_t>(std::max<uint64_t>(tp, 1), npx);
-    STY_ARG_CHECK(tp * (D + 1) < (1ull << 31), "too many training rows");
-    const uint32_t n = (uint32_t)tp;
-    sty_nrc_render_stats acc = {0, 0, 0.0f, 0};
-
+namespace {
+// The cache's feature rows for this scene (position normalised to its bounds, the cache's layout)
+FeatArgs feat_args(sty_scene *scene, uint32_t in_dims, uint32_t max_depth) {
     FeatArgs fa;
-    {
-        float bmin[3], bmax[3];
-        scene_bounds(scene, bmin, bmax);
-        for (int a = 0; a < 3; a++) {
-            fa.bmin[a] = bmin[a];
-            fa.bext[a] = std::max(bmax[a] - bmin[a], 1e-6f);
-        }
-        fa.max_depth = D;
-        fa.layout = in_dims == 11 ? STY_NRC_ROWS_SPHERICAL : STY_NRC_ROWS_REF;
-        fa.dims = in_dims;
+    float bmin[3], bmax[3];
+    scene_bounds(scene, bmin, bmax);
+    for (int a = 0; a < 3; a++) {
+        fa.bmin[a] = bmin[a];
+        fa.bext[a] = std::max(bmax[a] - bmin[a], 1e-6f);
     }
-    // ---- training
+    fa.max_depth = max_depth;
+    fa.layout = in_dims == 11 ? STY_NRC_ROWS_SPHERICAL : STY_NRC_ROWS_REF;
+    fa.dims = in_dims;
+    return fa;
+}
+
+// The NL-NRC training loop (NRCPathTracer::render's training iterations, nrc_pt.rs:1519-1690): per
+// iteration `n` paths from pixels drawn from their own Pcg32 streams (:1394), traced to max_depth;
+// the cache (training weights) predicts the radiance at every vertex of depth >= 1, styled at that
+// depth unless the cache learns styled radiance; each vertex of depth >= the training level gets
+// the target Le + NEE + f L_next mis / pdf with L_next that prediction; the rows train the cache.
+sty_status nrc_train_loop(sty_scene *scene, sty_nrc *nrc, const sty_nrc_render_config *cfg,
+                          const sty_style_program *programs, uint32_t n_programs, const FeatArgs &fa, uint32_t n,
+                          cudaStream_t st, void *stream, sty_nrc_render_stats &acc) {
+    const uint32_t D = cfg->max_depth;
+    const uint32_t npx = scene_camera(scene).width * scene_camera(scene).height;
     for (uint32_t it = 0; it < cfg->training_iters; it++) {
         TraceJob job;
         STY_TRY(job.init(scene, 1, D, programs, n_programs, cfg->seed * 0x9e3779b97f4a7c15ull + it, st, n));
@@ -1152,6 +1143,35 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
             acc.training_rows += h;
         }
     }
+    return STY_OK;
+}
+}  // namespace
+
+extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_nrc_render_config *cfg,
+                                     const sty_style_program *programs, uint32_t n_programs, double *film,
+                                     sty_nrc_render_stats *stats, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && nrc && cfg && film, "sty_nrc_render: null argument");
+    STY_ARG_CHECK(cfg->max_depth >= 1 && cfg->max_depth <= 30 && cfg->repeats >= 1 && cfg->batches_per_iter >= 1,
+                  "bad max_depth / repeats / batches_per_iter");
+    STY_ARG_CHECK(programs || n_programs == 0, "null programs");
+    STY_ARG_CHECK(n_programs <= 64, "at most 64 style programs");
+    const uint32_t in_dims = nrc_input_dims(nrc);
+    STY_ARG_CHECK(in_dims == 11 || in_dims == 20 + cfg->max_depth,
+                  "the cache must take 11-input rows (STY_NRC_ROWS_SPHERICAL) or 20 + max_depth (STY_NRC_ROWS_REF)");
+    cudaStream_t st = as_stream(stream);
+    const sty_camera &cam = scene_camera(scene);
+    const uint32_t npx = cam.width * cam.height, D = cfg->max_depth;
+    uint64_t tp = cfg->training_paths;
+    if (!tp) tp = (uint64_t)cfg->batches_per_iter * nrc_batch_size(nrc) / (D + 1);
+    tp = std::min<uint64_t>(std::max<uint64_t>(tp, 1), npx);
+    STY_ARG_CHECK(tp * (D + 1) < (1ull << 31), "too many training rows");
+    const uint32_t n = (uint32_t)tp;
+    sty_nrc_render_stats acc = {0, 0, 0.0f, 0};
+
+    const FeatArgs fa = feat_args(scene, in_dims, D);
+    // ---- training
+    STY_TRY(nrc_train_loop(scene, nrc, cfg, programs, n_programs, fa, n, st, stream, acc));
     // ---- rendering
     const int style0 = cfg->no_first_hit_stylization ? 0 : 1;
     const int stylize_pred = cfg->learn_stylized_radiance ? 0 : 1;
@@ -1243,6 +1263,66 @@ extern "C" sty_status sty_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_n
         STY_TRY(check_launch("k_fg_splat"));
     }
     STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync nrc render"));
+    if (stats) *stats = acc;
+    return STY_OK;
+}
+
+// NL-PF with the cache at the path ends (sty_pf_nrc_render): the cache trained by the NL-NRC loop,
+// then per repeat a SCREEN-mode trace to cache_depth, the cache's EMA prediction at the depth-K
+// vertices (styled at K) as out_K, the screen filter on depths K - 1 .. 0 and the splat.
+extern "C" sty_status sty_pf_nrc_render(sty_scene *scene, sty_nrc *nrc, const sty_pf_nrc_config *cfg,
+                                        const sty_style_program *programs, uint32_t n_programs, double *film,
+                                        sty_nrc_render_stats *stats, void *stream) {
+    clear_error();
+    STY_ARG_CHECK(scene && nrc && cfg && film, "sty_pf_nrc_render: null argument");
+    const sty_pf_render_config &pf = cfg->pf;
+    const sty_nrc_render_config &nc = cfg->nrc;
+    STY_ARG_CHECK(pf.mode == STY_PF_MODE_SCREEN, "sty_pf_nrc_render: pf.mode must be STY_PF_MODE_SCREEN");
+    STY_TRY(check_render_config(&pf, programs, n_programs));
+    const uint32_t K = cfg->cache_depth, D = nc.max_depth;
+    STY_ARG_CHECK(D >= 1 && D <= 30 && nc.batches_per_iter >= 1, "bad nrc.max_depth / batches_per_iter");
+    STY_ARG_CHECK(K >= 1 && K <= D, "cache_depth %u must be in [1, nrc.max_depth = %u]", K, D);
+    const uint32_t in_dims = nrc_input_dims(nrc);
+    STY_ARG_CHECK(in_dims == 11 || in_dims == 20 + D,
+                  "the cache must take 11-input rows (STY_NRC_ROWS_SPHERICAL) or 20 + nrc.max_depth (STY_NRC_ROWS_REF)");
+    cudaStream_t st = as_stream(stream);
+    const sty_camera &cam = scene_camera(scene);
+    const uint32_t npx = cam.width * cam.height;
+    uint64_t tp = nc.training_paths;
+    if (!tp) tp = (uint64_t)nc.batches_per_iter * nrc_batch_size(nrc) / (D + 1);
+    tp = std::min<uint64_t>(std::max<uint64_t>(tp, 1), npx);
+    STY_ARG_CHECK(tp * (D + 1) < (1ull << 31), "too many training rows");
+    sty_nrc_render_stats acc = {0, 0, 0.0f, 0};
+    const FeatArgs fa = feat_args(scene, in_dims, D);
+    STY_TRY(nrc_train_loop(scene, nrc, &nc, programs, n_programs, fa, (uint32_t)tp, st, stream, acc));
+    const sty_style_program *prog = pf.screen_style >= 0 ? &programs[pf.screen_style] : nullptr;
+    const int stylize_pred = nc.learn_stylized_radiance ? 0 : 1;
+    TraceJob job;
+    STY_TRY(job.init(scene, pf.branch, K, programs, n_programs, pf.seed, st, 0, pf.branch));
+    STY_TRY(job.init_records(nullptr));
+    const uint32_t n = job.n;
+    float *qin = (float *)job.alloc(kQueryIn, (size_t)n * fa.dims * 4, "alloc query rows");
+    float *qpred = (float *)job.alloc(kQueryPred, (size_t)n * 3 * 4, "alloc predictions");
+    float *qscr = (float *)job.alloc(kQueryScratch, (size_t)n * 3 * 4, "alloc query scratch");
+    STY_TRY(job.s);
+    const sty_pf_records rec = job.records(pf.branch);
+    const unsigned nb = (n + 255) / 256;
+    for (uint32_t r = 0; r < pf.repeats; r++) {
+        STY_TRY(job.trace(st));
+        k_nrc_query_rows<<<nb, 256, 0, st>>>(job.sv, fa, n, job.vo[K], qin, qscr, K);
+        STY_TRY(check_launch("k_nrc_query_rows"));
+        STY_TRY(sty_nrc_inference(nrc, n, qin, qpred, stream));
+        acc.inference_queries += n;
+        k_nrc_style_pred<<<nb, 256, 0, st>>>(job.sv, n, job.vo[K], qpred, job.dprog, n_programs, K, stylize_pred,
+                                             job.out(K));
+        STY_TRY(check_launch("k_nrc_style_pred"));
+        for (int d = (int)K - 1; d >= 0; d--)
+            STY_TRY(sty_pf_screen_filter_depth(&rec, (uint32_t)d, &pf.screen, prog, job.out((uint32_t)d + 1),
+                                               job.out((uint32_t)d), nullptr, stream));
+        STY_TRY(sty_film_accumulate(job.out(0), (int32_t)cam.width, (int32_t)cam.height, (int32_t)pf.branch,
+                                    1.0 / pf.repeats, film, st));
+    }
+    STY_TRY(check_cuda(cudaStreamSynchronize(st), "sync pf nrc render"));
     if (stats) *stats = acc;
     return STY_OK;
 }

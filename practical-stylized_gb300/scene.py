@@ -64,6 +64,10 @@ class NrcRenderConfig(C.Structure):
                 ("final_gather", C.c_uint32), ("reserved", C.c_uint32), ("seed", C.c_uint64)]
 
 
+class PfNrcConfig(C.Structure):
+    _fields_ = [("pf", RenderConfig), ("nrc", NrcRenderConfig), ("cache_depth", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 class NrcRenderStats(C.Structure):
     _fields_ = [("training_rows", C.c_uint64), ("inference_queries", C.c_uint64), ("last_loss", C.c_float),
                 ("reserved", C.c_uint32)]
@@ -499,6 +503,25 @@ class Scene:
         st = NrcRenderStats()
         check(lib().sty_nrc_render(self.h, net.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(st),
                                    _stream_ptr(stream)))
+        return film, st
+
+    def pf_nrc_render(self, net, pf_cfg: RenderConfig, nrc_cfg: NrcRenderConfig, cache_depth: int, programs=(),
+                      film=None, stream=None):
+        """NL-PF with the neural cache at the path ends (sty_pf_nrc_render): `net` trained by the
+        NL-NRC loop of `nrc_cfg`, then the SCREEN-mode render of `pf_cfg` traced to `cache_depth`,
+        the cache's prediction there feeding the filter. Returns (film [H, W, 3] float64, stats)."""
+        import torch
+        from .pf import _stream_ptr
+        W, H = self.camera.width, self.camera.height
+        if film is None:
+            film = torch.zeros((H, W, 3), dtype=torch.float64, device="cuda")
+        cfg = PfNrcConfig()
+        cfg.pf, cfg.nrc, cfg.cache_depth = pf_cfg, nrc_cfg, cache_depth
+        progs = list(programs)
+        arr = (abi.StyleProgram * max(1, len(progs)))(*progs) if progs else None
+        st = NrcRenderStats()
+        check(lib().sty_pf_nrc_render(self.h, net.h, C.byref(cfg), arr, len(progs), film.data_ptr(), C.byref(st),
+                                      _stream_ptr(stream)))
         return film, st
 
     def brpt_render(self, cfg: BrptConfig, programs=(), film=None, stream=None):

@@ -47,7 +47,7 @@ def test_struct_sizes_match_the_library(sty):
                "sty_camera": "scene.Camera", "sty_pf_render_config": "scene.RenderConfig",
                "sty_nrc_render_config": "scene.NrcRenderConfig", "sty_nrc_render_stats": "scene.NrcRenderStats",
                "sty_brpt_config": "scene.BrptConfig", "sty_brpt_stats": "scene.BrptStats",
-               "sty_pf_records_out": "scene.RecordsOut"}
+               "sty_pf_records_out": "scene.RecordsOut", "sty_pf_nrc_config": "scene.PfNrcConfig"}
     declared = set(re.findall(r"\}\s*(sty_\w+)\s*;", (ROOT / "include" / "sty_gb300.h").read_text()))
     assert declared == set(mirrors), declared ^ set(mirrors)
     lib = sty.abi.lib()
