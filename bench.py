@@ -244,10 +244,14 @@ def nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
             n2.close()
         m_all = float(np.mean([m[0] for m in per_seed]))
         m_unlit = float(np.mean([m[1] for m in per_seed]))
-        flops_q = 2.0 * (5 * 64 * 64 + (16 if prec else 3) * 64)  # MMA work incl. the padded output rows
+        # algorithmic FLOPs: the 3-wide output layer at N = 3 (the MMAs pad it to 16); training per
+        # sample = forward + weight gradients + input gradients of every layer but the first
+        flops_q = 2.0 * (5 * 64 * 64 + 3 * 64)
+        flops_t = 3.0 * flops_q - 2.0 * 64 * 64
         res[name] = {"ms_per_frame": ms, "msamples_per_s": (nq + nt) / ms / 1e3,
                      "inference_ms": inf_ms, "train_ms": ms - inf_ms,
                      "inference_tflops": nq * flops_q / (inf_ms / 1e3) / 1e12,
+                     "train_tflops": nt * flops_t / ((ms - inf_ms) / 1e3) / 1e12,
                      "image_mse": m_all, "image_mse_unlit": m_unlit,
                      "image_mse_per_seed": [round(m[0], 7) for m in per_seed], "frames": frames}
     res["speedup_bf16_over_fp32"] = res["bf16"]["msamples_per_s"] / res["fp32"]["msamples_per_s"]
@@ -326,7 +330,7 @@ def grid_nrc_bench(sty, frames: int, warmup: int, dev, bf16_peak: float):
                      "operands": "FP16 (loss scale 128)" if fp16 else "BF16",
                      "inference_path": "layer by layer" if (layered or fp16) else "fused tensor-core"}
         net.close()
-    mlp_flops = 2.0 * (144 * 128 + 4 * 128 * 128 + 16 * 128)  # MMA work per query incl. the padded output rows
+    mlp_flops = 2.0 * (144 * 128 + 4 * 128 * 128 + 3 * 128)  # algorithmic MLP FLOPs per query (output at N = 3)
     tc = res["tensor_core"]
     res["inference_speedup_tc_over_layered"] = res["layered"]["inference_ms"] / tc["inference_ms"]
     res["inference_mlp_tflops"] = nq * mlp_flops / (tc["inference_ms"] / 1e3) / 1e12
