@@ -731,6 +731,47 @@ def c5_full_bench(sty, W: int = 1920, H: int = 1080, ref_spp: int = 1024):
     return res
 
 
+def c2_alt_kernel(sty, rs, prm, style, out, D, steps, kernel, stream):
+    """The resident C2 pass on another screen-filter kernel (`kernel`: sty.SCREEN_KERNEL_*): mean ms per
+    depth launch from CUDA events on the launching stream, Mpath-vertices/s, and the largest relative
+    difference of its deepest-depth output (pure filter, no style node) from `out` (the headline run's)."""
+    import torch
+    sty.set_screen_kernel(kernel)
+    try:
+        alt = torch.empty_like(out)
+
+        def one_pass(evs=None):
+            for d in range(D - 1, -1, -1):
+                nxt = alt[d + 1] if d + 1 < D else None
+                if evs is not None:
+                    evs[d][0].record(stream)
+                sty.pf_screen_filter_depth(rs, d, prm, style, out_next=nxt, out=alt[d], stream=stream)
+                if evs is not None:
+                    evs[d][1].record(stream)
+
+        for _ in range(3):
+            one_pass()
+        torch.cuda.synchronize()
+        evs = [[[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(D)] for _ in range(steps)]
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for k in range(steps):
+            one_pass(evs[k])
+        t1.record(stream)
+        torch.cuda.synchronize()
+        launch_ms = statistics.mean(evs[k][d][0].elapsed_time(evs[k][d][1]) for k in range(steps) for d in range(D))
+        ms_pass = t0.elapsed_time(t1) / steps
+        m = rs.valid[(D - 1) * rs.n_per_depth:D * rs.n_per_depth].bool()
+        a, b = alt[D - 1][:, m], out[D - 1][:, m]
+        diff = ((a - b).abs() / b.abs().clamp_min(1e-6)).max().item()
+        nvalid = int(rs.valid.sum().item())
+        return {"ms_per_launch": launch_ms, "ms_per_pass": ms_pass,
+                "mpath_vertices_per_s": nvalid / (ms_pass / 1e3) / 1e6,
+                "max_rel_diff_deepest_vs_headline": diff}
+    finally:
+        sty.set_screen_kernel(sty.SCREEN_KERNEL_AUTO)
+
+
 def run_reference(args):
     rank, world, _ = _rank_env()
     if rank != 0:
@@ -796,6 +837,8 @@ def run(args):
         print(json.dumps({"brpt": brpt_bench(sty)}), flush=True)
         return
 
+    kernels = {"auto": sty.SCREEN_KERNEL_AUTO, "fp32": sty.SCREEN_KERNEL_FP32, "tensor": sty.SCREEN_KERNEL_TENSOR}
+    sty.set_screen_kernel(kernels[args.kernel])
     D_ = args.depths
     planes, valid = sty.synth.records(W_, H_, S_, D_, seed=rank)
     rs = sty.RecordSet.from_numpy(planes, valid, W_, H_, S_, D_, device=dev)
@@ -961,6 +1004,13 @@ def run(args):
                          "note": "the binding roof of this kernel (pair arithmetic); HBM traffic is ~0.6 % of it"},
         "clocks": clk,
     }
+    if world == 1 and not args.no_alt_kernel:
+        # the other screen-filter kernel family on the same resident records
+        alt = sty.SCREEN_KERNEL_FP32 if args.kernel == "tensor" else sty.SCREEN_KERNEL_TENSOR
+        line["c2_alt_kernel"] = {"kernel": "k_pf_screen4 (CUDA cores)" if alt == sty.SCREEN_KERNEL_FP32
+                                 else "k_pf_screen_tc (tcgen05 split-TF32)",
+                                 **c2_alt_kernel(sty, rs, prm, style, out, D_, max(3, args.steps), alt, stream)}
+        sty.set_screen_kernel(kernels[args.kernel])
     if world == 1 and not args.no_c1:
         line["c1_render"] = c1_bench(sty)
         line["c1_bilateral"], c1_rs = c1_bilateral_bench(sty)
@@ -995,6 +1045,10 @@ def main():
     ap.add_argument("--ref-budget", type=float, default=8.0)
     ap.add_argument("--depths", type=int, default=D_, help="path depths (profiling cases use fewer)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling cases)")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "fp32", "tensor"],
+                    help="screen-filter kernel of the headline pass (sty_pf_screen_set_kernel)")
+    ap.add_argument("--no-alt-kernel", action="store_true",
+                    help="skip timing the other screen-filter kernel on the same records")
     ap.add_argument("--no-nrc", action="store_true", help="skip the NL-NRC frames")
     ap.add_argument("--nrc-frames", type=int, default=256)
     ap.add_argument("--no-c1", action="store_true", help="skip the end-to-end Cornell box render")

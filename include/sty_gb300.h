@@ -195,6 +195,18 @@ STY_API sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_
                                       const sty_style_program *style, const float *out_next,
                                       float *out, float *filtered, void *stream);
 
+/* Which kernel serves the screen filter (process-wide; every sty_pf_screen_filter* call and SCREEN
+ * render after it). Returns STY_ERR_ARG for an unknown value.
+ *   STY_SCREEN_KERNEL_AUTO    the fastest kernel that serves the records' spp and radius
+ *   STY_SCREEN_KERNEL_FP32    the CUDA-core kernels (packed FP32 FMAs) at every spp and radius
+ *   STY_SCREEN_KERNEL_TENSOR  the tcgen05 kernel where it serves the configuration (4 spp, radius
+ *                             15 or 16: logits and weighted sums as split-TF32 products with FP32
+ *                             accumulation), the CUDA-core kernels elsewhere */
+#define STY_SCREEN_KERNEL_AUTO 0
+#define STY_SCREEN_KERNEL_FP32 1
+#define STY_SCREEN_KERNEL_TENSOR 2
+STY_API sty_status sty_pf_screen_set_kernel(int32_t kernel);
+
 /* Filter all depths, deepest first. `out` (device) holds 3 * depths planes laid out as
  * [depth][channel][height*width*spp]; on return out[d] = out_d for every depth. */
 STY_API sty_status sty_pf_screen_filter(const sty_pf_records *rec, const sty_pf_screen_params *params,

@@ -19,7 +19,7 @@ from .abi import (  # noqa: F401
 )
 from .pf import (  # noqa: F401
     ScreenParams, RecordSet, pf_screen_filter, pf_screen_filter_depth, film_accumulate,
-    c2_params, c2_style,
+    c2_params, c2_style, set_screen_kernel, SCREEN_KERNEL_AUTO, SCREEN_KERNEL_FP32, SCREEN_KERNEL_TENSOR,
 )
 from . import synth  # noqa: F401
 from . import pf_ref  # noqa: F401

@@ -100,6 +100,7 @@ SIGNATURES = {
                                                C.POINTER(StyleProgram), _VP, _VP, _VP, _VP]),
     "sty_pf_screen_filter": (C.c_int32, [C.POINTER(PfRecords), C.POINTER(PfScreenParams),
                                          C.POINTER(StyleProgram), _VP, _VP]),
+    "sty_pf_screen_set_kernel": (C.c_int32, [C.c_int32]),
     "sty_film_accumulate": (C.c_int32, [_VP, C.c_int32, C.c_int32, C.c_int32, C.c_double, _VP, _VP]),
     "sty_pf_ref_create": (C.c_int32, [C.c_uint64, C.c_uint32, C.POINTER(C.c_void_p)]),
     "sty_pf_ref_destroy": (C.c_int32, [C.c_void_p]),

@@ -12,6 +12,8 @@
 // pair costs 9 FFMA/FADD for the exponent, one MUFU.EX2 and 4 accumulations. Sums run in plain
 // FP32 across one candidate row (at most (2R+1) * S terms) and are then folded into
 // Kahan-compensated totals.
+#include <atomic>
+
 #include "common.cuh"
 #include "pf_screen.cuh"
 #include "style.cuh"
@@ -405,12 +407,29 @@ sty_status validate(const sty_pf_records *rec, const sty_pf_screen_params *p) {
     return STY_OK;
 }
 
+std::atomic<int32_t> g_screen_kernel{STY_SCREEN_KERNEL_AUTO};
+
+// the kernel family the dispatch uses (AUTO resolved)
+int32_t screen_kernel_choice() {
+    const int32_t k = g_screen_kernel.load(std::memory_order_relaxed);
+    return k == STY_SCREEN_KERNEL_AUTO ? STY_SCREEN_KERNEL_FP32 : k;
+}
+
 }  // namespace
 }  // namespace sty
 
 using namespace sty;
 
 extern "C" {
+
+sty_status sty_pf_screen_set_kernel(int32_t kernel) {
+    clear_error();
+    STY_ARG_CHECK(kernel == STY_SCREEN_KERNEL_AUTO || kernel == STY_SCREEN_KERNEL_FP32 ||
+                      kernel == STY_SCREEN_KERNEL_TENSOR,
+                  "sty_pf_screen_set_kernel: unknown kernel %d", kernel);
+    g_screen_kernel.store(kernel, std::memory_order_relaxed);
+    return STY_OK;
+}
 
 sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth, const sty_pf_screen_params *params,
                                       const sty_style_program *style, const float *out_next, float *out,
@@ -450,6 +469,8 @@ sty_status sty_pf_screen_filter_depth(const sty_pf_records *rec, uint32_t depth,
         case 1: return launch_screen<1>(a, prog, st);
         case 2: return launch_screen<2>(a, prog, st);
         case 4:  // the warp-specialised kernel's shared-memory ring fits up to radius 24
+            if (screen_kernel_choice() == STY_SCREEN_KERNEL_TENSOR && screen_tc_supports(a, 4))
+                return launch_screen_tc(a, prog, st);
             return a.R <= 24 ? launch_screen_s4(a, prog, st) : launch_screen<4>(a, prog, st);
         case 8: return launch_screen<8>(a, prog, st);
         default: {  // the warp-specialised kernel where its shared-memory ring fits

@@ -28,4 +28,8 @@ sty_status launch_screen_s4(const ScreenArgs &a, const sty_style_program &style,
 sty_status launch_screen_s16(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st);
 int screen_ws_max_radius(int spp, size_t optin);
 
+// tcgen05 split-TF32 kernel (pf_screen_tc.cu): 4 spp, radius 15 or 16, 16-byte aligned planes
+bool screen_tc_supports(const ScreenArgs &a, int spp);
+sty_status launch_screen_tc(const ScreenArgs &a, const sty_style_program &style, cudaStream_t st);
+
 }  // namespace sty

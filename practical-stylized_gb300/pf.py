@@ -94,6 +94,15 @@ def host_records(planes: np.ndarray, valid: np.ndarray, width, height, spp, dept
     return r
 
 
+SCREEN_KERNEL_AUTO, SCREEN_KERNEL_FP32, SCREEN_KERNEL_TENSOR = 0, 1, 2
+
+
+def set_screen_kernel(kernel: int) -> None:
+    """Process-wide choice of the screen filter's kernel (sty_pf_screen_set_kernel): AUTO, FP32 (the
+    CUDA-core kernels) or TENSOR (the tcgen05 split-TF32 kernel where it serves the configuration)."""
+    check(lib().sty_pf_screen_set_kernel(int(kernel)))
+
+
 def pf_screen_filter_depth(rs: RecordSet, depth: int, params: ScreenParams, style=None, out_next=None,
                            out=None, filtered=None, stream=None):
     """Filter one depth; returns `out` (device float32 [3, W*H*S])."""
