@@ -1,4 +1,5 @@
-// pf_screen_tc.cu -- screen-space NL-PF filter (4 spp, radius 15-16) on the tcgen05 tensor cores.
+// pf_screen_tc.cu -- screen-space NL-PF filter (4 spp, radius 15-16) with its logits on the tcgen05
+// tensor cores.
 //
 // The filter of one query q over its window is an attention-shaped product:
 //   out_q = sum_c w_qc in_c / sum_c w_qc,   w_qc = 2^(S_qc),
@@ -16,27 +17,36 @@
 // Invalid candidates (and those with |p'_c|^2 > kLimC, whose weights are below 2^-48 for every
 // query of the tile, as in the packed-FMA kernel's expanded form) get b_c = -2^14.
 //
-// FP32-level accuracy from TF32 operands (10-bit mantissas) comes from the 3-pass split
-// hi . hi + hi . lo + lo . hi (hi = RN-to-TF32, lo = x - hi, which the tensor core truncates):
-//   logits  S = [qh | qh | ql | onehot | onehot] . [ch | cl | ch | Mh | Ml]   (K = 40, 5 MMAs of K 8)
-//   sums    O = Ph . [vh | vl] + Pl . [vh | vl],  v = (in_r, in_g, in_b, 1), Ph = P with the low 13
-//           mantissa bits cleared, Pl = P - Ph (exact)       (N = 16: vh in 0-3, vl in 4-7, 8-15 zero)
-// Rows of the window outside |y_q - y_c| <= R are skipped by the warp that owns those queries (P
-// written as 0). Per window row the row's sums are read from TMEM and added in FP32.
+// FP32-level accuracy of the logits from TF32 operands (10-bit mantissas) comes from the 3-pass
+// split hi . hi + hi . lo + lo . hi (hi = RN-to-TF32, lo = x - hi, which the tensor core truncates):
+//   S = [qh | qh | ql | onehot | onehot] . [ch | cl | ch | Mh | Ml]     (K = 40: 5 MMAs of K 8, N 160)
+// The weights and the weighted sums stay on the CUDA cores in FP32: w = ex2(S) and two packed FMAs
+// per pair against the candidates' incoming radiance, broadcast from shared memory. Rows of the
+// window outside |y_q - y_c| <= R are skipped by the warps that own those queries. Every
+// kKahanRows window rows each thread adds its FP32 partial sums into Kahan totals.
+//
+// Measured on GB300 (1920x1080 x 4 spp, radius 16): 22.5 ms per depth launch against 13.8 ms for
+// the packed-FMA kernel. The bound is the radiance broadcast: a warp-uniform shared-memory load
+// delivers 4 bytes per wavefront, and 4 warps x 160 candidates x 3 channels = 1920 wavefronts per
+// window row keep the shared-memory pipe 65 % busy. Putting the sums on the tensor cores as well
+// (split-TF32 P . [v_hi | v_lo] with P written back to TMEM) needs 40 MMAs of N = 16 per window
+// row; a TF32 tcgen05.mma of M = 128, K = 8 costs its issuing thread ~63 cycles and holds the
+// tensor pipe ~39 cycles whatever its N (full rate only from N = 160: 80 cycles), so those sums
+// alone cost more pipe time than the whole packed-FMA kernel (measured 33-36 ms per launch).
 //
 // CTA = one 8 x 4 pixel tile = 128 queries = the 128 TMEM lanes (lane = 32 row + 4 x + sample),
-// 13 warps:
-//   warps 0-7   epilogue: warp w owns lanes 32 (w % 4) .. +31 (pixel row w % 4) and half w / 4 of
-//               the window row's columns: tcgen05.ld S, P = ex2(S), split, tcgen05.st Ph / Pl;
-//               warps 0-3 also read the row sums and write the outputs.
-//   warps 8-11  producers: stage the window row's candidate features and values into a ring of
-//               kNS shared-memory buffers (K-major core-matrix images, no swizzle).
-//   warp 12     lane 0 issues the MMAs: logits of row k+1 into TMEM buffer (k+1) % 2 while the
-//               epilogue works on row k, then the sums of row k.
-// TMEM (512 columns): S / Ph buffers [0, 160) and [160, 320), Pl [320, 480), row sums [480, 512).
-// Every mbarrier wait is bounded (~2 s); on expiry the thread records STY_DEV_WAIT_TIMEOUT and leaves
-// its loop, the outputs of the tile become NaN, and the MMA thread waits (bounded) for its last
-// commit before the columns are released.
+// 23 warps:
+//   warps 0-15  epilogue: warp w owns lanes 32 (w % 4) .. +31 (pixel row w % 4) and quarter w / 4
+//               of the window row's 160 candidates: tcgen05.ld S, release the TMEM buffer, then
+//               w = ex2(S) and the sums; warps 0-3 also write the query features and the outputs.
+//   warps 16-20 producers: the window row's candidate feature image (K-major core matrices, no
+//               swizzle) and radiance row, from the raw ring, into a ring of kNS stages.
+//   warp 21     lane 0 issues the logits of each window row into one of 3 TMEM buffers.
+//   warp 22     lane 0 copies each window row's 16 record fields (pos, nrm, rad, thr, valid,
+//               out_next) from HBM into a raw ring of kNR stages with cp.async.bulk.
+// Every mbarrier wait is bounded (~2 s); on expiry the thread records STY_DEV_WAIT_TIMEOUT and
+// leaves its loop, and the outputs of the tile become NaN; the MMA thread waits (bounded) for its
+// last commit and the loader for its last copies before the CTA ends.
 //
 // Tiles whose queries lie too far from their mean (|p'_q|^2 > kLimQ: the bilinear form would lose
 // digits to cancellation) take the direct form on the CUDA cores inside the same CTA.
@@ -54,13 +64,15 @@ constexpr int kTX = 8, kTY = 4;       // query tile in pixels
 constexpr int kM = kTX * kTY * kS;    // 128 queries = MMA rows
 constexpr int kK = 40;                // logit features
 constexpr int kNCol = 160;            // candidates per window row at radius 15-16 (40 px x 4)
-constexpr int kNH = kNCol / 2;        // columns per epilogue warp
-constexpr int kEW = 8, kPW = 5;       // epilogue and producer warps (one candidate per producer thread)
-constexpr int kMmaWarp = kEW + kPW;   // warp 13: MMA issue
-constexpr int kLoadWarp = kMmaWarp + 1;  // warp 14: bulk copies of the raw record rows
+constexpr int kEW = 16, kPW = 5;      // epilogue and producer warps (one candidate per producer thread)
+constexpr int kNH = kNCol / (kEW / 4); // candidates per epilogue warp (4 warps share a TMEM lane quarter)
+constexpr int kMmaWarp = kEW + kPW;   // warp 21: MMA issue
+constexpr int kLoadWarp = kMmaWarp + 1;  // warp 22: bulk copies of the raw record rows
+constexpr int kKahanRows = 4;         // window rows summed in FP32 before a Kahan step
 constexpr int kNT = (kLoadWarp + 1) * 32;
-constexpr int kNS = 4;                // staging ring depth (operand images)
+constexpr int kNS = 4;                // staging ring depth (feature images and radiance rows)
 constexpr int kNR = 4;                // raw ring depth (record rows)
+constexpr int kNB = 3;                // TMEM logit buffers
 constexpr float kBig = 16384.0f;
 constexpr float kLimQ = 16.0f, kLimC = 120.0f;
 
@@ -69,11 +81,8 @@ constexpr float kLimQ = 16.0f, kLimC = 120.0f;
 constexpr uint32_t kRowGroup = kK / 4 * 128;           // 1280
 constexpr uint32_t kQfBytes = kM / 8 * kRowGroup;      // 20480
 constexpr uint32_t kCfBytes = kNCol / 8 * kRowGroup;   // 25600
-// values image, B of the sums: (channel, candidate) at (ch / 8) * kVSbo + (cand / 4) * 128 +
-// (ch % 8) * 16 + (cand % 4) * 4 (LBO 128, SBO kVSbo)
-constexpr uint32_t kVSbo = kNCol / 4 * 128;            // 5120
-constexpr uint32_t kVBytes = 2 * kVSbo;                // 10240
-constexpr uint32_t kStageBytes = kCfBytes + kVBytes;   // 35840
+constexpr uint32_t kVBytes = 3 * kNCol * 4;            // incoming radiance, [channel][candidate]
+constexpr uint32_t kStageBytes = kCfBytes + kVBytes;   // 27520
 constexpr int kNpxMax = kNCol / 4;                     // 40 candidate pixels per window row
 constexpr uint32_t kTabBytes = kNpxMax * 16 * 4;       // horizontal table: Mh[8], Ml[8] per pixel
 // raw ring: per window row the 40 candidate pixels' records as copied from HBM, 16 fields x 160
@@ -82,11 +91,7 @@ constexpr int kNF = 16;
 constexpr uint32_t kRawField = kNCol * 4;           // 640 bytes
 constexpr uint32_t kRawBytes = kNF * kRawField;     // 10240
 constexpr uint32_t kSmemBytes = kQfBytes + kNS * kStageBytes + kTabBytes + kNR * kRawBytes;
-
-// TMEM columns
-constexpr uint32_t kColPl = 2 * kNCol;
-constexpr uint32_t kColO = 3 * kNCol;
-static_assert(kColO + 32 <= 512, "TMEM budget");
+static_assert(kNB * kNCol <= 512, "TMEM budget");
 
 __host__ __device__ constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
     // D f32 (bit 4), A / B TF32 (bits 7-9, 10-12 = 2), both K-major, N>>3 (bits 17-22), M>>4 (24-28)
@@ -98,34 +103,18 @@ __device__ __forceinline__ void mma_tf32_ss(uint32_t d, uint64_t a, uint64_t b, 
         "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
         "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
-// A operand from TMEM (lanes = rows, one TF32 column per K element)
-__device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
-        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t (&r)[16]) {
+__device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t *r) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_ld8u(uint32_t taddr, uint32_t (&r)[8]) {
+__device__ __forceinline__ void tmem_ld8u(uint32_t taddr, uint32_t *r) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
 }
-__device__ __forceinline__ void tmem_st16u(uint32_t taddr, const uint32_t (&r)[16]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
-            taddr),
-        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
-        "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
-        : "memory");
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void mbar_init1(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
@@ -149,18 +138,33 @@ __device__ __forceinline__ void split_tf32(float x, float &hi, float &lo) {
     hi = __uint_as_float(h);
     lo = x - hi;
 }
-// byte offset of element (row, k) in a 40-column K-major image
-__device__ __forceinline__ uint32_t kimg_off(int row, int k4) {  // k4 = k / 4 (16-byte group)
+// byte offset of element (row, 4 k4) in a 40-column K-major image (16-byte group k4)
+__device__ __forceinline__ uint32_t kimg_off(int row, int k4) {
     return (uint32_t)(row >> 3) * kRowGroup + (uint32_t)k4 * 128u + (uint32_t)(row & 7) * 16u;
+}
+// one 40-feature row: [a | b | c | d | e], 8 features each
+__device__ __forceinline__ void store_row40(uint8_t *dst, const float (&a)[8], const float (&b)[8], const float (&c)[8],
+                                            const float4 d0, const float4 d1, const float4 e0, const float4 e1) {
+    *reinterpret_cast<float4 *>(dst + 0 * 128) = make_float4(a[0], a[1], a[2], a[3]);
+    *reinterpret_cast<float4 *>(dst + 1 * 128) = make_float4(a[4], a[5], a[6], a[7]);
+    *reinterpret_cast<float4 *>(dst + 2 * 128) = make_float4(b[0], b[1], b[2], b[3]);
+    *reinterpret_cast<float4 *>(dst + 3 * 128) = make_float4(b[4], b[5], b[6], b[7]);
+    *reinterpret_cast<float4 *>(dst + 4 * 128) = make_float4(c[0], c[1], c[2], c[3]);
+    *reinterpret_cast<float4 *>(dst + 5 * 128) = make_float4(c[4], c[5], c[6], c[7]);
+    *reinterpret_cast<float4 *>(dst + 6 * 128) = d0;
+    *reinterpret_cast<float4 *>(dst + 7 * 128) = d1;
+    *reinterpret_cast<float4 *>(dst + 8 * 128) = e0;
+    *reinterpret_cast<float4 *>(dst + 9 * 128) = e1;
 }
 
 struct SmemTc {
     uint64_t stage_full[kNS], stage_empty[kNS];
     uint64_t raw_full[kNR], raw_empty[kNR];
-    uint64_t s_full[2], p_full[2], m2_done[2];
+    uint64_t s_full[kNB], s_empty[kNB];
     uint64_t qf_ready;
     uint32_t tmem_slot;
-    float red[4][8];  // per query warp: sum p'(3), sum n(3), count
+    float red[4][8];        // per query warp: sum p'(3), sum n(3), count
+    float part[kEW / 4 - 1][kM][4];  // the other column quarters' totals, per query
 };
 
 __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, const sty_style_program style) {
@@ -181,16 +185,15 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
     if (tid == 0) {
         for (int s = 0; s < kNS; s++) {
             mbar_init1(&sh.stage_full[s], kPW * 32);
-            mbar_init1(&sh.stage_empty[s], 1);
+            mbar_init1(&sh.stage_empty[s], 1 + kEW);  // the logits' commit + every epilogue warp
         }
         for (int r = 0; r < kNR; r++) {
             mbar_init1(&sh.raw_full[r], 1);  // the loader's arrive.expect_tx + the copies' bytes
             mbar_init1(&sh.raw_empty[r], kPW * 32);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < kNB; b++) {
             mbar_init1(&sh.s_full[b], 1);
-            mbar_init1(&sh.p_full[b], kEW);
-            mbar_init1(&sh.m2_done[b], 1);
+            mbar_init1(&sh.s_empty[b], kEW);
         }
         mbar_init1(&sh.qf_ready, kM);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -228,9 +231,8 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
 #pragma unroll
             for (int k = 0; k < 7; k++) sh.red[warp][k] = v[k];
     } else if (warp >= kEW && warp < kMmaWarp) {
-        // producers: the horizontal table and the constant rows of every values image
-        const int ptid = tid - kEW * 32;
-        for (int i = ptid; i < kNpxMax * 8; i += kPW * 32) {
+        // producers: the horizontal table
+        for (int i = tid - kEW * 32; i < kNpxMax * 8; i += kPW * 32) {
             const int p = i >> 3, k = i & 7;
             const int d = k - (p - R);  // query column minus candidate column
             const float m = (p < npx && d >= -R && d <= R) ? -a.pix2 * (float)(d * d) : -kBig;
@@ -239,21 +241,7 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             tab[p * 16 + k] = hi;
             tab[p * 16 + 8 + k] = lo;
         }
-        for (int s = 0; s < kNS; s++) {
-            float *vimg = reinterpret_cast<float *>(stage + s * kStageBytes + kCfBytes);
-            for (int i = ptid; i < kNCol / 4; i += kPW * 32) {
-                // channel 3 = 1 (the weight sum), 7 = 0, 8-15 = 0
-                *reinterpret_cast<float4 *>(reinterpret_cast<uint8_t *>(vimg) + i * 128 + 3 * 16) =
-                    make_float4(1.f, 1.f, 1.f, 1.f);
-                *reinterpret_cast<float4 *>(reinterpret_cast<uint8_t *>(vimg) + i * 128 + 7 * 16) =
-                    make_float4(0.f, 0.f, 0.f, 0.f);
-                for (int ch = 0; ch < 8; ch++)
-                    *reinterpret_cast<float4 *>(reinterpret_cast<uint8_t *>(vimg) + kVSbo + i * 128 + ch * 16) =
-                        make_float4(0.f, 0.f, 0.f, 0.f);
-            }
-        }
     }
-    fence_async_smem();
     fence_before();
     __syncthreads();
     fence_after();
@@ -336,9 +324,8 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
         const int p = n >> 2;
         const bool colin = p < npx && tx0 - R + p >= 0 && tx0 - R + p < a.W;
         const float4 *trow = reinterpret_cast<const float4 *>(tab + p * 16);
-        const int vp = n / 3, vch = n - vp * 3;  // value item (n < 120): pixel vp, channel vch
+        const int vp = n / 3, vch = n - vp * 3;  // radiance item (n < 120): pixel vp, channel vch
         const bool vcolin = n < 120 && vp < npx && tx0 - R + vp >= 0 && tx0 - R + vp < a.W;
-        uint8_t *dst_c = stage + kimg_off(n, 0);
         for (int k = 0; k < nrows; k++) {
             const int s = k % kNS, r = k % kNR;
             if (k >= kNS && !mbar_wait(&sh.stage_empty[s], ((k / kNS) - 1) & 1, a.status)) {
@@ -374,18 +361,9 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             float hi[8], lo[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) split_tf32(f[i], hi[i], lo[i]);
-            uint8_t *dst = dst_c + s * kStageBytes;
-            *reinterpret_cast<float4 *>(dst + 0 * 128) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4 *>(dst + 1 * 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-            *reinterpret_cast<float4 *>(dst + 2 * 128) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-            *reinterpret_cast<float4 *>(dst + 3 * 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
-            *reinterpret_cast<float4 *>(dst + 4 * 128) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4 *>(dst + 5 * 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-            *reinterpret_cast<float4 *>(dst + 6 * 128) = trow[0];
-            *reinterpret_cast<float4 *>(dst + 7 * 128) = trow[1];
-            *reinterpret_cast<float4 *>(dst + 8 * 128) = trow[2];
-            *reinterpret_cast<float4 *>(dst + 9 * 128) = trow[3];
-            if (n < 120) {  // values: the pixel's 4 samples of one channel
+            uint8_t *st_base = stage + s * kStageBytes;
+            store_row40(st_base + kimg_off(n, 0), hi, lo, hi, trow[0], trow[1], trow[2], trow[3]);
+            if (n < 120) {  // incoming radiance in = rad + thr * out_next of the pixel's 4 samples, one channel
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (rowin && vcolin) {
                     const int4 vl = *reinterpret_cast<const int4 *>(rw + 12 * kNCol + vp * 4);
@@ -398,15 +376,7 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
                     v.z = vl.z != 0 ? fmaf(th.z, on.z, rd.z) : 0.0f;
                     v.w = vl.w != 0 ? fmaf(th.w, on.w, rd.w) : 0.0f;
                 }
-                float vh[4], vlo[4];
-                split_tf32(v.x, vh[0], vlo[0]);
-                split_tf32(v.y, vh[1], vlo[1]);
-                split_tf32(v.z, vh[2], vlo[2]);
-                split_tf32(v.w, vh[3], vlo[3]);
-                uint8_t *vimg = stage + s * kStageBytes + kCfBytes;
-                *reinterpret_cast<float4 *>(vimg + vp * 128 + vch * 16) = make_float4(vh[0], vh[1], vh[2], vh[3]);
-                *reinterpret_cast<float4 *>(vimg + vp * 128 + (4 + vch) * 16) =
-                    make_float4(vlo[0], vlo[1], vlo[2], vlo[3]);
+                *reinterpret_cast<float4 *>(st_base + kCfBytes + (vch * kNCol + vp * 4) * 4) = v;
             }
             fence_async_smem();
             mbar_arrive1(&sh.stage_full[s]);
@@ -452,60 +422,38 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
                 mbar_wait(&sh.raw_full[k % kNR], (k / kNR) & 1, a.status);
         }
     } else if (warp == kMmaWarp) {
-        // ================= MMA issue (one thread) =================
+        // ================= MMA issue (one thread): the logits of every window row =================
         if (lane == 0) {
-            const uint32_t idesc_s = idesc_tf32(kM, kNCol), idesc_o = idesc_tf32(kM, 16);
+            const uint32_t idesc = idesc_tf32(kM, kNCol);
             const uint32_t qf_addr = smem_u32(qf), st_addr = smem_u32(stage);
-            int issued = -1;  // last chunk whose sums were committed
-            auto logits = [&](int k) {
-                const uint32_t cf = st_addr + (uint32_t)(k % kNS) * kStageBytes;
-                const uint32_t d = tmem + (uint32_t)(k & 1) * kNCol;
-#pragma unroll
-                for (int kk = 0; kk < kK / 8; kk++)
-                    mma_tf32_ss(d, make_desc(qf_addr + kk * 256u, 128u, kRowGroup),
-                                make_desc(cf + kk * 256u, 128u, kRowGroup), idesc_s, kk > 0 ? 1u : 0u);
-                mma_commit(&sh.s_full[k & 1]);
-            };
-            bool ok = mbar_wait(&sh.qf_ready, 0, a.status) && mbar_wait(&sh.stage_full[0], 0, a.status);
-            if (ok) {
-                fence_after();
-                logits(0);
-            }
+            int last = -1;
+            bool ok = mbar_wait(&sh.qf_ready, 0, a.status);
             for (int k = 0; ok && k < nrows; k++) {
-                if (k + 1 < nrows) {
-                    if (!mbar_wait(&sh.stage_full[(k + 1) % kNS], ((k + 1) / kNS) & 1, a.status)) {
-                        ok = false;
-                        break;
-                    }
-                    fence_after();
-                    logits(k + 1);
-                }
-                if (!mbar_wait(&sh.p_full[k & 1], (k >> 1) & 1, a.status)) {
+                const int b = k % kNB;
+                if (!mbar_wait(&sh.stage_full[k % kNS], (k / kNS) & 1, a.status) ||
+                    (k >= kNB && !mbar_wait(&sh.s_empty[b], ((k / kNB) - 1) & 1, a.status))) {
                     ok = false;
                     break;
                 }
                 fence_after();
-                const uint32_t vb = st_addr + (uint32_t)(k % kNS) * kStageBytes + kCfBytes;
-                const uint32_t o = tmem + kColO + 16u * (uint32_t)(k & 1);
-                const uint32_t ph = tmem + (uint32_t)(k & 1) * kNCol, pl = tmem + kColPl;
-#pragma unroll 4
-                for (int j = 0; j < kNCol / 8; j++)
-                    mma_tf32_ts(o, ph + 8u * j, make_desc(vb + j * 256u, 128u, kVSbo), idesc_o, j > 0 ? 1u : 0u);
-#pragma unroll 4
-                for (int j = 0; j < kNCol / 8; j++)
-                    mma_tf32_ts(o, pl + 8u * j, make_desc(vb + j * 256u, 128u, kVSbo), idesc_o, 1u);
-                mma_commit(&sh.m2_done[k & 1]);
+                const uint32_t cf = st_addr + (uint32_t)(k % kNS) * kStageBytes;
+                const uint32_t d = tmem + (uint32_t)b * kNCol;
+#pragma unroll
+                for (int kk = 0; kk < kK / 8; kk++)
+                    mma_tf32_ss(d, make_desc(qf_addr + kk * 256u, 128u, kRowGroup),
+                                make_desc(cf + kk * 256u, 128u, kRowGroup), idesc, kk > 0 ? 1u : 0u);
+                mma_commit(&sh.s_full[b]);
                 mma_commit(&sh.stage_empty[k % kNS]);
-                issued = k;
+                last = k;
             }
             if (!ok) {
                 failed = true;
                 // let the MMAs already issued finish before the columns are released
-                if (issued >= 0) mbar_wait(&sh.m2_done[issued & 1], (issued >> 1) & 1, a.status);
+                if (last >= 0) mbar_wait(&sh.s_full[last % kNB], (last / kNB) & 1, a.status);
             }
         }
     } else {
-        // ================= epilogue warps 0-7 =================
+        // ================= epilogue warps 0-15 =================
         const int qw = warp & 3, h = warp >> 2;
         const uint32_t lane_off = (uint32_t)(qw * 32) << 16;
         const uint32_t colh = (uint32_t)h * kNH;
@@ -528,104 +476,82 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             float oh[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) oh[i] = (qv && i == qx) ? 1.0f : 0.0f;
-            uint8_t *dst = qf + kimg_off(tid, 0);
-            *reinterpret_cast<float4 *>(dst + 0 * 128) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4 *>(dst + 1 * 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-            *reinterpret_cast<float4 *>(dst + 2 * 128) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-            *reinterpret_cast<float4 *>(dst + 3 * 128) = make_float4(hi[4], hi[5], hi[6], hi[7]);
-            *reinterpret_cast<float4 *>(dst + 4 * 128) = make_float4(lo[0], lo[1], lo[2], lo[3]);
-            *reinterpret_cast<float4 *>(dst + 5 * 128) = make_float4(lo[4], lo[5], lo[6], lo[7]);
-            *reinterpret_cast<float4 *>(dst + 6 * 128) = make_float4(oh[0], oh[1], oh[2], oh[3]);
-            *reinterpret_cast<float4 *>(dst + 7 * 128) = make_float4(oh[4], oh[5], oh[6], oh[7]);
-            *reinterpret_cast<float4 *>(dst + 8 * 128) = make_float4(oh[0], oh[1], oh[2], oh[3]);
-            *reinterpret_cast<float4 *>(dst + 9 * 128) = make_float4(oh[4], oh[5], oh[6], oh[7]);
+            const float4 oh0 = make_float4(oh[0], oh[1], oh[2], oh[3]), oh1 = make_float4(oh[4], oh[5], oh[6], oh[7]);
+            store_row40(qf + kimg_off(tid, 0), hi, hi, lo, oh0, oh1, oh0, oh1);
             fence_async_smem();
             mbar_arrive1(&sh.qf_ready);
         }
-        uint32_t zero[16];
-#pragma unroll
-        for (int i = 0; i < 16; i++) zero[i] = 0u;
+        KahanF kr = {0.f, 0.f}, kg = {0.f, 0.f}, kb = {0.f, 0.f}, kw = {0.f, 0.f};
+        const float2 one2 = make_float2(1.0f, 1.0f);
+        float2 ar = make_float2(0.f, 0.f), ag = ar, ab = ar, aw = ar;
         for (int k = 0; k < nrows; k++) {
-            const int b = k & 1;
-            if (!mbar_wait(&sh.s_full[b], (k >> 1) & 1, a.status)) {
+            const int b = k % kNB, s = k % kNS;
+            if (!mbar_wait(&sh.s_full[b], (k / kNB) & 1, a.status)) {
                 failed = true;
                 break;
             }
             fence_after();
-            const uint32_t sb = tmem + lane_off + (uint32_t)b * kNCol + colh;
-            const uint32_t pb = tmem + lane_off + kColPl + colh;
             const bool rows_in = k >= qw && k <= 2 * R + qw;  // |y_q - y_c| <= R for this warp's pixel row
-            bool m2ok = true;
+            uint32_t sv[kNH];
             if (rows_in) {
-                // columns in two passes: 48 (3 groups of 16) then 32 (2 groups)
-#pragma unroll
-                for (int pass = 0; pass < 2; pass++) {
-                    const int g0 = pass == 0 ? 0 : 3, gn = pass == 0 ? 3 : 2;
-                    uint32_t sv[3][16];
-#pragma unroll
-                    for (int g = 0; g < gn; g++) tmem_ld16u(sb + 16u * (g0 + g), sv[g]);
-                    tmem_wait_ld();
-                    if (pass == 0 && k > 0) {  // the previous row's sums have read the Pl columns
-                        m2ok = mbar_wait(&sh.m2_done[(k - 1) & 1], ((k - 1) >> 1) & 1, a.status);
-                        fence_after();
-                    }
-#pragma unroll
-                    for (int g = 0; g < gn; g++) {
-                        uint32_t ph[16], pl[16];
-#pragma unroll
-                        for (int i = 0; i < 16; i++) {
-                            const float p = ex2_approx(__uint_as_float(sv[g][i]));
-                            const uint32_t hb = __float_as_uint(p) & 0xFFFFE000u;
-                            ph[i] = hb;
-                            pl[i] = __float_as_uint(p - __uint_as_float(hb));
-                        }
-                        tmem_st16u(sb + 16u * (g0 + g), ph);
-                        tmem_st16u(pb + 16u * (g0 + g), pl);
-                    }
-                }
-            } else {
-                if (k > 0) {
-                    m2ok = mbar_wait(&sh.m2_done[(k - 1) & 1], ((k - 1) >> 1) & 1, a.status);
-                    fence_after();
-                }
-#pragma unroll
-                for (int g = 0; g < kNH / 16; g++) {
-                    tmem_st16u(sb + 16u * g, zero);
-                    tmem_st16u(pb + 16u * g, zero);
-                }
+                const uint32_t sb = tmem + lane_off + (uint32_t)b * kNCol + colh;
+                tmem_ld16u(sb, &sv[0]);
+                tmem_ld16u(sb + 16u, &sv[16]);
+                tmem_ld8u(sb + 32u, &sv[32]);
+                tmem_wait_ld();
             }
-            tmem_wait_st();
             fence_before();
             __syncwarp();
-            if (!__all_sync(0xffffffffu, m2ok)) {
-                failed = true;
-                break;
+            if (lane == 0) mbar_arrive1(&sh.s_empty[b]);  // the logits are in registers
+            if (rows_in) {
+                const float *vr = reinterpret_cast<const float *>(stage + s * kStageBytes + kCfBytes) + colh;
+#pragma unroll
+                for (int j = 0; j < kNH; j += 4) {
+                    const float2 w01 =
+                        make_float2(ex2_approx(__uint_as_float(sv[j])), ex2_approx(__uint_as_float(sv[j + 1])));
+                    const float2 w23 =
+                        make_float2(ex2_approx(__uint_as_float(sv[j + 2])), ex2_approx(__uint_as_float(sv[j + 3])));
+                    const float4 r4 = *reinterpret_cast<const float4 *>(vr + j);
+                    const float4 g4 = *reinterpret_cast<const float4 *>(vr + kNCol + j);
+                    const float4 b4 = *reinterpret_cast<const float4 *>(vr + 2 * kNCol + j);
+                    ar = ffma2(w01, make_float2(r4.x, r4.y), ar);
+                    ar = ffma2(w23, make_float2(r4.z, r4.w), ar);
+                    ag = ffma2(w01, make_float2(g4.x, g4.y), ag);
+                    ag = ffma2(w23, make_float2(g4.z, g4.w), ag);
+                    ab = ffma2(w01, make_float2(b4.x, b4.y), ab);
+                    ab = ffma2(w23, make_float2(b4.z, b4.w), ab);
+                    aw = ffma2(w01, one2, aw);
+                    aw = ffma2(w23, one2, aw);
+                }
             }
-            if (lane == 0) mbar_arrive1(&sh.p_full[b]);
-            if (h == 0 && k > 0) {  // the previous row's sums (complete: waited above)
-                uint32_t o[8];
-                tmem_ld8u(tmem + lane_off + kColO + 16u * (uint32_t)((k - 1) & 1), o);
-                tmem_wait_ld();
-                acc[0] += __uint_as_float(o[0]) + __uint_as_float(o[4]);
-                acc[1] += __uint_as_float(o[1]) + __uint_as_float(o[5]);
-                acc[2] += __uint_as_float(o[2]) + __uint_as_float(o[6]);
-                acc[3] += __uint_as_float(o[3]) + __uint_as_float(o[7]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&sh.stage_empty[s]);  // done with the radiance row
+            if (k % kKahanRows == kKahanRows - 1 || k == nrows - 1) {
+                kr.add(ar.x + ar.y);
+                kg.add(ag.x + ag.y);
+                kb.add(ab.x + ab.y);
+                kw.add(aw.x + aw.y);
+                ar = ag = ab = aw = make_float2(0.f, 0.f);
             }
         }
-        if (!failed && h == 0) {
-            const int k = nrows - 1;
-            if (mbar_wait(&sh.m2_done[k & 1], (k >> 1) & 1, a.status)) {
-                fence_after();
-                uint32_t o[8];
-                tmem_ld8u(tmem + lane_off + kColO + 16u * (uint32_t)(k & 1), o);
-                tmem_wait_ld();
-                acc[0] += __uint_as_float(o[0]) + __uint_as_float(o[4]);
-                acc[1] += __uint_as_float(o[1]) + __uint_as_float(o[5]);
-                acc[2] += __uint_as_float(o[2]) + __uint_as_float(o[6]);
-                acc[3] += __uint_as_float(o[3]) + __uint_as_float(o[7]);
-            } else {
-                failed = true;
-            }
+        // the four column quarters of each query: warps 4-15 hand their totals to warps 0-3
+        const int q = qw * 32 + lane;
+        if (h > 0) {
+            sh.part[h - 1][q][0] = kr.s - kr.c;
+            sh.part[h - 1][q][1] = kg.s - kg.c;
+            sh.part[h - 1][q][2] = kb.s - kb.c;
+            sh.part[h - 1][q][3] = kw.s - kw.c;
+        }
+        bar_sync_n(1, kEW * 32);
+        if (h == 0) {
+            acc[0] = kr.s - kr.c;
+            acc[1] = kg.s - kg.c;
+            acc[2] = kb.s - kb.c;
+            acc[3] = kw.s - kw.c;
+#pragma unroll
+            for (int o = 0; o < kEW / 4 - 1; o++)
+#pragma unroll
+                for (int c = 0; c < 4; c++) acc[c] += sh.part[o][q][c];
         }
     }
 
