@@ -25,24 +25,30 @@
 // window outside |y_q - y_c| <= R are skipped by the warps that own those queries. Every
 // kKahanRows window rows each thread adds its FP32 partial sums into Kahan totals.
 //
-// Measured on GB300 (1920x1080 x 4 spp, radius 16): 22.5 ms per depth launch against 13.8 ms for
-// the packed-FMA kernel. The bound is the radiance broadcast: a warp-uniform shared-memory load
-// delivers 4 bytes per wavefront, and 4 warps x 160 candidates x 3 channels = 1920 wavefronts per
-// window row keep the shared-memory pipe 65 % busy. Putting the sums on the tensor cores as well
-// (split-TF32 P . [v_hi | v_lo] with P written back to TMEM) needs 40 MMAs of N = 16 per window
-// row; a TF32 tcgen05.mma of M = 128, K = 8 costs its issuing thread ~63 cycles and holds the
-// tensor pipe ~39 cycles whatever its N (full rate only from N = 160: 80 cycles), so those sums
-// alone cost more pipe time than the whole packed-FMA kernel (measured 33-36 ms per launch).
+// Measured on GB300 (1920x1080 x 4 spp, radius 16): 16.6 ms per depth launch against 13.8 ms for
+// the packed-FMA kernel. Reading the logits as 16x256b fragments gives a thread 4 queries, so a
+// radiance load feeds 8 pairs; read one query per thread (32x32b) every pair needed its own
+// warp-uniform shared-memory load (4 bytes per wavefront, 1920 wavefronts per window row) and the
+// kernel took 22.5 ms with the shared-memory pipe 65 % busy. What remains is pipeline latency: the
+// stages overlap imperfectly and every tile fills and drains the pipeline (without the sums the
+// same kernel still takes 12.5 ms). Putting the sums on the tensor cores as well (split-TF32
+// P . [v_hi | v_lo] with P written back to TMEM) needs 40 MMAs of N = 16 per window row; a TF32
+// tcgen05.mma of M = 128, K = 8 costs its issuing thread ~63 cycles and holds the tensor pipe ~39
+// cycles whatever its N (full rate only from N = 160: 80 cycles), so those sums alone cost more
+// pipe time than the whole packed-FMA kernel (measured 33-36 ms per launch).
 //
 // CTA = one 8 x 4 pixel tile = 128 queries = the 128 TMEM lanes (lane = 32 row + 4 x + sample),
-// 23 warps:
-//   warps 0-15  epilogue: warp w owns lanes 32 (w % 4) .. +31 (pixel row w % 4) and quarter w / 4
-//               of the window row's 160 candidates: tcgen05.ld S, release the TMEM buffer, then
-//               w = ex2(S) and the sums; warps 0-3 also write the query features and the outputs.
-//   warps 16-20 producers: the window row's candidate feature image (K-major core matrices, no
+// 15 warps:
+//   warps 0-7   epilogue: warp w owns lanes 32 (w % 4) .. +31 (pixel row w % 4) and half w / 4 of
+//               the window row's 160 candidates, read as 16x256b fragments: per 8-candidate block a
+//               thread holds 4 queries (lanes t/4, t/4 + 8, 16 + t/4, 24 + t/4 of the quarter) x 2
+//               candidates (2 (t % 4), +1), so one 8-byte radiance load per channel serves 8 pairs;
+//               then w = ex2(S) and the sums on packed FMAs; warps 0-3 also write the query
+//               features and the outputs.
+//   warps 8-12  producers: the window row's candidate feature image (K-major core matrices, no
 //               swizzle) and radiance row, from the raw ring, into a ring of kNS stages.
-//   warp 21     lane 0 issues the logits of each window row into one of 3 TMEM buffers.
-//   warp 22     lane 0 copies each window row's 16 record fields (pos, nrm, rad, thr, valid,
+//   warp 13     lane 0 issues the logits of each window row into one of 3 TMEM buffers.
+//   warp 14     lane 0 copies each window row's 16 record fields (pos, nrm, rad, thr, valid,
 //               out_next) from HBM into a raw ring of kNR stages with cp.async.bulk.
 // Every mbarrier wait is bounded (~2 s); on expiry the thread records STY_DEV_WAIT_TIMEOUT and
 // leaves its loop, and the outputs of the tile become NaN; the MMA thread waits (bounded) for its
@@ -64,8 +70,9 @@ constexpr int kTX = 8, kTY = 4;       // query tile in pixels
 constexpr int kM = kTX * kTY * kS;    // 128 queries = MMA rows
 constexpr int kK = 40;                // logit features
 constexpr int kNCol = 160;            // candidates per window row at radius 15-16 (40 px x 4)
-constexpr int kEW = 16, kPW = 5;      // epilogue and producer warps (one candidate per producer thread)
-constexpr int kNH = kNCol / (kEW / 4); // candidates per epilogue warp (4 warps share a TMEM lane quarter)
+constexpr int kEW = 8, kPW = 5;       // epilogue and producer warps (one candidate per producer thread)
+constexpr int kNH = kNCol / (kEW / 4); // candidates per epilogue warp (2 warps share a TMEM lane quarter)
+constexpr int kNBlk = kNH / 8;        // 8-candidate blocks per epilogue warp
 constexpr int kMmaWarp = kEW + kPW;   // warp 21: MMA issue
 constexpr int kLoadWarp = kMmaWarp + 1;  // warp 22: bulk copies of the raw record rows
 constexpr int kKahanRows = 4;         // window rows summed in FP32 before a Kahan step
@@ -114,6 +121,44 @@ __device__ __forceinline__ void tmem_ld8u(uint32_t taddr, uint32_t *r) {
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                  : "r"(taddr));
+}
+// 16x256b fragments: per 8 columns, thread t gets (lane t / 4, columns 2 (t % 4), +1) and
+// (lane t / 4 + 8, the same columns); repetition i covers columns 8 i .. 8 i + 7 (registers 4 i ..)
+__device__ __forceinline__ void tmem_ld_frag4(uint32_t taddr, uint32_t *r) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.16x256b.x4.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_ld_frag2(uint32_t taddr, uint32_t *r) {
+    asm volatile("tcgen05.ld.sync.aligned.16x256b.x2.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+// weights and sums of nb 8-candidate blocks: lo / hi = the fragments of lane halves 0 / 1,
+// vr = the radiance row at this thread's first candidate column
+template <int nb>
+__device__ __forceinline__ void frag_sums(const uint32_t *lo, const uint32_t *hi, const float *vr, float2 (&acc)[4][4]) {
+    const float2 one2 = make_float2(1.0f, 1.0f);
+#pragma unroll
+    for (int i = 0; i < nb; i++) {
+        float2 w[4];
+        w[0] = make_float2(ex2_approx(__uint_as_float(lo[4 * i])), ex2_approx(__uint_as_float(lo[4 * i + 1])));
+        w[1] = make_float2(ex2_approx(__uint_as_float(lo[4 * i + 2])), ex2_approx(__uint_as_float(lo[4 * i + 3])));
+        w[2] = make_float2(ex2_approx(__uint_as_float(hi[4 * i])), ex2_approx(__uint_as_float(hi[4 * i + 1])));
+        w[3] = make_float2(ex2_approx(__uint_as_float(hi[4 * i + 2])), ex2_approx(__uint_as_float(hi[4 * i + 3])));
+        const float2 r2 = *reinterpret_cast<const float2 *>(vr + 8 * i);
+        const float2 g2 = *reinterpret_cast<const float2 *>(vr + kNCol + 8 * i);
+        const float2 b2 = *reinterpret_cast<const float2 *>(vr + 2 * kNCol + 8 * i);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            acc[q][0] = ffma2(w[q], r2, acc[q][0]);
+            acc[q][1] = ffma2(w[q], g2, acc[q][1]);
+            acc[q][2] = ffma2(w[q], b2, acc[q][2]);
+            acc[q][3] = ffma2(w[q], one2, acc[q][3]);
+        }
+    }
 }
 __device__ __forceinline__ void mbar_init1(uint64_t *bar, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -164,7 +209,7 @@ struct SmemTc {
     uint64_t qf_ready;
     uint32_t tmem_slot;
     float red[4][8];        // per query warp: sum p'(3), sum n(3), count
-    float part[kEW / 4 - 1][kM][4];  // the other column quarters' totals, per query
+    float part[kEW / 4][kM][4];  // per column half, each query's totals
 };
 
 __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, const sty_style_program style) {
@@ -275,7 +320,7 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
     const bool direct = __syncthreads_or(is_q && qv && !(q2 <= kLimQ)) != 0;
 
     bool failed = false;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};  // r, g, b, weight (threads 0-127)
+    float acc_out[4] = {0.f, 0.f, 0.f, 0.f};  // r, g, b, weight (threads 0-127)
     if (direct) {
         // ---- direct form on the CUDA cores (tiles spread wider than the bilinear form allows)
         if (is_q && qv) {
@@ -313,10 +358,10 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
                     }
                 }
             }
-            acc[0] = k0.s;
-            acc[1] = k1.s;
-            acc[2] = k2.s;
-            acc[3] = k3.s;
+            acc_out[0] = k0.s;
+            acc_out[1] = k1.s;
+            acc_out[2] = k2.s;
+            acc_out[3] = k3.s;
         }
     } else if (warp >= kEW && warp < kMmaWarp) {
         // ================= producers: operand images from the raw rows =================
@@ -453,9 +498,9 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             }
         }
     } else {
-        // ================= epilogue warps 0-15 =================
+        // ================= epilogue warps 0-7 =================
         const int qw = warp & 3, h = warp >> 2;
-        const uint32_t lane_off = (uint32_t)(qw * 32) << 16;
+        const int tq = lane >> 2, tc = lane & 3;  // fragment row group and column pair
         const uint32_t colh = (uint32_t)h * kNH;
         if (h == 0) {
             // this thread's query feature row (lane = query)
@@ -481,9 +526,17 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             fence_async_smem();
             mbar_arrive1(&sh.qf_ready);
         }
-        KahanF kr = {0.f, 0.f}, kg = {0.f, 0.f}, kb = {0.f, 0.f}, kw = {0.f, 0.f};
-        const float2 one2 = make_float2(1.0f, 1.0f);
-        float2 ar = make_float2(0.f, 0.f), ag = ar, ab = ar, aw = ar;
+        // acc[q][c]: query q of this thread (lanes tq, tq + 8, 16 + tq, 24 + tq of the quarter), channel
+        // c (r, g, b, weight); the two halves hold this thread's two candidate columns
+        float2 acc[4][4];
+        KahanF tot[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                acc[q][c] = make_float2(0.f, 0.f);
+                tot[q][c] = {0.f, 0.f};
+            }
         for (int k = 0; k < nrows; k++) {
             const int b = k % kNB, s = k % kNS;
             if (!mbar_wait(&sh.s_full[b], (k / kNB) & 1, a.status)) {
@@ -492,66 +545,61 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             }
             fence_after();
             const bool rows_in = k >= qw && k <= 2 * R + qw;  // |y_q - y_c| <= R for this warp's pixel row
-            uint32_t sv[kNH];
             if (rows_in) {
-                const uint32_t sb = tmem + lane_off + (uint32_t)b * kNCol + colh;
-                tmem_ld16u(sb, &sv[0]);
-                tmem_ld16u(sb + 16u, &sv[16]);
-                tmem_ld8u(sb + 32u, &sv[32]);
+                const uint32_t s0 = tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)b * kNCol + colh;
+                const uint32_t s1 = s0 + (16u << 16);
+                const float *vr =
+                    reinterpret_cast<const float *>(stage + s * kStageBytes + kCfBytes) + colh + 2 * tc;
+                uint32_t f0[16], f1[16];
+                tmem_ld_frag4(s0, f0);
+                tmem_ld_frag4(s1, f1);
                 tmem_wait_ld();
-            }
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive1(&sh.s_empty[b]);  // the logits are in registers
-            if (rows_in) {
-                const float *vr = reinterpret_cast<const float *>(stage + s * kStageBytes + kCfBytes) + colh;
-#pragma unroll
-                for (int j = 0; j < kNH; j += 4) {
-                    const float2 w01 =
-                        make_float2(ex2_approx(__uint_as_float(sv[j])), ex2_approx(__uint_as_float(sv[j + 1])));
-                    const float2 w23 =
-                        make_float2(ex2_approx(__uint_as_float(sv[j + 2])), ex2_approx(__uint_as_float(sv[j + 3])));
-                    const float4 r4 = *reinterpret_cast<const float4 *>(vr + j);
-                    const float4 g4 = *reinterpret_cast<const float4 *>(vr + kNCol + j);
-                    const float4 b4 = *reinterpret_cast<const float4 *>(vr + 2 * kNCol + j);
-                    ar = ffma2(w01, make_float2(r4.x, r4.y), ar);
-                    ar = ffma2(w23, make_float2(r4.z, r4.w), ar);
-                    ag = ffma2(w01, make_float2(g4.x, g4.y), ag);
-                    ag = ffma2(w23, make_float2(g4.z, g4.w), ag);
-                    ab = ffma2(w01, make_float2(b4.x, b4.y), ab);
-                    ab = ffma2(w23, make_float2(b4.z, b4.w), ab);
-                    aw = ffma2(w01, one2, aw);
-                    aw = ffma2(w23, one2, aw);
-                }
+                frag_sums<4>(f0, f1, vr, acc);
+                tmem_ld_frag4(s0 + 32u, f0);
+                tmem_ld_frag4(s1 + 32u, f1);
+                tmem_wait_ld();
+                frag_sums<4>(f0, f1, vr + 32, acc);
+                tmem_ld_frag2(s0 + 64u, f0);
+                tmem_ld_frag2(s1 + 64u, f1);
+                tmem_wait_ld();
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive1(&sh.s_empty[b]);  // every logit of the row is in registers
+                frag_sums<2>(f0, f1, vr + 64, acc);
+            } else {
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive1(&sh.s_empty[b]);
             }
             __syncwarp();
             if (lane == 0) mbar_arrive1(&sh.stage_empty[s]);  // done with the radiance row
             if (k % kKahanRows == kKahanRows - 1 || k == nrows - 1) {
-                kr.add(ar.x + ar.y);
-                kg.add(ag.x + ag.y);
-                kb.add(ab.x + ab.y);
-                kw.add(aw.x + aw.y);
-                ar = ag = ab = aw = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) {
+                        tot[q][c].add(acc[q][c].x + acc[q][c].y);
+                        acc[q][c] = make_float2(0.f, 0.f);
+                    }
             }
         }
-        // the four column quarters of each query: warps 4-15 hand their totals to warps 0-3
-        const int q = qw * 32 + lane;
-        if (h > 0) {
-            sh.part[h - 1][q][0] = kr.s - kr.c;
-            sh.part[h - 1][q][1] = kg.s - kg.c;
-            sh.part[h - 1][q][2] = kb.s - kb.c;
-            sh.part[h - 1][q][3] = kw.s - kw.c;
+        // each query's totals: add over the 4 column pairs (lanes tq * 4 + 0..3), then over the two
+        // column halves (warps w and w + 4) through shared memory
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int ql = qw * 32 + (q >> 1) * 16 + (q & 1) * 8 + tq;
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                float v = tot[q][c].s - tot[q][c].c;
+                v += __shfl_xor_sync(0xffffffffu, v, 1);
+                v += __shfl_xor_sync(0xffffffffu, v, 2);
+                if (tc == 0) sh.part[h][ql][c] = v;
+            }
         }
         bar_sync_n(1, kEW * 32);
         if (h == 0) {
-            acc[0] = kr.s - kr.c;
-            acc[1] = kg.s - kg.c;
-            acc[2] = kb.s - kb.c;
-            acc[3] = kw.s - kw.c;
 #pragma unroll
-            for (int o = 0; o < kEW / 4 - 1; o++)
-#pragma unroll
-                for (int c = 0; c < 4; c++) acc[c] += sh.part[o][q][c];
+            for (int c = 0; c < 4; c++) acc_out[c] = sh.part[0][tid][c] + sh.part[1][tid][c];
         }
     }
 
@@ -564,8 +612,8 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
                 f = {__int_as_float(0x7fc00000), __int_as_float(0x7fc00000), __int_as_float(0x7fc00000)};
                 o = f;
             } else {
-                const float iw = 1.0f / acc[3];
-                f = {acc[0] * iw, acc[1] * iw, acc[2] * iw};
+                const float iw = 1.0f / acc_out[3];
+                f = {acc_out[0] * iw, acc_out[1] * iw, acc_out[2] * iw};
                 o = style_apply(style, a.depth, f);
             }
         }
