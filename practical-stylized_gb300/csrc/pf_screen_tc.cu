@@ -25,7 +25,7 @@
 // window outside |y_q - y_c| <= R are skipped by the warps that own those queries. Every
 // kKahanRows window rows each thread adds its FP32 partial sums into Kahan totals.
 //
-// Measured on GB300 (1920x1080 x 4 spp, radius 16): 16.6 ms per depth launch against 13.8 ms for
+// Measured on GB300 (1920x1080 x 4 spp, radius 16): 16.5 ms per depth launch against 13.8 ms for
 // the packed-FMA kernel. Reading the logits as 16x256b fragments gives a thread 4 queries, so a
 // radiance load feeds 8 pairs; read one query per thread (32x32b) every pair needed its own
 // warp-uniform shared-memory load (4 bytes per wavefront, 1920 wavefronts per window row) and the
@@ -44,10 +44,11 @@
 //               thread holds 4 queries (lanes t/4, t/4 + 8, 16 + t/4, 24 + t/4 of the quarter) x 2
 //               candidates (2 (t % 4), +1), so one 8-byte radiance load per channel serves 8 pairs;
 //               then w = ex2(S) and the sums on packed FMAs; warps 0-3 also write the query
-//               features and the outputs.
+//               features (into TMEM: the A operand of the logits) and the outputs.
 //   warps 8-12  producers: the window row's candidate feature image (K-major core matrices, no
 //               swizzle) and radiance row, from the raw ring, into a ring of kNS stages.
-//   warp 13     lane 0 issues the logits of each window row into one of 3 TMEM buffers.
+//   warp 13     lane 0 issues the logits of each window row into one of 2 TMEM buffers of 160
+//               columns (A = the query features in TMEM columns 320-359, B = the candidate image).
 //   warp 14     lane 0 copies each window row's 16 record fields (pos, nrm, rad, thr, valid,
 //               out_next) from HBM into a raw ring of kNR stages with cp.async.bulk.
 // Every mbarrier wait is bounded (~2 s); on expiry the thread records STY_DEV_WAIT_TIMEOUT and
@@ -79,14 +80,14 @@ constexpr int kKahanRows = 4;         // window rows summed in FP32 before a Kah
 constexpr int kNT = (kLoadWarp + 1) * 32;
 constexpr int kNS = 4;                // staging ring depth (feature images and radiance rows)
 constexpr int kNR = 4;                // raw ring depth (record rows)
-constexpr int kNB = 3;                // TMEM logit buffers
+constexpr int kNB = 2;                // TMEM logit buffers
+constexpr uint32_t kColQ = kNB * kNCol;  // TMEM columns of the query features (A operand of the logits)
 constexpr float kBig = 16384.0f;
 constexpr float kLimQ = 16.0f, kLimC = 120.0f;
 
 // operand images: element (row, k) of a K-major image with 40 columns sits at
 // (row / 8) * 1280 + (k / 4) * 128 + (row % 8) * 16 + (k % 4) * 4 bytes (LBO 128, SBO 1280)
 constexpr uint32_t kRowGroup = kK / 4 * 128;           // 1280
-constexpr uint32_t kQfBytes = kM / 8 * kRowGroup;      // 20480
 constexpr uint32_t kCfBytes = kNCol / 8 * kRowGroup;   // 25600
 constexpr uint32_t kVBytes = 3 * kNCol * 4;            // incoming radiance, [channel][candidate]
 constexpr uint32_t kStageBytes = kCfBytes + kVBytes;   // 27520
@@ -97,31 +98,34 @@ constexpr uint32_t kTabBytes = kNpxMax * 16 * 4;       // horizontal table: Mh[8
 constexpr int kNF = 16;
 constexpr uint32_t kRawField = kNCol * 4;           // 640 bytes
 constexpr uint32_t kRawBytes = kNF * kRawField;     // 10240
-constexpr uint32_t kSmemBytes = kQfBytes + kNS * kStageBytes + kTabBytes + kNR * kRawBytes;
-static_assert(kNB * kNCol <= 512, "TMEM budget");
+constexpr uint32_t kSmemBytes = kNS * kStageBytes + kTabBytes + kNR * kRawBytes;
+static_assert(kColQ + kK <= 512, "TMEM budget");
 
 __host__ __device__ constexpr uint32_t idesc_tf32(uint32_t m, uint32_t n) {
     // D f32 (bit 4), A / B TF32 (bits 7-9, 10-12 = 2), both K-major, N>>3 (bits 17-22), M>>4 (24-28)
     return (1u << 4) | (2u << 7) | (2u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
-__device__ __forceinline__ void mma_tf32_ss(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+// A operand from TMEM (lanes = rows, one TF32 column per K element)
+__device__ __forceinline__ void mma_tf32_ts(uint32_t d, uint32_t a_tmem, uint64_t b, uint32_t idesc, uint32_t acc) {
     asm volatile(
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d),
+        "r"(a_tmem), "l"(b), "r"(idesc), "r"(acc));
 }
-__device__ __forceinline__ void tmem_ld16u(uint32_t taddr, uint32_t *r) {
+__device__ __forceinline__ void tmem_st16u(uint32_t taddr, const uint32_t *r) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]), "r"(r[9]),
+        "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+        : "memory");
 }
-__device__ __forceinline__ void tmem_ld8u(uint32_t taddr, uint32_t *r) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-                 : "r"(taddr));
+__device__ __forceinline__ void tmem_st8u(uint32_t taddr, const uint32_t *r) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr), "r"(r[0]),
+                 "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                 : "memory");
 }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 // 16x256b fragments: per 8 columns, thread t gets (lane t / 4, columns 2 (t % 4), +1) and
 // (lane t / 4 + 8, the same columns); repetition i covers columns 8 i .. 8 i + 7 (registers 4 i ..)
 __device__ __forceinline__ void tmem_ld_frag4(uint32_t taddr, uint32_t *r) {
@@ -215,10 +219,9 @@ struct SmemTc {
 __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, const sty_style_program style) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ SmemTc sh;
-    uint8_t *qf = smem;
-    uint8_t *stage = smem + kQfBytes;
-    float *tab = reinterpret_cast<float *>(smem + kQfBytes + kNS * kStageBytes);
-    uint8_t *raw = smem + kQfBytes + kNS * kStageBytes + kTabBytes;
+    uint8_t *stage = smem;
+    float *tab = reinterpret_cast<float *>(smem + kNS * kStageBytes);
+    uint8_t *raw = smem + kNS * kStageBytes + kTabBytes;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int R = a.R;
     const int npx = kTX + 2 * R;  // candidate pixels per window row (<= 40)
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
         // ================= MMA issue (one thread): the logits of every window row =================
         if (lane == 0) {
             const uint32_t idesc = idesc_tf32(kM, kNCol);
-            const uint32_t qf_addr = smem_u32(qf), st_addr = smem_u32(stage);
+            const uint32_t st_addr = smem_u32(stage);
             int last = -1;
             bool ok = mbar_wait(&sh.qf_ready, 0, a.status);
             for (int k = 0; ok && k < nrows; k++) {
@@ -485,8 +488,8 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
                 const uint32_t d = tmem + (uint32_t)b * kNCol;
 #pragma unroll
                 for (int kk = 0; kk < kK / 8; kk++)
-                    mma_tf32_ss(d, make_desc(qf_addr + kk * 256u, 128u, kRowGroup),
-                                make_desc(cf + kk * 256u, 128u, kRowGroup), idesc, kk > 0 ? 1u : 0u);
+                    mma_tf32_ts(d, tmem + kColQ + 8u * kk, make_desc(cf + kk * 256u, 128u, kRowGroup), idesc,
+                                kk > 0 ? 1u : 0u);
                 mma_commit(&sh.s_full[b]);
                 mma_commit(&sh.stage_empty[k % kNS]);
                 last = k;
@@ -521,9 +524,22 @@ __global__ void __launch_bounds__(kNT, 1) k_pf_screen_tc(const ScreenArgs a, con
             float oh[8];
 #pragma unroll
             for (int i = 0; i < 8; i++) oh[i] = (qv && i == qx) ? 1.0f : 0.0f;
-            const float4 oh0 = make_float4(oh[0], oh[1], oh[2], oh[3]), oh1 = make_float4(oh[4], oh[5], oh[6], oh[7]);
-            store_row40(qf + kimg_off(tid, 0), hi, hi, lo, oh0, oh1, oh0, oh1);
-            fence_async_smem();
+            // the row [qh | qh | ql | onehot | onehot] into TMEM (lane = query): the logits' A operand
+            uint32_t row[kK];
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                row[i] = __float_as_uint(hi[i]);
+                row[8 + i] = __float_as_uint(hi[i]);
+                row[16 + i] = __float_as_uint(lo[i]);
+                row[24 + i] = __float_as_uint(oh[i]);
+                row[32 + i] = __float_as_uint(oh[i]);
+            }
+            const uint32_t qa = tmem + ((uint32_t)(warp * 32) << 16) + kColQ;
+            tmem_st16u(qa, row);
+            tmem_st16u(qa + 16u, row + 16);
+            tmem_st8u(qa + 32u, row + 32);
+            tmem_wait_st();
+            fence_before();
             mbar_arrive1(&sh.qf_ready);
         }
         // acc[q][c]: query q of this thread (lanes tq, tq + 8, 16 + tq, 24 + tq of the quarter), channel
