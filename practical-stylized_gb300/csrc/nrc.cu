@@ -71,6 +71,115 @@ __global__ void __launch_bounds__(128) k_fwd_f32(NrcNet n, const float *__restri
     }
 }
 
+// ---- FP32 forward, register-tiled (the batched and inference path) ---------------------------
+// One persistent CTA per SM: every hidden layer's weights transposed into shared memory once
+// (wt[l][k][j] = W_l[j][k]), the output layer as stored. Two groups of 256 threads each walk their
+// own 128-sample tiles (named barrier per group), each with two activation buffers [64 k][kFP]
+// (k-major; a pitch of 132 floats puts consecutive rows 16 bytes apart in bank order). Thread
+// (ty, tx) = (t / 16, t % 16) of a group computes samples 8 ty .. 8 ty + 7 x outputs 4 tx .. 4 tx + 3:
+// per k two 16-byte activation loads and one 16-byte weight load feed 32 FMAs.
+// Every output is summed over k = 0 .. 63 in order with fmaf on the same operands as k_fwd_f32, so
+// the two kernels agree bit for bit.
+constexpr int kFT = 128;      // samples per tile
+constexpr int kFP = kFT + 4;  // activation row pitch (floats)
+__host__ __device__ inline size_t fwd_tiled_floats(const NrcNet &n) {
+    return (size_t)n.layers * W * W + (size_t)((n.out_dims * W + 3) & ~3) + 4 * (size_t)W * kFP;
+}
+__global__ void __launch_bounds__(512, 1) k_fwd_f32_tiled(NrcNet n, const float *__restrict__ wg, uint64_t count,
+                                                          const float *__restrict__ input,
+                                                          float *__restrict__ output, float *__restrict__ acts) {
+    extern __shared__ __align__(16) float sm[];
+    const int L = n.layers, O = n.out_dims;
+    float *wt = sm;
+    float *wo = wt + (size_t)L * W * W;
+    const int grp = threadIdx.x >> 8, tid = threadIdx.x & 255;
+    float *buf0 = wo + ((O * W + 3) & ~3) + (size_t)grp * 2 * W * kFP;
+    float *buf1 = buf0 + W * kFP;
+    for (int e = threadIdx.x; e < L * W * W; e += 512) {
+        const int l = e / (W * W), r = e - l * (W * W), j = r / W, k = r - j * W;
+        wt[(size_t)l * W * W + k * W + j] = wg[nrc_w_offset(l) + (size_t)j * W + k];
+    }
+    for (int e = threadIdx.x; e < O * W; e += 512) wo[e] = wg[nrc_w_offset(L) + e];
+    __syncthreads();
+    auto group_sync = [&]() { asm volatile("bar.sync %0, 256;" ::"r"(1 + grp) : "memory"); };
+    const int ty = tid >> 4, tx = tid & 15;
+    const uint64_t ntiles = (count + kFT - 1) / kFT;
+    for (uint64_t tile = 2 * (uint64_t)blockIdx.x + grp; tile < ntiles; tile += 2 * (uint64_t)gridDim.x) {
+        const uint64_t s0 = tile * kFT;
+        if (tid < kFT) {  // encode one sample per thread into buf0[k][sample]
+            const uint64_t i = s0 + tid;
+            float enc[W];
+            if (i < count) {
+                nrc_encode(n, input + i * n.in_dims, enc);
+            } else {
+#pragma unroll
+                for (int k = 0; k < W; k++) enc[k] = 0.0f;
+            }
+#pragma unroll
+            for (int k = 0; k < W; k++) buf0[k * kFP + tid] = enc[k];
+            if (acts && i < count)
+#pragma unroll
+                for (int k = 0; k < W; k += 4)
+                    *reinterpret_cast<float4 *>(acts + i * W + k) = make_float4(enc[k], enc[k + 1], enc[k + 2], enc[k + 3]);
+        }
+        group_sync();
+        float *cur = buf0, *nxt = buf1;
+        for (int l = 0; l < L; l++) {
+            const float *w = wt + (size_t)l * W * W + 4 * tx;
+            const float *av = cur + 8 * ty;
+            float acc[8][4];
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+#pragma unroll 4
+            for (int k = 0; k < W; k++) {
+                const float4 a0 = *reinterpret_cast<const float4 *>(av + k * kFP);
+                const float4 a1 = *reinterpret_cast<const float4 *>(av + k * kFP + 4);
+                const float4 w4 = *reinterpret_cast<const float4 *>(w + k * W);
+                const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+#pragma unroll
+                    for (int j = 0; j < 4; j++) acc[i][j] = fmaf(wv[j], a[i], acc[i][j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaxf(acc[i][j], 0.0f);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                float *dst = nxt + (4 * tx + j) * kFP + 8 * ty;
+                *reinterpret_cast<float4 *>(dst) = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+                *reinterpret_cast<float4 *>(dst + 4) = make_float4(acc[4][j], acc[5][j], acc[6][j], acc[7][j]);
+            }
+            if (acts) {
+#pragma unroll
+                for (int i = 0; i < 8; i++) {
+                    const uint64_t s = s0 + 8 * ty + i;
+                    if (s < count)
+                        *reinterpret_cast<float4 *>(acts + ((size_t)(l + 1) * count + s) * W + 4 * tx) =
+                            make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+                }
+            }
+            group_sync();
+            float *t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+        if (tid < kFT && s0 + tid < count) {
+            for (int c = 0; c < O; c++) {
+                float a = 0.0f;
+#pragma unroll
+                for (int k = 0; k < W; k++) a = fmaf(wo[c * W + k], cur[k * kFP + tid], a);
+                output[(s0 + tid) * O + c] = a;
+            }
+        }
+        group_sync();  // the next tile's encoding overwrites buf0
+    }
+}
+
 // ---- loss gradient + FP32 backward: one thread per sample -----------------------------------
 // dpre: [layers+1][B][64]: row l < layers = dL/d(pre-activation of hidden layer l),
 // row `layers` = dL/d(output) (first out_dims entries).
@@ -310,6 +419,20 @@ size_t fwd_smem(const sty_nrc *nr) { return nr->np * sizeof(float); }
 
 sty_status fwd_f32(sty_nrc *nr, const float *wts, uint64_t count, const float *in, float *out, float *acts,
                    cudaStream_t st) {
+    if (count == 0) return STY_OK;
+    int dev = 0, optin = 0, sms = 0;
+    STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    STY_TRY(check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attr smem"));
+    STY_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr SMs"));
+    const size_t tsmem = fwd_tiled_floats(nr->net) * sizeof(float);
+    if (tsmem <= (size_t)optin) {  // register-tiled kernel (bit-identical to k_fwd_f32)
+        STY_TRY(check_cuda(cudaFuncSetAttribute(k_fwd_f32_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem),
+                           "attr k_fwd_f32_tiled"));
+        const uint64_t ntiles = (count + kFT - 1) / kFT;
+        const unsigned grid = (unsigned)std::min<uint64_t>((ntiles + 1) / 2, (uint64_t)sms);
+        k_fwd_f32_tiled<<<grid, 512, tsmem, st>>>(nr->net, wts, count, in, out, acts);
+        return check_launch("k_fwd_f32_tiled");
+    }
     const size_t smem = fwd_smem(nr);
     STY_TRY(check_cuda(cudaFuncSetAttribute(k_fwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "attr k_fwd_f32"));
