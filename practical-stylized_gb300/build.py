@@ -19,6 +19,9 @@ CSRC = PKG / "csrc"
 OUT = PKG / "lib"
 OBJ = PKG / "_build"
 LIB = OUT / "libsty_gb300.so"
+# the same objects as a static archive, for a host that links the library into its own binary
+# (the reference's Rust build links its C++ extension statically); link with -lcudart -lstdc++
+STATIC = OUT / "libsty_gb300.a"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + [
@@ -76,6 +79,15 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if force or not _newer(STATIC, objs):
+        if STATIC.exists():
+            STATIC.unlink()
+        cmd = [nvcc, *ARCH, "-lib", "-o", str(STATIC), *map(str, objs)]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"archive failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
