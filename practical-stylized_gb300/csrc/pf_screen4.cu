@@ -442,7 +442,7 @@ __global__ void __launch_bounds__(NTH, 1) k_pf_screen4(const ScreenArgs a, const
                                 v[0] = px; v[1] = py; v[2] = pz;
                                 v[6] = m;
                                 v[7] = in[0] * m; v[8] = in[1] * m; v[9] = in[2] * m;
-                            } else {  // weight < 2^-60 for every query of this tile: dropped exactly
+                            } else {  // weight < 2^-48 for every query of this tile: dropped exactly
                                 v[0] = v[1] = v[2] = 0.0f;
                                 v[6] = v[7] = v[8] = v[9] = 0.0f;
                             }
