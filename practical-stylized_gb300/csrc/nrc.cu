@@ -257,6 +257,120 @@ __global__ void __launch_bounds__(128) k_bwd_f32(NrcNet n, const float *__restri
     }
 }
 
+// ---- loss gradient + FP32 backward, register-tiled ------------------------------------------
+// The same persistent layout as k_fwd_f32_tiled: the weights as stored ([j][k]: for a summed row j
+// the outputs k are contiguous), two groups of 256 threads on their own 128-sample tiles, thread
+// (ty, tx) holding samples 8 ty .. 8 ty + 7 x units 4 tx .. 4 tx + 3. Per tile: the relative-L2
+// gradient g of each sample, dH = W_out^T g, then per hidden layer l (last first) dP_l = dH where
+// act_{l+1} > 0 (to dpre and to a k-major buffer) and dH = W_l^T dP_l. Every sum runs over the same
+// index in the same order with fmaf on the same operands as k_bwd_f32, so dpre is bit-identical.
+__host__ __device__ inline size_t bwd_tiled_floats(const NrcNet &n) {
+    return (size_t)n.layers * W * W + (size_t)((n.out_dims * W + 3) & ~3) + 2 * ((size_t)W * kFP + kNrcOutPad * kFT);
+}
+__global__ void __launch_bounds__(512, 1) k_bwd_f32_tiled(NrcNet n, const float *__restrict__ wg, uint32_t B,
+                                                          const float *__restrict__ pred,
+                                                          const float *__restrict__ target,
+                                                          const float *__restrict__ acts, float *__restrict__ dpre,
+                                                          float *__restrict__ loss_acc) {
+    extern __shared__ __align__(16) float sm[];
+    const int L = n.layers, O = n.out_dims;
+    float *ws = sm;                              // [L][64 j][64 k] as stored
+    float *wo = ws + (size_t)L * W * W;          // [O][64]
+    const int grp = threadIdx.x >> 8, tid = threadIdx.x & 255;
+    float *dpb = wo + ((O * W + 3) & ~3) + (size_t)grp * ((size_t)W * kFP + kNrcOutPad * kFT);  // [64 j][kFP]
+    float *gb = dpb + W * kFP;                   // [O][128]: the loss gradient, k-major
+    for (size_t e = threadIdx.x; e < nrc_param_count(n); e += 512) ws[e] = wg[e];
+    __syncthreads();
+    auto group_sync = [&]() { asm volatile("bar.sync %0, 256;" ::"r"(1 + grp) : "memory"); };
+    const int ty = tid >> 4, tx = tid & 15;
+    const float norm = 1.0f / ((float)B * (float)O);
+    float lsum = 0.0f;
+    const uint32_t ntiles = (B + kFT - 1) / kFT;
+    for (uint32_t tile = 2 * blockIdx.x + grp; tile < ntiles; tile += 2 * gridDim.x) {
+        const uint32_t s0 = tile * kFT;
+        if (tid < kFT) {
+            const uint32_t i = s0 + tid;
+            for (int c = 0; c < O; c++) {
+                float g = 0.0f;
+                if (i < B) {
+                    const float p = pred[(size_t)i * O + c], t = target[(size_t)i * O + c];
+                    const float den = p * p + 0.01f;  // relative L2, prediction treated as constant below
+                    lsum += (p - t) * (p - t) / den;
+                    g = 2.0f * (p - t) / den * norm;
+                    dpre[((size_t)L * B + i) * W + c] = g;
+                }
+                gb[c * kFT + tid] = g;
+            }
+        }
+        group_sync();
+        // dH = W_out^T g
+        float acc[8][4];
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+        for (int c = 0; c < O; c++) {
+            const float4 w4 = *reinterpret_cast<const float4 *>(wo + c * W + 4 * tx);
+            const float4 g0 = *reinterpret_cast<const float4 *>(gb + c * kFT + 8 * ty);
+            const float4 g1 = *reinterpret_cast<const float4 *>(gb + c * kFT + 8 * ty + 4);
+            const float gv[8] = {g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w};
+            const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(wv[j], gv[i], acc[i][j]);
+        }
+        for (int l = L - 1; l >= 0; l--) {
+            // dP_l = dH where act_{l+1} > 0 -> dpre and dpb[j][sample]
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const uint32_t s = s0 + 8 * ty + i;
+                float4 h4 = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (s < B) h4 = *reinterpret_cast<const float4 *>(acts + ((size_t)(l + 1) * B + s) * W + 4 * tx);
+                acc[i][0] = h4.x > 0.0f ? acc[i][0] : 0.0f;
+                acc[i][1] = h4.y > 0.0f ? acc[i][1] : 0.0f;
+                acc[i][2] = h4.z > 0.0f ? acc[i][2] : 0.0f;
+                acc[i][3] = h4.w > 0.0f ? acc[i][3] : 0.0f;
+                if (s < B)
+                    *reinterpret_cast<float4 *>(dpre + ((size_t)l * B + s) * W + 4 * tx) =
+                        make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
+            }
+            if (l == 0) break;
+            group_sync();  // the previous layer's dpb reads are done
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                float *dst = dpb + (4 * tx + j) * kFP + 8 * ty;
+                *reinterpret_cast<float4 *>(dst) = make_float4(acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
+                *reinterpret_cast<float4 *>(dst + 4) = make_float4(acc[4][j], acc[5][j], acc[6][j], acc[7][j]);
+            }
+            group_sync();
+            // dH = W_l^T dP_l: dH[k] = sum_j W_l[j][k] dP_l[j]
+            const float *w = ws + nrc_w_offset(l) + 4 * tx;
+            const float *dv = dpb + 8 * ty;
+#pragma unroll
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) acc[i][j] = 0.0f;
+#pragma unroll 4
+            for (int j = 0; j < W; j++) {
+                const float4 d0 = *reinterpret_cast<const float4 *>(dv + j * kFP);
+                const float4 d1 = *reinterpret_cast<const float4 *>(dv + j * kFP + 4);
+                const float4 w4 = *reinterpret_cast<const float4 *>(w + j * W);
+                const float dd[8] = {d0.x, d0.y, d0.z, d0.w, d1.x, d1.y, d1.z, d1.w};
+                const float wv[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int i = 0; i < 8; i++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[i][q] = fmaf(wv[q], dd[i], acc[i][q]);
+            }
+        }
+        group_sync();  // the next tile overwrites gb and dpb
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if ((threadIdx.x & 31) == 0 && loss_acc && lsum != 0.0f) atomicAdd(loss_acc, lsum / ((float)B * (float)O));
+}
+
 // ---- weight gradient: grad_l[j][k] = sum_i dpre_l[i][j] * acts_l[i][k] ----------------------
 // grid: (chunks, layers+1); 256 threads; rows R = 64 (hidden) or out_dims (output layer). Each
 // chunk of kWgChunk samples stores its partial sums at part + chunk * np; k_sum_chunks adds the
@@ -444,11 +558,25 @@ sty_status fwd_f32(sty_nrc *nr, const float *wts, uint64_t count, const float *i
 // nr->acts (FP32 CUDA-core path, also used for the BF16 path's weight update).
 sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t st) {
     const NrcNet &n = nr->net;
-    const size_t smem = fwd_smem(nr);
-    STY_TRY(check_cuda(cudaFuncSetAttribute(k_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                       "attr k_bwd_f32"));
-    k_bwd_f32<<<(B + 127) / 128, 128, smem, st>>>(n, nr->w, B, nr->bpred, target, nr->acts, nr->dpre, nr->loss);
-    STY_TRY(check_launch("k_bwd_f32"));
+    int dev = 0, optin = 0, sms = 0;
+    STY_TRY(check_cuda(cudaGetDevice(&dev), "cudaGetDevice"));
+    STY_TRY(check_cuda(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev), "attr smem"));
+    STY_TRY(check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "attr SMs"));
+    const size_t tsmem = bwd_tiled_floats(n) * sizeof(float);
+    if (B > 0 && n.out_dims <= kNrcOutPad && tsmem <= (size_t)optin) {  // register-tiled (bit-identical dpre)
+        STY_TRY(check_cuda(cudaFuncSetAttribute(k_bwd_f32_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem),
+                           "attr k_bwd_f32_tiled"));
+        const uint32_t ntiles = (B + kFT - 1) / kFT;
+        const unsigned grid = std::min<uint32_t>((ntiles + 1) / 2, (uint32_t)sms);
+        k_bwd_f32_tiled<<<grid, 512, tsmem, st>>>(n, nr->w, B, nr->bpred, target, nr->acts, nr->dpre, nr->loss);
+        STY_TRY(check_launch("k_bwd_f32_tiled"));
+    } else {
+        const size_t smem = fwd_smem(nr);
+        STY_TRY(check_cuda(cudaFuncSetAttribute(k_bwd_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                           "attr k_bwd_f32"));
+        k_bwd_f32<<<(B + 127) / 128, 128, smem, st>>>(n, nr->w, B, nr->bpred, target, nr->acts, nr->dpre, nr->loss);
+        STY_TRY(check_launch("k_bwd_f32"));
+    }
     const uint32_t chunks = (B + kWgChunk - 1) / kWgChunk;
     dim3 grid(chunks, n.layers + 1);
     k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->np, nr->gpart);
