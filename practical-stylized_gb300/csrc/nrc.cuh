@@ -63,7 +63,7 @@ sty_status grid_init_params(GridModel *g, uint64_t seed, float *w, cudaStream_t 
 sty_status grid_pack(GridModel *g, const float *w, const float *ema, cudaStream_t st);
 // inference with the EMA or the current parameters (packed by grid_pack with both sets); the
 // tensor-core path (tile encoder + MMA kernel) when the network fits it and allow_tc, else the
-// cuBLAS layer-by-layer path
+// layer-by-layer path on the tcgen05 row GEMMs (gemm_tc.cu)
 sty_status grid_infer(GridModel *g, bool ema, bool allow_tc, uint64_t count, const float *in, float *out,
                       cudaStream_t st);
 // the optimiser step (tiny-cuda-nn's Adam: sparse over the tables, per-entry step counts) and the EMA;
