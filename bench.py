@@ -148,7 +148,7 @@ def cpu_baseline(sty, orc, planes, valid, depths: int = D_, budget_s: float = 12
     prm = sty.c2_params().c()
     style = sty.c2_style()
     target = budget_s / 4 / depths
-    rows = max(8, orc.num_threads())  # the restatement runs one row per host thread at a time
+    rows = 2 * max(8, orc.num_threads())  # the restatement splits the band's rows over the host threads
     while True:  # band height: depth 1 (the styled depth) alone takes about target seconds
         t0 = time.perf_counter()
         orc.pf_screen_filter_depth_f32(rec, min(1, depths - 1), prm, style, out_next=None, y0=540, y1=540 + rows)
