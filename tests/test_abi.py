@@ -95,6 +95,18 @@ def test_argument_validation_without_gpu(sty):
     assert ei.value.status == a.STY_ERR_ARG
 
 
+def test_screen_kernel_choice_without_gpu(sty):
+    """sty_pf_screen_set_kernel takes the three kernel families and rejects anything else (no GPU)."""
+    lib = sty.abi.lib()
+    for k in (sty.SCREEN_KERNEL_FP32, sty.SCREEN_KERNEL_TENSOR, sty.SCREEN_KERNEL_AUTO):
+        assert lib.sty_pf_screen_set_kernel(k) == sty.abi.STY_OK
+    assert lib.sty_pf_screen_set_kernel(3) == sty.abi.STY_ERR_ARG
+    assert b"unknown kernel" in lib.sty_last_error()
+    with pytest.raises(sty.StyError):
+        sty.set_screen_kernel(-1)
+    lib.sty_pf_screen_set_kernel(sty.SCREEN_KERNEL_AUTO)
+
+
 def test_style_builders_validate(sty):
     a = sty.abi
     with pytest.raises(ValueError):

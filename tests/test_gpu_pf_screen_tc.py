@@ -20,11 +20,6 @@ def tensor_kernel(sty):
     sty.set_screen_kernel(sty.SCREEN_KERNEL_AUTO)
 
 
-def test_set_kernel_rejects_unknown(sty):
-    with pytest.raises(sty.StyError):
-        sty.set_screen_kernel(7)
-
-
 @pytest.mark.parametrize("R", [15, 16])
 @pytest.mark.parametrize("sigma_pos", [0.5, 0.2])
 def test_tc_filter_depth_matches_oracle(sty, orc, cuda, tensor_kernel, R, sigma_pos):
@@ -36,6 +31,33 @@ def test_tc_filter_depth_matches_oracle(sty, orc, cuda, tensor_kernel, R, sigma_
     _, got_o, ref_o, _, m, ef = _depth_parity(sty, orc, rs, hrec, valid, 0, prm, None)
     assert ef < TOL, f"filtered rel err {ef:.3e}"
     assert rel_err(got_o[:, m], ref_o[:, m], 1e-6).max() < TOL
+
+
+def test_tc_image_smaller_than_a_tile(sty, orc, cuda, tensor_kernel):
+    """A 6 x 3 image: one partial tile, every candidate row and column partly outside the image."""
+    W, H, S, D = 6, 3, 4, 1
+    planes, valid, rs, hrec = _setup(sty, W, H, S, D, seed=91)
+    prm = sty.ScreenParams(radius=16, sigma_pixel=8.0, sigma_pos=0.5, sigma_nrm=0.2)
+    _, got_o, ref_o, _, m, ef = _depth_parity(sty, orc, rs, hrec, valid, 0, prm, None)
+    assert ef < TOL, f"filtered rel err {ef:.3e}"
+
+
+def test_tc_unaligned_planes_take_the_cuda_core_kernel(sty, cuda, tensor_kernel):
+    """Record planes off the 16-byte boundary cannot be bulk-copied: the call must give exactly the
+    CUDA-core kernel's result."""
+    import torch
+    W, H, S, D = 40, 24, 4, 1
+    planes, valid = sty.synth.records(W, H, S, D, seed=92)
+    n = W * H * S
+    big = torch.zeros((12, n + 1), dtype=torch.float32, device="cuda")
+    big[:, 1:] = torch.from_numpy(planes).cuda()
+    rs = sty.RecordSet(big[:, 1:], torch.from_numpy(valid).cuda(), W, H, S, D)  # planes 4 bytes past a boundary
+    prm = sty.ScreenParams(radius=16, sigma_pixel=8.0, sigma_pos=0.5, sigma_nrm=0.2)
+    got = sty.pf_screen_filter_depth(rs, 0, prm, None)
+    sty.set_screen_kernel(sty.SCREEN_KERNEL_FP32)
+    ref = sty.pf_screen_filter_depth(rs, 0, prm, None)
+    torch.cuda.synchronize()
+    assert torch.equal(got, ref)
 
 
 def test_tc_pixel_term_off_and_tight_records(sty, orc, cuda, tensor_kernel):
