@@ -453,6 +453,16 @@ STY_API sty_status sty_nrc_train(sty_nrc *nrc, uint64_t count, uint64_t n_iters,
  * check the backward pass. */
 STY_API sty_status sty_nrc_gradient(sty_nrc *nrc, uint32_t batch, const float *input, const float *target,
                                     float *grad, float *loss_out, void *stream);
+/* Which tcgen05 kernel runs the BF16 training step of the 64-wide network (process-wide; every
+ * later sty_nrc_train / sty_nrc_gradient call). Both give the same weight gradients bit for bit.
+ * Returns STY_ERR_ARG for an unknown value.
+ *   STY_NRC_TRAIN_KERNEL_AUTO       two 128-sample tiles in flight per SM (two epilogue warpgroups
+ *                                   and an MMA-issuing warp) for networks of at most 5 hidden
+ *                                   layers, one tile at a time for 6
+ *   STY_NRC_TRAIN_KERNEL_ONE_TILE   one warpgroup per SM walking its tiles in sequence */
+#define STY_NRC_TRAIN_KERNEL_AUTO 0
+#define STY_NRC_TRAIN_KERNEL_ONE_TILE 1
+STY_API sty_status sty_nrc_set_train_kernel(int32_t kernel);
 
 /* ----------------------------------------------------------------------------------------
  * Scene, wavefront tracer and the end-to-end NL-PF render

@@ -135,6 +135,7 @@ SIGNATURES = {
     "sty_nrc_train_inference": (C.c_int32, [C.c_void_p, C.c_uint64, _VP, _VP, _VP]),
     "sty_nrc_train": (C.c_int32, [C.c_void_p, C.c_uint64, C.c_uint64, _VP, _VP, C.POINTER(C.c_float), _VP]),
     "sty_nrc_gradient": (C.c_int32, [C.c_void_p, C.c_uint32, _VP, _VP, _VP, C.POINTER(C.c_float), _VP]),
+    "sty_nrc_set_train_kernel": (C.c_int32, [C.c_int32]),
     "sty_pcg32_streams": (C.c_int32, [_VP, C.c_uint64, C.c_uint64, C.c_uint32, _VP, _VP, _VP]),
     "sty_std_rng_u64": (C.c_int32, [C.c_uint64, C.c_uint64, C.c_uint64, _VP, _VP]),
     "sty_pf_trace_records": (C.c_int32, [C.c_void_p, _VP, _VP, C.c_uint32, _VP, C.POINTER(C.c_uint64), _VP]),

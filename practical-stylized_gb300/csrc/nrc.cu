@@ -413,20 +413,31 @@ __global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const f
         for (int c = 0; c < 16; c++) g[c] = acc[c];
     }
 }
-__global__ void k_sum_chunks(size_t np, uint32_t chunks, const float *__restrict__ part, float *__restrict__ grad) {
-    const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= np) return;
+// grad[p] = part[0][p] + part[1][p] + ... in chunk order (one sequential FP32 sum per parameter).
+// A block owns kSumP parameters: all 256 threads stage a slab of kSumC chunk rows into shared
+// memory (16 independent coalesced loads per thread), then kSumP threads continue their sums over
+// the slab in order. The chunk loads of a slab are all in flight at once instead of 8 per thread.
+constexpr int kSumP = 64, kSumC = 64;
+__global__ void __launch_bounds__(256) k_sum_chunks(size_t np, uint32_t chunks, const float *__restrict__ part,
+                                                    float *__restrict__ grad) {
+    __shared__ float slab[kSumC][kSumP];
+    const int t = threadIdx.x, col = t % kSumP, r0 = t / kSumP;
+    const size_t p0 = (size_t)blockIdx.x * kSumP, p = p0 + (size_t)col;
     float s = 0.0f;
-    uint32_t c = 0;
-    for (; c + 8 <= chunks; c += 8) {  // eight loads in flight, added in chunk order
-        float v[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) v[j] = part[(c + j) * np + p];
-#pragma unroll
-        for (int j = 0; j < 8; j++) s += v[j];
+    for (uint32_t c0 = 0; c0 < chunks; c0 += kSumC) {
+        const uint32_t nc = min((uint32_t)kSumC, chunks - c0);
+        __syncthreads();
+#pragma unroll 4
+        for (uint32_t r = (uint32_t)r0; r < nc; r += 256 / kSumP)
+            slab[r][col] = p < np ? part[(size_t)(c0 + r) * np + p] : 0.0f;
+        __syncthreads();
+        if (t < kSumP)
+            for (uint32_t r = 0; r < nc; r++) s += slab[r][t];
     }
-    for (; c < chunks; c++) s += part[c * np + p];
-    grad[p] = s;
+    if (t < kSumP && p < np) grad[p] = s;
+}
+void sum_chunks(size_t np, uint32_t chunks, const float *part, float *grad, cudaStream_t st) {
+    k_sum_chunks<<<(unsigned)((np + kSumP - 1) / kSumP), 256, 0, st>>>(np, chunks, part, grad);
 }
 
 // ---- batch sampling (collect_batch, akari_tcnn.cu:15-38) -------------------------------------
@@ -581,7 +592,7 @@ sty_status backward(sty_nrc *nr, uint32_t B, const float *target, cudaStream_t s
     dim3 grid(chunks, n.layers + 1);
     k_wgrad_f32<<<grid, 256, 0, st>>>(n, B, nr->acts, nr->dpre, nr->np, nr->gpart);
     STY_TRY(check_launch("k_wgrad_f32"));
-    k_sum_chunks<<<(unsigned)((nr->np + 127) / 128), 128, 0, st>>>(nr->np, chunks, nr->gpart, nr->g);
+    sum_chunks(nr->np, chunks, nr->gpart, nr->g, st);
     return check_launch("k_sum_chunks");
 }
 
@@ -610,7 +621,7 @@ sty_status batch_gradient(sty_nrc *nr, uint32_t B, const float *in, const float 
     nr->img_dirty = true;  // nr->img now holds w, which the optimiser step is about to change
     const uint32_t ctas = nrc_tc_train_ctas(B);
     STY_TRY(nrc_tc_train(nr->net, nr->img, B, in, target, nr->gpart, nr->np, nr->loss, ctas, st));
-    k_sum_chunks<<<(unsigned)((nr->np + 127) / 128), 128, 0, st>>>(nr->np, ctas, nr->gpart, nr->g);
+    sum_chunks(nr->np, ctas, nr->gpart, nr->g, st);
     return check_launch("k_sum_chunks");
 }
 

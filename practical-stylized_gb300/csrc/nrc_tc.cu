@@ -11,6 +11,8 @@
 // (K-direction) byte offset is 128 and the stride (8-row) byte offset is 1024.
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "nrc.cuh"
 #include "tc.cuh"
@@ -491,6 +493,270 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
 }
 
+// Training with two tiles in flight per SM (networks of at most kWsMaxLayers hidden layers):
+// warps 0-3 and 4-7 are two epilogue warpgroups, each walking every other tile of the CTA with its
+// own activation images and 64-column TMEM accumulator; lane 0 of warp 8 issues every MMA. The
+// hand-offs are mbarriers only: the MMA thread commits step k of slot s to done[s], the slot's 128
+// epilogue threads arrive on ready[s] once step k's outputs are in shared memory. The MMA thread
+// alternates the slots step by step (tile 2p in slot 0, tile 2p + 1 in slot 1), so one tile's
+// epilogue overlaps the other's MMAs, and the weight-gradient MMAs reach each TMEM accumulator in
+// the CTA's tile order: the per-CTA sums are those of k_nrc_train_tc bit for bit.
+// Per slot, L images hold the L + 1 activations (act_L reuses act_0's image; act_0 is re-encoded
+// for dW_0), dP_l overwrites act_{l+1} in place, and the 128 x 16 loss gradient g has its own
+// compact image (2 core matrices per 8-row group: SBO 256 read K-major, LBO 256 read MN-major).
+// TMEM: columns 0-63 / 64-127 the slots' accumulators, 128 + 64 l the dW_l sums, 128 + 64 L dW_out^T.
+constexpr int kWsMaxLayers = 5;
+std::atomic<int32_t> g_train_kernel{STY_NRC_TRAIN_KERNEL_AUTO};
+int32_t train_kernel() { return g_train_kernel.load(std::memory_order_relaxed) == STY_NRC_TRAIN_KERNEL_ONE_TILE; }
+constexpr uint32_t kGBytes = TM * kNrcOutPad * 2;  // 4 KB
+__host__ __device__ inline int ws_images(int L) { return L < 2 ? 2 : L; }
+__host__ __device__ inline uint32_t ws_slot_bytes(int L) { return (uint32_t)ws_images(L) * kTileBytes + kGBytes; }
+__device__ __forceinline__ uint32_t g_off(uint32_t row, uint32_t kb) {  // 8 columns kb*8.. of row
+    return ((row >> 3) * 2u + kb) * 128u + (row & 7u) * 16u;
+}
+
+__global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ uint64_t done[2], ready[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ float red[8];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int L = a.n.layers, O = a.n.out_dims, nimg = ws_images(L);
+    const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
+    uint8_t *wimg = smem;
+    uint8_t *slots = smem + ((wbytes + 1023u) & ~1023u);
+    for (uint32_t o = tid * 16u; o < wbytes; o += 288u * 16u)
+        *reinterpret_cast<uint4 *>(wimg + o) =
+            *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
+    if (tid == 0) {
+        for (int s = 0; s < 2; s++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&ready[s])) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t wbase = smem_u32(wimg), sbase = smem_u32(slots);
+    const uint32_t wout = wbase + (uint32_t)L * W * W * 2u;
+    const uint32_t c_dw = 128u, c_out = 128u + 64u * (uint32_t)L;
+    const uint32_t ntiles = (a.B + TM - 1) / TM;
+    const uint32_t nt = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0u;
+    const int nsteps = 2 * L + 2;
+    bool failed = false;
+    float lsum = 0.0f;
+
+    if (warp == 8) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            uint32_t rph[2] = {0u, 0u}, ncommit[2] = {0u, 0u};
+            for (uint32_t i = 0; i < nt && !failed; i += 2) {
+                const int nslot = i + 1 < nt ? 2 : 1;
+                for (int k = 0; k < nsteps && !failed; k++) {
+                    for (int s = 0; s < nslot; s++) {
+                        if (!mbar_wait(&ready[s], rph[s], a.status)) {
+                            failed = true;
+                            break;
+                        }
+                        rph[s] ^= 1u;
+                        fence_after();
+                        const bool first = i + (uint32_t)s == 0;  // the CTA's first tile starts the dW sums
+                        const uint32_t acc = tmem + 64u * (uint32_t)s;
+                        const uint32_t ab = sbase + (uint32_t)s * ws_slot_bytes(L);
+                        const uint32_t gb = ab + (uint32_t)nimg * kTileBytes;
+                        auto img = [&](int j) { return ab + (uint32_t)(j % nimg) * kTileBytes; };
+                        if (k <= L) {  // forward layer k
+                            const bool out_layer = k == L;
+                            const uint32_t al = img(k), wl = wbase + (uint32_t)k * W * W * 2u;
+                            const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
+#pragma unroll
+                            for (int kk = 0; kk < 4; kk++)
+                                mma_bf16(acc, make_desc(al + kk * 256u), make_desc(wl + kk * 256u), idesc,
+                                         kk > 0 ? 1u : 0u);
+                        } else if (k == L + 1) {  // dW_out^T += act_L^T g ; dH_{L-1} = g W_out
+                            const uint32_t aL = img(L);
+#pragma unroll 1
+                            for (int kk = 0; kk < TM / 16; kk++)
+                                mma_bf16(tmem + c_out, make_desc_mn(aL + kk * 2048u), make_desc(gb + kk * 512u, 256, 128),
+                                         idesc_bf16(64, kNrcOutPad, 1, 1), (first && kk == 0) ? 0u : 1u);
+                            mma_bf16(acc, make_desc(gb, 128, 256), make_desc_mn(wout), idesc_bf16(TM, W, 0, 1), 0u);
+                        } else {  // hidden layer l: dW_l += dP_l^T act_l ; dH_{l-1} = dP_l W_l
+                            const int l = 2 * L + 1 - k;
+                            const uint32_t dp = img(l + 1), al = img(l);
+#pragma unroll 1
+                            for (int kk = 0; kk < TM / 16; kk++)
+                                mma_bf16(tmem + c_dw + 64u * (uint32_t)l, make_desc_mn(dp + kk * 2048u),
+                                         make_desc_mn(al + kk * 2048u), idesc_bf16(64, W, 1, 1),
+                                         (first && kk == 0) ? 0u : 1u);
+                            if (l > 0) {
+                                const uint32_t wl = wbase + (uint32_t)l * W * W * 2u;
+#pragma unroll
+                                for (int kk = 0; kk < 4; kk++)
+                                    mma_bf16(acc, make_desc(dp + kk * 256u), make_desc_mn(wl + kk * 2048u),
+                                             idesc_bf16(TM, W, 0, 1), kk > 0 ? 1u : 0u);
+                            }
+                        }
+                        mma_commit(&done[s]);
+                        ncommit[s]++;
+                    }
+                }
+            }
+            if (failed)  // drain: every committed MMA completes before TMEM is released
+                for (int s = 0; s < 2; s++)
+                    if (ncommit[s]) mbar_wait(&done[s], (ncommit[s] - 1u) & 1u, a.status);
+        }
+        __syncwarp();
+    } else {
+        // ---- epilogue warpgroup s: one sample row per thread
+        const int s = warp >> 2, r = tid & 127;
+        const uint32_t lane_base = tmem + (((uint32_t)(warp & 3) * 32u) << 16) + 64u * (uint32_t)s;
+        uint8_t *ab = slots + (size_t)s * ws_slot_bytes(L);
+        uint8_t *gimg = ab + (size_t)nimg * kTileBytes;
+        auto img = [&](int j) { return ab + (size_t)(j % nimg) * kTileBytes; };
+        const float norm = 1.0f / ((float)a.B * (float)O);
+        uint32_t dph = 0;
+        auto publish = [&]() {
+            fence_async_smem();
+            fence_before();
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ready[s])) : "memory");
+        };
+        for (uint32_t i = (uint32_t)s; i < nt && !failed; i += 2) {
+            const uint32_t row = (blockIdx.x + i * gridDim.x) * TM + (uint32_t)r;
+            const bool valid = row < a.B;
+            const float *xin = valid ? a.input + (size_t)row * a.n.in_dims : nullptr;
+            encode_any(a.n, a.plan, a.c4 != 0, xin, img(0), (uint32_t)r);
+            publish();
+            for (int k = 0; k < nsteps; k++) {
+                const bool got = __all_sync(0xffffffffu, mbar_wait(&done[s], dph, a.status));
+                dph ^= 1u;
+                if (!got) {
+                    failed = true;
+                    break;
+                }
+                fence_after();
+                if (k == nsteps - 1) break;  // dW_0 done: the slot's images are free
+                if (k < L) {  // act_{k+1} = relu(acc)
+                    uint8_t *nxt = img(k + 1);
+                    float v[32];
+#pragma unroll
+                    for (int half = 0; half < 2; half++) {
+                        tmem_ld32(lane_base + half * 32u, v);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int kb = 0; kb < 4; kb++) {
+                            const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
+                                                       pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
+                                                       pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
+                                                       pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
+                            *reinterpret_cast<uint4 *>(nxt + img_off((uint32_t)r, half * 32 + kb * 8)) = q;
+                        }
+                    }
+                } else if (k == L) {  // relative-L2 loss gradient -> g (rows past the batch give zero)
+                    float v[16], gr[16];
+                    tmem_ld16(lane_base, v);
+                    tmem_wait_ld();
+#pragma unroll
+                    for (int c = 0; c < 16; c++) {
+                        gr[c] = 0.0f;
+                        if (valid && c < O) {
+                            const float p = v[c], t = a.target[(size_t)row * O + c];
+                            const float den = p * p + 0.01f;
+                            lsum += (p - t) * (p - t) / den;
+                            gr[c] = 2.0f * (p - t) / den * norm;
+                        }
+                    }
+#pragma unroll
+                    for (int kb = 0; kb < 2; kb++)
+                        *reinterpret_cast<uint4 *>(gimg + g_off((uint32_t)r, (uint32_t)kb)) =
+                            make_uint4(pack2_bf16(gr[kb * 8 + 0], gr[kb * 8 + 1]), pack2_bf16(gr[kb * 8 + 2], gr[kb * 8 + 3]),
+                                       pack2_bf16(gr[kb * 8 + 4], gr[kb * 8 + 5]), pack2_bf16(gr[kb * 8 + 6], gr[kb * 8 + 7]));
+                } else {  // dP_{l} = dH_{l} * [act_{l+1} > 0] in place of act_{l+1}, l = 2L - k
+                    const int l = 2 * L - k;
+                    uint8_t *hl = img(l + 1);
+                    float v[32];
+#pragma unroll
+                    for (int half = 0; half < 2; half++) {
+                        tmem_ld32(lane_base + half * 32u, v);
+                        tmem_wait_ld();
+#pragma unroll
+                        for (int kb = 0; kb < 4; kb++) {
+                            const uint32_t off = img_off((uint32_t)r, half * 32 + kb * 8);
+                            const uint4 h = *reinterpret_cast<const uint4 *>(hl + off);
+                            const uint32_t hw[4] = {h.x, h.y, h.z, h.w};
+                            uint32_t o[4];
+#pragma unroll
+                            for (int e = 0; e < 4; e++) {
+                                const float d0 = bf16_lo(hw[e]) > 0.0f ? v[kb * 8 + 2 * e] : 0.0f;
+                                const float d1 = bf16_hi(hw[e]) > 0.0f ? v[kb * 8 + 2 * e + 1] : 0.0f;
+                                o[e] = pack2_bf16(d0, d1);
+                            }
+                            *reinterpret_cast<uint4 *>(hl + off) = make_uint4(o[0], o[1], o[2], o[3]);
+                        }
+                    }
+                    // act_L took act_0's image: encode act_0 again for dW_0 (its image's last
+                    // reader, the step of dW_{L-1}, has completed)
+                    if (l == 0 && L % nimg == 0) encode_any(a.n, a.plan, a.c4 != 0, xin, img(0), (uint32_t)r);
+                }
+                publish();
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xffffffffu, lsum, o);
+    if (lane == 0 && warp < 8) red[warp] = lsum;
+    fence_before();
+    const bool ok = __syncthreads_and(!failed);
+    fence_after();
+    if (ok && warp < 8) {
+        float *dst = a.part + (size_t)blockIdx.x * a.np;
+        if (nt == 0) {
+            for (size_t p = tid; p < a.np; p += 256) dst[p] = 0.0f;
+        } else {
+            // M=64 accumulator row j lives in lane (j / 16) * 32 + j % 16: row j = 16 * (warp % 4) + lane
+            const uint32_t qbase = tmem + (((uint32_t)(warp & 3) * 32u) << 16);
+            const int j = 16 * (warp & 3) + lane;
+            for (int l = warp >> 2; l < L; l += 2) {
+                float v[32];
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    tmem_ld32(qbase + c_dw + 64u * (uint32_t)l + half * 32u, v);
+                    tmem_wait_ld();
+                    if (lane < 16) {
+                        float *d = dst + nrc_w_offset(l) + (size_t)j * W + half * 32;
+#pragma unroll
+                        for (int k = 0; k < 32; k += 4)
+                            *reinterpret_cast<float4 *>(d + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+                    }
+                }
+            }
+            if (warp < 4) {
+                float v[16];
+                tmem_ld16(qbase + c_out, v);  // row = input column k, column = output c
+                tmem_wait_ld();
+                if (lane < 16)
+                    for (int c = 0; c < O; c++) dst[nrc_w_offset(L) + (size_t)c * W + j] = v[c];
+            }
+        }
+    }
+    if (tid == 0 && a.loss && ok) {
+        float t = 0.0f;
+        for (int w = 0; w < 8; w++) t += red[w];
+        atomicAdd(a.loss, t * (1.0f / ((float)a.B * (float)O)));
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+}
+
 // FP32 [out][in] -> BF16 K-major images; output layer padded to 16 rows of zeros
 __global__ void k_pack(NrcNet n, const float *w, uint16_t *img) {
     const int L = n.layers;
@@ -591,6 +857,14 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
         set_error("device status word unavailable");
         return STY_ERR_CUDA;
     }
+    if (n.layers <= kWsMaxLayers && train_kernel() == 0) {
+        const size_t wbytes = nrc_tc_image_elems(n) * 2;
+        const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + 2 * (size_t)ws_slot_bytes(n.layers) + 1024;
+        STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_train_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                           "attr k_nrc_train_ws"));
+        k_nrc_train_ws<<<ctas, 288, smem, st>>>(a);
+        return check_launch("k_nrc_train_ws");
+    }
     const size_t smem = nrc_tc_train_smem(n);
     STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "attr k_nrc_train_tc"));
@@ -599,3 +873,13 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
 }
 
 }  // namespace sty
+
+using namespace sty;
+
+sty_status sty_nrc_set_train_kernel(int32_t kernel) {
+    clear_error();
+    STY_ARG_CHECK(kernel == STY_NRC_TRAIN_KERNEL_AUTO || kernel == STY_NRC_TRAIN_KERNEL_ONE_TILE,
+                  "sty_nrc_set_train_kernel: unknown kernel %d", kernel);
+    g_train_kernel.store(kernel, std::memory_order_relaxed);
+    return STY_OK;
+}

@@ -73,6 +73,16 @@ def grid_config(max_depth=12, output_dims=3, batch_size=1 << 16, hidden_layers=5
     return c
 
 
+TRAIN_KERNEL_AUTO, TRAIN_KERNEL_ONE_TILE = 0, 1
+
+
+def set_train_kernel(kernel: int) -> None:
+    """Process-wide choice of the BF16 training kernel (sty_nrc_set_train_kernel): AUTO (two tiles
+    in flight per SM where the network has at most 5 hidden layers) or ONE_TILE. Both give the same
+    gradients bit for bit."""
+    check(lib().sty_nrc_set_train_kernel(int(kernel)))
+
+
 def _sp(stream):
     from .pf import _stream_ptr
     return _stream_ptr(stream)

@@ -107,6 +107,18 @@ def test_screen_kernel_choice_without_gpu(sty):
     lib.sty_pf_screen_set_kernel(sty.SCREEN_KERNEL_AUTO)
 
 
+def test_train_kernel_choice_without_gpu(sty):
+    """sty_nrc_set_train_kernel takes AUTO and ONE_TILE and rejects anything else (no GPU)."""
+    lib = sty.abi.lib()
+    for k in (sty.nrc.TRAIN_KERNEL_ONE_TILE, sty.nrc.TRAIN_KERNEL_AUTO):
+        assert lib.sty_nrc_set_train_kernel(k) == sty.abi.STY_OK
+    assert lib.sty_nrc_set_train_kernel(2) == sty.abi.STY_ERR_ARG
+    assert b"unknown kernel" in lib.sty_last_error()
+    with pytest.raises(sty.StyError):
+        sty.nrc.set_train_kernel(-1)
+    lib.sty_nrc_set_train_kernel(sty.nrc.TRAIN_KERNEL_AUTO)
+
+
 def test_style_builders_validate(sty):
     a = sty.abi
     with pytest.raises(ValueError):

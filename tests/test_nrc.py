@@ -172,6 +172,38 @@ def test_bf16_tensor_core_gradient(sty, cuda, layers, batch):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("layers,batch,freqs", [
+    (5, 128 * 152 * 2 + 77, FREQS),  # 2-3 tiles per CTA: pairs and a lone last tile
+    (5, 128 * 152 * 4, FREQS),       # 4 tiles per CTA: two full pairs
+    (5, 300, FREQS),                 # 3 CTAs of one tile each: the second slot idles
+    (2, 128 * 400 + 1, FREQS),       # act_2 takes act_0's image, act_0 encoded again for dW_0
+    (1, 128 * 310, FREQS),           # two images for two activations, no re-encoding
+    (3, 128 * 500 + 9, (5, 1, 3, 0, 6, 2)),  # table-driven encoder (re-encoded for dW_0)
+])
+def test_bf16_training_kernels_agree(sty, cuda, layers, batch, freqs):
+    """The two-tiles-in-flight training kernel against the one-tile kernel: the same weight
+    gradient bit for bit (the weight-gradient MMAs reach TMEM in the same tile order), the same
+    loss up to the order of its float sums."""
+    net = sty.nrc.NRC(sty.nrc.config(freqs, 3, 1024, layers, sty.nrc.STY_NRC_BF16, seed=21))
+    rng = np.random.default_rng(22)
+    x = rng.random((batch, len(freqs)))
+    t = rng.random((batch, 3)) + 0.1
+    xd, td = _dev(x), _dev(t)
+    try:
+        sty.nrc.set_train_kernel(sty.nrc.TRAIN_KERNEL_ONE_TILE)
+        g1, l1 = net.gradient(xd, td)
+        sty.nrc.set_train_kernel(sty.nrc.TRAIN_KERNEL_AUTO)
+        g2, l2 = net.gradient(xd, td)
+    finally:
+        sty.nrc.set_train_kernel(sty.nrc.TRAIN_KERNEL_AUTO)
+    g1, g2 = g1.cpu().numpy(), g2.cpu().numpy()
+    assert np.isfinite(g1).all() and np.abs(g1).max() > 0
+    assert (g1 == g2).all(), int((g1 != g2).sum())
+    assert abs(l1 - l2) <= 1e-5 * abs(l1)
+    assert sty.abi.device_status() == 0
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", [0, 1])
 def test_training_reduces_loss(sty, cuda, precision):
     net = _make(sty, precision, batch=4096, seed=11)
