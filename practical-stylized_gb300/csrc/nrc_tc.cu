@@ -92,11 +92,8 @@ bool is_c4(const NrcNet &n) {
         if ((int)n.freqs[d] != f[d]) return false;
     return true;
 }
-__device__ __forceinline__ void encode_row_c4(const float *x, uint8_t *img, uint32_t row) {
-    float xin[kC4Dims];
-#pragma unroll
-    for (int d = 0; d < kC4Dims; d++) xin[d] = x ? x[d] : 0.0f;
-    uint32_t q[kNrcWidth / 2];
+// the packed BF16 encoding of an input row held in registers (has = false: a padding row of zeros)
+__device__ __forceinline__ void encode_c4_pack(const float (&xin)[kC4Dims], bool has, uint32_t (&q)[kNrcWidth / 2]) {
     int o = 0;
 #pragma unroll
     for (int d = 0; d < kC4Dims; d++) {
@@ -104,16 +101,26 @@ __device__ __forceinline__ void encode_row_c4(const float *x, uint8_t *img, uint
         sincospif(xin[d], &s, &c);
 #pragma unroll
         for (int k = 0; k < kC4Freqs[d]; k++) {
-            q[o++] = x ? pack2_bf16(s, c) : 0u;
+            q[o++] = has ? pack2_bf16(s, c) : 0u;
             const float s2 = 2.0f * s * c;
             c = fmaf(-2.0f * s, s, 1.0f);
             s = s2;
         }
     }
+}
+__device__ __forceinline__ void store_row(const uint32_t (&q)[kNrcWidth / 2], uint8_t *img, uint32_t row) {
 #pragma unroll
     for (int kb = 0; kb < 8; kb++)
         *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) =
             make_uint4(q[kb * 4], q[kb * 4 + 1], q[kb * 4 + 2], q[kb * 4 + 3]);
+}
+__device__ __forceinline__ void encode_row_c4(const float *x, uint8_t *img, uint32_t row) {
+    float xin[kC4Dims];
+#pragma unroll
+    for (int d = 0; d < kC4Dims; d++) xin[d] = x ? x[d] : 0.0f;
+    uint32_t q[kNrcWidth / 2];
+    encode_c4_pack(xin, x != nullptr, q);
+    store_row(q, img, row);
 }
 __device__ __forceinline__ void encode_any(const NrcNet &n, const EncPlan &e, bool c4, const float *x, uint8_t *img,
                                            uint32_t row) {
@@ -495,12 +502,19 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
 
 // Training with two tiles in flight per SM (networks of at most kWsMaxLayers hidden layers):
 // warps 0-3 and 4-7 are two epilogue warpgroups, each walking every other tile of the CTA with its
-// own activation images and 64-column TMEM accumulator; lane 0 of warp 8 issues every MMA. The
-// hand-offs are mbarriers only: the MMA thread commits step k of slot s to done[s], the slot's 128
-// epilogue threads arrive on ready[s] once step k's outputs are in shared memory. The MMA thread
-// alternates the slots step by step (tile 2p in slot 0, tile 2p + 1 in slot 1), so one tile's
-// epilogue overlaps the other's MMAs, and the weight-gradient MMAs reach each TMEM accumulator in
-// the CTA's tile order: the per-CTA sums are those of k_nrc_train_tc bit for bit.
+// own activation images and 64-column TMEM accumulator (tile 2p in slot 0, tile 2p + 1 in slot 1).
+// Three threads issue the MMAs: lane 0 of warp 8 + s the forward and dH products of slot s, lane 0
+// of warp 10 every weight-gradient product. The hand-offs are mbarriers only: the issuers wait on
+// ready[s] (the slot's 128 epilogue threads arrive once step k's operands are in shared memory) and
+// arrive on done[s] (count 2: slot s's forward issuer and the weight-gradient issuer, each with a
+// commit after its MMAs of step k or a plain arrive when it has none). One slot's epilogue overlaps
+// the other's MMAs. The weight-gradient issuer alternates the slots step by step, so its MMAs reach
+// each TMEM accumulator in the CTA's tile order: the per-CTA sums are those of k_nrc_train_tc bit
+// for bit. (A thread issues an MMA every ~100 cycles here, so one issuer for a tile pair's 178 MMAs
+// was the critical path.) The epilogue loads its next tile's input row and targets with
+// non-reorderable loads a tile ahead, and for the workload's encoder keeps the tile's packed
+// encoding in registers (act_0 is stored from them twice; the next tile's encoding is computed
+// while the dW_0 products run), so neither a global load nor the sines sit on the step chain.
 // Per slot, L images hold the L + 1 activations (act_L reuses act_0's image; act_0 is re-encoded
 // for dW_0), dP_l overwrites act_{l+1} in place, and the 128 x 16 loss gradient g has its own
 // compact image (2 core matrices per 8-row group: SBO 256 read K-major, LBO 256 read MN-major).
@@ -509,13 +523,24 @@ constexpr int kWsMaxLayers = 5;
 std::atomic<int32_t> g_train_kernel{STY_NRC_TRAIN_KERNEL_AUTO};
 int32_t train_kernel() { return g_train_kernel.load(std::memory_order_relaxed) == STY_NRC_TRAIN_KERNEL_ONE_TILE; }
 constexpr uint32_t kGBytes = TM * kNrcOutPad * 2;  // 4 KB
+constexpr int kWsThreads = 352;
 __host__ __device__ inline int ws_images(int L) { return L < 2 ? 2 : L; }
 __host__ __device__ inline uint32_t ws_slot_bytes(int L) { return (uint32_t)ws_images(L) * kTileBytes + kGBytes; }
 __device__ __forceinline__ uint32_t g_off(uint32_t row, uint32_t kb) {  // 8 columns kb*8.. of row
     return ((row >> 3) * 2u + kb) * 128u + (row & 7u) * 16u;
 }
+// a global load issued where it is written (an asm volatile is not moved past the other volatile
+// asm of the step loop), so its latency overlaps the steps before the value's first use
+__device__ __forceinline__ float ld_early(const float *p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
-__global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
+__global__ void __launch_bounds__(kWsThreads, 1) k_nrc_train_ws(const TrainArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t done[2], ready[2];
     __shared__ uint32_t tmem_slot;
@@ -525,12 +550,12 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
     const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
     uint8_t *wimg = smem;
     uint8_t *slots = smem + ((wbytes + 1023u) & ~1023u);
-    for (uint32_t o = tid * 16u; o < wbytes; o += 288u * 16u)
+    for (uint32_t o = tid * 16u; o < wbytes; o += kWsThreads * 16u)
         *reinterpret_cast<uint4 *>(wimg + o) =
             *reinterpret_cast<const uint4 *>(reinterpret_cast<const uint8_t *>(a.wimg) + o);
     if (tid == 0) {
         for (int s = 0; s < 2; s++) {
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&done[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(smem_u32(&done[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_u32(&ready[s])) : "memory");
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -554,69 +579,84 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
     bool failed = false;
     float lsum = 0.0f;
 
-    if (warp == 8) {
-        // ---- MMA issuer
+    if (warp >= 8) {
+        // ---- MMA issuers: warp 8 + s forward + dH of slot s, warp 10 the weight gradients
         if (lane == 0) {
-            uint32_t rph[2] = {0u, 0u}, ncommit[2] = {0u, 0u};
+            const bool wgrad = warp == 10;
+            const int own = warp - 8;  // the forward issuer's slot
+            uint32_t rph[2] = {0u, 0u}, narr[2] = {0u, 0u};
             for (uint32_t i = 0; i < nt && !failed; i += 2) {
                 const int nslot = i + 1 < nt ? 2 : 1;
                 for (int k = 0; k < nsteps && !failed; k++) {
                     for (int s = 0; s < nslot; s++) {
+                        if (!wgrad && s != own) continue;
                         if (!mbar_wait(&ready[s], rph[s], a.status)) {
                             failed = true;
                             break;
                         }
                         rph[s] ^= 1u;
                         fence_after();
-                        const bool first = i + (uint32_t)s == 0;  // the CTA's first tile starts the dW sums
                         const uint32_t acc = tmem + 64u * (uint32_t)s;
                         const uint32_t ab = sbase + (uint32_t)s * ws_slot_bytes(L);
                         const uint32_t gb = ab + (uint32_t)nimg * kTileBytes;
                         auto img = [&](int j) { return ab + (uint32_t)(j % nimg) * kTileBytes; };
-                        if (k <= L) {  // forward layer k
-                            const bool out_layer = k == L;
-                            const uint32_t al = img(k), wl = wbase + (uint32_t)k * W * W * 2u;
-                            const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
+                        bool issued = false;
+                        if (!wgrad) {
+                            if (k <= L) {  // forward layer k
+                                const uint32_t al = img(k), wl = wbase + (uint32_t)k * W * W * 2u;
+                                const uint32_t idesc = k == L ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
 #pragma unroll
-                            for (int kk = 0; kk < 4; kk++)
-                                mma_bf16(acc, make_desc(al + kk * 256u), make_desc(wl + kk * 256u), idesc,
-                                         kk > 0 ? 1u : 0u);
-                        } else if (k == L + 1) {  // dW_out^T += act_L^T g ; dH_{L-1} = g W_out
-                            const uint32_t aL = img(L);
-#pragma unroll 1
-                            for (int kk = 0; kk < TM / 16; kk++)
-                                mma_bf16(tmem + c_out, make_desc_mn(aL + kk * 2048u), make_desc(gb + kk * 512u, 256, 128),
-                                         idesc_bf16(64, kNrcOutPad, 1, 1), (first && kk == 0) ? 0u : 1u);
-                            mma_bf16(acc, make_desc(gb, 128, 256), make_desc_mn(wout), idesc_bf16(TM, W, 0, 1), 0u);
-                        } else {  // hidden layer l: dW_l += dP_l^T act_l ; dH_{l-1} = dP_l W_l
-                            const int l = 2 * L + 1 - k;
-                            const uint32_t dp = img(l + 1), al = img(l);
-#pragma unroll 1
-                            for (int kk = 0; kk < TM / 16; kk++)
-                                mma_bf16(tmem + c_dw + 64u * (uint32_t)l, make_desc_mn(dp + kk * 2048u),
-                                         make_desc_mn(al + kk * 2048u), idesc_bf16(64, W, 1, 1),
-                                         (first && kk == 0) ? 0u : 1u);
-                            if (l > 0) {
-                                const uint32_t wl = wbase + (uint32_t)l * W * W * 2u;
+                                for (int kk = 0; kk < 4; kk++)
+                                    mma_bf16(acc, make_desc(al + kk * 256u), make_desc(wl + kk * 256u), idesc,
+                                             kk > 0 ? 1u : 0u);
+                                issued = true;
+                            } else if (k == L + 1) {  // dH_{L-1} = g W_out
+                                mma_bf16(acc, make_desc(gb, 128, 256), make_desc_mn(wout), idesc_bf16(TM, W, 0, 1), 0u);
+                                issued = true;
+                            } else if (2 * L + 1 - k > 0) {  // dH_{l-1} = dP_l W_l
+                                const int l = 2 * L + 1 - k;
+                                const uint32_t dp = img(l + 1), wl = wbase + (uint32_t)l * W * W * 2u;
 #pragma unroll
                                 for (int kk = 0; kk < 4; kk++)
                                     mma_bf16(acc, make_desc(dp + kk * 256u), make_desc_mn(wl + kk * 2048u),
                                              idesc_bf16(TM, W, 0, 1), kk > 0 ? 1u : 0u);
+                                issued = true;
                             }
+                        } else if (k > L) {
+                            const bool first = i + (uint32_t)s == 0;  // the CTA's first tile starts the sums
+                            if (k == L + 1) {  // dW_out^T += act_L^T g
+                                const uint32_t aL = img(L);
+#pragma unroll 1
+                                for (int kk = 0; kk < TM / 16; kk++)
+                                    mma_bf16(tmem + c_out, make_desc_mn(aL + kk * 2048u),
+                                             make_desc(gb + kk * 512u, 256, 128), idesc_bf16(64, kNrcOutPad, 1, 1),
+                                             (first && kk == 0) ? 0u : 1u);
+                            } else {  // dW_l += dP_l^T act_l
+                                const int l = 2 * L + 1 - k;
+                                const uint32_t dp = img(l + 1), al = img(l);
+#pragma unroll 1
+                                for (int kk = 0; kk < TM / 16; kk++)
+                                    mma_bf16(tmem + c_dw + 64u * (uint32_t)l, make_desc_mn(dp + kk * 2048u),
+                                             make_desc_mn(al + kk * 2048u), idesc_bf16(64, W, 1, 1),
+                                             (first && kk == 0) ? 0u : 1u);
+                            }
+                            issued = true;
                         }
-                        mma_commit(&done[s]);
-                        ncommit[s]++;
+                        if (issued) mma_commit(&done[s]);
+                        else mbar_arrive(&done[s]);
+                        narr[s]++;
                     }
                 }
             }
-            if (failed)  // drain: every committed MMA completes before TMEM is released
+            if (failed)  // drain: this thread's MMAs complete before TMEM is released
                 for (int s = 0; s < 2; s++)
-                    if (ncommit[s]) mbar_wait(&done[s], (ncommit[s] - 1u) & 1u, a.status);
+                    if (narr[s]) mbar_wait(&done[s], (narr[s] - 1u) & 1u, a.status);
         }
         __syncwarp();
     } else {
         // ---- epilogue warpgroup s: one sample row per thread
         const int s = warp >> 2, r = tid & 127;
+        const bool c4 = a.c4 != 0;
         const uint32_t lane_base = tmem + (((uint32_t)(warp & 3) * 32u) << 16) + 64u * (uint32_t)s;
         uint8_t *ab = slots + (size_t)s * ws_slot_bytes(L);
         uint8_t *gimg = ab + (size_t)nimg * kTileBytes;
@@ -626,13 +666,38 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
         auto publish = [&]() {
             fence_async_smem();
             fence_before();
-            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&ready[s])) : "memory");
+            mbar_arrive(&ready[s]);
         };
+        auto row_of = [&](uint32_t i) { return (blockIdx.x + i * gridDim.x) * TM + (uint32_t)r; };
+        // input rows (workload encoder) and targets, loaded a tile ahead; q = the tile's packed encoding
+        float xr[kC4Dims], tr[kNrcOutPad];
+        uint32_t q[kNrcWidth / 2];
+        auto valid_row = [&](uint32_t i) { return i < nt && row_of(i) < a.B; };
+        auto load_x = [&](uint32_t i) {
+            const bool v = c4 && valid_row(i);
+            const float *p = a.input + (size_t)row_of(i) * kC4Dims;
+#pragma unroll
+            for (int d = 0; d < kC4Dims; d++) xr[d] = v ? ld_early(p + d) : 0.0f;
+        };
+        auto load_t = [&](uint32_t i) {
+            const bool v = valid_row(i);
+            const float *p = a.target + (size_t)row_of(i) * O;
+#pragma unroll
+            for (int c = 0; c < kNrcOutPad; c++) tr[c] = (v && c < O) ? ld_early(p + c) : 0.0f;
+        };
+        auto encode0 = [&](bool valid, const float *xin) {
+            if (c4) store_row(q, img(0), (uint32_t)r);
+            else encode_row(a.plan, xin, img(0), (uint32_t)r);
+        };
+        load_x((uint32_t)s);
+        load_t((uint32_t)s);
+        if (c4) encode_c4_pack(xr, valid_row((uint32_t)s), q);
+        load_x((uint32_t)s + 2u);
         for (uint32_t i = (uint32_t)s; i < nt && !failed; i += 2) {
-            const uint32_t row = (blockIdx.x + i * gridDim.x) * TM + (uint32_t)r;
+            const uint32_t row = row_of(i);
             const bool valid = row < a.B;
             const float *xin = valid ? a.input + (size_t)row * a.n.in_dims : nullptr;
-            encode_any(a.n, a.plan, a.c4 != 0, xin, img(0), (uint32_t)r);
+            encode0(valid, xin);
             publish();
             for (int k = 0; k < nsteps; k++) {
                 const bool got = __all_sync(0xffffffffu, mbar_wait(&done[s], dph, a.status));
@@ -645,20 +710,19 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
                 if (k == nsteps - 1) break;  // dW_0 done: the slot's images are free
                 if (k < L) {  // act_{k+1} = relu(acc)
                     uint8_t *nxt = img(k + 1);
-                    float v[32];
+                    float v[2][32];
+                    tmem_ld32(lane_base, v[0]);
+                    tmem_ld32(lane_base + 32u, v[1]);
+                    tmem_wait_ld();
 #pragma unroll
-                    for (int half = 0; half < 2; half++) {
-                        tmem_ld32(lane_base + half * 32u, v);
-                        tmem_wait_ld();
+                    for (int half = 0; half < 2; half++)
 #pragma unroll
                         for (int kb = 0; kb < 4; kb++) {
-                            const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
-                                                       pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
-                                                       pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
-                                                       pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
+                            const float *u = v[half] + kb * 8;
+                            const uint4 q = make_uint4(pack2_relu_bf16(u[0], u[1]), pack2_relu_bf16(u[2], u[3]),
+                                                       pack2_relu_bf16(u[4], u[5]), pack2_relu_bf16(u[6], u[7]));
                             *reinterpret_cast<uint4 *>(nxt + img_off((uint32_t)r, half * 32 + kb * 8)) = q;
                         }
-                    }
                 } else if (k == L) {  // relative-L2 loss gradient -> g (rows past the batch give zero)
                     float v[16], gr[16];
                     tmem_ld16(lane_base, v);
@@ -667,7 +731,7 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
                     for (int c = 0; c < 16; c++) {
                         gr[c] = 0.0f;
                         if (valid && c < O) {
-                            const float p = v[c], t = a.target[(size_t)row * O + c];
+                            const float p = v[c], t = tr[c];
                             const float den = p * p + 0.01f;
                             lsum += (p - t) * (p - t) / den;
                             gr[c] = 2.0f * (p - t) / den * norm;
@@ -678,14 +742,16 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
                         *reinterpret_cast<uint4 *>(gimg + g_off((uint32_t)r, (uint32_t)kb)) =
                             make_uint4(pack2_bf16(gr[kb * 8 + 0], gr[kb * 8 + 1]), pack2_bf16(gr[kb * 8 + 2], gr[kb * 8 + 3]),
                                        pack2_bf16(gr[kb * 8 + 4], gr[kb * 8 + 5]), pack2_bf16(gr[kb * 8 + 6], gr[kb * 8 + 7]));
-                } else {  // dP_{l} = dH_{l} * [act_{l+1} > 0] in place of act_{l+1}, l = 2L - k
+                    load_t(i + 2);
+                } else {  // dP_l = dH_l * [act_{l+1} > 0] in place of act_{l+1}, l = 2L - k
                     const int l = 2 * L - k;
                     uint8_t *hl = img(l + 1);
-                    float v[32];
+                    float v[2][32];
+                    tmem_ld32(lane_base, v[0]);
+                    tmem_ld32(lane_base + 32u, v[1]);
+                    tmem_wait_ld();
 #pragma unroll
-                    for (int half = 0; half < 2; half++) {
-                        tmem_ld32(lane_base + half * 32u, v);
-                        tmem_wait_ld();
+                    for (int half = 0; half < 2; half++)
 #pragma unroll
                         for (int kb = 0; kb < 4; kb++) {
                             const uint32_t off = img_off((uint32_t)r, half * 32 + kb * 8);
@@ -694,18 +760,21 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
                             uint32_t o[4];
 #pragma unroll
                             for (int e = 0; e < 4; e++) {
-                                const float d0 = bf16_lo(hw[e]) > 0.0f ? v[kb * 8 + 2 * e] : 0.0f;
-                                const float d1 = bf16_hi(hw[e]) > 0.0f ? v[kb * 8 + 2 * e + 1] : 0.0f;
+                                const float d0 = bf16_lo(hw[e]) > 0.0f ? v[half][kb * 8 + 2 * e] : 0.0f;
+                                const float d1 = bf16_hi(hw[e]) > 0.0f ? v[half][kb * 8 + 2 * e + 1] : 0.0f;
                                 o[e] = pack2_bf16(d0, d1);
                             }
                             *reinterpret_cast<uint4 *>(hl + off) = make_uint4(o[0], o[1], o[2], o[3]);
                         }
-                    }
-                    // act_L took act_0's image: encode act_0 again for dW_0 (its image's last
-                    // reader, the step of dW_{L-1}, has completed)
-                    if (l == 0 && L % nimg == 0) encode_any(a.n, a.plan, a.c4 != 0, xin, img(0), (uint32_t)r);
+                    // act_L took act_0's image: store act_0 again for dW_0 (its image's last reader,
+                    // the step of dW_{L-1}, has completed)
+                    if (l == 0 && L % nimg == 0) encode0(valid, xin);
                 }
                 publish();
+                if (k == 2 * L && c4) {  // the next tile's encoding, while the dW_0 products run
+                    encode_c4_pack(xr, valid_row(i + 2), q);
+                    load_x(i + 4);
+                }
             }
         }
     }
@@ -724,17 +793,18 @@ __global__ void __launch_bounds__(288, 1) k_nrc_train_ws(const TrainArgs a) {
             const uint32_t qbase = tmem + (((uint32_t)(warp & 3) * 32u) << 16);
             const int j = 16 * (warp & 3) + lane;
             for (int l = warp >> 2; l < L; l += 2) {
-                float v[32];
+                float v[2][32];
+                tmem_ld32(qbase + c_dw + 64u * (uint32_t)l, v[0]);
+                tmem_ld32(qbase + c_dw + 64u * (uint32_t)l + 32u, v[1]);
+                tmem_wait_ld();
+                if (lane < 16) {
+                    float *d = dst + nrc_w_offset(l) + (size_t)j * W;
 #pragma unroll
-                for (int half = 0; half < 2; half++) {
-                    tmem_ld32(qbase + c_dw + 64u * (uint32_t)l + half * 32u, v);
-                    tmem_wait_ld();
-                    if (lane < 16) {
-                        float *d = dst + nrc_w_offset(l) + (size_t)j * W + half * 32;
+                    for (int half = 0; half < 2; half++)
 #pragma unroll
                         for (int k = 0; k < 32; k += 4)
-                            *reinterpret_cast<float4 *>(d + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
-                    }
+                            *reinterpret_cast<float4 *>(d + half * 32 + k) =
+                                make_float4(v[half][k], v[half][k + 1], v[half][k + 2], v[half][k + 3]);
                 }
             }
             if (warp < 4) {
@@ -862,7 +932,7 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
         const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + 2 * (size_t)ws_slot_bytes(n.layers) + 1024;
         STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_train_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                            "attr k_nrc_train_ws"));
-        k_nrc_train_ws<<<ctas, 288, smem, st>>>(a);
+        k_nrc_train_ws<<<ctas, kWsThreads, smem, st>>>(a);
         return check_launch("k_nrc_train_ws");
     }
     const size_t smem = nrc_tc_train_smem(n);
