@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "fastmod.h"
 #include "nrc.cuh"
 
 namespace sty {
@@ -448,8 +449,9 @@ __device__ __forceinline__ uint32_t pcg_step(uint64_t &state, uint64_t inc) {
     const uint32_t rot = (uint32_t)(old >> 59);
     return (xs >> rot) | (xs << ((~rot + 1u) & 31u));
 }
-__global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t count, int in_dims, int out_dims,
-                          const float *in, const float *tg, float *bin, float *btg) {
+// count_magic = fastmod_magic(count): the row index r % count without a 64-bit division
+__global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t count, uint64_t count_magic, int in_dims,
+                          int out_dims, const float *in, const float *tg, float *bin, float *btg) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     uint64_t st = 0, inc = ((step * (uint64_t)B + b) << 1) | 1ull;
@@ -457,7 +459,7 @@ __global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t cou
     st += seed;
     pcg_step(st, inc);
     const uint64_t r = ((uint64_t)pcg_step(st, inc) << 32) | pcg_step(st, inc);
-    const uint64_t idx = r % count;
+    const uint64_t idx = fastmod(r, count, count_magic);
     for (int d = 0; d < in_dims; d++) bin[(size_t)b * in_dims + d] = in[idx * in_dims + d];
     for (int c = 0; c < out_dims; c++) btg[(size_t)b * out_dims + c] = tg[idx * out_dims + c];
 }
@@ -868,8 +870,8 @@ sty_status sty_nrc_train(sty_nrc *nr, uint64_t count, uint64_t n_iters, const fl
     const uint32_t B = c.batch_size;
     STY_TRY(check_cuda(cudaMemsetAsync(nr->loss, 0, 4, st), "zero loss"));
     for (uint64_t it = 0; it < n_iters; it++) {
-        k_collect<<<(B + 255) / 256, 256, 0, st>>>(B, c.seed, nr->step, count, nr->net.in_dims, nr->net.out_dims, in,
-                                                   target, nr->bin, nr->btg);
+        k_collect<<<(B + 255) / 256, 256, 0, st>>>(B, c.seed, nr->step, count, fastmod_magic(count), nr->net.in_dims,
+                                                   nr->net.out_dims, in, target, nr->bin, nr->btg);
         STY_TRY(check_launch("k_collect"));
         STY_TRY(batch_gradient(nr, B, nr->bin, nr->btg, st));
         nr->step++;

@@ -73,9 +73,8 @@ constexpr int kK = 40;                // logit features
 constexpr int kNCol = 160;            // candidates per window row at radius 15-16 (40 px x 4)
 constexpr int kEW = 8, kPW = 5;       // epilogue and producer warps (one candidate per producer thread)
 constexpr int kNH = kNCol / (kEW / 4); // candidates per epilogue warp (2 warps share a TMEM lane quarter)
-constexpr int kNBlk = kNH / 8;        // 8-candidate blocks per epilogue warp
-constexpr int kMmaWarp = kEW + kPW;   // warp 21: MMA issue
-constexpr int kLoadWarp = kMmaWarp + 1;  // warp 22: bulk copies of the raw record rows
+constexpr int kMmaWarp = kEW + kPW;   // warp 13: MMA issue
+constexpr int kLoadWarp = kMmaWarp + 1;  // warp 14: bulk copies of the raw record rows
 constexpr int kKahanRows = 4;         // window rows summed in FP32 before a Kahan step
 constexpr int kNT = (kLoadWarp + 1) * 32;
 constexpr int kNS = 4;                // staging ring depth (feature images and radiance rows)
