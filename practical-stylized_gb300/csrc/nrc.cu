@@ -414,31 +414,48 @@ __global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const f
         for (int c = 0; c < 16; c++) g[c] = acc[c];
     }
 }
-// grad[p] = part[0][p] + part[1][p] + ... in chunk order (one sequential FP32 sum per parameter).
-// A block owns kSumP parameters: all 256 threads stage a slab of kSumC chunk rows into shared
-// memory (16 independent coalesced loads per thread), then kSumP threads continue their sums over
-// the slab in order. The chunk loads of a slab are all in flight at once instead of 8 per thread.
-constexpr int kSumP = 64, kSumC = 64;
-__global__ void __launch_bounds__(256) k_sum_chunks(size_t np, uint32_t chunks, const float *__restrict__ part,
-                                                    float *__restrict__ grad) {
-    __shared__ float slab[kSumC][kSumP];
-    const int t = threadIdx.x, col = t % kSumP, r0 = t / kSumP;
-    const size_t p0 = (size_t)blockIdx.x * kSumP, p = p0 + (size_t)col;
+
+// grad[p] = part[0][p] + part[1][p] + ... in chunk order (one sequential FP32 sum per parameter;
+// np is a multiple of 64: layers x 64 x 64 + outputs x 64). A block owns kSumP parameters: its 256
+// threads stage a slab of up to kSumC chunk rows into shared memory with 16-byte loads, every load of
+// the slab issued before the first store (16 in flight per thread), then kSumP threads continue their
+// sums over the slab in order. The 152 per-CTA partials of a tensor-core training step are one slab.
+constexpr int kSumP = 64, kSumC = 256, kSumLd = kSumC / (256 / (kSumP / 4));
+__global__ void __launch_bounds__(256) k_sum_chunks(size_t np, uint32_t chunks, uint32_t slab_rows,
+                                                    const float *__restrict__ part, float *__restrict__ grad) {
+    extern __shared__ float4 slab4[];  // [slab_rows][kSumP / 4]
+    const float *slab = reinterpret_cast<const float *>(slab4);
+    const int t = threadIdx.x, c4 = t % (kSumP / 4), r0 = t / (kSumP / 4);
+    const size_t p0 = (size_t)blockIdx.x * kSumP;
+    const float4 *src = reinterpret_cast<const float4 *>(part + p0) + c4;
+    const size_t row4 = np / 4;
     float s = 0.0f;
-    for (uint32_t c0 = 0; c0 < chunks; c0 += kSumC) {
-        const uint32_t nc = min((uint32_t)kSumC, chunks - c0);
+    for (uint32_t c0 = 0; c0 < chunks; c0 += slab_rows) {
+        const uint32_t nc = min(slab_rows, chunks - c0);
+        float4 v[kSumLd];
+#pragma unroll
+        for (int j = 0; j < kSumLd; j++) {
+            const uint32_t r = (uint32_t)r0 + (uint32_t)j * (256 / (kSumP / 4));
+            if (r < nc) v[j] = src[(size_t)(c0 + r) * row4];
+        }
         __syncthreads();
-#pragma unroll 4
-        for (uint32_t r = (uint32_t)r0; r < nc; r += 256 / kSumP)
-            slab[r][col] = p < np ? part[(size_t)(c0 + r) * np + p] : 0.0f;
+#pragma unroll
+        for (int j = 0; j < kSumLd; j++) {
+            const uint32_t r = (uint32_t)r0 + (uint32_t)j * (256 / (kSumP / 4));
+            if (r < nc) slab4[r * (kSumP / 4) + c4] = v[j];
+        }
         __syncthreads();
         if (t < kSumP)
-            for (uint32_t r = 0; r < nc; r++) s += slab[r][t];
+            for (uint32_t r = 0; r < nc; r++) s += slab[r * kSumP + t];
     }
-    if (t < kSumP && p < np) grad[p] = s;
+    if (t < kSumP && p0 + (size_t)t < np) grad[p0 + t] = s;
 }
 void sum_chunks(size_t np, uint32_t chunks, const float *part, float *grad, cudaStream_t st) {
-    k_sum_chunks<<<(unsigned)((np + kSumP - 1) / kSumP), 256, 0, st>>>(np, chunks, part, grad);
+    const uint32_t rows = chunks < (uint32_t)kSumC ? (chunks > 0 ? chunks : 1u) : (uint32_t)kSumC;
+    const size_t smem = rows * kSumP * sizeof(float);
+    if (smem > 48 * 1024)  // beyond the default dynamic shared-memory limit (a check_launch follows)
+        cudaFuncSetAttribute(k_sum_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSumC * kSumP * 4));
+    k_sum_chunks<<<(unsigned)((np + kSumP - 1) / kSumP), 256, smem, st>>>(np, chunks, rows, part, grad);
 }
 
 // ---- batch sampling (collect_batch, akari_tcnn.cu:15-38) -------------------------------------
@@ -451,7 +468,8 @@ __device__ __forceinline__ uint32_t pcg_step(uint64_t &state, uint64_t inc) {
 }
 // count_magic = fastmod_magic(count): the row index r % count without a 64-bit division
 __global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t count, uint64_t count_magic, int in_dims,
-                          int out_dims, const float *in, const float *tg, float *bin, float *btg) {
+                          int out_dims, const float *__restrict__ in, const float *__restrict__ tg,
+                          float *__restrict__ bin, float *__restrict__ btg) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
     uint64_t st = 0, inc = ((step * (uint64_t)B + b) << 1) | 1ull;
@@ -460,8 +478,24 @@ __global__ void k_collect(uint32_t B, uint64_t seed, uint64_t step, uint64_t cou
     pcg_step(st, inc);
     const uint64_t r = ((uint64_t)pcg_step(st, inc) << 32) | pcg_step(st, inc);
     const uint64_t idx = fastmod(r, count, count_magic);
-    for (int d = 0; d < in_dims; d++) bin[(size_t)b * in_dims + d] = in[idx * in_dims + d];
-    for (int c = 0; c < out_dims; c++) btg[(size_t)b * out_dims + c] = tg[idx * out_dims + c];
+    // the row's loads in batches of 8 before their stores, so the random-row latency is paid once
+    // per batch, not once per value
+    const float *src = in + idx * in_dims;
+    float *dst = bin + (size_t)b * in_dims;
+    for (int d0 = 0; d0 < in_dims; d0 += 8) {
+        float v[8];
+#pragma unroll
+        for (int d = 0; d < 8; d++) v[d] = d0 + d < in_dims ? src[d0 + d] : 0.0f;
+#pragma unroll
+        for (int d = 0; d < 8; d++)
+            if (d0 + d < in_dims) dst[d0 + d] = v[d];
+    }
+    float u[kNrcOutPad];
+#pragma unroll
+    for (int c = 0; c < kNrcOutPad; c++) u[c] = c < out_dims ? tg[idx * out_dims + c] : 0.0f;
+#pragma unroll
+    for (int c = 0; c < kNrcOutPad; c++)
+        if (c < out_dims) btg[(size_t)b * out_dims + c] = u[c];
 }
 
 // ---- Adam + EMA (akari_tcnn.cu:42-83 for the EMA) --------------------------------------------

@@ -98,6 +98,24 @@ def test_fp32_gradient_matches_oracle(sty, cuda):
 
 
 @pytest.mark.gpu
+def test_fp32_gradient_many_chunks(sty, cuda):
+    """261 weight-gradient chunks of 1024 samples: the ordered chunk sum stages them in two slabs
+    (256 + 5). Against the FP64 oracle, and bit-equal to itself (the order is fixed)."""
+    B = 260 * 1024 + 5
+    net = _make(sty, sty.nrc.STY_NRC_FP32, batch=1024, layers=2)
+    p = net.save_params().astype(np.float64)
+    x = np.random.default_rng(3).random((B, 11))
+    t = target_fn(x)
+    g, loss = net.gradient(_dev(x), _dev(t))
+    g2, _ = net.gradient(_dev(x), _dev(t))
+    rl, rg = onrc.loss_and_grad(p, x, t, FREQS, 2, 3)
+    g, g2 = g.cpu().numpy(), g2.cpu().numpy()
+    assert (g == g2).all()
+    assert abs(loss - rl) <= 1e-4 * abs(rl)
+    assert np.linalg.norm(g - rg) <= 1e-4 * np.linalg.norm(rg)
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("layers", [1, 5])
 def test_bf16_tensor_core_inference(sty, cuda, layers):
     """tcgen05 path vs the oracle's BF16 emulation (tight) and vs FP64 (statistical)."""
