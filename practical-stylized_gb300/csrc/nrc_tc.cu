@@ -11,6 +11,7 @@
 // (K-direction) byte offset is 128 and the stride (8-row) byte offset is 1024.
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "common.cuh"
@@ -51,32 +52,26 @@ EncPlan make_plan(const NrcNet &n) {
     return e;
 }
 
-// encode one sample (x = its input row, or nullptr for a padding row) into row `row` of a K-major
-// image, one 16-byte store per 8 columns
-__device__ __forceinline__ void encode_row(const EncPlan &e, const float *x, uint8_t *img, uint32_t row) {
+// the packed BF16 encoding of one sample (x = its input row, or nullptr for a padding row): column
+// pair p in q[p] (sin in the low half)
+__device__ __forceinline__ void encode_row_pack(const EncPlan &e, const float *x, uint32_t (&q)[kNrcWidth / 2]) {
     float s = 0.0f, c = 0.0f;
 #pragma unroll
-    for (int kb = 0; kb < 8; kb++) {
-        uint32_t q[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int p = kb * 4 + j;
-            const uint32_t d = e.pdim[p];
-            float vs = 0.0f, vc = 0.0f;
-            if (d != 0xffu && x) {
-                if (e.pfirst[p]) {
-                    sincospif(x[d], &s, &c);
-                } else {
-                    const float s2 = 2.0f * s * c;
-                    c = fmaf(-2.0f * s, s, 1.0f);
-                    s = s2;
-                }
-                vs = s;
-                vc = c;
+    for (int p = 0; p < kNrcWidth / 2; p++) {
+        const uint32_t d = e.pdim[p];
+        float vs = 0.0f, vc = 0.0f;
+        if (d != 0xffu && x) {
+            if (e.pfirst[p]) {
+                sincospif(x[d], &s, &c);
+            } else {
+                const float s2 = 2.0f * s * c;
+                c = fmaf(-2.0f * s, s, 1.0f);
+                s = s2;
             }
-            q[j] = pack2_bf16(vs, vc);
+            vs = s;
+            vc = c;
         }
-        *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) = make_uint4(q[0], q[1], q[2], q[3]);
+        q[p] = pack2_bf16(vs, vc);
     }
 }
 
@@ -114,18 +109,27 @@ __device__ __forceinline__ void store_row(const uint32_t (&q)[kNrcWidth / 2], ui
         *reinterpret_cast<uint4 *>(img + img_off(row, kb * 8)) =
             make_uint4(q[kb * 4], q[kb * 4 + 1], q[kb * 4 + 2], q[kb * 4 + 3]);
 }
-__device__ __forceinline__ void encode_row_c4(const float *x, uint8_t *img, uint32_t row) {
-    float xin[kC4Dims];
+__device__ __forceinline__ void encode_any_pack(const EncPlan &e, bool c4, const float *x, uint32_t (&q)[kNrcWidth / 2]) {
+    if (c4) {
+        float xin[kC4Dims];
 #pragma unroll
-    for (int d = 0; d < kC4Dims; d++) xin[d] = x ? x[d] : 0.0f;
-    uint32_t q[kNrcWidth / 2];
-    encode_c4_pack(xin, x != nullptr, q);
-    store_row(q, img, row);
+        for (int d = 0; d < kC4Dims; d++) xin[d] = x ? x[d] : 0.0f;
+        encode_c4_pack(xin, x != nullptr, q);
+    } else {
+        encode_row_pack(e, x, q);
+    }
 }
+// encode one sample into row `row` of a K-major image, one 16-byte store per 8 columns
 __device__ __forceinline__ void encode_any(const NrcNet &n, const EncPlan &e, bool c4, const float *x, uint8_t *img,
                                            uint32_t row) {
-    if (c4) encode_row_c4(x, img, row);
-    else encode_row(e, x, img, row);
+    uint32_t q[kNrcWidth / 2];
+    encode_any_pack(e, c4, x, q);
+    store_row(q, img, row);
+}
+__device__ __forceinline__ void encode_row(const EncPlan &e, const float *x, uint8_t *img, uint32_t row) {
+    uint32_t q[kNrcWidth / 2];
+    encode_row_pack(e, x, q);
+    store_row(q, img, row);
 }
 
 
@@ -140,14 +144,38 @@ struct TcArgs {
     uint32_t *status;
 };
 
-// Inference: kFwdWG warpgroups per CTA share one copy of the weight images; each warpgroup owns
-// one 128-sample tile at a time (its own activation image, 64 TMEM columns, mbarrier and named
-// barrier), so 2 CTAs x kFwdWG tiles are in flight per SM and one tile's epilogue overlaps
-// another's MMAs. Per layer: thread 0 of the warpgroup issues 4 x tcgen05.mma (M=128, N=64 (16
-// for the output layer), K=16) and commits to the warpgroup's mbarrier; the warpgroup waits
-// (bounded), tcgen05.ld's its rows and writes ReLU'd BF16 rows back as the next A operand.
-constexpr int kFwdWG = 4;
-__global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) {
+// Inference: one CTA per SM, kFwdWG warpgroups sharing one copy of the weight images in shared
+// memory; each warpgroup owns one 128-sample tile at a time: 96 TMEM columns (a 64-column FP32
+// accumulator and the next layer's A operand, 32 columns of BF16 pairs: element k of row m in lane
+// m, column k / 2, half k % 2), an mbarrier and a named barrier. The activations never touch shared
+// memory: per layer the warpgroup tcgen05.ld's its accumulator rows, applies ReLU and BF16 rounding
+// and tcgen05.st's the row as the next layer's A; thread 0 issues 4 x tcgen05.mma (A from TMEM at
+// +8 columns per K = 16 step, B the layer's weight image; N = 64, or 16 for the output layer) and
+// commits to the mbarrier. Shared memory then carries only the B operands (2 KB per MMA instead of
+// 6 KB plus a 16 KB activation store per layer); 5 tiles are in flight per SM (5 x 96 of the 512
+// TMEM columns).
+constexpr int kFwdWG = 5;
+constexpr uint32_t kFwdCols = 96;
+__device__ __forceinline__ void mma_bf16_ts(uint32_t tmem_d, uint32_t a_tmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "r"(a_tmem), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+// one row (32 lanes of this warp, 32 columns) of BF16 pairs into TMEM
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&q)[32]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+        "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+        "r"(q[0]), "r"(q[1]), "r"(q[2]), "r"(q[3]), "r"(q[4]), "r"(q[5]), "r"(q[6]), "r"(q[7]), "r"(q[8]), "r"(q[9]),
+        "r"(q[10]), "r"(q[11]), "r"(q[12]), "r"(q[13]), "r"(q[14]), "r"(q[15]), "r"(q[16]), "r"(q[17]), "r"(q[18]),
+        "r"(q[19]), "r"(q[20]), "r"(q[21]), "r"(q[22]), "r"(q[23]), "r"(q[24]), "r"(q[25]), "r"(q[26]), "r"(q[27]),
+        "r"(q[28]), "r"(q[29]), "r"(q[30]), "r"(q[31])
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+__global__ void __launch_bounds__(128 * kFwdWG, 1) k_nrc_fwd_tc(const TcArgs a) {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ uint64_t mbar[kFwdWG];
     __shared__ uint32_t tmem_slot;
@@ -156,7 +184,6 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
     const int L = a.n.layers;
     const uint32_t wbytes = (uint32_t)(L * W * W + kNrcOutPad * W) * 2u;
     uint8_t *wimg = smem;
-    uint8_t *act = smem + ((wbytes + 1023u) & ~1023u) + (size_t)wg * kTileBytes;
 
     for (uint32_t o = tid * 16u; o < wbytes; o += 128u * kFwdWG * 16u)
         *reinterpret_cast<uint4 *>(wimg + o) =
@@ -167,8 +194,7 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(64u * kFwdWG)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&tmem_slot))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -176,9 +202,10 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tmem = tmem_slot + 64u * (uint32_t)wg;
-    const uint32_t lane_base = tmem + (((uint32_t)(warp & 3) * 32u) << 16);
-    const uint32_t wbase = smem_u32(wimg), abase = smem_u32(act);
+    const uint32_t tmem = tmem_slot + kFwdCols * (uint32_t)wg;  // accumulator
+    const uint32_t areg = tmem + 64u;                            // A operand of the next layer
+    const uint32_t lane_off = ((uint32_t)(warp & 3) * 32u) << 16;
+    const uint32_t wbase = smem_u32(wimg);
     uint64_t *bar = &mbar[wg];
     uint32_t phase = 0;
     bool failed = false;  // uniform over the warpgroup (decided through bar.red.and)
@@ -187,8 +214,11 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
     for (uint64_t tile = (uint64_t)blockIdx.x * kFwdWG + wg; tile < ntiles && !failed;
          tile += (uint64_t)gridDim.x * kFwdWG) {
         const uint64_t row = tile * TM + t;
-        encode_any(a.n, a.plan, a.c4 != 0, row < a.count ? a.input + row * a.n.in_dims : nullptr, act, t);
-        fence_async_smem();
+        {
+            uint32_t q[kNrcWidth / 2];
+            encode_any_pack(a.plan, a.c4 != 0, row < a.count ? a.input + row * a.n.in_dims : nullptr, q);
+            tmem_st32(areg + lane_off, q);
+        }
         fence_before();
         wg_sync(bar_id);
         for (int l = 0; l <= L; l++) {
@@ -199,7 +229,7 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
                 const uint32_t idesc = out_layer ? idesc_bf16(TM, kNrcOutPad) : idesc_bf16(TM, W);
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++)
-                    mma_bf16(tmem, make_desc(abase + kk * 256u), make_desc(wl + kk * 256u), idesc, kk > 0 ? 1u : 0u);
+                    mma_bf16_ts(tmem, areg + 8u * kk, make_desc(wl + kk * 256u), idesc, kk > 0 ? 1u : 0u);
                 mma_commit(bar);
             }
             const bool got = mbar_wait(bar, phase, a.status);
@@ -210,24 +240,19 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
             phase ^= 1u;
             fence_after();
             if (!out_layer) {
-                float v[32];
+                uint32_t q[kNrcWidth / 2];
 #pragma unroll
                 for (int half = 0; half < 2; half++) {
-                    tmem_ld32(lane_base + half * 32u, v);
+                    float v[32];
+                    tmem_ld32(tmem + lane_off + half * 32u, v);
                     tmem_wait_ld();
 #pragma unroll
-                    for (int kb = 0; kb < 4; kb++) {
-                        const uint4 q = make_uint4(pack2_relu_bf16(v[kb * 8 + 0], v[kb * 8 + 1]),
-                                                   pack2_relu_bf16(v[kb * 8 + 2], v[kb * 8 + 3]),
-                                                   pack2_relu_bf16(v[kb * 8 + 4], v[kb * 8 + 5]),
-                                                   pack2_relu_bf16(v[kb * 8 + 6], v[kb * 8 + 7]));
-                        *reinterpret_cast<uint4 *>(act + img_off(t, half * 32 + kb * 8)) = q;
-                    }
+                    for (int j = 0; j < 16; j++) q[half * 16 + j] = pack2_relu_bf16(v[2 * j], v[2 * j + 1]);
                 }
-                fence_async_smem();
+                tmem_st32(areg + lane_off, q);
             } else {
                 float v[16];
-                tmem_ld16(lane_base, v);
+                tmem_ld16(tmem + lane_off, v);
                 tmem_wait_ld();
                 if (row < a.count)
                     for (int c = 0; c < a.n.out_dims; c++) a.output[row * a.n.out_dims + c] = v[c];
@@ -244,9 +269,7 @@ __global__ void __launch_bounds__(128 * kFwdWG, 2) k_nrc_fwd_tc(const TcArgs a) 
     fence_before();
     __syncthreads();
     fence_after();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"(64u * kFwdWG)
-                     : "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem_slot) : "memory");
 }
 
 // ---- fused BF16 training step --------------------------------------------------------------
@@ -877,7 +900,8 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
         return STY_ERR_CUDA;
     }
     const size_t wbytes = nrc_tc_image_elems(n) * 2;
-    const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + (size_t)kFwdWG * kTileBytes + 1024;
+    // at least 120 KB so that one CTA (and its 512 TMEM columns) owns the SM
+    const size_t smem = std::max<size_t>(((wbytes + 1023) & ~(size_t)1023) + 1024, 122880);
     STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_fwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                        "attr k_nrc_fwd_tc"));
     int dev = 0, sms = 0;
@@ -885,7 +909,7 @@ sty_status nrc_tc_forward(const NrcNet &n, const uint16_t *img, uint64_t count, 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const uint64_t ntiles = (count + TM - 1) / TM;
     const uint64_t ctas = (ntiles + kFwdWG - 1) / kFwdWG;
-    const uint64_t grid = ctas < (uint64_t)sms * 2 ? ctas : (uint64_t)sms * 2;
+    const uint64_t grid = ctas < (uint64_t)sms ? ctas : (uint64_t)sms;
     k_nrc_fwd_tc<<<(unsigned)grid, 128 * kFwdWG, smem, st>>>(a);
     return check_launch("k_nrc_fwd_tc");
 }
