@@ -1,11 +1,11 @@
-// nrc_tc.cu -- BF16 tcgen05 forward of the NRC MLP (inference), FP32 accumulation in TMEM.
+// nrc_tc.cu -- the BF16 tcgen05 paths of the NRC MLP: inference and the fused training step, FP32
+// accumulation in TMEM.
 //
-// One CTA = one warpgroup (128 threads), persistent over tiles of 128 samples (one sample per TMEM
-// lane / thread). Shared memory holds every layer's weights as BF16 UMMA operand images plus one
-// 128 x 64 BF16 activation tile; TMEM holds the 128 x 64 FP32 accumulator. Per layer:
-//   thread 0 issues 4 x tcgen05.mma (M=128, N=64 (16 for the output layer), K=16) and commits to an
-//   mbarrier; all threads wait (bounded), tcgen05.ld their row, apply ReLU, convert to BF16 and write
-//   the row back as the next layer's A operand (generic-proxy writes fenced for the async proxy).
+// Inference: persistent CTAs, one warpgroup per 128-sample tile (one sample per TMEM lane /
+// thread), every layer's weights as BF16 UMMA operand images in shared memory, the activations in
+// TMEM as the next layer's A operand (k_nrc_fwd_tc). Training: forward, loss gradient, backward and
+// weight gradient of a tile in one kernel, the activations as shared-memory images (k_nrc_train_tc,
+// one tile at a time; k_nrc_train_ws, two tiles in flight per SM).
 // Operand images are K-major with no swizzle: an R x 64 matrix is stored as R/8 x 8 "core matrices"
 // of 8 rows x 16 bytes, core matrix (rb, kb) at byte ((rb * 8) + kb) * 128, so the leading
 // (K-direction) byte offset is 128 and the stride (8-row) byte offset is 1024.
