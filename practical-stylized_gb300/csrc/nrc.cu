@@ -377,41 +377,69 @@ __global__ void __launch_bounds__(512, 1) k_bwd_f32_tiled(NrcNet n, const float 
 // chunk of kWgChunk samples stores its partial sums at part + chunk * np; k_sum_chunks adds the
 // chunks in order, so the gradient does not depend on scheduling.
 constexpr int kWgChunk = 1024;
+// Register-tiled: thread (ty, tx) = (t / 16, t % 16) owns outputs j = 4 ty .. 4 ty + 3 x
+// k = 4 tx .. 4 tx + 3, so per sample two 16-byte shared-memory loads feed 16 FMAs; the next
+// 64-sample tile's rows are loaded into registers while the current one is summed. Every output
+// is summed over the chunk's samples in order with fmaf(dpre, act, acc) (padding samples add
+// fmaf(0, 0, acc)), as the one-output-row-per-thread version did, so the partials are unchanged.
 __global__ void __launch_bounds__(256) k_wgrad_f32(NrcNet n, uint32_t B, const float *__restrict__ acts,
                                                    const float *__restrict__ dpre, size_t np,
                                                    float *__restrict__ part) {
-    __shared__ float sd[64][W + 1];
-    __shared__ float sh[64][W + 1];
+    __shared__ __align__(16) float sd[64][W];  // dpre rows of 64 samples
+    __shared__ __align__(16) float sh[64][W];  // activation rows (the input of weight matrix l)
     const int l = blockIdx.y;
     const int rows = l < n.layers ? W : n.out_dims;
     const uint32_t i0 = blockIdx.x * kWgChunk, i1 = min(B, i0 + kWgChunk);
-    const int j = threadIdx.x >> 2, k0 = (threadIdx.x & 3) * 16;
-    float acc[16];
+    const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+    const float4 *dl = reinterpret_cast<const float4 *>(dpre + (size_t)l * B * W);
+    const float4 *al = reinterpret_cast<const float4 *>(acts + (size_t)l * B * W);
+    constexpr int kPer = 64 * W / 4 / 256;  // float4 of each array per thread per tile
+    float4 pd[kPer], pa[kPer];
+    auto fetch = [&](uint32_t s0) {
 #pragma unroll
-    for (int c = 0; c < 16; c++) acc[c] = 0.0f;
-    const float *dl = dpre + (size_t)l * B * W;
-    const float *al = acts + (size_t)l * B * W;  // input of weight matrix l = post-activation row l
+        for (int u = 0; u < kPer; u++) {
+            const int e = threadIdx.x + u * 256, r = e / (W / 4), c4 = e % (W / 4);
+            const uint32_t s = s0 + (uint32_t)r;
+            const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            pd[u] = s < i1 ? dl[(size_t)s * (W / 4) + c4] : z;
+            pa[u] = s < i1 ? al[(size_t)s * (W / 4) + c4] : z;
+        }
+    };
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) acc[i][c] = 0.0f;
+    fetch(i0);
     for (uint32_t s0 = i0; s0 < i1; s0 += 64) {
         __syncthreads();
-        for (int e = threadIdx.x; e < 64 * W; e += 256) {
-            const int r = e / W, c = e % W;
-            const uint32_t s = s0 + r;
-            sd[r][c] = s < i1 ? dl[(size_t)s * W + c] : 0.0f;
-            sh[r][c] = s < i1 ? al[(size_t)s * W + c] : 0.0f;
+#pragma unroll
+        for (int u = 0; u < kPer; u++) {
+            const int e = threadIdx.x + u * 256, r = e / (W / 4), c4 = e % (W / 4);
+            reinterpret_cast<float4 *>(&sd[r][0])[c4] = pd[u];
+            reinterpret_cast<float4 *>(&sh[r][0])[c4] = pa[u];
         }
         __syncthreads();
-        if (j < rows) {
+        if (s0 + 64 < i1) fetch(s0 + 64);
+        if (4 * ty < rows) {
+#pragma unroll 4
             for (int r = 0; r < 64; r++) {
-                const float a = sd[r][j];
+                const float4 a4 = *reinterpret_cast<const float4 *>(&sd[r][4 * ty]);
+                const float4 b4 = *reinterpret_cast<const float4 *>(&sh[r][4 * tx]);
+                const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
 #pragma unroll
-                for (int c = 0; c < 16; c++) acc[c] = fmaf(a, sh[r][k0 + c], acc[c]);
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int c = 0; c < 4; c++) acc[i][c] = fmaf(av[i], bv[c], acc[i][c]);
             }
         }
     }
-    if (j < rows) {
-        float *g = part + blockIdx.x * np + nrc_w_offset(l) + (size_t)j * W + k0;
 #pragma unroll
-        for (int c = 0; c < 16; c++) g[c] = acc[c];
+    for (int i = 0; i < 4; i++) {
+        const int j = 4 * ty + i;
+        if (j < rows)
+            *reinterpret_cast<float4 *>(part + blockIdx.x * np + nrc_w_offset(l) + (size_t)j * W + 4 * tx) =
+                make_float4(acc[i][0], acc[i][1], acc[i][2], acc[i][3]);
     }
 }
 
