@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(128, 1) k_nrc_train_tc(const TrainArgs a) {
 // TMEM: columns 0-63 / 64-127 the slots' accumulators, 128 + 64 l the dW_l sums, 128 + 64 L dW_out^T.
 constexpr int kWsMaxLayers = 5;
 std::atomic<int32_t> g_train_kernel{STY_NRC_TRAIN_KERNEL_AUTO};
-int32_t train_kernel() { return g_train_kernel.load(std::memory_order_relaxed) == STY_NRC_TRAIN_KERNEL_ONE_TILE; }
+bool one_tile_selected() { return g_train_kernel.load(std::memory_order_relaxed) == STY_NRC_TRAIN_KERNEL_ONE_TILE; }
 constexpr uint32_t kGBytes = TM * kNrcOutPad * 2;  // 4 KB
 constexpr int kWsThreads = 352;
 __host__ __device__ inline int ws_images(int L) { return L < 2 ? 2 : L; }
@@ -951,7 +951,7 @@ sty_status nrc_tc_train(const NrcNet &n, const uint16_t *img, uint32_t B, const 
         set_error("device status word unavailable");
         return STY_ERR_CUDA;
     }
-    if (n.layers <= kWsMaxLayers && train_kernel() == 0) {
+    if (n.layers <= kWsMaxLayers && !one_tile_selected()) {
         const size_t wbytes = nrc_tc_image_elems(n) * 2;
         const size_t smem = ((wbytes + 1023) & ~(size_t)1023) + 2 * (size_t)ws_slot_bytes(n.layers) + 1024;
         STY_TRY(check_cuda(cudaFuncSetAttribute(k_nrc_train_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
