@@ -158,6 +158,27 @@ def test_f32_restatement_close_to_f64(orc, sty):
     assert rel_err(got[:, m], ref[:, m]).max() < 1e-5
 
 
+def test_f32_band_equals_full_image(orc, sty):
+    """The band form of the FP32 restatement (rows y0..y1 only; the reference arm and the CPU
+    baseline time it) gives those rows bit for bit as the full image does, styled and with a child
+    input, and leaves the other rows zero."""
+    W, H, S, D = 40, 24, 4, 3
+    planes, valid, rec = _tiny(sty, W, H, S, D, seed=13)
+    prm = sty.ScreenParams(6, 3.0, 0.5, 0.2).c()
+    style = sty.c2_style()  # the toon node acts at depth 1
+    n = W * H * S
+    child = orc.pf_screen_filter_depth_f32(rec, 2, prm, None)
+    full = orc.pf_screen_filter_depth_f32(rec, 1, prm, style, out_next=child)
+    unstyled = orc.pf_screen_filter_depth_f32(rec, 1, prm, None, out_next=child)
+    assert not np.array_equal(full, unstyled)  # the style does act on this depth
+    y0, y1 = 9, 15
+    band = orc.pf_screen_filter_depth_f32(rec, 1, prm, style, out_next=child, y0=y0, y1=y1)
+    rows = slice(y0 * W * S, y1 * W * S)
+    assert np.array_equal(band[:, rows], full[:, rows])
+    assert (band[:, :y0 * W * S] == 0).all() and (band[:, y1 * W * S:] == 0).all()
+    assert np.abs(full[:, rows]).max() > 0 and full.shape == (3, n)
+
+
 def test_synthetic_records_distribution(sty):
     planes, valid = sty.synth.records(64, 48, 4, 2, seed=0)
     n = planes.shape[1]
